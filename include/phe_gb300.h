@@ -1,0 +1,200 @@
+/* phe_gb300.h - C ABI of the GB300 ray-cast and wavefront-shading core.
+ *
+ * A drop-in for the ray-cast path of PetorSFZ/PhantasyEngineTestbed. All structs are
+ * byte-identical to the reference's (static_asserts in the implementation); all entry points
+ * return a phe_status and never abort; phe_last_error() describes the last failure on the
+ * calling thread. Device pointers are plain CUDA device addresses; `stream` is a cudaStream_t
+ * (NULL = legacy default stream). Launch functions are asynchronous on `stream` unless stated.
+ *
+ * Reference paths below are relative to the reference project root.
+ */
+#ifndef PHE_GB300_H
+#define PHE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------------------------------------
+ * Status codes. The reference has none (CHECK_CUDA_ERROR logs and continues,
+ * source/cuda_ray_tracer/CudaHelpers.hpp:13-25); every function here returns one of these.
+ * ------------------------------------------------------------------------------------------- */
+typedef int phe_status;
+#define PHE_OK 0
+#define PHE_ERR_INVALID_ARGUMENT 1   /* null pointer, zero size where not allowed, bad enum */
+#define PHE_ERR_INVALID_SCENE 2      /* BVH fails validation (index out of range, cycle, too deep) */
+#define PHE_ERR_CUDA 3               /* a CUDA runtime call failed; text in phe_last_error() */
+#define PHE_ERR_OUT_OF_MEMORY 4      /* device or host allocation failed */
+#define PHE_ERR_BUDGET 5             /* admission refused: device-memory budget exhausted */
+#define PHE_ERR_TIMEOUT 6            /* a bounded device-side wait ran out */
+#define PHE_ERR_NOT_FOUND 7          /* unknown scene / request id */
+#define PHE_ERR_TOO_LARGE 8          /* size beyond a documented maximum */
+#define PHE_ERR_NOT_READY 9          /* result not available yet (poll again) */
+#define PHE_ERR_NO_DEVICE 10         /* no CUDA device is visible */
+
+/* ---------------------------------------------------------------------------------------------
+ * Layouts (byte-identical to the reference)
+ * ------------------------------------------------------------------------------------------- */
+
+/* phe::BVHNode, source/phantasy_engine/ray_tracer_common/BVHNode.hpp:23-149 (64 bytes).
+ * fData = [lc.min.xyz, lc.max.x] [lc.max.yz, rc.min.xy] [rc.min.z, rc.max.xyz];
+ * iData = [lcIndex, rcIndex, lcNumTriangles, rcNumTriangles]; a leaf child has a non-zero
+ * triangle count and a bitwise-negated (~) first-slot index; node 0 is the root. */
+typedef struct phe_bvh_node { float fData[12]; int32_t iData[4]; } phe_bvh_node;
+
+/* phe::TriangleVertices, ray_tracer_common/Triangle.hpp:17-23 (48 bytes). The .w lanes are
+ * 0, or -1 on the last triangle of each leaf (StaticBVHBuilder.cpp:33-45). */
+typedef struct phe_triangle_vertices { float v0[4]; float v1[4]; float v2[4]; } phe_triangle_vertices;
+
+/* phe::TriangleData, ray_tracer_common/Triangle.hpp:25-37 (64 bytes), same slot order. */
+typedef struct phe_triangle_data {
+	float n0[3], n1[3], n2[3];
+	float uv0[2], uv1[2], uv2[2];
+	uint32_t materialIndex;
+} phe_triangle_data;
+
+/* phe::RayIn, cuda_ray_tracer/kernels/RayCastKernel.hpp:22-37 (32 bytes):
+ * data1 = (origin.xyz, tMin), data2 = (dir.xyz, tMax). */
+typedef struct phe_ray_in { float data1[4]; float data2[4]; } phe_ray_in;
+
+/* phe::RayHit, cuda_ray_tracer/kernels/RayCastKernel.hpp:39-45 (16 bytes).
+ * Hit: triangleIndex = slot index, t, barycentric u, v. Miss: triangleIndex = ~0u, t = the ray's
+ * tMax (as rayCastKernel, RayCastKernel.cu:396-409), u = v = 0 (the reference leaves them unset).
+ * A hit is accepted when tMin <= t < tMax (exclusive tMax, RayCastKernel.cu:361). */
+typedef struct phe_ray_hit { uint32_t triangleIndex; float t; float u; float v; } phe_ray_hit;
+
+/* phe::CameraDef, ray_tracer_common/GenerateRays.hpp:14-24. */
+typedef struct phe_camera_def { float origin[3]; float dir[3]; float dX[3]; float dY[3]; } phe_camera_def;
+
+/* The shading inputs of phe::SphereLight (level/SphereLight.hpp:13-26). */
+typedef struct phe_sphere_light {
+	float pos[3]; float radius; float range; float strength[3]; int32_t staticShadows;
+} phe_sphere_light;
+
+/* Material values read at a hit (rendering/Material.hpp:17-55 without textures):
+ * albedo rgb + alpha, roughness, metallic. */
+typedef struct phe_material { float albedo[4]; float roughness; float metallic; float pad[2]; } phe_material;
+
+/* ---------------------------------------------------------------------------------------------
+ * Library
+ * ------------------------------------------------------------------------------------------- */
+
+/* Version as 10000*major + 100*minor + patch. */
+int phe_version(void);
+/* Text of the last error on this thread ("" if none). The pointer stays valid until the next
+ * call on this thread. */
+const char* phe_last_error(void);
+
+/* ---------------------------------------------------------------------------------------------
+ * Host-side scene tools (no GPU needed)
+ * ------------------------------------------------------------------------------------------- */
+
+/* Synthetic scene recipe: an N x N-cell heightfield (2 triangles per cell, height = sum of 4
+ * seeded sine octaves) plus `numCubes` cubes resting on it; the world is scaled by N/64 so the
+ * cell size stays 1/64 (keeps the reference's absolute 1e-5 determinant epsilon,
+ * Intersection.hpp:28, far from the triangle scale). Materials: one per triangle, albedo
+ * U[0.2, 0.8] per channel, roughness 1, metallic 0. */
+typedef struct phe_scene_recipe {
+	uint32_t gridCells;      /* N */
+	uint32_t numCubes;
+	int32_t rotatedCubes;    /* 0 = axis-aligned, 1 = uniformly random rotation */
+	uint32_t pad;
+	uint64_t seed;
+} phe_scene_recipe;
+/* Triangle count of a recipe (2*N*N + 12*numCubes). */
+uint64_t phe_scene_recipe_triangles(const phe_scene_recipe* recipe);
+/* Writes `triVerts` (9 floats per triangle: v0 v1 v2), `datas` (flat normals, zero uv,
+ * materialIndex = triangle index) and `materials` (one per triangle); each may be NULL. */
+phe_status phe_scene_generate(const phe_scene_recipe* recipe, float* triVerts, phe_triangle_data* datas,
+                              phe_material* materials);
+
+/* Host BVH in the reference layout, produced by the project's SBVH builder. */
+typedef struct phe_host_bvh phe_host_bvh;
+typedef struct phe_sbvh_params {
+	float splitAlpha;        /* spatial-split overlap threshold relative to the root area (1e-5) */
+	int32_t maxDepth;        /* leaf depth limit (64) */
+	int32_t maxSpatialDepth; /* no spatial splits at or below this depth (48) */
+	int32_t numThreads;      /* 0 = all hardware threads */
+} phe_sbvh_params;
+/* Defaults of the reference builder (sbvh-stuff/BVH.h:68-81, SplitBVHBuilder.h:38-44). */
+void phe_sbvh_default_params(phe_sbvh_params* params);
+/* Spatial-split SAH builder (Stich, Friedrich, Dietrich 2009) over `numTris` triangles given as 9
+ * floats each. Output is sanitized like sanitizeBVH (StaticBVHBuilder.cpp:19-78, 253-260): node 0
+ * is the root, nodes in depth-first order, leaf indices negated, end markers in .w. Replaces
+ * buildStaticFrom (StaticBVHBuilder.cpp:213-251). */
+phe_status phe_sbvh_build(const float* triVerts, uint32_t numTris, const phe_sbvh_params* params,
+                          phe_host_bvh** out);
+phe_status phe_host_bvh_info(const phe_host_bvh* bvh, uint32_t* numNodes, uint32_t* numSlots, uint32_t* maxDepth);
+/* Copies nodes, slot vertices and the slot -> input-triangle map (any may be NULL). */
+phe_status phe_host_bvh_copy(const phe_host_bvh* bvh, phe_bvh_node* nodes, phe_triangle_vertices* verts,
+                             uint32_t* slotToTri);
+void phe_host_bvh_free(phe_host_bvh* bvh);
+
+/* Checks a BVH in the reference layout: every node reachable from the root exactly once, child
+ * and slot indices in range, leaf counts > 0, leaf depth <= 64. Returns PHE_OK or
+ * PHE_ERR_INVALID_SCENE; `maxDepth` (optional) receives the deepest leaf level. */
+phe_status phe_bvh_validate(const phe_bvh_node* nodes, uint32_t numNodes, uint32_t numSlots, uint32_t* maxDepth);
+
+/* BVH cache file (testbed_application/Main.cpp:105-154): three headerless raw arrays
+ * <base>_nodes.bin, <base>_verts.bin, <base>_datas.bin. Read sizes come from the file sizes;
+ * datas must have as many entries as verts (the reference's only check, Main.cpp:131-133). */
+phe_status phe_bvh_cache_write(const char* basePath, const phe_bvh_node* nodes, uint32_t numNodes,
+                               const phe_triangle_vertices* verts, const phe_triangle_data* datas, uint32_t numSlots);
+phe_status phe_bvh_cache_sizes(const char* basePath, uint32_t* numNodes, uint32_t* numSlots);
+phe_status phe_bvh_cache_read(const char* basePath, phe_bvh_node* nodes, uint32_t numNodes,
+                              phe_triangle_vertices* verts, phe_triangle_data* datas, uint32_t numSlots);
+
+/* generateCameraDef (ray_tracer_common/GenerateRays.cpp:12-35). */
+void phe_generate_camera_def(const float pos[3], const float dir[3], const float up[3], float vertFovRad,
+                             float resX, float resY, phe_camera_def* out);
+/* Entry i (mod 16) of the Halton(2,3) jitter table minus 0.5 (screens/GameScreen.cpp:21-39). */
+void phe_halton_jitter(uint32_t index, float out[2]);
+
+/* ---------------------------------------------------------------------------------------------
+ * Device scenes
+ * ------------------------------------------------------------------------------------------- */
+
+typedef struct phe_scene phe_scene;
+#define PHE_PTR_HOST 0
+#define PHE_PTR_DEVICE 1
+/* Validates and uploads a scene (setStaticScene, CudaTracerRenderer.cpp:251-315): the reference
+ * node and triangle arrays are re-laid out on the device into the traversal layout. `datas` and
+ * `materials` may be NULL (ray queries only). `where` says whether the array pointers are host
+ * or device memory. Synchronous. */
+phe_status phe_scene_create(const phe_bvh_node* nodes, uint32_t numNodes, const phe_triangle_vertices* verts,
+                            const phe_triangle_data* datas, uint32_t numSlots, const phe_material* materials,
+                            uint32_t numMaterials, int where, phe_scene** out);
+phe_status phe_scene_destroy(phe_scene* scene);
+/* Device bytes held by the scene. */
+phe_status phe_scene_device_bytes(const phe_scene* scene, uint64_t* bytes);
+
+/* ---------------------------------------------------------------------------------------------
+ * Ray casting (the hot path). Rays and results are device arrays of n entries.
+ * ------------------------------------------------------------------------------------------- */
+
+/* Closest hit, persistent warps with dynamic ray fetch (replaces launchRayCastKernel,
+ * RayCastKernel.cu:806-839). */
+phe_status phe_cast_closest(const phe_scene* scene, const phe_ray_in* rays, phe_ray_hit* hits, uint32_t n,
+                            void* stream);
+/* Closest hit, one ray per thread (replaces launchRayCastNoPersistenceKernel, RayCastKernel.cu:841-851). */
+phe_status phe_cast_closest_plain(const phe_scene* scene, const phe_ray_in* rays, phe_ray_hit* hits, uint32_t n,
+                                  void* stream);
+/* Any hit: inLight[i] = 1 when no triangle has tMin <= t < tMax, else 0 (replaces
+ * launchShadowRayCastKernel, RayCastKernel.cu:853-886; bool is one byte there too).
+ * `scatter` (optional, device) redirects result i to inLight[scatter[i]]. */
+phe_status phe_cast_any(const phe_scene* scene, const phe_ray_in* rays, uint8_t* inLight, uint32_t n,
+                        const uint32_t* scatter, void* stream);
+
+/* Primary rays (genPrimaryRaysKernel, RayCastKernel.cu:899-919) with a sub-pixel offset
+ * (jitterX, jitterY) added to the pixel location; order 0 = row-major, 1 = 8x8-tile-major
+ * (getRayIdx, CudaDeviceHelpers.cuh:49-62; needs resX and resY multiples of 8). */
+phe_status phe_gen_primary_rays(phe_ray_in* rays, const phe_camera_def* cam, uint32_t resX, uint32_t resY,
+                                float jitterX, float jitterY, int order, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PHE_GB300_H */

@@ -1,0 +1,276 @@
+"""Test infrastructure only: ctypes wrappers of the oracle (oracle/liboracle.so) and, where it was
+built from the reference sources, of the reference harness (oracle/_ref/libpheref.so).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may import this module; it is
+the checker, never the thing measured or shipped.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+ORACLE_SO = HERE / "liboracle.so"
+REF_SO = HERE / "_ref" / "libpheref.so"
+REFERENCE_ROOT = Path(os.environ.get("PHE_REFERENCE_ROOT", "/root/reference"))
+
+MODE_CPU = 0   # castRay accept rule: t < closest && tMin <= t <= tMax (BVHTraversal.hpp:176)
+MODE_GPU = 1   # rayCastKernel accept rule: tMin <= t < current (RayCastKernel.cu:361)
+
+NODE_DTYPE = np.dtype([("fData", "<f4", (12,)), ("iData", "<i4", (4,))])
+TRI_VERTS_DTYPE = np.dtype([("v0", "<f4", (4,)), ("v1", "<f4", (4,)), ("v2", "<f4", (4,))])
+RAY_IN_DTYPE = np.dtype([("origin", "<f4", (3,)), ("tMin", "<f4"), ("dir", "<f4", (3,)), ("tMax", "<f4")])
+RAY_HIT_DTYPE = np.dtype([("triangleIndex", "<u4"), ("t", "<f4"), ("u", "<f4"), ("v", "<f4")])
+LIGHT_DTYPE = np.dtype([("pos", "<f4", (3,)), ("radius", "<f4"), ("range", "<f4"), ("strength", "<f4", (3,)),
+                        ("staticShadows", "<i4")])
+
+
+class FrameParams(C.Structure):
+    _fields_ = [("resX", C.c_uint32), ("resY", C.c_uint32), ("cam", C.c_float * 12), ("jitter", C.c_float * 2),
+                ("camPos", C.c_float * 3), ("lights", C.c_void_p), ("numLights", C.c_uint32),
+                ("materials", C.c_void_p), ("seed", C.c_uint64), ("frame", C.c_uint32)]
+
+
+def build() -> None:
+    """Builds liboracle.so, and the reference harness when the reference sources are present."""
+    subprocess.run(["make", "-s", "-C", str(HERE), "oracle"], check=True)
+    if (REFERENCE_ROOT / "source").exists():
+        subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={REFERENCE_ROOT}"], check=True)
+
+
+_o = None
+_r = None
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data
+
+
+def lib():
+    global _o
+    if _o is None:
+        if not ORACLE_SO.exists():
+            build()
+        L = C.CDLL(str(ORACLE_SO))
+        V = C.c_void_p
+        L.oracle_cast_rays.argtypes = [V, V, V, C.c_uint32, C.c_int, V, V, C.c_int]
+        L.oracle_any_rays.argtypes = [V, V, V, C.c_uint32, V, C.c_int]
+        L.oracle_brute_closest.argtypes = [V, C.c_uint32, V, C.c_uint32, C.c_int, V]
+        L.oracle_brute_closest.restype = None
+        L.oracle_intersect_tri.argtypes = [V, V, V, V, V, V]
+        L.oracle_camera_def.argtypes = [V, V, V, C.c_float, C.c_float, C.c_float, V]
+        L.oracle_camera_def.restype = None
+        L.oracle_gen_primary.argtypes = [V, C.c_uint32, C.c_uint32, C.c_float, C.c_float, C.c_int, V]
+        L.oracle_gen_primary.restype = None
+        L.oracle_render_frame.argtypes = [V, V, V, C.POINTER(FrameParams), V, V, V, V, C.c_int]
+        L.oracle_taa.argtypes = [C.c_uint32, C.c_uint32, V, V, V, V, V, V, V]
+        L.oracle_taa.restype = None
+        L.oracle_halton_jitter.argtypes = [C.c_uint32, V]
+        L.oracle_halton_jitter.restype = None
+        L.oracle_sincos_2pi.argtypes = [C.c_float, V, V]
+        L.oracle_sincos_2pi.restype = None
+        L.oracle_pixel_stream.argtypes = [V, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32]
+        L.oracle_pixel_stream.restype = None
+        L.oracle_pcg_uniform.argtypes = [V]
+        L.oracle_pcg_uniform.restype = C.c_float
+        L.oracle_pcg_next.argtypes = [V]
+        L.oracle_pcg_next.restype = C.c_uint32
+        _o = L
+    return _o
+
+
+def ref_available() -> bool:
+    return REF_SO.exists()
+
+
+def ref():
+    global _r
+    if _r is None:
+        L = C.CDLL(str(REF_SO))
+        V = C.c_void_p
+        L.ref_build_sbvh.argtypes = [V, V, C.c_uint32]
+        L.ref_build_sbvh.restype = V
+        L.ref_bvh_sizes.argtypes = [V, V, V]
+        L.ref_bvh_copy.argtypes = [V, V, V, V]
+        L.ref_bvh_free.argtypes = [V]
+        L.ref_cast_rays.argtypes = [V, V, V, C.c_uint32, V, V, C.c_int]
+        L.ref_intersect_tri.argtypes = [V, V, V, V]
+        L.ref_camera_def.argtypes = [V, V, V, C.c_float, C.c_float, C.c_float, V]
+        _r = L
+    return _r
+
+
+def threads() -> int:
+    return os.cpu_count() or 1
+
+
+# ---------------------------------------------------------------------------------------------
+# oracle
+
+def cast_rays(nodes, verts, rays, mode=MODE_GPU, debug=False, nthreads=None):
+    n = len(rays)
+    hits = np.empty(n, RAY_HIT_DTYPE)
+    dbg = np.empty((n, 2), np.uint32) if debug else None
+    rc = lib().oracle_cast_rays(_p(nodes), _p(verts), _p(rays), n, mode, _p(hits), _p(dbg), nthreads or threads())
+    if rc:
+        raise RuntimeError(f"oracle: {rc} rays overflowed the traversal stack")
+    return (hits, dbg) if debug else hits
+
+
+def any_rays(nodes, verts, rays, nthreads=None):
+    n = len(rays)
+    out = np.empty(n, np.uint8)
+    rc = lib().oracle_any_rays(_p(nodes), _p(verts), _p(rays), n, _p(out), nthreads or threads())
+    if rc:
+        raise RuntimeError(f"oracle: {rc} rays overflowed the traversal stack")
+    return out
+
+
+def brute_closest(tris, rays, mode=MODE_GPU):
+    hits = np.empty(len(rays), RAY_HIT_DTYPE)
+    lib().oracle_brute_closest(_p(tris), len(tris), _p(rays), len(rays), mode, _p(hits))
+    return hits
+
+
+def intersect_tri(tri_verts_row, origin, direction):
+    tri = np.ascontiguousarray(tri_verts_row)
+    o = np.asarray(origin, np.float32)
+    d = np.asarray(direction, np.float32)
+    t, u, v = (C.c_float(), C.c_float(), C.c_float())
+    h = lib().oracle_intersect_tri(_p(tri), _p(o), _p(d), C.addressof(t), C.addressof(u), C.addressof(v))
+    return bool(h), t.value, u.value, v.value
+
+
+def camera_def(pos, direction, up, vfov_rad, res):
+    out = np.empty(12, np.float32)
+    a, b, c = (np.asarray(x, np.float32) for x in (pos, direction, up))
+    lib().oracle_camera_def(_p(a), _p(b), _p(c), vfov_rad, float(res[0]), float(res[1]), _p(out))
+    return out
+
+
+def gen_primary(cam12, res, jitter=(0.0, 0.0), order=0):
+    rays = np.empty(res[0] * res[1], RAY_IN_DTYPE)
+    cam = np.ascontiguousarray(cam12, np.float32)
+    lib().oracle_gen_primary(_p(cam), res[0], res[1], jitter[0], jitter[1], order, _p(rays))
+    return rays
+
+
+def halton_jitter(i):
+    out = np.empty(2, np.float32)
+    lib().oracle_halton_jitter(i, _p(out))
+    return out
+
+
+def sincos_2pi(r):
+    s, c = C.c_float(), C.c_float()
+    lib().oracle_sincos_2pi(r, C.addressof(s), C.addressof(c))
+    return s.value, c.value
+
+
+def render_frame(nodes, verts, slot_datas, materials, lights, cam12, res, jitter, cam_pos, seed, frame,
+                 primary_hits=None, nthreads=None):
+    fp = FrameParams()
+    fp.resX, fp.resY = res
+    fp.cam[:] = [float(x) for x in cam12]
+    fp.jitter[:] = [float(jitter[0]), float(jitter[1])]
+    fp.camPos[:] = [float(x) for x in cam_pos]
+    lights = np.ascontiguousarray(lights, LIGHT_DTYPE)
+    fp.lights = lights.ctypes.data
+    fp.numLights = len(lights)
+    fp.materials = materials.ctypes.data
+    fp.seed = seed
+    fp.frame = frame
+    color = np.empty((res[1], res[0], 4), np.float32)
+    rough = np.empty((res[1], res[0]), np.float32)
+    counts = np.zeros(4, np.uint64)
+    rc = lib().oracle_render_frame(_p(nodes), _p(verts), _p(slot_datas), C.byref(fp), _p(primary_hits), _p(color),
+                                   _p(rough), _p(counts), nthreads or threads())
+    if rc:
+        raise RuntimeError(f"oracle: {rc} rays overflowed the traversal stack")
+    return color, rough, counts
+
+
+def taa(cur, hist, roughness, velocity=None, prev_velocity=None):
+    H, W = cur.shape[:2]
+    out_c = np.empty_like(cur)
+    out_h = np.empty_like(cur)
+    lib().oracle_taa(W, H, _p(cur), _p(hist), _p(velocity), _p(prev_velocity), _p(roughness), _p(out_c), _p(out_h))
+    return out_c, out_h
+
+
+# ---------------------------------------------------------------------------------------------
+# reference harness (only where oracle/_ref was built from the reference sources)
+
+def ref_build_sbvh(tri_verts):
+    tv = np.ascontiguousarray(tri_verts, np.float32).reshape(-1, 9)
+    h = ref().ref_build_sbvh(_p(tv), None, tv.shape[0])
+    nn, ns = C.c_uint32(), C.c_uint32()
+    ref().ref_bvh_sizes(h, C.addressof(nn), C.addressof(ns))
+    nodes = np.empty(nn.value, NODE_DTYPE)
+    verts = np.empty(ns.value, TRI_VERTS_DTYPE)
+    s2t = np.empty(ns.value, np.uint32)
+    ref().ref_bvh_copy(h, _p(nodes), _p(verts), _p(s2t))
+    ref().ref_bvh_free(h)
+    return nodes, verts, s2t
+
+
+def ref_cast_rays(nodes, verts, rays, debug=False, nthreads=None):
+    n = len(rays)
+    hits = np.empty(n, RAY_HIT_DTYPE)
+    dbg = np.empty((n, 2), np.uint32) if debug else None
+    ref().ref_cast_rays(_p(nodes), _p(verts), _p(rays), n, _p(hits), _p(dbg), nthreads or threads())
+    return (hits, dbg) if debug else hits
+
+
+def ref_camera_def(pos, direction, up, vfov_rad, res):
+    out = np.empty(12, np.float32)
+    a, b, c = (np.asarray(x, np.float32) for x in (pos, direction, up))
+    ref().ref_camera_def(_p(a), _p(b), _p(c), vfov_rad, float(res[0]), float(res[1]), _p(out))
+    return out
+
+
+# ---------------------------------------------------------------------------------------------
+# comparison rule for closest-hit results
+
+def compare_closest(test_hits, oracle_hits, rays, slot_to_tri, verts, rel_t=1e-6, rel_tuv=1e-5):
+    """Compares closest-hit results under the parity rule: hit/miss identical; the original
+    triangle identical with t, u, v within `rel_tuv` relative; or a documented near-tie — a different
+    triangle whose t is within `rel_t` relative of the oracle's and which the oracle's own triangle
+    test confirms at exactly the reported (t, u, v). Returns a dict of counts and the failing indices."""
+    th, oh = test_hits, oracle_hits
+    miss_t = th["triangleIndex"] == 0xFFFFFFFF
+    miss_o = oh["triangleIndex"] == 0xFFFFFFFF
+    flip = np.nonzero(miss_t != miss_o)[0]
+    both = np.nonzero(~miss_t & ~miss_o)[0]
+    ot = slot_to_tri[th["triangleIndex"][both]]
+    oo = slot_to_tri[oh["triangleIndex"][both]]
+    same = both[ot == oo]
+    diff = both[ot != oo]
+    bad_vals = []
+    for k in ("t", "u", "v"):
+        a = th[k][same].astype(np.float64)
+        b = oh[k][same].astype(np.float64)
+        tol = rel_tuv * np.maximum(np.abs(b), 1.0 if k != "t" else np.abs(b))
+        bad = same[np.abs(a - b) > np.maximum(tol, 1e-30)]
+        bad_vals.append(bad)
+    bad_vals = np.unique(np.concatenate(bad_vals)) if bad_vals else np.array([], np.int64)
+    near_ties, bad_ties = [], []
+    for i in diff:
+        tt, to = float(th["t"][i]), float(oh["t"][i])
+        ok = abs(tt - to) <= rel_t * abs(to)
+        if ok:
+            r = rays[i]
+            hit, t, u, v = intersect_tri(verts[th["triangleIndex"][i]], r["origin"], r["dir"])
+            ok = hit and np.float32(t) == th["t"][i] and np.float32(u) == th["u"][i] and np.float32(v) == th["v"][i]
+        (near_ties if ok else bad_ties).append(int(i))
+    miss_vals = np.nonzero(miss_t & miss_o & (th["t"] != oh["t"]))[0]
+    return {
+        "rays": len(rays), "hits": int((~miss_o).sum()), "exact": int(len(same)) - len(bad_vals),
+        "near_ties": len(near_ties), "hit_miss_flips": flip.tolist(), "bad_values": bad_vals.tolist(),
+        "bad_ties": bad_ties, "miss_t_mismatch": miss_vals.tolist(),
+        "ok": len(flip) == 0 and len(bad_vals) == 0 and len(bad_ties) == 0 and len(miss_vals) == 0,
+    }

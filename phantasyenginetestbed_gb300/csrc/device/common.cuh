@@ -1,0 +1,149 @@
+// Device helpers shared by the kernels: explicitly rounded FP32 arithmetic in the reference's
+// operation order (sfz vector math, externals/sfzCore/include/sfz/math/Vector.inl), the device-side
+// scene layout, PCG32 and the sampling sine/cosine. Every float operation that decides a hit or a
+// sampled direction goes through __fadd_rn/__fsub_rn/__fmul_rn/__fdiv_rn/__fsqrt_rn, which the
+// compiler never fuses, so results equal the host's IEEE single-precision results bit for bit.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "phe_gb300.h"
+
+namespace phe_gb300 {
+
+// ------------------------------------------------------------------------------------------------
+// Device scene layout (built on upload from the reference arrays)
+//
+// nodes: 64 B per node, 4 x float4 — bytes 0..47 are the reference fData (child boxes), bytes
+//        48..63 are (child0, child1, count0, count1) with inner children as node indices >= 0 and
+//        leaf children as ~firstSlot (< 0); count is 0 for inner children.
+// tris:  48 B per slot, 3 x float4 — (p0.xyz, endMarker), (e1 = p1 - p0, 0), (e2 = p2 - p0, 0).
+//        e1 and e2 are the exact float subtractions Moller-Trumbore performs first, so storing them
+//        changes no result bit. endMarker is -1 on the last slot of each leaf, else 0.
+// ------------------------------------------------------------------------------------------------
+
+struct DeviceScene {
+	const float4* nodes;
+	const float4* tris;
+	const phe_triangle_data* datas;
+	const phe_material* materials;
+	uint32_t numNodes, numSlots, numMaterials, maxDepth;
+};
+
+// Traversal stack depth: leaves of a valid scene are at most 64 levels deep, and a node pushes at
+// most one entry per inner level, plus the sentinel.
+constexpr int kStackSize = 68;
+constexpr int32_t kSentinel = 0x7FFFFFFF;
+
+// Error bits written to the per-launch status word.
+constexpr uint32_t kErrStackOverflow = 1u;
+
+struct f3 { float x, y, z; };
+
+__device__ __forceinline__ f3 mk3(float x, float y, float z) { return f3{x, y, z}; }
+__device__ __forceinline__ f3 add3(f3 a, f3 b) { return mk3(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z)); }
+__device__ __forceinline__ f3 sub3(f3 a, f3 b) { return mk3(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z)); }
+__device__ __forceinline__ f3 mul3(f3 a, f3 b) { return mk3(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y), __fmul_rn(a.z, b.z)); }
+__device__ __forceinline__ f3 muls3(f3 a, float s) { return mk3(__fmul_rn(a.x, s), __fmul_rn(a.y, s), __fmul_rn(a.z, s)); }
+__device__ __forceinline__ f3 divs3(f3 a, float s) { return mk3(__fdiv_rn(a.x, s), __fdiv_rn(a.y, s), __fdiv_rn(a.z, s)); }
+__device__ __forceinline__ float dot3(f3 a, f3 b)
+{
+	return __fadd_rn(__fadd_rn(__fmul_rn(a.x, b.x), __fmul_rn(a.y, b.y)), __fmul_rn(a.z, b.z));
+}
+__device__ __forceinline__ f3 cross3(f3 a, f3 b)
+{
+	return mk3(__fsub_rn(__fmul_rn(a.y, b.z), __fmul_rn(a.z, b.y)), __fsub_rn(__fmul_rn(a.z, b.x), __fmul_rn(a.x, b.z)),
+	           __fsub_rn(__fmul_rn(a.x, b.y), __fmul_rn(a.y, b.x)));
+}
+__device__ __forceinline__ float length3(f3 a) { return __fsqrt_rn(dot3(a, a)); }
+__device__ __forceinline__ f3 normalize3(f3 a) { return divs3(a, length3(a)); }
+// std::min / std::max semantics (b < a ? b : a / a < b ? b : a), including NaN behaviour.
+__device__ __forceinline__ float stdmin(float a, float b) { return (b < a) ? b : a; }
+__device__ __forceinline__ float stdmax(float a, float b) { return (a < b) ? b : a; }
+
+// ------------------------------------------------------------------------------------------------
+// Moller-Trumbore with the reference's absolute determinant epsilon (Intersection.hpp:24-67,
+// RayCastKernel.cu:96-131), on a slot stored as (p0, e1, e2). Returns true on a hit.
+// ------------------------------------------------------------------------------------------------
+__device__ __forceinline__ bool intersect_tri(float4 a, float4 b, float4 c, f3 o, f3 d, float& t, float& u, float& v)
+{
+	const float EPS = 0.00001f;
+	f3 p0 = mk3(a.x, a.y, a.z), e1 = mk3(b.x, b.y, b.z), e2 = mk3(c.x, c.y, c.z);
+	f3 q = cross3(d, e2);
+	float det = dot3(e1, q);
+	if (-EPS < det && det < EPS) return false;
+	float f = __fdiv_rn(1.0f, det);
+	f3 s = sub3(o, p0);
+	float uu = __fmul_rn(f, dot3(s, q));
+	if (uu < 0.0f) return false;
+	f3 r = cross3(s, e1);
+	float vv = __fmul_rn(f, dot3(d, r));
+	if (vv < 0.0f || __fadd_rn(uu, vv) > 1.0f) return false;
+	t = __fmul_rn(f, dot3(e2, r));
+	u = uu;
+	v = vv;
+	return true;
+}
+
+// ------------------------------------------------------------------------------------------------
+// PCG32 (O'Neill 2014), identical to the host generator (host/pcg.hpp).
+// ------------------------------------------------------------------------------------------------
+struct DevPcg {
+	uint64_t state, inc;
+	__device__ __forceinline__ uint32_t next()
+	{
+		uint64_t old = state;
+		state = old * 6364136223846793005ull + inc;
+		uint32_t xorshifted = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+		uint32_t rot = (uint32_t)(old >> 59u);
+		return (xorshifted >> rot) | (xorshifted << ((32u - rot) & 31u));
+	}
+	__device__ __forceinline__ void seed(uint64_t initstate, uint64_t initseq)
+	{
+		state = 0u;
+		inc = (initseq << 1u) | 1u;
+		next();
+		state += initstate;
+		next();
+	}
+	__device__ __forceinline__ float uniform() { return __fmul_rn((float)(next() >> 8), 0x1.0p-24f); }
+};
+
+// Stream of pixel `pixel` for shading stage `stage` of frame `frame`.
+__device__ __forceinline__ void pixel_stream(DevPcg& r, uint64_t seed, uint32_t frame, uint32_t pixel, uint32_t stage)
+{
+	uint64_t initstate = seed ^ ((uint64_t)frame * 0x9E3779B97F4A7C15ull);
+	uint64_t initseq = ((uint64_t)pixel << 2) | (uint64_t)(stage & 3u);
+	r.seed(initstate, initseq);
+}
+
+// sin(2 pi r), cos(2 pi r) for r in [0, 1): exact quadrant reduction, then Taylor polynomials of
+// degree 9 (sine) and 10 (cosine) on [0, pi/4] evaluated in Horner form with single roundings.
+// Truncation error below 2e-9; the host restatement performs the same operations.
+__device__ __forceinline__ void sincos_2pi(float r, float& s, float& c)
+{
+	float q = __fmul_rn(r, 4.0f);
+	int k = (int)q;
+	k = k > 3 ? 3 : (k < 0 ? 0 : k);
+	float f = __fsub_rn(q, (float)k);
+	bool swap = f > 0.5f;
+	float g = swap ? __fsub_rn(1.0f, f) : f;
+	float x = __fmul_rn(g, 0x1.921fb6p+0f);
+	float x2 = __fmul_rn(x, x);
+	float sp = __fmul_rn(x, __fadd_rn(1.0f, __fmul_rn(x2, __fadd_rn(-0x1.555556p-3f, __fmul_rn(x2, __fadd_rn(0x1.111112p-7f,
+	                         __fmul_rn(x2, __fadd_rn(-0x1.a01a02p-13f, __fmul_rn(x2, 0x1.71de3ap-19f)))))))));
+	float cp = __fadd_rn(1.0f, __fmul_rn(x2, __fadd_rn(-0x1.0p-1f, __fmul_rn(x2, __fadd_rn(0x1.555556p-5f,
+	                         __fmul_rn(x2, __fadd_rn(-0x1.6c16c2p-10f, __fmul_rn(x2, __fsub_rn(0x1.a01a02p-16f,
+	                         __fmul_rn(x2, 0x1.27e4fcp-22f))))))))));
+	float sq = swap ? cp : sp;
+	float cq = swap ? sp : cp;
+	switch (k) {
+	case 0: s = sq; c = cq; break;
+	case 1: s = cq; c = -sq; break;
+	case 2: s = -sq; c = -cq; break;
+	default: s = -cq; c = sq; break;
+	}
+}
+
+} // namespace phe_gb300

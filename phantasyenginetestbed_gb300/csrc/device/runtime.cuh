@@ -1,0 +1,47 @@
+// Per-device runtime state of the library: device properties, kernel occupancy and the pool of
+// per-launch work counters used by the persistent kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../host/common.hpp"
+#include "common.cuh"
+
+struct phe_scene {
+	phe_gb300::DeviceScene dev;
+	void* allocation = nullptr;   // one cudaMalloc holding nodes, tris, datas, materials
+	uint64_t bytes = 0;
+	uint32_t* status = nullptr;   // device word: OR of error bits raised by kernels on this scene
+	int device = 0;
+};
+
+namespace phe_gb300 {
+
+struct DeviceInfo {
+	int device = -1;
+	int numSMs = 0;
+	int maxThreadsPerSM = 0;
+	uint32_t* counterPool = nullptr; // kCounterPool words
+};
+
+constexpr uint32_t kCounterPool = 4096;
+
+// Returns the runtime state of the current device, initialising it on first use.
+phe_status device_info(DeviceInfo** out);
+// A zeroed work counter for one persistent launch on `stream` (a memset is queued on the stream).
+phe_status acquire_counter(cudaStream_t stream, uint32_t** counter);
+
+inline phe_status cuda_fail(cudaError_t e, const char* what)
+{
+	return fail(e == cudaErrorMemoryAllocation ? PHE_ERR_OUT_OF_MEMORY : PHE_ERR_CUDA, "%s: %s", what,
+	            cudaGetErrorString(e));
+}
+
+#define PHE_CUDA_TRY(call, what)                                  \
+	do {                                                          \
+		cudaError_t e_ = (call);                                  \
+		if (e_ != cudaSuccess) return ::phe_gb300::cuda_fail(e_, what); \
+	} while (0)
+
+} // namespace phe_gb300

@@ -1,0 +1,232 @@
+// Scene upload: validates the reference-layout arrays on the host, re-lays them out into the
+// traversal layout (device/common.cuh) and uploads them in one allocation. Replaces setStaticScene
+// (cuda_ray_tracer/CudaTracerRenderer.cpp:251-315), which uploaded the arrays unchanged into linear
+// texture objects.
+
+#include <atomic>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "runtime.cuh"
+
+namespace phe_gb300 {
+
+static std::mutex g_devMutex;
+static DeviceInfo g_devices[64];
+static std::atomic<uint32_t> g_counterNext{0};
+
+phe_status device_info(DeviceInfo** out)
+{
+	int dev = 0;
+	cudaError_t e = cudaGetDevice(&dev);
+	if (e != cudaSuccess) return fail(PHE_ERR_NO_DEVICE, "no CUDA device: %s", cudaGetErrorString(e));
+	if (dev < 0 || dev >= 64) return fail(PHE_ERR_NO_DEVICE, "device ordinal %d out of range", dev);
+	std::lock_guard<std::mutex> lock(g_devMutex);
+	DeviceInfo& d = g_devices[dev];
+	if (d.device < 0) {
+		cudaDeviceProp prop;
+		PHE_CUDA_TRY(cudaGetDeviceProperties(&prop, dev), "cudaGetDeviceProperties");
+		uint32_t* pool = nullptr;
+		PHE_CUDA_TRY(cudaMalloc(&pool, sizeof(uint32_t) * kCounterPool), "cudaMalloc(counter pool)");
+		PHE_CUDA_TRY(cudaMemset(pool, 0, sizeof(uint32_t) * kCounterPool), "cudaMemset(counter pool)");
+		d.numSMs = prop.multiProcessorCount;
+		d.maxThreadsPerSM = prop.maxThreadsPerMultiProcessor;
+		d.counterPool = pool;
+		d.device = dev;
+	}
+	*out = &d;
+	return PHE_OK;
+}
+
+phe_status acquire_counter(cudaStream_t stream, uint32_t** counter)
+{
+	DeviceInfo* d = nullptr;
+	phe_status s = device_info(&d);
+	if (s) return s;
+	uint32_t slot = g_counterNext.fetch_add(1) % kCounterPool;
+	uint32_t* c = d->counterPool + slot;
+	PHE_CUDA_TRY(cudaMemsetAsync(c, 0, sizeof(uint32_t), stream), "cudaMemsetAsync(counter)");
+	*counter = c;
+	return PHE_OK;
+}
+
+} // namespace phe_gb300
+
+using namespace phe_gb300;
+
+static_assert(sizeof(phe_bvh_node) == 64, "BVHNode is 64 bytes");
+static_assert(sizeof(phe_triangle_vertices) == 48, "TriangleVertices is 48 bytes");
+static_assert(sizeof(phe_triangle_data) == 64, "TriangleData is 64 bytes");
+static_assert(sizeof(phe_ray_in) == 32, "RayIn is 32 bytes");
+static_assert(sizeof(phe_ray_hit) == 16, "RayHit is 16 bytes");
+
+static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+extern "C" phe_status phe_scene_create(const phe_bvh_node* nodes, uint32_t numNodes, const phe_triangle_vertices* verts,
+                                       const phe_triangle_data* datas, uint32_t numSlots, const phe_material* materials,
+                                       uint32_t numMaterials, int where, phe_scene** out)
+{
+	if (!out) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_scene_create: out is null");
+	*out = nullptr;
+	if (!nodes || !verts || numNodes == 0 || numSlots == 0)
+		return fail(PHE_ERR_INVALID_ARGUMENT, "phe_scene_create: empty scene");
+	if (where != PHE_PTR_HOST && where != PHE_PTR_DEVICE)
+		return fail(PHE_ERR_INVALID_ARGUMENT, "phe_scene_create: where must be PHE_PTR_HOST or PHE_PTR_DEVICE");
+	if (numNodes >= (uint32_t)kSentinel || numSlots >= 0x7FFFFFFFu)
+		return fail(PHE_ERR_TOO_LARGE, "phe_scene_create: more than 2^31-2 nodes or slots");
+	DeviceInfo* dinfo = nullptr;
+	phe_status s = device_info(&dinfo);
+	if (s) return s;
+
+	// Host copies of the reference arrays (device input is read back once).
+	std::vector<phe_bvh_node> hn;
+	std::vector<phe_triangle_vertices> hv;
+	std::vector<phe_triangle_data> hd;
+	std::vector<phe_material> hm;
+	try {
+		hn.resize(numNodes);
+		hv.resize(numSlots);
+		if (datas) hd.resize(numSlots);
+		if (materials && numMaterials) hm.resize(numMaterials);
+	} catch (const std::bad_alloc&) {
+		return fail(PHE_ERR_OUT_OF_MEMORY, "phe_scene_create: host staging allocation failed");
+	}
+	cudaMemcpyKind kind = where == PHE_PTR_HOST ? cudaMemcpyHostToHost : cudaMemcpyDeviceToHost;
+	PHE_CUDA_TRY(cudaMemcpy(hn.data(), nodes, sizeof(phe_bvh_node) * (size_t)numNodes, kind), "copy nodes");
+	PHE_CUDA_TRY(cudaMemcpy(hv.data(), verts, sizeof(phe_triangle_vertices) * (size_t)numSlots, kind), "copy verts");
+	if (datas) PHE_CUDA_TRY(cudaMemcpy(hd.data(), datas, sizeof(phe_triangle_data) * (size_t)numSlots, kind), "copy datas");
+	if (!hm.empty()) PHE_CUDA_TRY(cudaMemcpy(hm.data(), materials, sizeof(phe_material) * (size_t)numMaterials, kind), "copy materials");
+
+	uint32_t maxDepth = 0;
+	s = phe_bvh_validate(hn.data(), numNodes, numSlots, &maxDepth);
+	if (s) return s;
+	if (!hd.empty() && !hm.empty())
+		for (uint32_t i = 0; i < numSlots; i++)
+			if (hd[i].materialIndex >= numMaterials)
+				return fail(PHE_ERR_INVALID_SCENE, "slot %u: materialIndex %u >= %u materials", i, hd[i].materialIndex,
+				            numMaterials);
+
+	// Traversal layout: child indices normalised (leaf = ~first), leaf end markers rewritten from
+	// the counts so that leaf loops always stop inside the slot array, triangles as (p0, e1, e2).
+	std::vector<float4> dn((size_t)numNodes * 4);
+	std::vector<float4> dt((size_t)numSlots * 3);
+	std::vector<uint8_t> used(numSlots, 0);
+	for (uint32_t i = 0; i < numNodes; i++) {
+		const phe_bvh_node& n = hn[i];
+		float4* o = &dn[(size_t)i * 4];
+		o[0] = make_float4(n.fData[0], n.fData[1], n.fData[2], n.fData[3]);
+		o[1] = make_float4(n.fData[4], n.fData[5], n.fData[6], n.fData[7]);
+		o[2] = make_float4(n.fData[8], n.fData[9], n.fData[10], n.fData[11]);
+		int32_t idx[2], cnt[2];
+		for (int c = 0; c < 2; c++) {
+			int32_t raw = n.iData[c];
+			cnt[c] = n.iData[2 + c];
+			if (cnt[c] > 0) {
+				int32_t first = raw < 0 ? ~raw : raw;
+				idx[c] = ~first;
+			} else {
+				idx[c] = raw;
+				cnt[c] = 0;
+			}
+		}
+		int4 iv = make_int4(idx[0], idx[1], cnt[0], cnt[1]);
+		std::memcpy(&o[3], &iv, sizeof(iv));
+	}
+	for (uint32_t i = 0; i < numSlots; i++) {
+		const phe_triangle_vertices& t = hv[i];
+		float e1x = t.v1[0] - t.v0[0], e1y = t.v1[1] - t.v0[1], e1z = t.v1[2] - t.v0[2];
+		float e2x = t.v2[0] - t.v0[0], e2y = t.v2[1] - t.v0[1], e2z = t.v2[2] - t.v0[2];
+		dt[(size_t)i * 3 + 0] = make_float4(t.v0[0], t.v0[1], t.v0[2], 0.0f);
+		dt[(size_t)i * 3 + 1] = make_float4(e1x, e1y, e1z, 0.0f);
+		dt[(size_t)i * 3 + 2] = make_float4(e2x, e2y, e2z, 0.0f);
+	}
+	// End markers from the leaf ranges of the reachable tree (phe_bvh_validate checked the ranges).
+	{
+		std::vector<uint32_t> stack{0};
+		while (!stack.empty()) {
+			uint32_t ni = stack.back();
+			stack.pop_back();
+			const int32_t* iv = reinterpret_cast<const int32_t*>(&dn[(size_t)ni * 4 + 3]);
+			for (int c = 0; c < 2; c++) {
+				if (iv[2 + c] > 0) {
+					uint32_t first = (uint32_t)~iv[c];
+					uint32_t last = first + (uint32_t)iv[2 + c] - 1;
+					for (uint32_t k = first; k <= last; k++) {
+						if (used[k])
+							return fail(PHE_ERR_INVALID_SCENE, "slot %u belongs to two leaves", k);
+						used[k] = 1;
+					}
+					dt[(size_t)last * 3].w = -1.0f;
+				} else {
+					stack.push_back((uint32_t)iv[c]);
+				}
+			}
+		}
+	}
+
+	size_t nodeBytes = align256(dn.size() * sizeof(float4));
+	size_t triBytes = align256(dt.size() * sizeof(float4));
+	size_t dataBytes = align256(hd.size() * sizeof(phe_triangle_data));
+	size_t matBytes = align256(hm.size() * sizeof(phe_material));
+	size_t statusBytes = 256;
+	size_t total = nodeBytes + triBytes + dataBytes + matBytes + statusBytes;
+	char* base = nullptr;
+	cudaError_t e = cudaMalloc(&base, total);
+	if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(scene)");
+	auto cleanup = [&](phe_status st) { cudaFree(base); return st; };
+	char* p = base;
+	float4* dNodes = (float4*)p; p += nodeBytes;
+	float4* dTris = (float4*)p; p += triBytes;
+	phe_triangle_data* dDatas = hd.empty() ? nullptr : (phe_triangle_data*)p; p += dataBytes;
+	phe_material* dMats = hm.empty() ? nullptr : (phe_material*)p; p += matBytes;
+	uint32_t* dStatus = (uint32_t*)p;
+	if ((e = cudaMemcpy(dNodes, dn.data(), dn.size() * sizeof(float4), cudaMemcpyHostToDevice)) != cudaSuccess)
+		return cleanup(cuda_fail(e, "upload nodes"));
+	if ((e = cudaMemcpy(dTris, dt.data(), dt.size() * sizeof(float4), cudaMemcpyHostToDevice)) != cudaSuccess)
+		return cleanup(cuda_fail(e, "upload triangles"));
+	if (dDatas && (e = cudaMemcpy(dDatas, hd.data(), hd.size() * sizeof(phe_triangle_data), cudaMemcpyHostToDevice)) != cudaSuccess)
+		return cleanup(cuda_fail(e, "upload triangle data"));
+	if (dMats && (e = cudaMemcpy(dMats, hm.data(), hm.size() * sizeof(phe_material), cudaMemcpyHostToDevice)) != cudaSuccess)
+		return cleanup(cuda_fail(e, "upload materials"));
+	if ((e = cudaMemset(dStatus, 0, statusBytes)) != cudaSuccess) return cleanup(cuda_fail(e, "clear status"));
+
+	phe_scene* sc = new phe_scene();
+	sc->dev.nodes = dNodes;
+	sc->dev.tris = dTris;
+	sc->dev.datas = dDatas;
+	sc->dev.materials = dMats;
+	sc->dev.numNodes = numNodes;
+	sc->dev.numSlots = numSlots;
+	sc->dev.numMaterials = (uint32_t)hm.size();
+	sc->dev.maxDepth = maxDepth;
+	sc->allocation = base;
+	sc->bytes = total;
+	sc->status = dStatus;
+	sc->device = dinfo->device;
+	*out = sc;
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_scene_destroy(phe_scene* scene)
+{
+	if (!scene) return PHE_OK;
+	cudaError_t e = cudaFree(scene->allocation);
+	delete scene;
+	if (e != cudaSuccess) return cuda_fail(e, "cudaFree(scene)");
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_scene_device_bytes(const phe_scene* scene, uint64_t* bytes)
+{
+	if (!scene || !bytes) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_scene_device_bytes: null argument");
+	*bytes = scene->bytes;
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_scene_status(const phe_scene* scene, uint32_t* bits)
+{
+	if (!scene || !bits) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_scene_status: null argument");
+	PHE_CUDA_TRY(cudaMemcpy(bits, scene->status, sizeof(uint32_t), cudaMemcpyDeviceToHost), "read scene status");
+	return PHE_OK;
+}

@@ -1,0 +1,169 @@
+// BVH traversal for one ray per thread: the while-while loop of Aila & Laine ("Understanding the
+// Efficiency of Ray Traversal on GPUs", HPG 2009) as the reference's kernels use it
+// (RayCastKernel.cu:286-383): inner nodes are traversed until every active lane of the warp holds a
+// postponed leaf, then leaves are intersected. Closest hit visits the nearer child first; any hit
+// stops at the first accepted triangle.
+//
+// Child boxes are tested with the reference CPU arithmetic (Intersection.hpp:77-90,
+// BVHTraversal.hpp:152-156): t = (bound - origin) * (1 / dir) per plane, the std::min/std::max
+// reduction, and the visit rule hit && tOut > tMin && tIn < tCurrentMax. Box culling is therefore
+// the same decision the CPU oracle makes for the same current best t. For rays whose 1/dir is finite
+// no NaN can appear and fminf/fmaxf give the same values; other rays use the exact std::min/max
+// selects (a NaN in the x lane culls a box on the CPU, a NaN in y or z does not).
+#pragma once
+
+#include "common.cuh"
+
+namespace phe_gb300 {
+
+struct RayState {
+	f3 o, d, inv;
+	float tMin, tMax;
+	bool safe;
+};
+
+__device__ __forceinline__ RayState load_ray(const phe_ray_in* __restrict__ rays, uint32_t i)
+{
+	const float4* p = reinterpret_cast<const float4*>(rays + i);
+	float4 a = __ldg(p), b = __ldg(p + 1);
+	RayState r;
+	r.o = mk3(a.x, a.y, a.z);
+	r.tMin = a.w;
+	r.d = mk3(b.x, b.y, b.z);
+	r.tMax = b.w;
+	r.inv = mk3(__frcp_rn(b.x), __frcp_rn(b.y), __frcp_rn(b.z));
+	r.safe = isfinite(a.x) && isfinite(a.y) && isfinite(a.z) && isfinite(b.x) && isfinite(b.y) && isfinite(b.z) &&
+	         isfinite(r.inv.x) && isfinite(r.inv.y) && isfinite(r.inv.z);
+	return r;
+}
+
+template <bool SAFE>
+__device__ __forceinline__ float mn(float a, float b) { return SAFE ? fminf(a, b) : stdmin(a, b); }
+template <bool SAFE>
+__device__ __forceinline__ float mx(float a, float b) { return SAFE ? fmaxf(a, b) : stdmax(a, b); }
+
+template <bool SAFE>
+__device__ __forceinline__ bool visit_box(const RayState& r, float lx, float ly, float lz, float hx, float hy, float hz,
+                                          float tCur, float& tIn)
+{
+	float t1x = __fmul_rn(__fsub_rn(lx, r.o.x), r.inv.x);
+	float t1y = __fmul_rn(__fsub_rn(ly, r.o.y), r.inv.y);
+	float t1z = __fmul_rn(__fsub_rn(lz, r.o.z), r.inv.z);
+	float t2x = __fmul_rn(__fsub_rn(hx, r.o.x), r.inv.x);
+	float t2y = __fmul_rn(__fsub_rn(hy, r.o.y), r.inv.y);
+	float t2z = __fmul_rn(__fsub_rn(hz, r.o.z), r.inv.z);
+	float tmin = mx<SAFE>(mx<SAFE>(mn<SAFE>(t1x, t2x), mn<SAFE>(t1y, t2y)), mn<SAFE>(t1z, t2z));
+	float tmax = mn<SAFE>(mn<SAFE>(mx<SAFE>(t1x, t2x), mx<SAFE>(t1y, t2y)), mx<SAFE>(t1z, t2z));
+	tIn = tmin;
+	return tmax >= tmin && tmax > r.tMin && tmin < tCur;
+}
+
+struct HitRecord {
+	uint32_t slot;
+	float t, u, v;
+};
+
+// Traverses the scene for one ray. ANY = true stops at the first triangle with tMin <= t < tMax.
+// Returns the error bits (0, or kErrStackOverflow when the stack would overflow).
+template <bool SAFE, bool ANY>
+__device__ __forceinline__ uint32_t traverse(const float4* __restrict__ nodes, const float4* __restrict__ tris,
+                                             const RayState& r, HitRecord& hit)
+{
+	int32_t stack[kStackSize];
+	int sp = 0;
+	stack[0] = kSentinel;
+	int32_t nodeAddr = 0;
+	int32_t leafAddr = 0;
+	uint32_t err = 0;
+
+	while (nodeAddr != kSentinel) {
+		while (nodeAddr >= 0 && nodeAddr != kSentinel) {
+			const float4* np = nodes + 4 * (size_t)nodeAddr;
+			float4 b0 = __ldg(np), b1 = __ldg(np + 1), b2 = __ldg(np + 2);
+			int4 ix = __ldg(reinterpret_cast<const int4*>(np + 3));
+			float tIn0, tIn1;
+			bool v0 = visit_box<SAFE>(r, b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, hit.t, tIn0);
+			bool v1 = visit_box<SAFE>(r, b1.z, b1.w, b2.x, b2.y, b2.z, b2.w, hit.t, tIn1);
+			if (!v0 && !v1) {
+				nodeAddr = stack[sp--];
+			} else {
+				nodeAddr = v0 ? ix.x : ix.y;
+				if (v0 && v1) {
+					int32_t other = ix.y;
+					if (!ANY && tIn1 < tIn0) {
+						other = ix.x;
+						nodeAddr = ix.y;
+					}
+					if (sp >= kStackSize - 1) {
+						err |= kErrStackOverflow;
+						nodeAddr = kSentinel;
+						leafAddr = 0;
+						break;
+					}
+					stack[++sp] = other;
+				}
+			}
+			if (nodeAddr < 0 && leafAddr >= 0) {
+				leafAddr = nodeAddr;
+				nodeAddr = stack[sp--];
+			}
+			if (!__any_sync(__activemask(), leafAddr >= 0)) break;
+		}
+
+		while (leafAddr < 0) {
+			int32_t slot = ~leafAddr;
+			for (;;) {
+				const float4* tp = tris + 3 * (size_t)slot;
+				float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+				float t, u, v;
+				if (intersect_tri(a, b, c, r.o, r.d, t, u, v) && r.tMin <= t && t < hit.t) {
+					hit.slot = (uint32_t)slot;
+					hit.t = t;
+					hit.u = u;
+					hit.v = v;
+					if (ANY) {
+						nodeAddr = kSentinel;
+						leafAddr = 0;
+						break;
+					}
+				}
+				if (a.w < 0.0f) break;
+				slot++;
+			}
+			if (ANY && nodeAddr == kSentinel && leafAddr == 0) break;
+			leafAddr = nodeAddr;
+			if (nodeAddr < 0) nodeAddr = stack[sp--];
+		}
+	}
+	return err;
+}
+
+// Initial record: no hit, current best = std::min(tMax, FLT_MAX) (the CPU castRay starts from
+// FLT_MAX; RayCastKernel.cu:267 starts from maxDist).
+__device__ __forceinline__ HitRecord empty_hit(const RayState& r)
+{
+	HitRecord h;
+	h.slot = ~0u;
+	h.t = stdmin(r.tMax, 3.402823466e+38f);
+	h.u = 0.0f;
+	h.v = 0.0f;
+	return h;
+}
+
+template <bool ANY>
+__device__ __forceinline__ uint32_t trace(const float4* __restrict__ nodes, const float4* __restrict__ tris,
+                                          const RayState& r, HitRecord& hit)
+{
+	if (r.safe) return traverse<true, ANY>(nodes, tris, r, hit);
+	return traverse<false, ANY>(nodes, tris, r, hit);
+}
+
+__device__ __forceinline__ void store_hit(phe_ray_hit* __restrict__ hits, uint32_t i, const RayState& r, const HitRecord& h)
+{
+	float4 o;
+	if (h.slot != ~0u) o = make_float4(__uint_as_float(h.slot), h.t, h.u, h.v);
+	else o = make_float4(__uint_as_float(~0u), r.tMax, 0.0f, 0.0f);
+	reinterpret_cast<float4*>(hits)[i] = o;
+}
+
+} // namespace phe_gb300

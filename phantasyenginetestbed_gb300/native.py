@@ -1,0 +1,137 @@
+"""ctypes binding of libphe_gb300.so (the C ABI declared in include/phe_gb300.h).
+
+The library is the product: there is no Python or CPU fallback for any GPU entry point. Loading fails
+loudly when the library has not been built (``python -m phantasyenginetestbed_gb300.build``).
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+LIB_PATH = Path(__file__).resolve().parent / "libphe_gb300.so"
+
+# Status codes (include/phe_gb300.h).
+PHE_OK = 0
+PHE_ERR_INVALID_ARGUMENT = 1
+PHE_ERR_INVALID_SCENE = 2
+PHE_ERR_CUDA = 3
+PHE_ERR_OUT_OF_MEMORY = 4
+PHE_ERR_BUDGET = 5
+PHE_ERR_TIMEOUT = 6
+PHE_ERR_NOT_FOUND = 7
+PHE_ERR_TOO_LARGE = 8
+PHE_ERR_NOT_READY = 9
+PHE_ERR_NO_DEVICE = 10
+
+PTR_HOST = 0
+PTR_DEVICE = 1
+
+# numpy views of the reference layouts
+NODE_DTYPE = np.dtype([("fData", "<f4", (12,)), ("iData", "<i4", (4,))])            # phe::BVHNode, 64 B
+TRI_VERTS_DTYPE = np.dtype([("v0", "<f4", (4,)), ("v1", "<f4", (4,)), ("v2", "<f4", (4,))])  # 48 B
+TRI_DATA_DTYPE = np.dtype([("n0", "<f4", (3,)), ("n1", "<f4", (3,)), ("n2", "<f4", (3,)),
+                           ("uv0", "<f4", (2,)), ("uv1", "<f4", (2,)), ("uv2", "<f4", (2,)),
+                           ("materialIndex", "<u4")])                                 # 64 B
+RAY_IN_DTYPE = np.dtype([("origin", "<f4", (3,)), ("tMin", "<f4"), ("dir", "<f4", (3,)), ("tMax", "<f4")])  # 32 B
+RAY_HIT_DTYPE = np.dtype([("triangleIndex", "<u4"), ("t", "<f4"), ("u", "<f4"), ("v", "<f4")])  # 16 B
+MATERIAL_DTYPE = np.dtype([("albedo", "<f4", (4,)), ("roughness", "<f4"), ("metallic", "<f4"), ("pad", "<f4", (2,))])
+LIGHT_DTYPE = np.dtype([("pos", "<f4", (3,)), ("radius", "<f4"), ("range", "<f4"), ("strength", "<f4", (3,)),
+                        ("staticShadows", "<i4")])
+assert NODE_DTYPE.itemsize == 64 and TRI_VERTS_DTYPE.itemsize == 48 and TRI_DATA_DTYPE.itemsize == 64
+assert RAY_IN_DTYPE.itemsize == 32 and RAY_HIT_DTYPE.itemsize == 16 and MATERIAL_DTYPE.itemsize == 32
+assert LIGHT_DTYPE.itemsize == 36
+
+
+class CameraDef(C.Structure):
+    _fields_ = [("origin", C.c_float * 3), ("dir", C.c_float * 3), ("dX", C.c_float * 3), ("dY", C.c_float * 3)]
+
+
+class SceneRecipe(C.Structure):
+    _fields_ = [("gridCells", C.c_uint32), ("numCubes", C.c_uint32), ("rotatedCubes", C.c_int32),
+                ("pad", C.c_uint32), ("seed", C.c_uint64)]
+
+
+class SbvhParams(C.Structure):
+    _fields_ = [("splitAlpha", C.c_float), ("maxDepth", C.c_int32), ("maxSpatialDepth", C.c_int32),
+                ("numThreads", C.c_int32)]
+
+
+class PheError(RuntimeError):
+    def __init__(self, status: int, where: str, text: str):
+        super().__init__(f"{where}: status {status}: {text}")
+        self.status = status
+
+
+_VP = C.c_void_p
+_U32 = C.c_uint32
+_I32 = C.c_int
+_F = C.c_float
+_PF = C.POINTER(C.c_float)
+
+# name -> (restype, argtypes); every function declared in include/phe_gb300.h
+SIGNATURES: dict[str, tuple] = {
+    "phe_version": (C.c_int, []),
+    "phe_last_error": (C.c_char_p, []),
+    "phe_scene_recipe_triangles": (C.c_uint64, [C.POINTER(SceneRecipe)]),
+    "phe_scene_generate": (_I32, [C.POINTER(SceneRecipe), _VP, _VP, _VP]),
+    "phe_sbvh_default_params": (None, [C.POINTER(SbvhParams)]),
+    "phe_sbvh_build": (_I32, [_VP, _U32, C.POINTER(SbvhParams), C.POINTER(_VP)]),
+    "phe_host_bvh_info": (_I32, [_VP, C.POINTER(_U32), C.POINTER(_U32), C.POINTER(_U32)]),
+    "phe_host_bvh_copy": (_I32, [_VP, _VP, _VP, _VP]),
+    "phe_host_bvh_free": (None, [_VP]),
+    "phe_bvh_validate": (_I32, [_VP, _U32, _U32, C.POINTER(_U32)]),
+    "phe_bvh_cache_write": (_I32, [C.c_char_p, _VP, _U32, _VP, _VP, _U32]),
+    "phe_bvh_cache_sizes": (_I32, [C.c_char_p, C.POINTER(_U32), C.POINTER(_U32)]),
+    "phe_bvh_cache_read": (_I32, [C.c_char_p, _VP, _U32, _VP, _VP, _U32]),
+    "phe_generate_camera_def": (None, [_PF, _PF, _PF, _F, _F, _F, C.POINTER(CameraDef)]),
+    "phe_halton_jitter": (None, [_U32, _PF]),
+    "phe_scene_create": (_I32, [_VP, _U32, _VP, _VP, _U32, _VP, _U32, _I32, C.POINTER(_VP)]),
+    "phe_scene_destroy": (_I32, [_VP]),
+    "phe_scene_device_bytes": (_I32, [_VP, C.POINTER(C.c_uint64)]),
+    "phe_cast_closest": (_I32, [_VP, _VP, _VP, _U32, _VP]),
+    "phe_cast_closest_plain": (_I32, [_VP, _VP, _VP, _U32, _VP]),
+    "phe_cast_any": (_I32, [_VP, _VP, _VP, _U32, _VP, _VP]),
+    "phe_gen_primary_rays": (_I32, [_VP, C.POINTER(CameraDef), _U32, _U32, _F, _F, _I32, _VP]),
+}
+
+_lib: C.CDLL | None = None
+
+
+def lib() -> C.CDLL:
+    """Loads libphe_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -m phantasyenginetestbed_gb300.build`")
+        L = C.CDLL(str(LIB_PATH))
+        for name, (res, args) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def check(status: int, where: str) -> None:
+    if status != PHE_OK:
+        raise PheError(status, where, lib().phe_last_error().decode(errors="replace"))
+
+
+def ptr(a) -> int | None:
+    """Raw address of a numpy array or torch tensor (None for None)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    if isinstance(a, int):
+        return a
+    raise TypeError(f"cannot take the address of {type(a)}")
+
+
+def fvec(v) -> C.Array:
+    a = (C.c_float * 3)(*[float(x) for x in v])
+    return a

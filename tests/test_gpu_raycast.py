@@ -1,0 +1,204 @@
+"""GPU parity of the ray-cast kernels against the oracle and the reference's golden fixtures.
+
+Rule (closest hit): hit/miss identical, the original triangle identical with t/u/v within 1e-5
+relative (bit-exact in practice), or a documented near-tie (|dt|/t <= 1e-6, confirmed by the oracle's
+triangle test). Any hit: identical, bit for bit.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import phantasyenginetestbed_gb300 as P
+from oracle import oracle as O
+from tests.helpers import (C1_CAM, built_scene, cam_struct, device_empty, from_device, golden_scene, load_golden,
+                           random_rays, to_device)
+
+pytestmark = pytest.mark.gpu
+
+NEAR_TIE_BUDGET = 1e-4  # fraction of rays allowed to be documented near-ties
+
+
+def _gpu_closest(scene, rays, kind="persistent"):
+    import torch
+    d_rays = to_device(rays)
+    d_hits = device_empty(len(rays), P.RAY_HIT_DTYPE)
+    fn = P.cast_closest if kind == "persistent" else P.cast_closest_plain
+    fn(scene, d_rays, d_hits, len(rays))
+    torch.cuda.synchronize()
+    return from_device(d_hits, P.RAY_HIT_DTYPE)
+
+
+def _gpu_any(scene, rays):
+    import torch
+    d_rays = to_device(rays)
+    d_out = device_empty(len(rays), np.uint8)
+    P.cast_any(scene, d_rays, d_out, len(rays))
+    torch.cuda.synchronize()
+    return from_device(d_out, np.uint8)
+
+
+def _check(report, n):
+    assert report["ok"], {k: (v[:20] if isinstance(v, list) else v) for k, v in report.items()}
+    assert report["near_ties"] <= max(2, NEAR_TIE_BUDGET * n), report["near_ties"]
+
+
+@pytest.mark.parametrize("kind", ["persistent", "plain"])
+def test_closest_matches_reference_fixture_c1(kind):
+    """The reference's own castRay output over the reference builder's SBVH (fixture), every 16th of
+    the 512x512 primary rays plus 4096 incoherent rays."""
+    g = load_golden("ref_c1.npz")
+    s, nodes, verts, s2t = golden_scene("ref_c1.npz")
+    scene = P.Scene(nodes, verts)
+    rays = O.gen_primary(g["cam"], C1_CAM["res"])[::16].copy()
+    gpu = _gpu_closest(scene, rays, kind)
+    ref = g["hits"].copy()
+    miss = ref["triangleIndex"] == 0xFFFFFFFF
+    ref["t"][miss] = rays["tMax"][miss]   # the GPU miss convention (t = tMax, u = v = 0)
+    ref["u"][miss] = 0
+    ref["v"][miss] = 0
+    _check(O.compare_closest(gpu, ref, rays, s2t, verts), len(rays))
+    inc = g["inc_rays"]
+    gpu = _gpu_closest(scene, inc, kind)
+    ref = g["inc_hits"].copy()
+    miss = ref["triangleIndex"] == 0xFFFFFFFF
+    ref["t"][miss] = inc["tMax"][miss]
+    ref["u"][miss] = 0
+    ref["v"][miss] = 0
+    _check(O.compare_closest(gpu, ref, inc, s2t, verts), len(inc))
+
+
+def test_small_fixture_every_ray_and_primary_generation():
+    g = load_golden("ref_small.npz")
+    s, nodes, verts, s2t = golden_scene("ref_small.npz")
+    scene = P.Scene(nodes, verts)
+    import torch
+    for order in (0, 1):
+        d_rays = device_empty(64 * 64, P.RAY_IN_DTYPE)
+        P.gen_primary_rays(d_rays, cam_struct(g["cam"]), (64, 64), order=order)
+        torch.cuda.synchronize()
+        gpu_rays = from_device(d_rays, P.RAY_IN_DTYPE)
+        want = O.gen_primary(g["cam"], (64, 64), order=order)
+        assert np.array_equal(gpu_rays.view(np.uint8), want.view(np.uint8))
+    rays = O.gen_primary(g["cam"], (64, 64))
+    gpu = _gpu_closest(scene, rays)
+    orc = O.cast_rays(nodes, verts, rays, mode=O.MODE_GPU)
+    _check(O.compare_closest(gpu, orc, rays, s2t, verts), len(rays))
+
+
+@pytest.mark.parametrize("name", ["c1_64_100", "c2_256_2000"])
+def test_closest_and_any_full_size_vs_oracle(name):
+    """Every primary ray of the configuration (512x512 for the plain scene, 1920x1080 for the
+    wavefront scene), incoherent bounce-like rays, and shadow rays, over the project builder's SBVH."""
+    s, b = built_scene(name)
+    scene = P.Scene(b.nodes, b.verts)
+    if name == "c1_64_100":
+        cam = O.camera_def(C1_CAM["pos"], C1_CAM["dir"], C1_CAM["up"], math.radians(60), (512, 512))
+        res = (512, 512)
+    else:
+        k = s.scale
+        cam = O.camera_def((0.5 * k, -0.3 * k, 0.6 * k), C1_CAM["dir"], C1_CAM["up"], math.radians(60), (1920, 1080))
+        res = (1920, 1080)
+    rays = O.gen_primary(cam, res, jitter=(0.25, -0.125))
+    gpu = _gpu_closest(scene, rays)
+    orc = O.cast_rays(b.nodes, b.verts, rays, mode=O.MODE_GPU)
+    _check(O.compare_closest(gpu, orc, rays, b.slot_to_tri, b.verts), len(rays))
+    assert np.array_equal(gpu["triangleIndex"] == 0xFFFFFFFF, orc["triangleIndex"] == 0xFFFFFFFF)
+
+    # incoherent rays from the hit points
+    hit = orc["triangleIndex"] != 0xFFFFFFFF
+    pos = rays["origin"][hit] + rays["dir"][hit] * orc["t"][hit][:, None]
+    rng = np.random.default_rng(5)
+    d = rng.normal(size=pos.shape).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    d[:, 2] = np.abs(d[:, 2])
+    inc = np.zeros(len(pos), P.RAY_IN_DTYPE)
+    inc["origin"] = pos.astype(np.float32)
+    inc["dir"] = d.astype(np.float32)
+    inc["tMin"] = np.float32(1e-3)
+    inc["tMax"] = np.float32(3.4028235e38)
+    inc = inc[: 400_000]
+    gpu = _gpu_closest(scene, inc)
+    orc2 = O.cast_rays(b.nodes, b.verts, inc, mode=O.MODE_GPU)
+    _check(O.compare_closest(gpu, orc2, inc, b.slot_to_tri, b.verts), len(inc))
+
+    # shadow rays toward a point light: any hit must be bit-identical
+    light = np.array([0.5, 0.5, 2.0], np.float32) * np.float32(s.scale)
+    sh = np.zeros(len(pos), P.RAY_IN_DTYPE)
+    diff = (light[None, :] - pos).astype(np.float32)
+    dist = np.sqrt((diff * diff).sum(1)).astype(np.float32)
+    sh["origin"] = pos.astype(np.float32)
+    sh["dir"] = (diff / dist[:, None]).astype(np.float32)
+    sh["tMin"] = np.float32(1e-3)
+    sh["tMax"] = dist
+    gpu_any = _gpu_any(scene, sh)
+    orc_any = O.any_rays(b.nodes, b.verts, sh)
+    assert np.array_equal(gpu_any, orc_any)
+    assert 0.05 < orc_any.mean() < 0.999
+
+
+def test_edge_cases():
+    """Axis-aligned rays on cell planes (NaN slab lanes), rays with tMin > tMax, tMax = 0, origins
+    exactly on vertices, zero-length directions and NaN rays: GPU equals the oracle bit for bit."""
+    s, b = built_scene("c1_64_100")
+    scene = P.Scene(b.nodes, b.verts)
+    rng = np.random.default_rng(3)
+    n = 6000
+    rays = random_rays(n, [0, 0, 0.02], [1, 1, 0.3], 17)
+    k = np.arange(n)
+    axes = np.array([[1, 0, 0], [0, 1, 0], [0, 0, -1], [-1, 0, 0], [0, -1, 0], [0, 0, 1]], np.float32)
+    sel = k % 4 == 0
+    rays["dir"][sel] = axes[(k[sel] // 4) % 6]
+    rays["origin"][sel, 0] = (np.round(rays["origin"][sel, 0] * 64) / 64).astype(np.float32)
+    rays["origin"][sel, 1] = (np.round(rays["origin"][sel, 1] * 64) / 64).astype(np.float32)
+    rays["tMin"][k % 13 == 1] = np.float32(5.0)       # tMin > tMax for some below
+    rays["tMax"][k % 13 == 1] = np.float32(1.0)
+    rays["tMax"][k % 13 == 2] = np.float32(0.0)
+    rays["tMax"][k % 13 == 3] = np.float32(0.05)
+    tv = s.tri_verts[b.slot_to_tri[rng.integers(0, len(b.slot_to_tri), n)]]
+    on_vertex = k % 13 == 4
+    rays["origin"][on_vertex] = tv[on_vertex, 0:3] + np.float32(0.0)
+    rays["dir"][k % 97 == 5] = 0.0
+    rays["dir"][k % 89 == 6] = np.nan
+    gpu = _gpu_closest(scene, rays)
+    gpu_plain = _gpu_closest(scene, rays, "plain")
+    orc = O.cast_rays(b.nodes, b.verts, rays, mode=O.MODE_GPU)
+    for res in (gpu, gpu_plain):
+        _check(O.compare_closest(res, orc, rays, b.slot_to_tri, b.verts), n)
+    assert np.array_equal(_gpu_any(scene, rays), O.any_rays(b.nodes, b.verts, rays))
+
+
+def test_sizes_zero_one_and_ragged():
+    import torch
+    s, b = built_scene("c1_64_100")
+    scene = P.Scene(b.nodes, b.verts)
+    d_rays = device_empty(1, P.RAY_IN_DTYPE)
+    d_hits = device_empty(1, P.RAY_HIT_DTYPE)
+    P.cast_closest(scene, d_rays, d_hits, 0)
+    P.cast_any(scene, d_rays, device_empty(1, np.uint8), 0)
+    for n in (1, 31, 33, 1000, 4097):
+        rays = random_rays(n, [0, 0, 0.05], [1, 1, 0.4], n)
+        orc = O.cast_rays(b.nodes, b.verts, rays, mode=O.MODE_GPU)
+        for kind in ("persistent", "plain"):
+            gpu = _gpu_closest(scene, rays, kind)
+            _check(O.compare_closest(gpu, orc, rays, b.slot_to_tri, b.verts), n)
+    torch.cuda.synchronize()
+
+
+def test_invalid_scene_and_arguments_are_rejected():
+    s, b = built_scene("c1_64_100")
+    bad = b.nodes.copy()
+    bad["iData"][0, 0] = len(bad) + 5          # child index out of range
+    bad["iData"][0, 2] = 0
+    with pytest.raises(P.PheError) as e:
+        P.Scene(bad, b.verts)
+    assert e.value.status == 2
+    cyc = b.nodes.copy()
+    inner = np.nonzero(cyc["iData"][:, 2] == 0)[0]
+    cyc["iData"][inner[1], 0] = 0               # points back at the root
+    cyc["iData"][inner[1], 2] = 0
+    with pytest.raises(P.PheError):
+        P.Scene(cyc, b.verts)
+    scene = P.Scene(b.nodes, b.verts)
+    with pytest.raises(P.PheError):
+        P.cast_closest(scene, None, device_empty(4, P.RAY_HIT_DTYPE), 4)

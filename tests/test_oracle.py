@@ -1,0 +1,146 @@
+"""The oracle pinned against the reference: golden fixtures produced by the reference's own code
+(tests/golden/make_golden.py) and, where the reference sources are present, the live reference
+harness oracle/_ref/libpheref.so. CPU only."""
+import math
+
+import numpy as np
+import pytest
+
+import phantasyenginetestbed_gb300 as P
+from oracle import oracle as O
+from tests.helpers import C1_CAM, golden_scene, load_golden, random_rays
+
+needs_ref = pytest.mark.skipif(not O.ref_available(), reason="reference sources not present")
+
+
+def test_intersect_matches_reference_fixture():
+    g = load_golden("ref_isect.npz")
+    tris, orig, dirs, out = g["tris"], g["origins"], g["dirs"], g["out"]
+    hits = 0
+    for i in range(len(tris)):
+        h, t, u, v = O.intersect_tri(tris[i], orig[i], dirs[i])
+        assert h == bool(out[i, 0]), i
+        if h:
+            hits += 1
+            assert (np.float32(t), np.float32(u), np.float32(v)) == tuple(out[i, 1:]), i
+    assert 200 < hits < len(tris) - 200
+
+
+@pytest.mark.parametrize("fixture", ["ref_small.npz", "ref_c1.npz"])
+def test_castray_matches_reference_fixture(fixture):
+    """oracle castRay (reference accept rule) == the reference's castRay output, bit for bit,
+    including the castDebugRay traversal counters."""
+    g = load_golden(fixture)
+    s, nodes, verts, s2t = golden_scene(fixture)
+    if fixture == "ref_small.npz":
+        assert np.array_equal(verts.view(np.uint8), g["verts"].view(np.uint8))
+        rays = O.gen_primary(g["cam"], (64, 64))
+    else:
+        rays = O.gen_primary(g["cam"], C1_CAM["res"])[::16].copy()
+    hits, dbg = O.cast_rays(nodes, verts, rays, mode=O.MODE_CPU, debug=True)
+    assert np.array_equal(hits.view(np.uint8), g["hits"].view(np.uint8))
+    assert np.array_equal(dbg, g["debug"])
+    assert (hits["triangleIndex"] != 0xFFFFFFFF).mean() > 0.5
+    if "inc_rays" in g:
+        inc = O.cast_rays(nodes, verts, g["inc_rays"], mode=O.MODE_CPU)
+        assert np.array_equal(inc.view(np.uint8), g["inc_hits"].view(np.uint8))
+
+
+def test_camera_and_jitter_match_reference_fixture():
+    g = load_golden("ref_c1.npz")
+    cam = O.camera_def(C1_CAM["pos"], C1_CAM["dir"], C1_CAM["up"], math.radians(60.0), C1_CAM["res"])
+    assert np.array_equal(cam, g["cam"])
+    pc = P.camera_def(C1_CAM["pos"], C1_CAM["dir"], C1_CAM["up"], 60.0, C1_CAM["res"])
+    assert np.array_equal(P.camera_def_array(pc), g["cam"])
+    table = np.load("tests/golden/ref_halton.npy") if False else load_halton()
+    for i in range(16):
+        assert np.array_equal(O.halton_jitter(i), table[i] - np.float32(0.5))
+        assert P.halton_jitter(i) == tuple(float(x) for x in table[i] - np.float32(0.5))
+
+
+def load_halton():
+    from tests.helpers import GOLDEN
+    return np.load(GOLDEN / "ref_halton.npy")
+
+
+@needs_ref
+@pytest.mark.parametrize("seed", [3, 4])
+def test_castray_matches_live_reference(seed):
+    """Random scenes, both the reference builder's tree and the project builder's tree, coherent and
+    incoherent rays: the oracle reproduces castRay bit for bit."""
+    s = P.generate_scene(24, 20, seed == 4, seed)
+    rn, rv, _ = O.ref_build_sbvh(s.tri_verts)
+    b = P.build_sbvh(s.tri_verts)
+    scale = s.scale
+    rays = np.concatenate([random_rays(3000, [0, 0, 0.05], [scale, scale, 0.4 * scale], seed),
+                           O.gen_primary(O.camera_def((0.5 * scale, -0.3 * scale, 0.6 * scale), (0, 0.8, -0.6),
+                                                      (0, 0.6, 0.8), math.radians(60), (48, 48)), (48, 48))])
+    # axis-aligned directions exercise the NaN lanes of the slab test
+    ax = rays[:300].copy()
+    ax["dir"] = np.array([[1, 0, 0], [0, 1, 0], [0, 0, -1]], np.float32)[np.arange(300) % 3]
+    ax["origin"][:, 0] = np.round(ax["origin"][:, 0] * 64) / 64
+    rays = np.concatenate([rays, ax])
+    for nodes, verts in ((rn, rv), (b.nodes, b.verts)):
+        mine, dbg = O.cast_rays(nodes, verts, rays, mode=O.MODE_CPU, debug=True)
+        ref, rdbg = O.ref_cast_rays(nodes, verts, rays, debug=True)
+        assert np.array_equal(mine.view(np.uint8), ref.view(np.uint8))
+        assert np.array_equal(dbg, rdbg)
+
+
+@needs_ref
+def test_camera_def_matches_live_reference():
+    for res in [(512, 512), (1920, 1080), (64, 48)]:
+        a = O.camera_def((1, 2, 3), (0.1, 0.9, -0.3), (0, 0.3, 0.9), math.radians(47.0), res)
+        b = O.ref_camera_def((1, 2, 3), (0.1, 0.9, -0.3), (0, 0.3, 0.9), math.radians(47.0), res)
+        assert np.array_equal(a, b)
+
+
+def test_gpu_rule_matches_cpu_rule_except_tmax():
+    """The GPU accept rule (tMin <= t < tMax) gives the CPU rule's result except for hits exactly at
+    tMax; on random rays they agree on every ray."""
+    g = load_golden("ref_c1.npz")
+    s, nodes, verts, s2t = golden_scene("ref_c1.npz")
+    rays = g["inc_rays"]
+    a = O.cast_rays(nodes, verts, rays, mode=O.MODE_CPU)
+    b = O.cast_rays(nodes, verts, rays, mode=O.MODE_GPU)
+    hit = a["triangleIndex"] != 0xFFFFFFFF
+    assert np.array_equal(a["triangleIndex"], b["triangleIndex"])
+    assert np.array_equal(a[hit].view(np.uint8), b[hit].view(np.uint8))
+    assert np.all(b["t"][~hit] == rays["tMax"][~hit])
+
+
+def test_bvh_traversal_matches_brute_force():
+    s = P.generate_scene(12, 8, True, 9)
+    b = P.build_sbvh(s.tri_verts)
+    rays = random_rays(4000, [0, 0, 0.02], [s.scale, s.scale, 0.3 * s.scale], 21)
+    tris = np.zeros(len(s.tri_verts), P.TRI_VERTS_DTYPE)
+    tris["v0"][:, :3] = s.tri_verts[:, 0:3]
+    tris["v1"][:, :3] = s.tri_verts[:, 3:6]
+    tris["v2"][:, :3] = s.tri_verts[:, 6:9]
+    bf = O.brute_closest(tris, rays, mode=O.MODE_GPU)
+    bvh = O.cast_rays(b.nodes, b.verts, rays, mode=O.MODE_GPU)
+    ident = np.arange(len(tris), dtype=np.uint32)
+    # express the BVH result in original triangle ids for the comparator
+    bvh_orig = bvh.copy()
+    hit = bvh["triangleIndex"] != 0xFFFFFFFF
+    bvh_orig["triangleIndex"][hit] = b.slot_to_tri[bvh["triangleIndex"][hit]]
+    r = O.compare_closest(bvh_orig, bf, rays, ident, tris)
+    assert r["ok"], r
+    assert r["near_ties"] <= 4
+
+
+def test_sincos_accuracy_and_pcg_reference_stream():
+    xs = np.linspace(0, 1, 40001, endpoint=False, dtype=np.float32)
+    err = 0.0
+    for x in xs[::7]:
+        s, c = O.sincos_2pi(float(x))
+        err = max(err, abs(s - math.sin(2 * math.pi * float(x))), abs(c - math.cos(2 * math.pi * float(x))))
+    assert err < 3e-7
+    # pcg32_srandom_r(42, 54) first outputs, as printed by the PCG reference demo
+    import ctypes as C
+    st = (C.c_uint64 * 2)()
+    L = O.lib()
+    L.oracle_pcg_seed.argtypes = [C.c_void_p, C.c_uint64, C.c_uint64]
+    L.oracle_pcg_seed(C.addressof(st), 42, 54)
+    got = [L.oracle_pcg_next(C.addressof(st)) for _ in range(6)]
+    assert got == [0xa15c02b7, 0x7b47f409, 0xba1d3330, 0x83d2f293, 0xbfa4784b, 0xcbed606e]
