@@ -194,6 +194,69 @@ phe_status phe_cast_any(const phe_scene* scene, const phe_ray_in* rays, uint8_t*
 phe_status phe_gen_primary_rays(phe_ray_in* rays, const phe_camera_def* cam, uint32_t resX, uint32_t resY,
                                 float jitterX, float jitterY, int order, void* stream);
 
+/* OR of error bits raised by kernels on this scene (1 = traversal stack overflow; never set for a
+ * scene that passed validation). Synchronous. */
+phe_status phe_scene_status(const phe_scene* scene, uint32_t* bits);
+
+/* ---------------------------------------------------------------------------------------------
+ * Wavefront renderer (CudaTracerRenderer, cuda_ray_tracer/CudaTracerRenderer.hpp:14-58, and the
+ * BaseRenderer entry points, phantasy_engine/rendering/BaseRenderer.hpp:56-90)
+ *
+ * One render() is a frame: primary closest hit -> shading + one shadow ray per light -> one
+ * bounce ray per hit -> closest hit -> shading + shadow rays -> resolve -> TAA. Shadow and bounce
+ * rays are compacted into queues. Colours are linear float RGBA, row-major from the bottom row.
+ * ------------------------------------------------------------------------------------------- */
+typedef struct phe_renderer phe_renderer;
+typedef struct phe_render_result {
+	uint32_t resX, resY;
+	const float* color;      /* device, float4 per pixel: TAA output (RenderResult::colorTexture) */
+	const float* history;    /* device, float4 per pixel: TAA history, alpha = sample count */
+	const float* rawColor;   /* device, float4 per pixel: resolved frame before TAA */
+	const float* roughness;  /* device, float per pixel: roughness at the primary hit (materialTexture) */
+} phe_render_result;
+phe_status phe_renderer_create(phe_renderer** out);
+phe_status phe_renderer_destroy(phe_renderer* renderer);
+/* setStaticScene: the scene must carry triangle data and materials. */
+phe_status phe_renderer_set_static_scene(phe_renderer* renderer, const phe_scene* scene);
+/* setTargetResolution: multiples of 8 (CudaTracerRenderer.cpp:470-471); reallocates frame buffers. */
+phe_status phe_renderer_set_target_resolution(phe_renderer* renderer, uint32_t resX, uint32_t resY);
+/* updateCamera(ViewFrustum): position, direction, up, vertical FOV in degrees and the TAA pixel
+ * offset (ViewFrustum::setPixelOffset, GameScreen.cpp:187-203). */
+phe_status phe_renderer_update_camera(phe_renderer* renderer, const float pos[3], const float dir[3], const float up[3],
+                                      float vertFovDeg, float pixelOffsetX, float pixelOffsetY);
+/* The same with an explicit CameraDef and eye position. */
+phe_status phe_renderer_set_camera_def(phe_renderer* renderer, const phe_camera_def* cam, const float camPos[3],
+                                       float pixelOffsetX, float pixelOffsetY);
+/* Seed of the random streams and the index of the next frame (advanced by each render). */
+phe_status phe_renderer_set_seed(phe_renderer* renderer, uint64_t seed, uint32_t frame);
+/* 1 = replay the frame from a CUDA graph captured on first use (default 0). */
+phe_status phe_renderer_set_graph(phe_renderer* renderer, int enable);
+/* Clears the TAA history (GameScreen::resetTAA). */
+phe_status phe_renderer_reset_taa(phe_renderer* renderer, void* stream);
+/* render(objects, lights): asynchronous on `stream`; lights are host memory (at most 8). */
+phe_status phe_renderer_render(phe_renderer* renderer, const phe_sphere_light* lights, uint32_t numLights, void* stream);
+phe_status phe_renderer_result(const phe_renderer* renderer, phe_render_result* out);
+/* Copies one result buffer to host memory (0 = color, 1 = history, 2 = rawColor: 16 bytes per pixel;
+ * 3 = roughness: 4 bytes per pixel). Synchronises `stream`. The headless stand-in for reading the
+ * GL result texture. */
+phe_status phe_renderer_read(const phe_renderer* renderer, int which, void* hostDst, void* stream);
+/* Rays cast by the last frame: primary, primary shadow, bounce, bounce shadow. Synchronises `stream`. */
+phe_status phe_renderer_ray_counts(const phe_renderer* renderer, uint64_t counts[4], void* stream);
+
+/* Per-kernel timing with CUDA events on the render stream (direct launches; ignored while a graph is
+ * replayed). Enabling resets the totals. kernel_times returns the summed milliseconds of the 5 frame
+ * kernels (primary, primary shadow, bounce, bounce shadow, resolve + TAA) and the frames timed. */
+phe_status phe_renderer_set_kernel_timing(phe_renderer* renderer, int enable);
+/* Bytes copied host -> device per frame (the frame parameter block: camera, jitter, lights). */
+uint32_t phe_renderer_frame_param_bytes(void);
+phe_status phe_renderer_kernel_times(phe_renderer* renderer, double msTotal[5], uint32_t* frames);
+
+/* TAA resolve alone (taa.frag:25-71) on device float4 buffers; velocity and prevVelocity are float2
+ * uv velocities (NULL = static), roughness float (NULL = 0). */
+phe_status phe_taa_resolve(uint32_t resX, uint32_t resY, const float* cur, const float* hist, const float* velocity,
+                           const float* prevVelocity, const float* roughness, float* outColor, float* outHist,
+                           void* stream);
+
 #ifdef __cplusplus
 }
 #endif

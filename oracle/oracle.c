@@ -504,12 +504,16 @@ static int shade_light(const or_light* light, v3 mask, v3 normal, v3 toCamera, v
 typedef struct {
 	const or_node* nodes; const or_tri* tris; const or_tri_data* datas; const or_frame_params* fp;
 	const or_hit* primaryHits; float* color; float* roughnessOut;
-	atomic_uint next; atomic_ullong counts[4]; atomic_int overflows;
+	atomic_uint next; atomic_ullong counts[4]; atomic_ullong work[8]; atomic_int overflows;
 } frame_job;
 
-static int cast1(const frame_job* j, const or_ray* r, or_hit* h)
+static int cast1(frame_job* j, const or_ray* r, or_hit* h, int stage)
 {
-	return oracle_cast_ray(j->nodes, j->tris, r, OR_MODE_REFERENCE_GPU, h, NULL, NULL);
+	uint32_t nv = 0, nt = 0;
+	int rc = oracle_cast_ray(j->nodes, j->tris, r, OR_MODE_REFERENCE_GPU, h, &nv, &nt);
+	atomic_fetch_add(&j->work[2 * stage], (unsigned long long)nv);
+	atomic_fetch_add(&j->work[2 * stage + 1], (unsigned long long)nt);
+	return rc;
 }
 
 static void frame_pixel(frame_job* j, uint32_t x, uint32_t y)
@@ -528,7 +532,7 @@ static void frame_pixel(frame_job* j, uint32_t x, uint32_t y)
 	pr.tmin = 0.0001f; pr.d[0] = d.x; pr.d[1] = d.y; pr.d[2] = d.z; pr.tmax = FLT_MAX;
 	or_hit ph;
 	if (j->primaryHits) ph = j->primaryHits[pid];
-	else if (cast1(j, &pr, &ph)) atomic_fetch_add(&j->overflows, 1);
+	else if (cast1(j, &pr, &ph, 0)) atomic_fetch_add(&j->overflows, 1);
 	if (ph.tri == ~0u) goto done;
 	{
 		hit_info hi = interpret(j->datas, fp->materials, &pr, &ph);
@@ -544,7 +548,7 @@ static void frame_pixel(frame_job* j, uint32_t x, uint32_t y)
 			if (shade_light(&fp->lights[li], mk(1.0f, 1.0f, 1.0f), hi.normal, toCamera, hi.pos, hi.mat, &rng, c, &sr)) {
 				or_hit sh;
 				counts[1]++;
-				if (cast1(j, &sr, &sh)) atomic_fetch_add(&j->overflows, 1);
+				if (cast1(j, &sr, &sh, 1)) atomic_fetch_add(&j->overflows, 1);
 				inLight = sh.tri == ~0u;
 			}
 			if (inLight) accum = add(accum, ld3(c));
@@ -582,7 +586,7 @@ static void frame_pixel(frame_job* j, uint32_t x, uint32_t y)
 		br.d[0] = bdir.x; br.d[1] = bdir.y; br.d[2] = bdir.z;
 		counts[2]++;
 		or_hit bh;
-		if (cast1(j, &br, &bh)) atomic_fetch_add(&j->overflows, 1);
+		if (cast1(j, &br, &bh, 2)) atomic_fetch_add(&j->overflows, 1);
 		if (bh.tri != ~0u) {
 			hit_info bi = interpret(j->datas, fp->materials, &br, &bh);
 			or_pcg rng2;
@@ -595,7 +599,7 @@ static void frame_pixel(frame_job* j, uint32_t x, uint32_t y)
 				if (shade_light(&fp->lights[li], throughput, bi.normal, toCam2, bi.pos, bi.mat, &rng2, c, &sr)) {
 					or_hit sh;
 					counts[3]++;
-					if (cast1(j, &sr, &sh)) atomic_fetch_add(&j->overflows, 1);
+					if (cast1(j, &sr, &sh, 3)) atomic_fetch_add(&j->overflows, 1);
 					inLight = sh.tri == ~0u;
 				}
 				if (inLight) accum = add(accum, ld3(c));
@@ -621,7 +625,7 @@ static void* frame_worker(void* arg)
 
 int oracle_render_frame(const or_node* nodes, const or_tri* tris, const or_tri_data* datas,
                         const or_frame_params* fp, const or_hit* primaryHits, float* color, float* roughnessOut,
-                        uint64_t* rayCounts, int threads)
+                        uint64_t* rayCounts, uint64_t* workSums, int threads)
 {
 	frame_job j;
 	memset(&j, 0, sizeof(j));
@@ -629,6 +633,7 @@ int oracle_render_frame(const or_node* nodes, const or_tri* tris, const or_tri_d
 	j.color = color; j.roughnessOut = roughnessOut;
 	atomic_init(&j.next, 0u);
 	for (int i = 0; i < 4; i++) atomic_init(&j.counts[i], 0ull);
+	for (int i = 0; i < 8; i++) atomic_init(&j.work[i], 0ull);
 	atomic_init(&j.overflows, 0);
 	if (threads < 1) threads = 1;
 	pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)threads);
@@ -641,6 +646,8 @@ int oracle_render_frame(const or_node* nodes, const or_tri* tris, const or_tri_d
 	free(th);
 	if (rayCounts)
 		for (int i = 0; i < 4; i++) rayCounts[i] = atomic_load(&j.counts[i]);
+	if (workSums)
+		for (int i = 0; i < 8; i++) workSums[i] = atomic_load(&j.work[i]);
 	return atomic_load(&j.overflows);
 }
 

@@ -113,9 +113,11 @@ typedef struct {
 	const or_material* materials;
 	uint64_t seed; uint32_t frame;
 } or_frame_params;
+/* `rayCounts` (optional, 4): rays cast per stage (primary, primary shadow, bounce, bounce shadow);
+ * `workSums` (optional, 8): castDebugRay's nodesVisited and triangleIntersectionTests summed per stage. */
 int oracle_render_frame(const or_node* nodes, const or_tri* tris, const or_tri_data* datas,
                         const or_frame_params* fp, const or_hit* primaryHits, float* color, float* roughnessOut,
-                        uint64_t* rayCounts, int threads);
+                        uint64_t* rayCounts, uint64_t* workSums, int threads);
 
 /* TAA resolve (resources/shaders/taa.frag:25-71) on row-major float4 buffers. velocity and
  * prevVelocity are float2 uv-velocities (NULL = zero). History alpha holds the sample count. */

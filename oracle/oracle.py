@@ -66,7 +66,7 @@ def lib():
         L.oracle_camera_def.restype = None
         L.oracle_gen_primary.argtypes = [V, C.c_uint32, C.c_uint32, C.c_float, C.c_float, C.c_int, V]
         L.oracle_gen_primary.restype = None
-        L.oracle_render_frame.argtypes = [V, V, V, C.POINTER(FrameParams), V, V, V, V, C.c_int]
+        L.oracle_render_frame.argtypes = [V, V, V, C.POINTER(FrameParams), V, V, V, V, V, C.c_int]
         L.oracle_taa.argtypes = [C.c_uint32, C.c_uint32, V, V, V, V, V, V, V]
         L.oracle_taa.restype = None
         L.oracle_halton_jitter.argtypes = [C.c_uint32, V]
@@ -172,7 +172,9 @@ def sincos_2pi(r):
 
 
 def render_frame(nodes, verts, slot_datas, materials, lights, cam12, res, jitter, cam_pos, seed, frame,
-                 primary_hits=None, nthreads=None):
+                 primary_hits=None, nthreads=None, work=None):
+    """Oracle frame: (color (H, W, 4), roughness (H, W), ray counts per stage). `work` (optional
+    uint64 array of 8) receives nodesVisited / triangle tests summed per stage."""
     fp = FrameParams()
     fp.resX, fp.resY = res
     fp.cam[:] = [float(x) for x in cam12]
@@ -188,7 +190,7 @@ def render_frame(nodes, verts, slot_datas, materials, lights, cam12, res, jitter
     rough = np.empty((res[1], res[0]), np.float32)
     counts = np.zeros(4, np.uint64)
     rc = lib().oracle_render_frame(_p(nodes), _p(verts), _p(slot_datas), C.byref(fp), _p(primary_hits), _p(color),
-                                   _p(rough), _p(counts), nthreads or threads())
+                                   _p(rough), _p(counts), _p(work), nthreads or threads())
     if rc:
         raise RuntimeError(f"oracle: {rc} rays overflowed the traversal stack")
     return color, rough, counts

@@ -1,0 +1,362 @@
+// The renderer object behind the C ABI: the headless counterpart of CudaTracerRenderer
+// (cuda_ray_tracer/CudaTracerRenderer.{hpp,cpp}) and the BaseRenderer entry points it implements
+// (phantasy_engine/rendering/BaseRenderer.hpp:56-90): setStaticScene, setTargetResolution,
+// updateCamera, render. RenderResult's GL textures become device pointers.
+//
+// Buffers are (re)allocated in set_target_resolution, as targetResolutionUpdated does
+// (CudaTracerRenderer.cpp:735-793). A frame is either launched directly or replayed from a CUDA
+// graph captured on first use; per-frame values travel in one small parameter copy.
+
+#include <cmath>
+#include <cstring>
+
+#include "runtime.cuh"
+#include "wavefront.cuh"
+
+using namespace phe_gb300;
+
+struct phe_renderer {
+	const phe_scene* scene = nullptr;
+	uint32_t resX = 0, resY = 0, numLights = 0;
+	FrameBuffers fb{};
+	void* allocation = nullptr;
+	FrameParamsDev* dParams = nullptr;
+	FrameParamsDev* hParams = nullptr;   // pinned staging
+	phe_camera_def cam{};
+	float camPos[3] = {0, 0, 0};
+	float jitter[2] = {0, 0};
+	uint64_t seed = 1;
+	uint32_t frame = 0;
+	uint32_t parity = 0;
+	int useGraph = 0;
+	cudaGraphExec_t graphExec = nullptr;
+	cudaStream_t graphStream = nullptr;  // stream the graph was captured for (graphs relaunch on any stream)
+	bool cameraSet = false;
+	bool timing = false;                   // record events around each kernel (direct launches only)
+	cudaEvent_t events[kFrameKernels + 1] = {};
+	double kernelMs[kFrameKernels] = {};   // accumulated since timing was enabled
+	uint32_t timedFrames = 0;
+	bool pendingTimes = false;
+};
+
+static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+static void free_buffers(phe_renderer* r)
+{
+	if (r->graphExec) cudaGraphExecDestroy(r->graphExec);
+	r->graphExec = nullptr;
+	if (r->allocation) cudaFree(r->allocation);
+	r->allocation = nullptr;
+	std::memset(&r->fb, 0, sizeof(r->fb));
+}
+
+static phe_status allocate(phe_renderer* r, uint32_t resX, uint32_t resY, uint32_t numLights)
+{
+	free_buffers(r);
+	const size_t P = (size_t)resX * resY;
+	const size_t LP = P * (numLights ? numLights : 1);
+	size_t sizes[] = {
+		2 * LP * sizeof(float4),      // contrib
+		2 * LP,                       // inLight
+		2 * LP * sizeof(phe_ray_in),  // shadowRays
+		2 * LP * sizeof(uint32_t),    // shadowSlots
+		P * sizeof(phe_ray_in),       // bounceRays
+		P * sizeof(uint32_t),         // bouncePixel
+		P * sizeof(float4),           // bounceThroughput
+		P * sizeof(float),            // roughness
+		P * sizeof(float4),           // rawColor
+		P * sizeof(float4),           // history[0]
+		P * sizeof(float4),           // history[1]
+		P * sizeof(float4),           // color
+		kNumCounters * sizeof(uint32_t),
+	};
+	size_t total = 0;
+	for (size_t s : sizes) total += align256(s);
+	char* base = nullptr;
+	cudaError_t e = cudaMalloc(&base, total);
+	if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(frame buffers)");
+	char* p = base;
+	auto take = [&](size_t i) { char* q = p; p += align256(sizes[i]); return q; };
+	FrameBuffers& fb = r->fb;
+	fb.contrib = (float4*)take(0);
+	fb.inLight = (uint8_t*)take(1);
+	fb.shadowRays = (phe_ray_in*)take(2);
+	fb.shadowSlots = (uint32_t*)take(3);
+	fb.bounceRays = (phe_ray_in*)take(4);
+	fb.bouncePixel = (uint32_t*)take(5);
+	fb.bounceThroughput = (float4*)take(6);
+	fb.roughness = (float*)take(7);
+	fb.rawColor = (float4*)take(8);
+	fb.history[0] = (float4*)take(9);
+	fb.history[1] = (float4*)take(10);
+	fb.color = (float4*)take(11);
+	fb.counters = (uint32_t*)take(12);
+	fb.capacityLP = (uint32_t)LP;
+	r->allocation = base;
+	r->resX = resX;
+	r->resY = resY;
+	r->numLights = numLights;
+	if ((e = cudaMemset(base, 0, total)) != cudaSuccess) return cuda_fail(e, "clear frame buffers");
+	r->parity = 0;
+	return PHE_OK;
+}
+
+// Adds the elapsed times of the last timed frame (waits for its last event).
+static phe_status collect_times(phe_renderer* r)
+{
+	if (!r->pendingTimes) return PHE_OK;
+	PHE_CUDA_TRY(cudaEventSynchronize(r->events[kFrameKernels]), "wait for timed frame");
+	for (int i = 0; i < kFrameKernels; i++) {
+		float ms = 0.0f;
+		PHE_CUDA_TRY(cudaEventElapsedTime(&ms, r->events[i], r->events[i + 1]), "kernel time");
+		r->kernelMs[i] += ms;
+	}
+	r->timedFrames++;
+	r->pendingTimes = false;
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_renderer_set_kernel_timing(phe_renderer* r, int enable)
+{
+	if (!r) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_set_kernel_timing: null renderer");
+	if (enable && !r->events[0])
+		for (int i = 0; i <= kFrameKernels; i++) PHE_CUDA_TRY(cudaEventCreate(&r->events[i]), "cudaEventCreate");
+	r->timing = enable != 0;
+	r->pendingTimes = false;
+	r->timedFrames = 0;
+	for (int i = 0; i < kFrameKernels; i++) r->kernelMs[i] = 0.0;
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_renderer_kernel_times(phe_renderer* r, double msTotal[5], uint32_t* frames)
+{
+	if (!r || !msTotal || !frames) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_kernel_times: null argument");
+	phe_status st = collect_times(r);
+	if (st) return st;
+	for (int i = 0; i < kFrameKernels; i++) msTotal[i] = r->kernelMs[i];
+	*frames = r->timedFrames;
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_renderer_create(phe_renderer** out)
+{
+	if (!out) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_create: out is null");
+	*out = nullptr;
+	DeviceInfo* d = nullptr;
+	phe_status st = device_info(&d);
+	if (st) return st;
+	phe_renderer* r = new phe_renderer();
+	cudaError_t e = cudaMalloc(&r->dParams, sizeof(FrameParamsDev));
+	if (e == cudaSuccess) e = cudaMallocHost(&r->hParams, sizeof(FrameParamsDev));
+	if (e != cudaSuccess) {
+		if (r->dParams) cudaFree(r->dParams);
+		delete r;
+		return cuda_fail(e, "allocate frame parameters");
+	}
+	std::memset(r->hParams, 0, sizeof(FrameParamsDev));
+	*out = r;
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_renderer_destroy(phe_renderer* r)
+{
+	if (!r) return PHE_OK;
+	cudaDeviceSynchronize();
+	for (int i = 0; i <= kFrameKernels; i++)
+		if (r->events[i]) cudaEventDestroy(r->events[i]);
+	free_buffers(r);
+	cudaFree(r->dParams);
+	cudaFreeHost(r->hParams);
+	delete r;
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_renderer_set_static_scene(phe_renderer* r, const phe_scene* scene)
+{
+	if (!r || !scene) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_set_static_scene: null argument");
+	if (!scene->dev.datas || !scene->dev.materials)
+		return fail(PHE_ERR_INVALID_SCENE, "rendering needs a scene created with triangle data and materials");
+	r->scene = scene;
+	if (r->graphExec) cudaGraphExecDestroy(r->graphExec);
+	r->graphExec = nullptr;
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_renderer_set_target_resolution(phe_renderer* r, uint32_t resX, uint32_t resY)
+{
+	if (!r) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_set_target_resolution: null renderer");
+	if (resX == 0 || resY == 0 || (resX % 8u) || (resY % 8u))
+		return fail(PHE_ERR_INVALID_ARGUMENT, "target resolution must be a non-zero multiple of 8 (CudaTracerRenderer.cpp:470-471)");
+	if ((uint64_t)resX * resY * kMaxLights * 2 >= 0xFFFFFFFFull)
+		return fail(PHE_ERR_TOO_LARGE, "target resolution too large");
+	return allocate(r, resX, resY, r->numLights ? r->numLights : 1);
+}
+
+extern "C" phe_status phe_renderer_update_camera(phe_renderer* r, const float pos[3], const float dir[3], const float up[3],
+                                                 float vertFovDeg, float pixelOffsetX, float pixelOffsetY)
+{
+	if (!r || !pos || !dir || !up) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_update_camera: null argument");
+	if (!r->resX) return fail(PHE_ERR_INVALID_ARGUMENT, "set the target resolution before the camera");
+	phe_generate_camera_def(pos, dir, up, vertFovDeg * 0.017453292519943295f, (float)r->resX, (float)r->resY, &r->cam);
+	std::memcpy(r->camPos, pos, sizeof(r->camPos));
+	r->jitter[0] = pixelOffsetX;
+	r->jitter[1] = pixelOffsetY;
+	r->cameraSet = true;
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_renderer_set_camera_def(phe_renderer* r, const phe_camera_def* cam, const float camPos[3],
+                                                  float pixelOffsetX, float pixelOffsetY)
+{
+	if (!r || !cam || !camPos) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_set_camera_def: null argument");
+	r->cam = *cam;
+	std::memcpy(r->camPos, camPos, sizeof(r->camPos));
+	r->jitter[0] = pixelOffsetX;
+	r->jitter[1] = pixelOffsetY;
+	r->cameraSet = true;
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_renderer_set_seed(phe_renderer* r, uint64_t seed, uint32_t frame)
+{
+	if (!r) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_set_seed: null renderer");
+	r->seed = seed;
+	r->frame = frame;
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_renderer_set_graph(phe_renderer* r, int enable)
+{
+	if (!r) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_set_graph: null renderer");
+	r->useGraph = enable ? 1 : 0;
+	if (!enable && r->graphExec) {
+		cudaGraphExecDestroy(r->graphExec);
+		r->graphExec = nullptr;
+	}
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_renderer_reset_taa(phe_renderer* r, void* stream)
+{
+	if (!r || !r->allocation) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_reset_taa: no frame buffers");
+	size_t P = (size_t)r->resX * r->resY;
+	PHE_CUDA_TRY(cudaMemsetAsync(r->fb.history[0], 0, P * sizeof(float4), (cudaStream_t)stream), "reset TAA");
+	PHE_CUDA_TRY(cudaMemsetAsync(r->fb.history[1], 0, P * sizeof(float4), (cudaStream_t)stream), "reset TAA");
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_light* lights, uint32_t numLights, void* stream)
+{
+	if (!r) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_render: null renderer");
+	if (!r->scene) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_render: no static scene");
+	if (!r->resX) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_render: no target resolution");
+	if (!r->cameraSet) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_render: no camera");
+	if (numLights > kMaxLights) return fail(PHE_ERR_TOO_LARGE, "at most %u lights", kMaxLights);
+	if (numLights && !lights) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_render: lights is null");
+	cudaStream_t s = (cudaStream_t)stream;
+	uint32_t L = numLights ? numLights : 1;
+	if (L != r->numLights) {
+		// Contribution and queue buffers scale with the light count.
+		cudaStreamSynchronize(s);
+		phe_status st = allocate(r, r->resX, r->resY, L);
+		if (st) return st;
+	}
+	FrameParamsDev& fp = *r->hParams;
+	// The pinned staging buffer is rewritten below: wait until the previous frame's copy has read it.
+	PHE_CUDA_TRY(cudaStreamSynchronize(s), "wait for previous frame parameters");
+	fp.cam = r->cam;
+	fp.jitter[0] = r->jitter[0];
+	fp.jitter[1] = r->jitter[1];
+	std::memcpy(fp.camPos, r->camPos, sizeof(fp.camPos));
+	fp.resX = r->resX;
+	fp.resY = r->resY;
+	fp.numPixels = r->resX * r->resY;
+	fp.numLights = numLights;
+	fp.frame = r->frame;
+	fp.parity = r->parity;
+	fp.seed = r->seed;
+	std::memset(fp.lights, 0, sizeof(fp.lights));
+	if (numLights) std::memcpy(fp.lights, lights, sizeof(phe_sphere_light) * numLights);
+	PHE_CUDA_TRY(cudaMemcpyAsync(r->dParams, r->hParams, sizeof(FrameParamsDev), cudaMemcpyHostToDevice, s),
+	             "upload frame parameters");
+	if (r->useGraph) {
+		if (!r->graphExec) {
+			phe_status pst = prepare_frame();
+			if (pst) return pst;
+			cudaStream_t cap = nullptr;
+			PHE_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), "create capture stream");
+			cudaGraph_t g = nullptr;
+			cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+			phe_status st = PHE_OK;
+			if (e == cudaSuccess) {
+				st = launch_frame(r->scene, r->dParams, r->fb, r->resX, r->resY, cap);
+				e = cudaStreamEndCapture(cap, &g);
+			}
+			cudaStreamDestroy(cap);
+			if (st) { if (g) cudaGraphDestroy(g); return st; }
+			if (e != cudaSuccess) return cuda_fail(e, "capture frame graph");
+			e = cudaGraphInstantiate(&r->graphExec, g, 0);
+			cudaGraphDestroy(g);
+			if (e != cudaSuccess) return cuda_fail(e, "instantiate frame graph");
+		}
+		PHE_CUDA_TRY(cudaGraphLaunch(r->graphExec, s), "launch frame graph");
+	} else {
+		phe_status st;
+		if (r->timing) {
+			if ((st = collect_times(r))) return st;
+			st = launch_frame(r->scene, r->dParams, r->fb, r->resX, r->resY, s, r->events);
+			r->pendingTimes = true;
+		} else {
+			st = launch_frame(r->scene, r->dParams, r->fb, r->resX, r->resY, s);
+		}
+		if (st) return st;
+	}
+	r->frame++;
+	r->parity ^= 1u;
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_renderer_result(const phe_renderer* r, phe_render_result* out)
+{
+	if (!r || !out) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_result: null argument");
+	out->resX = r->resX;
+	out->resY = r->resY;
+	out->color = (const float*)r->fb.color;
+	out->history = (const float*)r->fb.history[r->parity];   // written by the last frame
+	out->rawColor = (const float*)r->fb.rawColor;
+	out->roughness = r->fb.roughness;
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_renderer_ray_counts(const phe_renderer* r, uint64_t counts[4], void* stream)
+{
+	if (!r || !counts || !r->fb.counters) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_ray_counts: no frame");
+	uint32_t c[kNumCounters];
+	PHE_CUDA_TRY(cudaMemcpyAsync(c, r->fb.counters, sizeof(c), cudaMemcpyDeviceToHost, (cudaStream_t)stream), "read counters");
+	PHE_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream), "read counters");
+	counts[0] = (uint64_t)r->resX * r->resY;
+	counts[1] = c[kCtrShadow0];
+	counts[2] = c[kCtrBounce];
+	counts[3] = c[kCtrShadow1];
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_renderer_read(const phe_renderer* r, int which, void* hostDst, void* stream)
+{
+	if (!r || !hostDst || !r->allocation) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_read: no frame");
+	size_t P = (size_t)r->resX * r->resY;
+	const void* src = nullptr;
+	size_t bytes = P * sizeof(float4);
+	switch (which) {
+	case 0: src = r->fb.color; break;
+	case 1: src = r->fb.history[r->parity]; break;
+	case 2: src = r->fb.rawColor; break;
+	case 3: src = r->fb.roughness; bytes = P * sizeof(float); break;
+	default: return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_read: which must be 0..3");
+	}
+	PHE_CUDA_TRY(cudaMemcpyAsync(hostDst, src, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)stream), "read result");
+	PHE_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream), "read result");
+	return PHE_OK;
+}
+
+extern "C" uint32_t phe_renderer_frame_param_bytes(void) { return (uint32_t)sizeof(FrameParamsDev); }

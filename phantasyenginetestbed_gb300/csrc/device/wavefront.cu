@@ -1,0 +1,415 @@
+// Wavefront frame renderer: the CUDA path of CudaTracerRenderer::render (normal path,
+// cuda_ray_tracer/CudaTracerRenderer.cpp:612-728) with the raster G-buffer replaced by ray-cast
+// primary hits, followed by the TAA resolve of resources/shaders/taa.frag:25-71.
+//
+// One frame is five kernels on one stream (the reference issues ~10 launches, each followed by
+// cudaDeviceSynchronize):
+//   1. primary_kernel     persistent: camera ray -> closest hit -> shading of every light -> append
+//                         the shadow rays that matter and one bounce ray per hit to compacted queues
+//                         (warp-aggregated atomics; the reference casts dummy rays instead,
+//                         MaterialKernel.cu:41-47,105-109)
+//   2. any_queue_kernel   persistent any hit over the primary shadow queue, scattered to the
+//                         (light, pixel) visibility slots
+//   3. bounce_kernel      persistent: bounce closest hit -> shading (throughput as mask) -> append
+//                         shadow rays
+//   4. any_queue_kernel   over the bounce shadow queue
+//   5. resolve_taa_kernel sum of lit contributions (primary lights, then bounce lights, in light
+//                         order: shadowLogicKernel, MaterialKernel.cu:361-388) and the TAA blend
+// Queue counts stay on the device; persistent kernels read them when they start, so a frame needs
+// no host synchronisation and can be captured in a CUDA graph.
+
+#include <cstring>
+#include <vector>
+
+#include "raygen.cuh"
+#include "runtime.cuh"
+#include "shading.cuh"
+#include "traverse.cuh"
+#include "wavefront.cuh"
+
+namespace phe_gb300 {
+
+constexpr int kWaveBlock = 128;
+
+__device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
+
+// Warp-aggregated append: every lane of `mask` calls it; lanes with pred get consecutive indices.
+__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred, uint32_t mask)
+{
+	uint32_t b = __ballot_sync(mask, pred);
+	if (b == 0) return 0xFFFFFFFFu;
+	uint32_t leader = (uint32_t)__ffs(b) - 1u;
+	uint32_t base = 0;
+	if (lane_id() == leader) base = atomicAdd(counter, (uint32_t)__popc(b));
+	base = __shfl_sync(mask, base, leader);
+	return base + (uint32_t)__popc(b & ((1u << lane_id()) - 1u));
+}
+
+__device__ __forceinline__ void store_ray(phe_ray_in* rays, uint32_t i, f3 o, float tMin, f3 d, float tMax)
+{
+	float4* p = reinterpret_cast<float4*>(rays + i);
+	p[0] = make_float4(o.x, o.y, o.z, tMin);
+	p[1] = make_float4(d.x, d.y, d.z, tMax);
+}
+
+// Shades one hit for every light and appends shadow rays. `stage` 0 = primary, 1 = bounce.
+__device__ __forceinline__ void shade_all_lights(const FrameParamsDev& fp, const FrameBuffers& fb, uint32_t stage,
+                                                 bool valid, const HitInfo& hi, f3 mask, f3 toCamera, DevPcg& rng,
+                                                 uint32_t pid)
+{
+	const uint32_t P = fp.numPixels;
+	const uint32_t L = fp.numLights;
+	uint32_t* queueCount = fb.counters + (stage == 0 ? kCtrShadow0 : kCtrShadow1);
+	phe_ray_in* qRays = fb.shadowRays + (size_t)stage * fb.capacityLP;
+	uint32_t* qSlots = fb.shadowSlots + (size_t)stage * fb.capacityLP;
+	for (uint32_t l = 0; l < L; l++) {
+		bool cast = false;
+		f3 sdir = mk3(0.0f, 0.0f, 0.0f);
+		float stmax = 0.0f;
+		f3 c = mk3(0.0f, 0.0f, 0.0f);
+		if (valid) c = shade_light(fp.lights[l], mask, hi, toCamera, rng, cast, sdir, stmax);
+		uint32_t slot = (stage * L + l) * P + pid;
+		uint32_t q = warp_append(queueCount, valid && cast, 0xFFFFFFFFu);
+		if (valid) {
+			fb.contrib[slot] = make_float4(c.x, c.y, c.z, 0.0f);
+			if (cast) {
+				store_ray(qRays, q, hi.pos, 0.001f, sdir, stmax);
+				qSlots[q] = slot;
+			} else {
+				fb.inLight[slot] = 1;   // the reference's dummy ray is never occluded
+			}
+		}
+	}
+}
+
+__global__ void __launch_bounds__(kWaveBlock) primary_kernel(DeviceScene s, const FrameParamsDev* __restrict__ fpp,
+                                                             FrameBuffers fb, uint32_t* __restrict__ status)
+{
+	const FrameParamsDev& fp = *fpp;
+	const uint32_t P = fp.numPixels, W = fp.resX, L = fp.numLights;
+	uint32_t* work = fb.counters + kCtrWork0;
+	for (;;) {
+		uint32_t base = 0;
+		if (lane_id() == 0) base = atomicAdd(work, 32u);
+		base = __shfl_sync(0xFFFFFFFFu, base, 0);
+		if (base >= P) break;
+		uint32_t i = base + lane_id();
+		bool active = i < P;
+		// 8x8-tile-major ray order (getRayIdx, CudaDeviceHelpers.cuh:49-62): coherent warps
+		uint32_t tile = i >> 6, within = i & 63u;
+		uint32_t tilesX = W >> 3;
+		uint32_t x = (tile % tilesX) * 8u + (within & 7u);
+		uint32_t y = (tile / tilesX) * 8u + (within >> 3);
+		uint32_t pid = y * W + x;
+		RayState r;
+		HitRecord h;
+		h.slot = ~0u;
+		if (active) {
+			f3 d = primary_dir(fp.cam, x, y, W, fp.resY, fp.jitter[0], fp.jitter[1]);
+			r.o = mk3(fp.cam.origin[0], fp.cam.origin[1], fp.cam.origin[2]);
+			r.d = d;
+			r.tMin = 0.0001f;
+			r.tMax = 3.402823466e+38f;
+			r.inv = mk3(__frcp_rn(d.x), __frcp_rn(d.y), __frcp_rn(d.z));
+			r.safe = isfinite(r.inv.x) && isfinite(r.inv.y) && isfinite(r.inv.z) && isfinite(d.x) && isfinite(d.y) &&
+			         isfinite(d.z) && isfinite(r.o.x) && isfinite(r.o.y) && isfinite(r.o.z);
+			h = empty_hit(r);
+			uint32_t err = trace<false>(s.nodes, s.tris, r, h);
+			if (err) atomicOr(status, err);
+		}
+		__syncwarp();
+		bool hit = active && h.slot != ~0u;
+		HitInfo hi;
+		DevPcg rng;
+		f3 toCamera = mk3(0.0f, 0.0f, 0.0f);
+		f3 camPos = mk3(fp.camPos[0], fp.camPos[1], fp.camPos[2]);
+		if (hit) {
+			hi = interpret_hit(s.datas, s.materials, r.o, r.d, h.slot, h.t, h.u, h.v);
+			pixel_stream(rng, fp.seed, fp.frame, pid, 0);
+			toCamera = normalize3(sub3(camPos, hi.pos));
+		} else {
+			hi.pos = hi.normal = hi.albedo = mk3(0.0f, 0.0f, 0.0f);
+			hi.alpha = hi.roughness = hi.metallic = 0.0f;
+		}
+		if (active) fb.roughness[pid] = hit ? hi.roughness : 0.0f;
+		shade_all_lights(fp, fb, 0, hit, hi, mk3(1.0f, 1.0f, 1.0f), toCamera, rng, pid);
+		// Bounce ray (one per hit) into the bounce queue.
+		float btMin = 0.001f;
+		f3 thr = mk3(0.0f, 0.0f, 0.0f), bdir = mk3(0.0f, 0.0f, 0.0f);
+		if (hit) bdir = sample_bounce(hi, camPos, rng, btMin, thr);
+		uint32_t q = warp_append(fb.counters + kCtrBounce, hit, 0xFFFFFFFFu);
+		if (hit) {
+			store_ray(fb.bounceRays, q, hi.pos, btMin, bdir, 3.402823466e+38f);
+			fb.bouncePixel[q] = pid;
+			fb.bounceThroughput[q] = make_float4(thr.x, thr.y, thr.z, 0.0f);
+		} else if (active) {
+			// no primary hit: nothing to add for this pixel in either stage
+			for (uint32_t l = 0; l < L; l++) {
+				fb.contrib[(size_t)l * P + pid] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+				fb.inLight[(size_t)l * P + pid] = 1;
+				fb.contrib[(size_t)(L + l) * P + pid] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+				fb.inLight[(size_t)(L + l) * P + pid] = 1;
+			}
+		}
+		__syncwarp();
+	}
+}
+
+__global__ void __launch_bounds__(kWaveBlock) any_queue_kernel(DeviceScene s, const phe_ray_in* __restrict__ rays,
+                                                               const uint32_t* __restrict__ slots,
+                                                               const uint32_t* __restrict__ count, uint8_t* __restrict__ inLight,
+                                                               uint32_t* __restrict__ work, uint32_t* __restrict__ status)
+{
+	const uint32_t n = *count;
+	for (;;) {
+		uint32_t base = 0;
+		if (lane_id() == 0) base = atomicAdd(work, 32u);
+		base = __shfl_sync(0xFFFFFFFFu, base, 0);
+		if (base >= n) break;
+		uint32_t i = base + lane_id();
+		if (i < n) {
+			RayState r = load_ray(rays, i);
+			HitRecord h = empty_hit(r);
+			uint32_t err = trace<true>(s.nodes, s.tris, r, h);
+			if (err) atomicOr(status, err);
+			inLight[__ldg(slots + i)] = h.slot == ~0u ? 1 : 0;
+		}
+		__syncwarp();
+	}
+}
+
+__global__ void __launch_bounds__(kWaveBlock) bounce_kernel(DeviceScene s, const FrameParamsDev* __restrict__ fpp,
+                                                            FrameBuffers fb, uint32_t* __restrict__ status)
+{
+	const FrameParamsDev& fp = *fpp;
+	const uint32_t P = fp.numPixels, L = fp.numLights;
+	const uint32_t n = fb.counters[kCtrBounce];
+	uint32_t* work = fb.counters + kCtrWork1;
+	for (;;) {
+		uint32_t base = 0;
+		if (lane_id() == 0) base = atomicAdd(work, 32u);
+		base = __shfl_sync(0xFFFFFFFFu, base, 0);
+		if (base >= n) break;
+		uint32_t i = base + lane_id();
+		bool active = i < n;
+		RayState r;
+		HitRecord h;
+		h.slot = ~0u;
+		uint32_t pid = 0;
+		f3 thr = mk3(0.0f, 0.0f, 0.0f);
+		if (active) {
+			r = load_ray(fb.bounceRays, i);
+			pid = fb.bouncePixel[i];
+			float4 t4 = fb.bounceThroughput[i];
+			thr = mk3(t4.x, t4.y, t4.z);
+			h = empty_hit(r);
+			uint32_t err = trace<false>(s.nodes, s.tris, r, h);
+			if (err) atomicOr(status, err);
+		}
+		__syncwarp();
+		bool hit = active && h.slot != ~0u;
+		HitInfo hi;
+		DevPcg rng;
+		f3 toCamera = mk3(0.0f, 0.0f, 0.0f);
+		if (hit) {
+			hi = interpret_hit(s.datas, s.materials, r.o, r.d, h.slot, h.t, h.u, h.v);
+			pixel_stream(rng, fp.seed, fp.frame, pid, 1);
+			toCamera = mk3(-r.d.x, -r.d.y, -r.d.z);
+		} else {
+			hi.pos = hi.normal = hi.albedo = mk3(0.0f, 0.0f, 0.0f);
+			hi.alpha = hi.roughness = hi.metallic = 0.0f;
+		}
+		shade_all_lights(fp, fb, 1, hit, hi, thr, toCamera, rng, pid);
+		if (active && !hit) {
+			for (uint32_t l = 0; l < L; l++) {
+				fb.contrib[(size_t)(L + l) * P + pid] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+				fb.inLight[(size_t)(L + l) * P + pid] = 1;
+			}
+		}
+		__syncwarp();
+	}
+}
+
+// TAA (taa.frag:25-71) with the history fetched in pixel space: (x + 0.5) - velocity * res.
+__device__ __forceinline__ float glsl_mix(float a, float b, float t)
+{
+	return __fadd_rn(__fmul_rn(a, __fsub_rn(1.0f, t)), __fmul_rn(b, t));
+}
+
+template <int CH>
+__device__ __forceinline__ void bilinear(const float* tex, uint32_t W, uint32_t H, float px, float py, float* out)
+{
+	float fx = __fsub_rn(px, 0.5f), fy = __fsub_rn(py, 0.5f);
+	float x0f = floorf(fx), y0f = floorf(fy);
+	float ax = __fsub_rn(fx, x0f), ay = __fsub_rn(fy, y0f);
+	long x0 = (long)x0f, y0 = (long)y0f, x1 = x0 + 1, y1 = y0 + 1;
+	long Wm = (long)W - 1, Hm = (long)H - 1;
+	x0 = x0 < 0 ? 0 : (x0 > Wm ? Wm : x0);
+	x1 = x1 < 0 ? 0 : (x1 > Wm ? Wm : x1);
+	y0 = y0 < 0 ? 0 : (y0 > Hm ? Hm : y0);
+	y1 = y1 < 0 ? 0 : (y1 > Hm ? Hm : y1);
+	for (int c = 0; c < CH; c++) {
+		float t00 = tex[((size_t)y0 * W + x0) * CH + c], t10 = tex[((size_t)y0 * W + x1) * CH + c];
+		float t01 = tex[((size_t)y1 * W + x0) * CH + c], t11 = tex[((size_t)y1 * W + x1) * CH + c];
+		out[c] = glsl_mix(glsl_mix(t00, t10, ax), glsl_mix(t01, t11, ax), ay);
+	}
+}
+
+__device__ __forceinline__ void taa_pixel(uint32_t x, uint32_t y, uint32_t W, uint32_t H, float4 cur,
+                                          const float4* __restrict__ hist, const float2* __restrict__ vel,
+                                          const float2* __restrict__ prevVel, float roughness, float4& outColor,
+                                          float4& outHist)
+{
+	size_t p = (size_t)y * W + x;
+	float vx = vel ? vel[p].x : 0.0f, vy = vel ? vel[p].y : 0.0f;
+	float hx = __fsub_rn(__fadd_rn((float)x, 0.5f), __fmul_rn(vx, (float)W));
+	float hy = __fsub_rn(__fadd_rn((float)y, 0.5f), __fmul_rn(vy, (float)H));
+	if (hx < 0.0f || hx > (float)W || hy < 0.0f || hy > (float)H) {
+		outHist = make_float4(cur.x, cur.y, cur.z, 1.0f);
+		outColor = make_float4(cur.x, cur.y, cur.z, 1.0f);
+		return;
+	}
+	bool still = vx == 0.0f && vy == 0.0f;
+	float hv[2] = {0.0f, 0.0f};
+	if (prevVel) {
+		if (still) { hv[0] = prevVel[p].x; hv[1] = prevVel[p].y; }
+		else bilinear<2>(reinterpret_cast<const float*>(prevVel), W, H, hx, hy, hv);
+	}
+	float pvx = __fmul_rn((float)W, vx), pvy = __fmul_rn((float)H, vy);
+	float hpx = __fmul_rn((float)W, hv[0]), hpy = __fmul_rn((float)H, hv[1]);
+	float lp = __fsqrt_rn(__fadd_rn(__fmul_rn(pvx, pvx), __fmul_rn(pvy, pvy)));
+	float lh = __fsqrt_rn(__fadd_rn(__fmul_rn(hpx, hpx), __fmul_rn(hpy, hpy)));
+	float velocityDistrust = fminf(1.0f, __fmul_rn(1.2f, __fsqrt_rn(fabsf(__fsub_rn(lp, lh)))));
+	float roughnessDistrust = glsl_mix(3.0f, 1.0f, roughness);
+	float trust = clampf(__fsub_rn(1.0f, __fmul_rn(roughnessDistrust, velocityDistrust)), 0.0f, 1.0f);
+	float h4[4];
+	if (still) {
+		float4 t = hist[p];
+		h4[0] = t.x; h4[1] = t.y; h4[2] = t.z; h4[3] = t.w;
+	} else {
+		bilinear<4>(reinterpret_cast<const float*>(hist), W, H, hx, hy, h4);
+	}
+	float newSamples = __fadd_rn(__fmul_rn(h4[3], trust), 1.0f);
+	float blend = __fsub_rn(1.0f, __fdiv_rn(1.0f, newSamples));
+	outHist = make_float4(glsl_mix(cur.x, h4[0], blend), glsl_mix(cur.y, h4[1], blend), glsl_mix(cur.z, h4[2], blend),
+	                      newSamples);
+	outColor = make_float4(outHist.x, outHist.y, outHist.z, 1.0f);
+}
+
+__global__ void resolve_taa_kernel(const FrameParamsDev* __restrict__ fpp, FrameBuffers fb)
+{
+	const FrameParamsDev& fp = *fpp;
+	uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+	uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
+	if (x >= fp.resX || y >= fp.resY) return;
+	const uint32_t P = fp.numPixels, L = fp.numLights;
+	uint32_t pid = y * fp.resX + x;
+	f3 acc = mk3(0.0f, 0.0f, 0.0f);
+	for (uint32_t k = 0; k < 2 * L; k++) {
+		size_t slot = (size_t)k * P + pid;
+		if (fb.inLight[slot]) {
+			float4 c = fb.contrib[slot];
+			acc = add3(acc, mk3(c.x, c.y, c.z));
+		}
+	}
+	float4 cur = make_float4(acc.x, acc.y, acc.z, 1.0f);
+	fb.rawColor[pid] = cur;
+	const float4* hin = fb.history[fp.parity];
+	float4* hout = fb.history[fp.parity ^ 1u];
+	float4 oc, oh;
+	taa_pixel(x, y, fp.resX, fp.resY, cur, hin, nullptr, nullptr, fb.roughness[pid], oc, oh);
+	fb.color[pid] = oc;
+	hout[pid] = oh;
+}
+
+__global__ void taa_kernel(uint32_t W, uint32_t H, const float4* __restrict__ cur, const float4* __restrict__ hist,
+                           const float2* __restrict__ vel, const float2* __restrict__ prevVel,
+                           const float* __restrict__ roughness, float4* __restrict__ outColor, float4* __restrict__ outHist)
+{
+	uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
+	uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
+	if (x >= W || y >= H) return;
+	size_t p = (size_t)y * W + x;
+	float4 oc, oh;
+	taa_pixel(x, y, W, H, cur[p], hist, vel, prevVel, roughness ? roughness[p] : 0.0f, oc, oh);
+	outColor[p] = oc;
+	outHist[p] = oh;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Launch sequence of one frame
+// ------------------------------------------------------------------------------------------------
+
+static int g_waveBlocksPerSM[3] = {0, 0, 0};
+
+static phe_status wave_grid(int which, const void* kernel, int* grid)
+{
+	DeviceInfo* d = nullptr;
+	phe_status st = device_info(&d);
+	if (st) return st;
+	if (g_waveBlocksPerSM[which] == 0) {
+		int b = 0;
+		PHE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, kWaveBlock, 0), "occupancy");
+		g_waveBlocksPerSM[which] = b > 0 ? b : 1;
+	}
+	*grid = g_waveBlocksPerSM[which] * d->numSMs;
+	return PHE_OK;
+}
+
+phe_status prepare_frame()
+{
+	int g;
+	phe_status st;
+	if ((st = wave_grid(0, (const void*)primary_kernel, &g))) return st;
+	if ((st = wave_grid(1, (const void*)any_queue_kernel, &g))) return st;
+	return wave_grid(2, (const void*)bounce_kernel, &g);
+}
+
+phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, const FrameBuffers& fb, uint32_t resX,
+                        uint32_t resY, cudaStream_t stream, cudaEvent_t* ev)
+{
+	phe_status st;
+	int g0 = 0, g1 = 0, g2 = 0;
+	if ((st = wave_grid(0, (const void*)primary_kernel, &g0))) return st;
+	if ((st = wave_grid(1, (const void*)any_queue_kernel, &g1))) return st;
+	if ((st = wave_grid(2, (const void*)bounce_kernel, &g2))) return st;
+	PHE_CUDA_TRY(cudaMemsetAsync(fb.counters, 0, sizeof(uint32_t) * kNumCounters, stream), "clear frame counters");
+	auto mark = [&](int i) { if (ev) cudaEventRecord(ev[i], stream); };
+	mark(0);
+	primary_kernel<<<g0, kWaveBlock, 0, stream>>>(scene->dev, dParams, fb, scene->status);
+	mark(1);
+	any_queue_kernel<<<g1, kWaveBlock, 0, stream>>>(scene->dev, fb.shadowRays, fb.shadowSlots, fb.counters + kCtrShadow0,
+	                                                fb.inLight, fb.counters + kCtrWork2, scene->status);
+	mark(2);
+	bounce_kernel<<<g2, kWaveBlock, 0, stream>>>(scene->dev, dParams, fb, scene->status);
+	mark(3);
+	any_queue_kernel<<<g1, kWaveBlock, 0, stream>>>(scene->dev, fb.shadowRays + fb.capacityLP,
+	                                                fb.shadowSlots + fb.capacityLP, fb.counters + kCtrShadow1, fb.inLight,
+	                                                fb.counters + kCtrWork3, scene->status);
+	mark(4);
+	dim3 block(16, 8);
+	dim3 grid((resX + 15) / 16, (resY + 7) / 8);
+	resolve_taa_kernel<<<grid, block, 0, stream>>>(dParams, fb);
+	mark(5);
+	PHE_CUDA_TRY(cudaGetLastError(), "frame kernel launch");
+	return PHE_OK;
+}
+
+} // namespace phe_gb300
+
+using namespace phe_gb300;
+
+extern "C" phe_status phe_taa_resolve(uint32_t resX, uint32_t resY, const float* cur, const float* hist,
+                                      const float* velocity, const float* prevVelocity, const float* roughness,
+                                      float* outColor, float* outHist, void* stream)
+{
+	if (!cur || !hist || !outColor || !outHist) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_taa_resolve: null buffer");
+	if (resX == 0 || resY == 0) return PHE_OK;
+	dim3 block(16, 8);
+	dim3 grid((resX + 15) / 16, (resY + 7) / 8);
+	taa_kernel<<<grid, block, 0, (cudaStream_t)stream>>>(resX, resY, (const float4*)cur, (const float4*)hist,
+	                                                     (const float2*)velocity, (const float2*)prevVelocity, roughness,
+	                                                     (float4*)outColor, (float4*)outHist);
+	PHE_CUDA_TRY(cudaGetLastError(), "taa_kernel launch");
+	return PHE_OK;
+}

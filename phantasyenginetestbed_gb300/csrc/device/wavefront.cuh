@@ -1,0 +1,63 @@
+// Frame state shared by the wavefront kernels (wavefront.cu) and the renderer object (renderer.cu).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+struct phe_scene;
+
+namespace phe_gb300 {
+
+constexpr uint32_t kMaxLights = 8;
+
+// Counters in device memory, cleared at the start of every frame.
+enum : uint32_t {
+	kCtrShadow0 = 0,  // primary shadow-queue length
+	kCtrBounce = 1,   // bounce-queue length
+	kCtrShadow1 = 2,  // bounce shadow-queue length
+	kCtrWork0 = 3,    // persistent work counters of the four traversal kernels
+	kCtrWork1 = 4,
+	kCtrWork2 = 5,
+	kCtrWork3 = 6,
+	kNumCounters = 8,
+};
+
+// Per-frame parameters, read by the kernels from device memory (so a captured graph replays
+// with new values after one small copy).
+struct FrameParamsDev {
+	phe_camera_def cam;      // jitter is applied in ray generation
+	float jitter[2];
+	float camPos[3];
+	uint32_t resX, resY, numPixels, numLights;
+	uint32_t frame, parity;  // frame index (random streams) and history ping-pong side
+	uint64_t seed;
+	phe_sphere_light lights[kMaxLights];
+};
+
+struct FrameBuffers {
+	float4* contrib;          // [2][L][P] light contributions (primary lights, then bounce lights)
+	uint8_t* inLight;         // [2][L][P] visibility of each contribution
+	phe_ray_in* shadowRays;   // [2][L*P] compacted shadow queues
+	uint32_t* shadowSlots;    // [2][L*P] visibility slot of each queued shadow ray
+	phe_ray_in* bounceRays;   // [P] compacted bounce queue
+	uint32_t* bouncePixel;    // [P]
+	float4* bounceThroughput; // [P]
+	float* roughness;         // [P] roughness at the primary hit (0 on a miss), read by TAA
+	float4* rawColor;         // [P] resolved colour before TAA
+	float4* history[2];       // [P] TAA history ping-pong (rgb + effective sample count)
+	float4* color;            // [P] TAA output
+	uint32_t* counters;       // [kNumCounters]
+	uint32_t capacityLP;      // L * P
+};
+
+// Resolves launch shapes (occupancy queries); call before capturing a frame into a graph.
+phe_status prepare_frame();
+// Number of kernels in a frame (primary, primary any-hit, bounce, bounce any-hit, resolve + TAA).
+constexpr int kFrameKernels = 5;
+// `events` (optional, kFrameKernels + 1 entries) are recorded on `stream` around each kernel.
+phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, const FrameBuffers& fb, uint32_t resX,
+                        uint32_t resY, cudaStream_t stream, cudaEvent_t* events = nullptr);
+
+} // namespace phe_gb300

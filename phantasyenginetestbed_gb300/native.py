@@ -58,6 +58,11 @@ class SbvhParams(C.Structure):
                 ("numThreads", C.c_int32)]
 
 
+class RenderResult(C.Structure):
+    _fields_ = [("resX", C.c_uint32), ("resY", C.c_uint32), ("color", C.c_void_p), ("history", C.c_void_p),
+                ("rawColor", C.c_void_p), ("roughness", C.c_void_p)]
+
+
 class PheError(RuntimeError):
     def __init__(self, status: int, where: str, text: str):
         super().__init__(f"{where}: status {status}: {text}")
@@ -94,6 +99,24 @@ SIGNATURES: dict[str, tuple] = {
     "phe_cast_closest_plain": (_I32, [_VP, _VP, _VP, _U32, _VP]),
     "phe_cast_any": (_I32, [_VP, _VP, _VP, _U32, _VP, _VP]),
     "phe_gen_primary_rays": (_I32, [_VP, C.POINTER(CameraDef), _U32, _U32, _F, _F, _I32, _VP]),
+    "phe_scene_status": (_I32, [_VP, C.POINTER(_U32)]),
+    "phe_renderer_create": (_I32, [C.POINTER(_VP)]),
+    "phe_renderer_destroy": (_I32, [_VP]),
+    "phe_renderer_set_static_scene": (_I32, [_VP, _VP]),
+    "phe_renderer_set_target_resolution": (_I32, [_VP, _U32, _U32]),
+    "phe_renderer_update_camera": (_I32, [_VP, _PF, _PF, _PF, _F, _F, _F]),
+    "phe_renderer_set_camera_def": (_I32, [_VP, C.POINTER(CameraDef), _PF, _F, _F]),
+    "phe_renderer_set_seed": (_I32, [_VP, C.c_uint64, _U32]),
+    "phe_renderer_set_graph": (_I32, [_VP, _I32]),
+    "phe_renderer_reset_taa": (_I32, [_VP, _VP]),
+    "phe_renderer_render": (_I32, [_VP, _VP, _U32, _VP]),
+    "phe_renderer_result": (_I32, [_VP, C.POINTER(RenderResult)]),
+    "phe_renderer_read": (_I32, [_VP, _I32, _VP, _VP]),
+    "phe_renderer_ray_counts": (_I32, [_VP, C.POINTER(C.c_uint64), _VP]),
+    "phe_renderer_set_kernel_timing": (_I32, [_VP, _I32]),
+    "phe_renderer_frame_param_bytes": (_U32, []),
+    "phe_renderer_kernel_times": (_I32, [_VP, C.POINTER(C.c_double), C.POINTER(_U32)]),
+    "phe_taa_resolve": (_I32, [_U32, _U32, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
 }
 
 _lib: C.CDLL | None = None

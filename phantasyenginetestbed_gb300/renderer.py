@@ -1,0 +1,129 @@
+"""CudaTracerRenderer: the headless renderer object over the C ABI (phe_renderer_*).
+
+Mirrors the reference's renderer entry points (phantasy_engine/rendering/BaseRenderer.hpp:56-90,
+cuda_ray_tracer/CudaTracerRenderer.hpp:14-58): setStaticScene, setTargetResolution, updateCamera,
+render. render() returns a RenderResult whose buffers are device pointers instead of GL textures.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import native as _n
+from .native import LIGHT_DTYPE, check, lib, ptr
+
+READ_COLOR, READ_HISTORY, READ_RAW, READ_ROUGHNESS = 0, 1, 2, 3
+
+
+@dataclass
+class RenderResult:
+    res: tuple
+    color: int
+    history: int
+    raw_color: int
+    roughness: int
+
+
+def _stream(stream):
+    if stream is None:
+        return None
+    return stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+
+
+class CudaTracerRenderer:
+    def __init__(self, use_graph: bool = False):
+        h = C.c_void_p()
+        check(lib().phe_renderer_create(C.byref(h)), "phe_renderer_create")
+        self.handle = h
+        self.res = (0, 0)
+        self.scene = None
+        if use_graph:
+            self.set_graph(True)
+
+    def setStaticScene(self, scene) -> None:
+        check(lib().phe_renderer_set_static_scene(self.handle, scene.handle), "phe_renderer_set_static_scene")
+        self.scene = scene
+
+    def setTargetResolution(self, res) -> None:
+        check(lib().phe_renderer_set_target_resolution(self.handle, int(res[0]), int(res[1])),
+              "phe_renderer_set_target_resolution")
+        self.res = (int(res[0]), int(res[1]))
+
+    def updateCamera(self, pos, direction, up, vfov_deg: float, pixel_offset=(0.0, 0.0)) -> None:
+        check(lib().phe_renderer_update_camera(self.handle, _n.fvec(pos), _n.fvec(direction), _n.fvec(up),
+                                               C.c_float(vfov_deg), C.c_float(pixel_offset[0]),
+                                               C.c_float(pixel_offset[1])), "phe_renderer_update_camera")
+
+    def set_camera_def(self, cam: _n.CameraDef, cam_pos, pixel_offset=(0.0, 0.0)) -> None:
+        check(lib().phe_renderer_set_camera_def(self.handle, C.byref(cam), _n.fvec(cam_pos), C.c_float(pixel_offset[0]),
+                                                C.c_float(pixel_offset[1])), "phe_renderer_set_camera_def")
+
+    def set_seed(self, seed: int, frame: int = 0) -> None:
+        check(lib().phe_renderer_set_seed(self.handle, seed, frame), "phe_renderer_set_seed")
+
+    def set_graph(self, enable: bool) -> None:
+        check(lib().phe_renderer_set_graph(self.handle, 1 if enable else 0), "phe_renderer_set_graph")
+
+    def resetTAA(self, stream=None) -> None:
+        check(lib().phe_renderer_reset_taa(self.handle, _stream(stream)), "phe_renderer_reset_taa")
+
+    def render(self, lights: np.ndarray, stream=None) -> RenderResult:
+        lights = np.ascontiguousarray(lights, LIGHT_DTYPE)
+        check(lib().phe_renderer_render(self.handle, ptr(lights) if len(lights) else None, len(lights), _stream(stream)),
+              "phe_renderer_render")
+        r = _n.RenderResult()
+        check(lib().phe_renderer_result(self.handle, C.byref(r)), "phe_renderer_result")
+        return RenderResult((r.resX, r.resY), r.color, r.history, r.rawColor, r.roughness)
+
+    def read(self, which: int = READ_COLOR, out: np.ndarray | None = None, stream=None) -> np.ndarray:
+        W, H = self.res
+        if out is None:
+            out = np.empty((H, W) if which == READ_ROUGHNESS else (H, W, 4), np.float32)
+        check(lib().phe_renderer_read(self.handle, which, ptr(out), _stream(stream)), "phe_renderer_read")
+        return out
+
+    def ray_counts(self, stream=None) -> np.ndarray:
+        c = (C.c_uint64 * 4)()
+        check(lib().phe_renderer_ray_counts(self.handle, c, _stream(stream)), "phe_renderer_ray_counts")
+        return np.array(list(c), np.uint64)
+
+    def set_kernel_timing(self, enable: bool) -> None:
+        check(lib().phe_renderer_set_kernel_timing(self.handle, 1 if enable else 0), "phe_renderer_set_kernel_timing")
+
+    def kernel_times(self):
+        """(summed ms per frame kernel, frames timed)."""
+        ms = (C.c_double * 5)()
+        n = C.c_uint32()
+        check(lib().phe_renderer_kernel_times(self.handle, ms, C.byref(n)), "phe_renderer_kernel_times")
+        return np.array(list(ms)), int(n.value)
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            check(lib().phe_renderer_destroy(self.handle), "phe_renderer_destroy")
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def make_lights(positions, strength=(20.0, 20.0, 20.0), range_=1000.0, radius=0.0) -> np.ndarray:
+    """Point lights (radius 0) with static shadows, as SphereLight (level/SphereLight.hpp:13-26)."""
+    pos = np.asarray(positions, np.float32).reshape(-1, 3)
+    L = np.zeros(len(pos), LIGHT_DTYPE)
+    L["pos"] = pos
+    L["radius"] = radius
+    L["range"] = range_
+    L["strength"] = strength
+    L["staticShadows"] = 1
+    return L
+
+
+def taa_resolve(res, cur, hist, out_color, out_hist, velocity=None, prev_velocity=None, roughness=None, stream=None):
+    """TAA resolve on device buffers (phe_taa_resolve)."""
+    check(lib().phe_taa_resolve(int(res[0]), int(res[1]), ptr(cur), ptr(hist), ptr(velocity), ptr(prev_velocity),
+                                ptr(roughness), ptr(out_color), ptr(out_hist), _stream(stream)), "phe_taa_resolve")

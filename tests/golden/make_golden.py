@@ -27,7 +27,7 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 ROOT = HERE.parents[1]
-sys.path.insert(0, str(ROOT))
+sys.path[0] = str(ROOT)
 
 import phantasyenginetestbed_gb300 as P  # noqa: E402
 from oracle import oracle as O  # noqa: E402
