@@ -199,6 +199,48 @@ phe_status phe_gen_primary_rays(phe_ray_in* rays, const phe_camera_def* cam, uin
 phe_status phe_scene_status(const phe_scene* scene, uint32_t* bits);
 
 /* ---------------------------------------------------------------------------------------------
+ * Batched multi-scene casting (no reference counterpart: the reference launches and synchronises
+ * once per batch, RayCastKernel.cu:806-886). Many batches of uneven size over several resident
+ * scenes, closest and any hit mixed, run in ONE persistent launch, replayed from a CUDA graph.
+ * ------------------------------------------------------------------------------------------- */
+#define PHE_QUERY_CLOSEST 0
+#define PHE_QUERY_ANY 1
+#define PHE_BATCH_ORDER_GIVEN 0
+#define PHE_BATCH_ORDER_LARGEST_FIRST 1
+typedef struct phe_batch phe_batch;
+typedef struct phe_batch_item {
+	uint32_t scene;          /* index into the scene list given to phe_batch_create */
+	uint32_t kind;           /* PHE_QUERY_CLOSEST (out: phe_ray_hit[count]) or PHE_QUERY_ANY (out: uint8_t[count]) */
+	uint32_t count;
+	uint32_t pad;
+	const phe_ray_in* rays;  /* device */
+	void* out;               /* device */
+} phe_batch_item;
+typedef struct phe_batch_params {
+	int32_t blockSize;       /* 64, 128 or 256 threads */
+	int32_t blocksPerSM;     /* resident blocks per SM (0 = occupancy limit) */
+	int32_t order;           /* PHE_BATCH_ORDER_* */
+	int32_t useGraph;        /* 1 = replay from a CUDA graph captured on first launch */
+} phe_batch_params;
+typedef struct phe_batch_tuning_row { phe_batch_params params; float ms; } phe_batch_tuning_row;
+void phe_batch_default_params(phe_batch_params* params);
+/* The batch keeps the scene handles and the item table (device buffers stay owned by the caller). */
+phe_status phe_batch_create(const phe_scene* const* scenes, uint32_t numScenes, const phe_batch_item* items,
+                            uint32_t numItems, const phe_batch_params* params, phe_batch** out);
+/* New buffers / counts for the same number of items (the captured graph is rebuilt on next launch). */
+phe_status phe_batch_update(phe_batch* batch, const phe_batch_item* items, uint32_t numItems);
+phe_status phe_batch_set_params(phe_batch* batch, const phe_batch_params* params);
+/* One persistent launch over every item, asynchronous on `stream`. */
+phe_status phe_batch_launch(phe_batch* batch, void* stream);
+phe_status phe_batch_info(const phe_batch* batch, uint64_t* totalRays, uint32_t* paddedRays);
+/* Times every candidate (block size x batch order x occupancy) `repeats` times on this batch with
+ * CUDA events on `stream`, sets the fastest on the batch and returns it; `rows` (optional) receives
+ * every candidate's time. Synchronous. */
+phe_status phe_batch_autotune(phe_batch* batch, int repeats, void* stream, phe_batch_params* best, float* bestMs,
+                              phe_batch_tuning_row* rows, uint32_t maxRows, uint32_t* numRows);
+phe_status phe_batch_destroy(phe_batch* batch);
+
+/* ---------------------------------------------------------------------------------------------
  * Wavefront renderer (CudaTracerRenderer, cuda_ray_tracer/CudaTracerRenderer.hpp:14-58, and the
  * BaseRenderer entry points, phantasy_engine/rendering/BaseRenderer.hpp:56-90)
  *

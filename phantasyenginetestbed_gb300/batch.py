@@ -1,0 +1,83 @@
+"""Batched multi-scene casting over the C ABI (phe_batch_*): many ray batches of uneven size over
+several resident scenes, closest and any hit mixed, in one persistent launch replayed from a CUDA
+graph, with launch parameters chosen by the autotuner."""
+from __future__ import annotations
+
+import ctypes as C
+import json
+
+from . import native as _n
+from .native import check, lib, ptr
+
+CLOSEST, ANY = 0, 1
+ORDER_GIVEN, ORDER_LARGEST_FIRST = 0, 1
+
+
+def _stream(stream):
+    if stream is None:
+        return None
+    return stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+
+
+class Batch:
+    def __init__(self, scenes, items, block_size=128, blocks_per_sm=0, order=ORDER_GIVEN, use_graph=True):
+        """scenes: list of Scene; items: list of (scene index, kind, count, device rays, device out)."""
+        self.scenes = list(scenes)
+        arr = (C.c_void_p * len(scenes))(*[s.handle.value for s in scenes])
+        self._items = self._table(items)
+        p = _n.BatchParams(block_size, blocks_per_sm, order, 1 if use_graph else 0)
+        h = C.c_void_p()
+        check(lib().phe_batch_create(arr, len(scenes), self._items, len(items), C.byref(p), C.byref(h)), "phe_batch_create")
+        self.handle = h
+
+    @staticmethod
+    def _table(items):
+        t = (_n.BatchItem * max(1, len(items)))()
+        for i, (scene, kind, count, rays, out) in enumerate(items):
+            t[i] = _n.BatchItem(scene, kind, count, 0, ptr(rays), ptr(out))
+        return t
+
+    def update(self, items) -> None:
+        self._items = self._table(items)
+        check(lib().phe_batch_update(self.handle, self._items, len(items)), "phe_batch_update")
+
+    def set_params(self, block_size=128, blocks_per_sm=0, order=ORDER_GIVEN, use_graph=True) -> None:
+        p = _n.BatchParams(block_size, blocks_per_sm, order, 1 if use_graph else 0)
+        check(lib().phe_batch_set_params(self.handle, C.byref(p)), "phe_batch_set_params")
+
+    def launch(self, stream=None) -> None:
+        check(lib().phe_batch_launch(self.handle, _stream(stream)), "phe_batch_launch")
+
+    def info(self):
+        t, p = C.c_uint64(), C.c_uint32()
+        check(lib().phe_batch_info(self.handle, C.byref(t), C.byref(p)), "phe_batch_info")
+        return int(t.value), int(p.value)
+
+    def autotune(self, repeats=3, stream=None):
+        """Returns (best params dict, best ms, all candidate rows)."""
+        best = _n.BatchParams()
+        ms = C.c_float()
+        rows = (_n.BatchTuningRow * 64)()
+        n = C.c_uint32()
+        check(lib().phe_batch_autotune(self.handle, repeats, _stream(stream), C.byref(best), C.byref(ms), rows, 64,
+                                       C.byref(n)), "phe_batch_autotune")
+        as_dict = lambda p: {"blockSize": p.blockSize, "blocksPerSM": p.blocksPerSM, "order": p.order,
+                             "useGraph": p.useGraph}
+        table = [dict(as_dict(rows[i].params), ms=rows[i].ms) for i in range(min(n.value, 64))]
+        return as_dict(best), float(ms.value), table
+
+    def close(self) -> None:
+        if getattr(self, "handle", None):
+            check(lib().phe_batch_destroy(self.handle), "phe_batch_destroy")
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def save_tuning(path, best, ms, table) -> None:
+    with open(path, "w") as f:
+        json.dump({"best": best, "best_ms": ms, "candidates": table}, f, indent=1)

@@ -1,0 +1,396 @@
+// Batched multi-scene ray casting: many ray batches of uneven sizes over several resident scenes,
+// closest-hit and any-hit mixed, in ONE persistent launch (replayed from a CUDA graph). The
+// reference has no counterpart: it launches one kernel per batch and synchronises the device after
+// each (RayCastKernel.cu:806-886).
+//
+// Work layout: batch i owns the global ray indices [base_i, base_i + count_i) with every base a
+// multiple of 32, so a warp's 32-ray fetch never straddles two batches: scene, query kind and
+// buffers are warp-uniform. Warps take 32-ray chunks from one atomic counter; the batch of a chunk
+// is found by binary search over the bases.
+//
+// Launch parameters (block size, resident blocks per SM, batch order) come from phe_batch_params,
+// which the autotuner (phe_batch_autotune) picks by timing candidates on the actual batch mix.
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+#include "runtime.cuh"
+#include "traverse.cuh"
+
+namespace phe_gb300 {
+
+struct BatchItemDev {
+	uint32_t scene, kind, count, base;
+	const phe_ray_in* rays;
+	void* out;
+};
+static_assert(sizeof(BatchItemDev) == 32, "BatchItemDev is 32 bytes");
+
+struct BatchTableDev {
+	const BatchItemDev* items;
+	const DeviceScene* scenes;
+	uint32_t numItems;
+	uint32_t totalPadded;
+};
+
+__device__ __forceinline__ uint32_t find_item(const BatchItemDev* __restrict__ items, uint32_t n, uint32_t g)
+{
+	uint32_t lo = 0, hi = n;  // largest i with base_i <= g
+	while (hi - lo > 1) {
+		uint32_t mid = (lo + hi) >> 1;
+		if (__ldg(&items[mid].base) <= g) lo = mid;
+		else hi = mid;
+	}
+	return lo;
+}
+
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK) batch_kernel(BatchTableDev t, uint32_t* __restrict__ counter,
+                                                      uint32_t* __restrict__ status)
+{
+	const uint32_t lane = threadIdx.x & 31u;
+	for (;;) {
+		uint32_t g = 0;
+		if (lane == 0) g = atomicAdd(counter, 32u);
+		g = __shfl_sync(0xFFFFFFFFu, g, 0);
+		if (g >= t.totalPadded) break;
+		uint32_t it = find_item(t.items, t.numItems, g);
+		const BatchItemDev item = t.items[it];
+		uint32_t i = g - item.base + lane;
+		if (i < item.count) {
+			const DeviceScene s = t.scenes[item.scene];
+			RayState r = load_ray(item.rays, i);
+			HitRecord h = empty_hit(r);
+			uint32_t err;
+			if (item.kind == 0) {
+				err = trace<false>(s.nodes, s.tris, r, h);
+				store_hit((phe_ray_hit*)item.out, i, r, h);
+			} else {
+				err = trace<true>(s.nodes, s.tris, r, h);
+				((uint8_t*)item.out)[i] = h.slot == ~0u ? 1 : 0;
+			}
+			if (err) atomicOr(status, err);
+		}
+		__syncwarp();
+	}
+}
+
+template <int BLOCK>
+static phe_status launch_batch_kernel(const BatchTableDev& t, int blocksPerSM, int numSMs, uint32_t* counter,
+                                      uint32_t* status, cudaStream_t stream, int* occupancyOut)
+{
+	int maxB = 0;
+	PHE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxB, batch_kernel<BLOCK>, BLOCK, 0), "occupancy");
+	if (occupancyOut) {
+		*occupancyOut = maxB;
+		return PHE_OK;
+	}
+	int b = blocksPerSM > 0 ? std::min(blocksPerSM, maxB) : maxB;
+	if (b < 1) b = 1;
+	uint32_t grid = (uint32_t)(b * numSMs);
+	uint32_t need = (t.totalPadded + BLOCK - 1) / BLOCK;
+	if (grid > need) grid = need > 0 ? need : 1;
+	batch_kernel<BLOCK><<<grid, BLOCK, 0, stream>>>(t, counter, status);
+	PHE_CUDA_TRY(cudaGetLastError(), "batch_kernel launch");
+	return PHE_OK;
+}
+
+} // namespace phe_gb300
+
+using namespace phe_gb300;
+
+struct phe_batch {
+	std::vector<phe_batch_item> items;     // as given
+	std::vector<uint32_t> order;           // launch order of the items
+	std::vector<DeviceScene> scenes;
+	std::vector<const phe_scene*> sceneHandles;
+	phe_batch_params params{};
+	void* allocation = nullptr;            // items table + scene table + counter + status
+	BatchItemDev* dItems = nullptr;
+	DeviceScene* dScenes = nullptr;
+	uint32_t* dCounter = nullptr;
+	uint32_t* dStatus = nullptr;
+	uint32_t totalPadded = 0;
+	uint64_t totalRays = 0;
+	cudaGraphExec_t graph = nullptr;
+};
+
+static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+extern "C" void phe_batch_default_params(phe_batch_params* p)
+{
+	if (!p) return;
+	std::memset(p, 0, sizeof(*p));
+	p->blockSize = 128;
+	p->blocksPerSM = 0;
+	p->order = PHE_BATCH_ORDER_GIVEN;
+	p->useGraph = 1;
+}
+
+static phe_status upload_table(phe_batch* b)
+{
+	// Launch order.
+	const size_t n = b->items.size();
+	b->order.resize(n);
+	for (size_t i = 0; i < n; i++) b->order[i] = (uint32_t)i;
+	if (b->params.order == PHE_BATCH_ORDER_LARGEST_FIRST) {
+		// Estimated cost: rays x log2(scene size); heavy batches first so the tail is made of small ones.
+		auto cost = [&](uint32_t i) {
+			const phe_batch_item& it = b->items[i];
+			double tri = (double)b->scenes[it.scene].numSlots;
+			return (double)it.count * std::log2(tri + 2.0) * (it.kind == PHE_QUERY_ANY ? 0.6 : 1.0);
+		};
+		std::stable_sort(b->order.begin(), b->order.end(), [&](uint32_t a, uint32_t c) { return cost(a) > cost(c); });
+	}
+	std::vector<BatchItemDev> dev(n);
+	uint32_t base = 0;
+	uint64_t total = 0;
+	for (size_t k = 0; k < n; k++) {
+		const phe_batch_item& it = b->items[b->order[k]];
+		dev[k].scene = it.scene;
+		dev[k].kind = it.kind;
+		dev[k].count = it.count;
+		dev[k].base = base;
+		dev[k].rays = it.rays;
+		dev[k].out = it.out;
+		uint64_t next = (uint64_t)base + ((uint64_t)it.count + 31u) / 32u * 32u;
+		if (next > 0xFFFFFFF0ull) return fail(PHE_ERR_TOO_LARGE, "batch: more than 2^32 rays in one launch");
+		base = (uint32_t)next;
+		total += it.count;
+	}
+	b->totalPadded = base;
+	b->totalRays = total;
+	PHE_CUDA_TRY(cudaMemcpy(b->dItems, dev.data(), n * sizeof(BatchItemDev), cudaMemcpyHostToDevice), "upload batch table");
+	if (b->graph) {
+		cudaGraphExecDestroy(b->graph);
+		b->graph = nullptr;
+	}
+	return PHE_OK;
+}
+
+static phe_status check_items(const phe_batch_item* items, uint32_t numItems, uint32_t numScenes)
+{
+	for (uint32_t i = 0; i < numItems; i++) {
+		const phe_batch_item& it = items[i];
+		if (it.scene >= numScenes) return fail(PHE_ERR_NOT_FOUND, "batch item %u: scene %u out of range", i, it.scene);
+		if (it.kind != PHE_QUERY_CLOSEST && it.kind != PHE_QUERY_ANY)
+			return fail(PHE_ERR_INVALID_ARGUMENT, "batch item %u: kind must be closest or any", i);
+		if (it.count && (!it.rays || !it.out)) return fail(PHE_ERR_INVALID_ARGUMENT, "batch item %u: null buffer", i);
+		if (((uintptr_t)it.rays & 15u) || (it.kind == PHE_QUERY_CLOSEST && ((uintptr_t)it.out & 15u)))
+			return fail(PHE_ERR_INVALID_ARGUMENT, "batch item %u: buffers must be 16-byte aligned", i);
+	}
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_batch_create(const phe_scene* const* scenes, uint32_t numScenes, const phe_batch_item* items,
+                                       uint32_t numItems, const phe_batch_params* params, phe_batch** out)
+{
+	if (!out || !scenes || numScenes == 0 || (!items && numItems))
+		return fail(PHE_ERR_INVALID_ARGUMENT, "phe_batch_create: null argument");
+	*out = nullptr;
+	for (uint32_t i = 0; i < numScenes; i++)
+		if (!scenes[i]) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_batch_create: scene %u is null", i);
+	phe_status st = check_items(items, numItems, numScenes);
+	if (st) return st;
+	DeviceInfo* d = nullptr;
+	if ((st = device_info(&d))) return st;
+	phe_batch* b = new phe_batch();
+	if (params) b->params = *params;
+	else phe_batch_default_params(&b->params);
+	b->items.assign(items, items + numItems);
+	for (uint32_t i = 0; i < numScenes; i++) {
+		b->scenes.push_back(scenes[i]->dev);
+		b->sceneHandles.push_back(scenes[i]);
+	}
+	size_t itemBytes = align256(std::max<size_t>(1, numItems) * sizeof(BatchItemDev));
+	size_t sceneBytes = align256(numScenes * sizeof(DeviceScene));
+	char* base = nullptr;
+	cudaError_t e = cudaMalloc(&base, itemBytes + sceneBytes + 256);
+	if (e != cudaSuccess) {
+		delete b;
+		return cuda_fail(e, "cudaMalloc(batch)");
+	}
+	b->allocation = base;
+	b->dItems = (BatchItemDev*)base;
+	b->dScenes = (DeviceScene*)(base + itemBytes);
+	b->dCounter = (uint32_t*)(base + itemBytes + sceneBytes);
+	b->dStatus = b->dCounter + 1;
+	cudaMemset(b->dCounter, 0, 256);
+	e = cudaMemcpy(b->dScenes, b->scenes.data(), numScenes * sizeof(DeviceScene), cudaMemcpyHostToDevice);
+	if (e != cudaSuccess) {
+		cudaFree(base);
+		delete b;
+		return cuda_fail(e, "upload scene table");
+	}
+	if ((st = upload_table(b))) {
+		cudaFree(base);
+		delete b;
+		return st;
+	}
+	*out = b;
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_batch_update(phe_batch* b, const phe_batch_item* items, uint32_t numItems)
+{
+	if (!b || (!items && numItems)) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_batch_update: null argument");
+	if (numItems != b->items.size()) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_batch_update: item count changed");
+	phe_status st = check_items(items, numItems, (uint32_t)b->scenes.size());
+	if (st) return st;
+	b->items.assign(items, items + numItems);
+	return upload_table(b);
+}
+
+static phe_status batch_enqueue(phe_batch* b, cudaStream_t stream)
+{
+	DeviceInfo* d = nullptr;
+	phe_status st = device_info(&d);
+	if (st) return st;
+	BatchTableDev t{b->dItems, b->dScenes, (uint32_t)b->items.size(), b->totalPadded};
+	PHE_CUDA_TRY(cudaMemsetAsync(b->dCounter, 0, sizeof(uint32_t), stream), "clear batch counter");
+	if (b->totalPadded == 0) return PHE_OK;
+	switch (b->params.blockSize) {
+	case 64: return launch_batch_kernel<64>(t, b->params.blocksPerSM, d->numSMs, b->dCounter, b->dStatus, stream, nullptr);
+	case 256: return launch_batch_kernel<256>(t, b->params.blocksPerSM, d->numSMs, b->dCounter, b->dStatus, stream, nullptr);
+	case 128: return launch_batch_kernel<128>(t, b->params.blocksPerSM, d->numSMs, b->dCounter, b->dStatus, stream, nullptr);
+	default: return fail(PHE_ERR_INVALID_ARGUMENT, "batch block size must be 64, 128 or 256");
+	}
+}
+
+extern "C" phe_status phe_batch_launch(phe_batch* b, void* stream)
+{
+	if (!b) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_batch_launch: null batch");
+	cudaStream_t s = (cudaStream_t)stream;
+	if (!b->params.useGraph) return batch_enqueue(b, s);
+	if (!b->graph) {
+		// Resolve occupancy outside capture.
+		int occ = 0;
+		BatchTableDev t{};
+		switch (b->params.blockSize) {
+		case 64: launch_batch_kernel<64>(t, 0, 1, nullptr, nullptr, nullptr, &occ); break;
+		case 256: launch_batch_kernel<256>(t, 0, 1, nullptr, nullptr, nullptr, &occ); break;
+		default: launch_batch_kernel<128>(t, 0, 1, nullptr, nullptr, nullptr, &occ); break;
+		}
+		cudaStream_t cap = nullptr;
+		PHE_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), "create capture stream");
+		cudaGraph_t g = nullptr;
+		cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+		phe_status st = PHE_OK;
+		if (e == cudaSuccess) {
+			st = batch_enqueue(b, cap);
+			e = cudaStreamEndCapture(cap, &g);
+		}
+		cudaStreamDestroy(cap);
+		if (st) { if (g) cudaGraphDestroy(g); return st; }
+		if (e != cudaSuccess) return cuda_fail(e, "capture batch graph");
+		e = cudaGraphInstantiate(&b->graph, g, 0);
+		cudaGraphDestroy(g);
+		if (e != cudaSuccess) return cuda_fail(e, "instantiate batch graph");
+	}
+	PHE_CUDA_TRY(cudaGraphLaunch(b->graph, s), "launch batch graph");
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_batch_set_params(phe_batch* b, const phe_batch_params* params)
+{
+	if (!b || !params) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_batch_set_params: null argument");
+	if (params->blockSize != 64 && params->blockSize != 128 && params->blockSize != 256)
+		return fail(PHE_ERR_INVALID_ARGUMENT, "batch block size must be 64, 128 or 256");
+	b->params = *params;
+	return upload_table(b);
+}
+
+extern "C" phe_status phe_batch_info(const phe_batch* b, uint64_t* totalRays, uint32_t* paddedRays)
+{
+	if (!b) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_batch_info: null batch");
+	if (totalRays) *totalRays = b->totalRays;
+	if (paddedRays) *paddedRays = b->totalPadded;
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_batch_destroy(phe_batch* b)
+{
+	if (!b) return PHE_OK;
+	if (b->graph) cudaGraphExecDestroy(b->graph);
+	cudaFree(b->allocation);
+	delete b;
+	return PHE_OK;
+}
+
+// ------------------------------------------------------------------------------------------------
+// Autotuner: times every candidate launch configuration on the batch as given (after a warm-up
+// launch each) with CUDA events on `stream`, keeps the fastest, and leaves it set on the batch.
+// ------------------------------------------------------------------------------------------------
+
+extern "C" phe_status phe_batch_autotune(phe_batch* b, int repeats, void* stream, phe_batch_params* best,
+                                         float* bestMs, phe_batch_tuning_row* rows, uint32_t maxRows, uint32_t* numRows)
+{
+	if (!b) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_batch_autotune: null batch");
+	if (repeats < 1) repeats = 3;
+	cudaStream_t s = (cudaStream_t)stream;
+	DeviceInfo* d = nullptr;
+	phe_status st = device_info(&d);
+	if (st) return st;
+	const int blocks[] = {64, 128, 256};
+	const int orders[] = {PHE_BATCH_ORDER_GIVEN, PHE_BATCH_ORDER_LARGEST_FIRST};
+	const int occFrac[] = {4, 3, 2};  // quarters of the occupancy limit: 4/4, 3/4, 2/4
+	cudaEvent_t e0, e1;
+	PHE_CUDA_TRY(cudaEventCreate(&e0), "cudaEventCreate");
+	PHE_CUDA_TRY(cudaEventCreate(&e1), "cudaEventCreate");
+	phe_batch_params saved = b->params;
+	phe_batch_params winner = saved;
+	float winnerMs = 1e30f;
+	uint32_t n = 0;
+	for (int bs : blocks) {
+		int occ = 0;
+		BatchTableDev t{};
+		if (bs == 64) launch_batch_kernel<64>(t, 0, 1, nullptr, nullptr, nullptr, &occ);
+		else if (bs == 128) launch_batch_kernel<128>(t, 0, 1, nullptr, nullptr, nullptr, &occ);
+		else launch_batch_kernel<256>(t, 0, 1, nullptr, nullptr, nullptr, &occ);
+		for (int ord : orders)
+			for (int q : occFrac) {
+				phe_batch_params p = saved;
+				p.blockSize = bs;
+				p.order = ord;
+				p.blocksPerSM = std::max(1, occ * q / 4);
+				p.useGraph = 0;
+				b->params = p;
+				if ((st = upload_table(b))) goto done;
+				if ((st = batch_enqueue(b, s))) goto done;  // warm-up
+				cudaEventRecord(e0, s);
+				for (int r = 0; r < repeats; r++)
+					if ((st = batch_enqueue(b, s))) goto done;
+				cudaEventRecord(e1, s);
+				PHE_CUDA_TRY(cudaEventSynchronize(e1), "autotune sync");
+				float ms = 0;
+				cudaEventElapsedTime(&ms, e0, e1);
+				ms /= (float)repeats;
+				if (rows && n < maxRows) {
+					rows[n].params = p;
+					rows[n].ms = ms;
+				}
+				n++;
+				if (ms < winnerMs) {
+					winnerMs = ms;
+					winner = p;
+				}
+			}
+	}
+done:
+	cudaEventDestroy(e0);
+	cudaEventDestroy(e1);
+	if (st) {
+		b->params = saved;
+		upload_table(b);
+		return st;
+	}
+	winner.useGraph = saved.useGraph;
+	b->params = winner;
+	if ((st = upload_table(b))) return st;
+	if (best) *best = winner;
+	if (bestMs) *bestMs = winnerMs;
+	if (numRows) *numRows = n;
+	return PHE_OK;
+}

@@ -63,6 +63,19 @@ class RenderResult(C.Structure):
                 ("rawColor", C.c_void_p), ("roughness", C.c_void_p)]
 
 
+class BatchItem(C.Structure):
+    _fields_ = [("scene", C.c_uint32), ("kind", C.c_uint32), ("count", C.c_uint32), ("pad", C.c_uint32),
+                ("rays", C.c_void_p), ("out", C.c_void_p)]
+
+
+class BatchParams(C.Structure):
+    _fields_ = [("blockSize", C.c_int32), ("blocksPerSM", C.c_int32), ("order", C.c_int32), ("useGraph", C.c_int32)]
+
+
+class BatchTuningRow(C.Structure):
+    _fields_ = [("params", BatchParams), ("ms", C.c_float)]
+
+
 class PheError(RuntimeError):
     def __init__(self, status: int, where: str, text: str):
         super().__init__(f"{where}: status {status}: {text}")
@@ -116,6 +129,15 @@ SIGNATURES: dict[str, tuple] = {
     "phe_renderer_set_kernel_timing": (_I32, [_VP, _I32]),
     "phe_renderer_frame_param_bytes": (_U32, []),
     "phe_renderer_kernel_times": (_I32, [_VP, C.POINTER(C.c_double), C.POINTER(_U32)]),
+    "phe_batch_default_params": (None, [C.POINTER(BatchParams)]),
+    "phe_batch_create": (_I32, [C.POINTER(_VP), _U32, C.POINTER(BatchItem), _U32, C.POINTER(BatchParams), C.POINTER(_VP)]),
+    "phe_batch_update": (_I32, [_VP, C.POINTER(BatchItem), _U32]),
+    "phe_batch_set_params": (_I32, [_VP, C.POINTER(BatchParams)]),
+    "phe_batch_launch": (_I32, [_VP, _VP]),
+    "phe_batch_info": (_I32, [_VP, C.POINTER(C.c_uint64), C.POINTER(_U32)]),
+    "phe_batch_autotune": (_I32, [_VP, _I32, _VP, C.POINTER(BatchParams), C.POINTER(C.c_float),
+                                  C.POINTER(BatchTuningRow), _U32, C.POINTER(_U32)]),
+    "phe_batch_destroy": (_I32, [_VP]),
     "phe_taa_resolve": (_I32, [_U32, _U32, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
 }
 

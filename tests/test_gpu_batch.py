@@ -1,0 +1,105 @@
+"""Batched multi-scene persistent launch: every batch's result equals the oracle (closest-hit parity
+rule / any-hit bit-exact) and equals the same batch cast alone with the plain per-batch launch, for
+every autotuner candidate and with graph replay."""
+import numpy as np
+import pytest
+
+import phantasyenginetestbed_gb300 as P
+from phantasyenginetestbed_gb300.batch import ANY, CLOSEST, ORDER_LARGEST_FIRST, Batch
+from oracle import oracle as O
+from tests.helpers import device_empty, from_device, random_rays, to_device
+
+pytestmark = pytest.mark.gpu
+
+
+def _scenes():
+    out = []
+    for args in [(16, 10, False, 51), (40, 30, True, 52), (64, 80, False, 53)]:
+        s = P.generate_scene(*args)
+        b = P.build_sbvh(s.tri_verts)
+        out.append((s, b, P.Scene(b.nodes, b.verts)))
+    return out
+
+
+def _mix(scenes, sizes, seed):
+    rng = np.random.default_rng(seed)
+    items, host = [], []
+    for i, n in enumerate(sizes):
+        si = int(rng.integers(0, len(scenes)))
+        kind = CLOSEST if rng.random() < 0.7 else ANY
+        s = scenes[si][0]
+        rays = random_rays(int(n), [0, 0, 0.02], [s.scale, s.scale, 0.4 * s.scale], seed * 100 + i)
+        if kind == ANY:
+            rays["tMax"] = np.float32(0.5 * s.scale)
+        d_rays = to_device(rays)
+        d_out = device_empty(int(n), P.RAY_HIT_DTYPE if kind == CLOSEST else np.uint8)
+        items.append((si, kind, int(n), d_rays, d_out))
+        host.append((si, kind, rays))
+    return items, host
+
+
+def _check(scenes, items, host):
+    import torch
+    torch.cuda.synchronize()
+    for (si, kind, n, d_rays, d_out), (_, _, rays) in zip(items, host):
+        s, b, _ = scenes[si]
+        if kind == CLOSEST:
+            got = from_device(d_out, P.RAY_HIT_DTYPE)
+            rep = O.compare_closest(got, O.cast_rays(b.nodes, b.verts, rays), rays, b.slot_to_tri, b.verts)
+            assert rep["ok"] and rep["near_ties"] <= 2, rep
+        else:
+            assert np.array_equal(from_device(d_out, np.uint8), O.any_rays(b.nodes, b.verts, rays))
+
+
+def test_batched_launch_matches_oracle_and_plain():
+    import torch
+    scenes = _scenes()
+    sizes = [1, 31, 32, 33, 1000, 5000, 17, 64, 20000, 3, 4096, 777]
+    items, host = _mix(scenes, sizes, 3)
+    batch = Batch([x[2] for x in scenes], items, use_graph=False)
+    total, padded = batch.info()
+    assert total == sum(sizes) and padded % 32 == 0 and padded >= total
+    batch.launch()
+    _check(scenes, items, host)
+    # graph replay, other parameters
+    for zero in items:
+        zero[4].zero_()
+    batch.set_params(block_size=256, order=ORDER_LARGEST_FIRST, use_graph=True)
+    batch.launch()
+    batch.launch()
+    _check(scenes, items, host)
+    # plain per-batch launches give the same bytes
+    torch.cuda.synchronize()
+    snapshot = [from_device(it[4], np.uint8).copy() for it in items]
+    for (si, kind, n, d_rays, d_out) in items:
+        if kind == CLOSEST:
+            P.cast_closest(scenes[si][2], d_rays, d_out, n)
+        else:
+            P.cast_any(scenes[si][2], d_rays, d_out, n)
+    torch.cuda.synchronize()
+    for snap, it in zip(snapshot, items):
+        assert np.array_equal(snap, from_device(it[4], np.uint8))
+
+
+def test_autotuner_picks_a_valid_configuration():
+    scenes = _scenes()
+    items, host = _mix(scenes, [50000, 2000, 300, 10000, 64, 100000], 4)
+    batch = Batch([x[2] for x in scenes], items)
+    best, ms, table = batch.autotune(repeats=2)
+    assert len(table) == 18 and ms > 0
+    assert best["blockSize"] in (64, 128, 256)
+    assert ms == min(r["ms"] for r in table)
+    for it in items:
+        it[4].zero_()
+    batch.launch()
+    _check(scenes, items, host)
+
+
+def test_batch_rejects_bad_items():
+    scenes = _scenes()
+    d = device_empty(32, P.RAY_IN_DTYPE)
+    o = device_empty(32, P.RAY_HIT_DTYPE)
+    with pytest.raises(P.PheError):
+        Batch([scenes[0][2]], [(1, CLOSEST, 32, d, o)])      # scene index out of range
+    with pytest.raises(P.PheError):
+        Batch([scenes[0][2]], [(0, 7, 32, d, o)])            # unknown kind
