@@ -239,6 +239,17 @@ phe_status phe_batch_info(const phe_batch* batch, uint64_t* totalRays, uint32_t*
 phe_status phe_batch_autotune(phe_batch* batch, int repeats, void* stream, phe_batch_params* best, float* bestMs,
                               phe_batch_tuning_row* rows, uint32_t maxRows, uint32_t* numRows);
 phe_status phe_batch_destroy(phe_batch* batch);
+/* The batched launch without any device allocation (no counterpart in the reference). For callers
+ * that manage all device memory themselves and cannot let a library call cudaMalloc (an engine's
+ * renderer or a plugin host with its own allocator and memory budget; cudaMalloc may also wait for
+ * the whole device). The descriptor table, scene table and work counter live in a fixed 9,984-byte
+ * array inside the library (per GPU, until exit) instead of device memory the call allocates.
+ * At most 256 batch items and 32 scenes per call (PHE_ERR_TOO_LARGE beyond). All calls share the
+ * array: calls whose GPU work overlaps race, so serialise them on one stream. The first call on a
+ * device looks up the array's address on that (current) device; make it before any stream capture.
+ * Asynchronous on `stream`; results as phe_batch_launch. */
+phe_status phe_batch_cast_noalloc(const phe_scene* const* scenes, uint32_t numScenes, const phe_batch_item* items,
+                                  uint32_t numItems, void* stream);
 
 /* ---------------------------------------------------------------------------------------------
  * Wavefront renderer (CudaTracerRenderer, cuda_ray_tracer/CudaTracerRenderer.hpp:14-58, and the

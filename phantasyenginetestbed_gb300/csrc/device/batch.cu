@@ -14,6 +14,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "runtime.cuh"
@@ -392,5 +393,119 @@ done:
 	if (best) *best = winner;
 	if (bestMs) *bestMs = winnerMs;
 	if (numRows) *numRows = n;
+	return PHE_OK;
+}
+
+// ------------------------------------------------------------------------------------------------
+// phe_batch_cast_noalloc: the batched launch for callers that must not allocate device memory.
+//
+// Some callers own every byte of device memory through their own allocator or memory budget (a game
+// engine's renderer, a plugin host) and do not let a library call cudaMalloc: it can block until the
+// whole device is idle and it takes memory outside their accounting. For them this entry point keeps
+// its scratch (the batch descriptor table, the scene table, the work counter and the status word) in
+// the fixed array below, which lives in the library image. The caller passes the scenes, rays and
+// output buffers as usual.
+//
+// Limits and sharing rules:
+//   * at most kNoAllocMaxItems batches and kNoAllocMaxScenes scenes per call (9,984 bytes of scratch,
+//     held by every GPU that loads the library until the process exits); larger calls fail with
+//     PHE_ERR_TOO_LARGE;
+//   * every call uses the same array and leaves its table there; the counter and status word are
+//     cleared at the start of each call. Two calls whose work overlaps on the GPU (for example on two
+//     streams at once) race on the array: serialise them on one stream;
+//   * the first call on a device looks up the array's device address for that device (the call
+//     must be made with that device current); make that first call before any stream capture.
+// ------------------------------------------------------------------------------------------------
+
+namespace phe_gb300 {
+
+constexpr uint32_t kNoAllocMaxItems = 256;
+constexpr uint32_t kNoAllocMaxScenes = 32;
+constexpr size_t kNoAllocItemsBytes = kNoAllocMaxItems * sizeof(BatchItemDev);          // 8192
+constexpr size_t kNoAllocScenesBytes = kNoAllocMaxScenes * sizeof(DeviceScene);         // 1536
+constexpr size_t kNoAllocScratchBytes = kNoAllocItemsBytes + kNoAllocScenesBytes + 256; // + counter, status
+static_assert(sizeof(DeviceScene) % 16 == 0, "scene table entries stay 16-byte aligned");
+
+static __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocScratchBytes];
+
+static std::mutex g_noallocMutex;
+static unsigned char* g_noallocAddr[64] = {};   // device address of g_noallocScratch, per device
+
+// Looks up (once per device) the device address of the scratch array on the current device.
+static phe_status noalloc_scratch(unsigned char** out)
+{
+	int dev = 0;
+	cudaError_t e = cudaGetDevice(&dev);
+	if (e != cudaSuccess) return fail(PHE_ERR_NO_DEVICE, "no CUDA device: %s", cudaGetErrorString(e));
+	if (dev < 0 || dev >= 64) return fail(PHE_ERR_NO_DEVICE, "device ordinal %d out of range", dev);
+	std::lock_guard<std::mutex> lock(g_noallocMutex);
+	if (!g_noallocAddr[dev]) {
+		void* p = nullptr;
+		e = cudaGetSymbolAddress(&p, g_noallocScratch);
+		if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(no-alloc scratch)");
+		g_noallocAddr[dev] = (unsigned char*)p;
+	}
+	*out = g_noallocAddr[dev];
+	return PHE_OK;
+}
+
+} // namespace phe_gb300
+
+extern "C" phe_status phe_batch_cast_noalloc(const phe_scene* const* scenes, uint32_t numScenes,
+                                             const phe_batch_item* items, uint32_t numItems, void* stream)
+{
+	if (!scenes || numScenes == 0 || (!items && numItems))
+		return fail(PHE_ERR_INVALID_ARGUMENT, "phe_batch_cast_noalloc: null argument");
+	if (numItems > kNoAllocMaxItems)
+		return fail(PHE_ERR_TOO_LARGE, "phe_batch_cast_noalloc: %u batches, at most %u fit the fixed scratch", numItems,
+		            kNoAllocMaxItems);
+	if (numScenes > kNoAllocMaxScenes)
+		return fail(PHE_ERR_TOO_LARGE, "phe_batch_cast_noalloc: %u scenes, at most %u fit the fixed scratch", numScenes,
+		            kNoAllocMaxScenes);
+	for (uint32_t i = 0; i < numScenes; i++)
+		if (!scenes[i]) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_batch_cast_noalloc: scene %u is null", i);
+	phe_status st = check_items(items, numItems, numScenes);
+	if (st) return st;
+	unsigned char* scratch = nullptr;
+	if ((st = noalloc_scratch(&scratch))) return st;
+
+	// Tables are built on the stack (no heap, no device allocation) and copied into the scratch.
+	BatchItemDev table[kNoAllocMaxItems];
+	DeviceScene sceneTable[kNoAllocMaxScenes];
+	uint32_t base = 0;
+	for (uint32_t k = 0; k < numItems; k++) {
+		table[k].scene = items[k].scene;
+		table[k].kind = items[k].kind;
+		table[k].count = items[k].count;
+		table[k].base = base;
+		table[k].rays = items[k].rays;
+		table[k].out = items[k].out;
+		uint64_t next = (uint64_t)base + ((uint64_t)items[k].count + 31u) / 32u * 32u;
+		if (next > 0xFFFFFFF0ull) return fail(PHE_ERR_TOO_LARGE, "phe_batch_cast_noalloc: more than 2^32 rays");
+		base = (uint32_t)next;
+	}
+	for (uint32_t i = 0; i < numScenes; i++) sceneTable[i] = scenes[i]->dev;
+	BatchItemDev* dItems = (BatchItemDev*)scratch;
+	DeviceScene* dScenes = (DeviceScene*)(scratch + kNoAllocItemsBytes);
+	uint32_t* dCounter = (uint32_t*)(scratch + kNoAllocItemsBytes + kNoAllocScenesBytes);
+	uint32_t* dStatus = dCounter + 1;
+	cudaStream_t s = (cudaStream_t)stream;
+	if (numItems)
+		PHE_CUDA_TRY(cudaMemcpyAsync(dItems, table, numItems * sizeof(BatchItemDev), cudaMemcpyHostToDevice, s),
+		             "copy batch table into scratch");
+	PHE_CUDA_TRY(cudaMemcpyAsync(dScenes, sceneTable, numScenes * sizeof(DeviceScene), cudaMemcpyHostToDevice, s),
+	             "copy scene table into scratch");
+	PHE_CUDA_TRY(cudaMemsetAsync(dCounter, 0, 2 * sizeof(uint32_t), s), "clear scratch counter");
+	if (base == 0) return PHE_OK;
+	int dev = 0, numSMs = 0, perSM = 0;
+	PHE_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
+	PHE_CUDA_TRY(cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, dev), "SM count");
+	PHE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, batch_kernel<128>, 128, 0), "occupancy");
+	uint32_t grid = (uint32_t)(perSM > 0 ? perSM : 1) * (uint32_t)numSMs;
+	uint32_t need = (base + 127u) / 128u;
+	if (grid > need) grid = need;
+	BatchTableDev t{dItems, dScenes, numItems, base};
+	batch_kernel<128><<<grid, 128, 0, s>>>(t, dCounter, dStatus);
+	PHE_CUDA_TRY(cudaGetLastError(), "batch_kernel launch (no-alloc)");
 	return PHE_OK;
 }

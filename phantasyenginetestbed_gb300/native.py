@@ -138,6 +138,7 @@ SIGNATURES: dict[str, tuple] = {
     "phe_batch_autotune": (_I32, [_VP, _I32, _VP, C.POINTER(BatchParams), C.POINTER(C.c_float),
                                   C.POINTER(BatchTuningRow), _U32, C.POINTER(_U32)]),
     "phe_batch_destroy": (_I32, [_VP]),
+    "phe_batch_cast_noalloc": (_I32, [C.POINTER(_VP), _U32, C.POINTER(BatchItem), _U32, _VP]),
     "phe_taa_resolve": (_I32, [_U32, _U32, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
 }
 
