@@ -37,7 +37,12 @@ RES = (1920, 1080)
 SEED = 2024
 CAM_DIR = (0.0, 0.8, -0.6)
 CAM_UP = (0.0, 0.6, 0.8)
-KERNELS = ["primary", "primary_shadow", "bounce", "bounce_shadow", "resolve_taa"]
+KERNELS = ["primary_trace", "primary_shade", "primary_shadow", "bounce_trace", "bounce_shade", "bounce_shadow",
+           "resolve_taa"]
+KERNELS_FUSED = ["primary", "primary_shadow", "bounce", "bounce_shadow", "resolve_taa"]
+# traversal kernel -> the pass whose rays it casts
+TRACE_PASS = {"primary_trace": "primary", "primary": "primary", "primary_shadow": "primary_shadow",
+              "bounce_trace": "bounce", "bounce": "bounce", "bounce_shadow": "bounce_shadow"}
 
 
 def parse():
@@ -47,7 +52,16 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-graph", action="store_true")
+    ap.add_argument("--pipeline", choices=["fused", "split"], default="fused",
+                    help="fused: traversal + shading in one kernel per bounce (5 kernels); split: 7 kernels")
+    ap.add_argument("--refill", type=int, default=28, help="lane-refill threshold of the split pipeline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--workload", choices=["frame", "batch", "large", "serve"], default="frame",
+                    help="frame (default, the headline): 1080p wavefront frame; batch: 64 uneven batches over 4 "
+                         "scenes in one launch vs 64 plain launches; large: 8.6M-triangle scene, 4096x4096, 4 "
+                         "lights; serve: Poisson request arrivals through the serving loop")
+    ap.add_argument("--rates", default="200,500,1000", help="serve: arrival rates (requests/s)")
+    ap.add_argument("--duration", type=float, default=2.0, help="serve: seconds of arrivals per rate")
     return ap.parse_args()
 
 
@@ -202,6 +216,7 @@ def run_ours(args, world, rank, local):
     s, b, cam_pos, lights, build_s = frame_inputs()
     scene = P.Scene(b.nodes, b.verts, b.slot_datas(s.datas), s.materials)
     r = CudaTracerRenderer(use_graph=not args.no_graph)
+    r.set_pipeline(fused=args.pipeline == "fused", refill=args.refill)
     r.setStaticScene(scene)
     r.setTargetResolution(RES)
     r.set_seed(SEED, 0)
@@ -285,17 +300,19 @@ def run_ours(args, world, rank, local):
     io = {"primary": 48, "primary_shadow": 33, "bounce": 48, "bounce_shadow": 33}
     stage_rays = dict(zip(["primary", "primary_shadow", "bounce", "bounce_shadow"], (counts / args.steps).tolist()))
     per_kernel = {}
-    for i, name in enumerate(KERNELS):
+    names = KERNELS_FUSED if args.pipeline == "fused" else KERNELS
+    for i, name in enumerate(names):
         entry = {"ms": round(float(avg_kernel_ms[i]), 4)}
-        if name in stage_rays:
-            n = stage_rays[name]
-            w = work[name]
-            bytes_per_ray = io[name] + 64 * w["n_node"] + 48 * w["n_tri"]
+        if name in TRACE_PASS:
+            pas = TRACE_PASS[name]
+            n = stage_rays[pas]
+            w = work[pas]
+            bytes_per_ray = io[pas] + 64 * w["n_node"] + 48 * w["n_tri"]
             entry.update({"rays": round(n, 1), "Mrays_s": round(n / (avg_kernel_ms[i] / 1e3) / 1e6, 1),
                           "alg_bytes_per_ray": round(bytes_per_ray, 1),
                           "GB_s": round(n * bytes_per_ray / (avg_kernel_ms[i] / 1e3) / 1e9, 1)})
         per_kernel[name] = entry
-    dominant = max(KERNELS, key=lambda k: per_kernel[k]["ms"])
+    dominant = max((k for k in names if k in TRACE_PASS), key=lambda k: per_kernel[k]["ms"])
     peaks_path = ROOT / "MEASURED_PEAKS.json"
     if peaks_path.exists():
         peak = float(json.loads(peaks_path.read_text())["hbm_gbs"])
@@ -314,7 +331,7 @@ def run_ours(args, world, rank, local):
         v, cores, frames, _ = cpu_frame_rate(s, b, cam_pos, lights)
         cpu = {"value": round(v, 3), "unit": "Mrays/s", "cores": cores, "kind": "port",
                "sample": f"{frames} full {RES[0]}x{RES[1]} frames (~8 s) through the castRay restatement"}
-    launches_per_frame = 5
+    launches_per_frame = len(names)
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
@@ -325,7 +342,8 @@ def run_ours(args, world, rank, local):
                    "scene": SCENE, "triangles": int(len(s.tri_verts)), "bvh_nodes": int(len(b.nodes)),
                    "bvh_slots": int(len(b.verts)), "sbvh_build_s": round(build_s, 2), "lights": 1,
                    "rays_per_frame": round(rays_per_frame, 1), "rays_by_pass": {k: round(v, 1) for k, v in stage_rays.items()},
-                   "cuda_graph": not args.no_graph, "l2": "flushed before every timed frame (512 MiB write)",
+                   "cuda_graph": not args.no_graph, "pipeline": args.pipeline,
+                   "refill_threshold": args.refill, "l2": "flushed before every timed frame (512 MiB write)",
                    "parallelism": f"replicas x{world}"},
         "latency_ms": {"p50": round(lat[len(lat) // 2], 4), "p99": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 4)},
         "passes": per_kernel,
@@ -346,13 +364,287 @@ def run_ours(args, world, rank, local):
         dist.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------------------------
+# Additional workloads (not the headline line): uneven batches, large incoherent scene, serving.
+# ---------------------------------------------------------------------------------------------
+
+def _scene_with_bvh(name):
+    import phantasyenginetestbed_gb300 as P
+    s = P.standard_scene(name)
+    t = time.perf_counter()
+    b = P.build_sbvh(s.tri_verts)
+    return s, b, time.perf_counter() - t
+
+
+def _surface_rays(s, n, rng, tmax=3.4028235e38):
+    """Rays from random points on random triangles in uniformly random directions."""
+    import phantasyenginetestbed_gb300 as P
+    tri = s.tri_verts[rng.integers(0, len(s.tri_verts), n)]
+    a, b2 = rng.random((n, 1), np.float32), rng.random((n, 1), np.float32)
+    flip = (a + b2) > 1
+    a = np.where(flip, 1 - a, a)
+    b2 = np.where(flip, 1 - b2, b2)
+    p = tri[:, 0:3] + a * (tri[:, 3:6] - tri[:, 0:3]) + b2 * (tri[:, 6:9] - tri[:, 0:3])
+    d = rng.normal(size=(n, 3)).astype(np.float32)
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    rays = np.zeros(n, P.RAY_IN_DTYPE)
+    rays["origin"] = p
+    rays["dir"] = d
+    rays["tMin"] = np.float32(1e-3)
+    rays["tMax"] = np.float32(tmax)
+    return rays
+
+
+def _timed(fn, steps, stream, flush=None):
+    import torch
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for k in range(steps):
+        if flush is not None:
+            flush.zero_()
+        ev[k][0].record(stream)
+        fn()
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    return [a.elapsed_time(b) for a, b in ev]
+
+
+def run_batch(args):
+    """64 ray batches of uneven size (log-uniform 1K..1M), 50% pinhole / 50% random-surface rays, over 4
+    resident scenes (10K/155K/1M/2M triangles), 70/30 closest/any: one autotuned persistent launch
+    replayed from a CUDA graph vs 64 plain launches (and vs 64 launches each followed by a device
+    synchronisation, as the reference's launchers do)."""
+    import torch
+    import phantasyenginetestbed_gb300 as P
+    from phantasyenginetestbed_gb300.batch import ANY, CLOSEST, Batch, save_tuning
+    torch.cuda.set_device(0)
+    stream = torch.cuda.current_stream()
+    names = ["c3_10k", "c3_155k", "c3_1m", "c3_2m"]
+    built = [_scene_with_bvh(n) for n in names]
+    scenes = [P.Scene(b.nodes, b.verts) for _, b, _ in built]
+    rng = np.random.default_rng(2024)
+    items, total = [], 0
+    for i in range(64):
+        n = int(np.exp(rng.uniform(np.log(1024), np.log(1 << 20))))
+        si = int(rng.integers(0, 4))
+        kind = CLOSEST if rng.random() < 0.7 else ANY
+        s = built[si][0]
+        d_rays = torch.empty(n * 32, dtype=torch.uint8, device="cuda")
+        if i % 2 == 0:
+            k = s.scale
+            w = 1024
+            h = (n + w - 1) // w
+            cam = P.camera_def((0.5 * k, -0.3 * k, 0.6 * k), CAM_DIR, CAM_UP, 60.0, (w, h))
+            full = torch.empty(w * h * 32, dtype=torch.uint8, device="cuda")
+            P.gen_primary_rays(full, cam, (w, h), order=0)
+            d_rays.copy_(full[: n * 32])
+        else:
+            d_rays.copy_(torch.from_numpy(_surface_rays(s, n, rng).view(np.uint8)))
+        out = torch.empty(n * (16 if kind == CLOSEST else 1), dtype=torch.uint8, device="cuda")
+        items.append((si, kind, n, d_rays, out))
+        total += n
+    torch.cuda.synchronize()
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    batch = Batch(scenes, items, use_graph=False)
+    best, best_ms, table = batch.autotune(repeats=3)
+    save_tuning(ROOT / "profiles" / "batch_autotune.json", best, best_ms, table)
+    batch.set_params(block_size=best["blockSize"], blocks_per_sm=best["blocksPerSM"], order=best["order"], use_graph=True)
+    for _ in range(args.warmup):
+        batch.launch(stream)
+    t_batched = _timed(lambda: batch.launch(stream), args.steps, stream, flush)
+
+    def plain():
+        for si, kind, n, d_rays, out in items:
+            (P.cast_closest if kind == CLOSEST else P.cast_any)(scenes[si], d_rays, out, n, stream=stream)
+
+    def plain_sync():
+        for si, kind, n, d_rays, out in items:
+            (P.cast_closest if kind == CLOSEST else P.cast_any)(scenes[si], d_rays, out, n, stream=stream)
+            torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        plain()
+    t_plain = _timed(plain, args.steps, stream, flush)
+    steps_sync = max(3, args.steps // 5)
+    # wall clock of the synchronised variant (host waits are part of that launch model)
+    walls = []
+    for _ in range(steps_sync):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        plain_sync()
+        walls.append((time.perf_counter() - t) * 1e3)
+    mb = statistics.median(t_batched)
+    mp = statistics.median(t_plain)
+    ms_sync = statistics.median(walls)
+    line = {"workload": "batch", "metric": METRIC, "unit": "Mrays/s", "batches": 64, "rays": total,
+            "scenes": {n: int(len(b.verts)) for n, (_, b, _) in zip(names, built)},
+            "batched_graph": {"ms": round(mb, 4), "Mrays_s": round(total / mb / 1e3, 1), "params": best},
+            "plain_64_launches": {"ms": round(mp, 4), "Mrays_s": round(total / mp / 1e3, 1)},
+            "plain_64_launches_synchronised": {"ms": round(ms_sync, 4), "Mrays_s": round(total / ms_sync / 1e3, 1)},
+            "speedup_vs_plain": round(mp / mb, 3), "speedup_vs_synchronised": round(ms_sync / mb, 3),
+            "autotune_candidates": len(table), "l2": "flushed before every timed step"}
+    print(json.dumps(line), flush=True)
+
+
+def run_large(args):
+    """8.63M-triangle scene (2048x2048-cell heightfield + 20,000 cubes, world x32), 4096x4096 frame with
+    4 point lights: 16.8M primary rays, ~16M bounce rays (cosine-weighted), shadow rays to 4 lights."""
+    import torch
+    import phantasyenginetestbed_gb300 as P
+    from phantasyenginetestbed_gb300.renderer import CudaTracerRenderer, make_lights
+    torch.cuda.set_device(0)
+    res = (4096, 4096)
+    s, b, build_s = _scene_with_bvh("c4_2048_20000")
+    scene = P.Scene(b.nodes, b.verts, b.slot_datas(s.datas), s.materials)
+    k = s.scale
+    cam_pos = (0.5 * k, -0.3 * k, 0.6 * k)
+    lights = make_lights(np.array([[0.5, 0.5, 2.0], [0.1, 0.1, 1.0], [0.9, 0.2, 1.5], [0.3, 0.9, 0.8]], np.float32)
+                         * np.float32(k), range_=1000.0 * k)
+    r = CudaTracerRenderer(use_graph=True)
+    r.setStaticScene(scene)
+    r.setTargetResolution(res)
+    stream = torch.cuda.current_stream()
+    r.set_seed(SEED, 0)
+    for f in range(args.warmup):
+        r.updateCamera(cam_pos, CAM_DIR, CAM_UP, 60.0, P.halton_jitter(f))
+        r.render(lights, stream=stream)
+    steps = max(3, min(args.steps, 10))
+    r.set_graph(False)
+    r.set_kernel_timing(True)
+    r.set_seed(SEED, args.warmup)
+    counts = np.zeros(4, np.int64)
+    walls = []
+    for f in range(steps):
+        r.updateCamera(cam_pos, CAM_DIR, CAM_UP, 60.0, P.halton_jitter(f))
+        r.render(lights, stream=stream)
+        counts += r.ray_counts(stream=stream).astype(np.int64)
+    kms, frames = r.kernel_times()
+    avg = kms / frames
+    counts = counts / steps
+    frame_ms = float(avg.sum())
+    names = KERNELS_FUSED
+    passes = {}
+    for i, nm in enumerate(names):
+        e = {"ms": round(float(avg[i]), 3)}
+        if nm in TRACE_PASS:
+            n = counts[["primary", "primary_shadow", "bounce", "bounce_shadow"].index(TRACE_PASS[nm])]
+            e.update({"rays": int(n), "Mrays_s": round(n / avg[i] / 1e3, 1)})
+        passes[nm] = e
+    line = {"workload": "large", "metric": METRIC, "unit": "Mrays/s", "triangles": int(len(s.tri_verts)),
+            "bvh_nodes": int(len(b.nodes)), "bvh_slots": int(len(b.verts)), "sbvh_build_s": round(build_s, 1),
+            "scene_bytes": scene.device_bytes(), "res": res, "lights": 4, "frame_ms": round(frame_ms, 3),
+            "rays_per_frame": int(counts.sum()), "value": round(counts.sum() / frame_ms / 1e3, 1), "passes": passes}
+    print(json.dumps(line), flush=True)
+
+
+def run_serve(args):
+    """Poisson arrivals of render requests (256x256..1920x1080 log-uniform, 1-4 spp) and ray-query
+    requests (4K..512K rays log-uniform, 70/30 closest/any) against 8 resident scenes of 50K..4M
+    triangles, under a 120 GB budget, through the continuous-batching server and the serial baseline."""
+    import threading as th
+    import torch
+    import phantasyenginetestbed_gb300 as P
+    from phantasyenginetestbed_gb300.renderer import make_lights
+    from phantasyenginetestbed_gb300.serve import REQ_ANY, REQ_CLOSEST, Server, pinned
+    torch.cuda.set_device(0)
+    grids = [160, 256, 362, 512, 724, 1024, 1240, 1448]
+    built, scenes = [], []
+    t0 = time.perf_counter()
+    for i, g in enumerate(grids):
+        s = P.generate_scene(g, 100, False, 500 + i)
+        b = P.build_sbvh(s.tri_verts)
+        built.append((s, b))
+        scenes.append(P.Scene(b.nodes, b.verts, b.slot_datas(s.datas), s.materials))
+    build_s = time.perf_counter() - t0
+    rng = np.random.default_rng(7)
+    pools = []
+    for s, _ in built:
+        rp = pinned(1 << 19, P.RAY_IN_DTYPE)
+        rp[:] = _surface_rays(s, 1 << 19, rng)
+        pools.append(rp)
+    out_ring = [pinned((1 << 19) * 16, np.uint8) for _ in range(8)]
+    img_ring = [pinned((1080, 1920, 4), np.float32) for _ in range(8)]
+
+    def make_requests(rate, duration, seed):
+        r = np.random.default_rng(seed)
+        t, reqs = 0.0, []
+        while True:
+            t += r.exponential(1.0 / rate)
+            if t > duration:
+                break
+            si = int(r.integers(0, len(scenes)))
+            if r.random() < 0.5:
+                pix = np.exp(r.uniform(np.log(256 * 256), np.log(1920 * 1080)))
+                w = int(min(1920, max(256, round(np.sqrt(pix * 16 / 9) / 8) * 8)))
+                h = int(max(256 // 2, round(pix / w / 8) * 8))
+                h = min(h, (1920 * 1080) // w // 8 * 8)
+                reqs.append((t, "render", si, (w, h), int(r.integers(1, 5))))
+            else:
+                n = int(np.exp(r.uniform(np.log(4096), np.log(1 << 19))))
+                reqs.append((t, "rays", si, n, REQ_CLOSEST if r.random() < 0.7 else REQ_ANY))
+        return reqs
+
+    def run(server, ids, reqs):
+        cams = {}
+        start = time.perf_counter() + 0.05
+        sub = []
+        for j, q in enumerate(reqs):
+            dt = start + q[0] - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            arrival = (start + q[0])
+            if q[1] == "render":
+                s, _ = built[q[2]]
+                k = s.scale
+                cp = (0.5 * k, -0.3 * k, 0.6 * k)
+                key = (q[2], q[3])
+                if key not in cams:
+                    cams[key] = P.camera_def(cp, CAM_DIR, CAM_UP, 60.0, q[3])
+                lights = make_lights(np.array([[0.5, 0.5, 2.0]], np.float32) * np.float32(k), range_=1000.0 * k)
+                rid = server.submit_render(ids[q[2]], q[3], q[4], cams[key], cp, lights, 11 + j, img_ring[j % 8])
+            else:
+                rid = server.submit_rays(ids[q[2]], pools[q[2]][: q[3]], out_ring[j % 8], q[4])
+            sub.append((rid, arrival))
+        server.drain()
+        lat, rays, t_first, t_last = [], 0, None, 0.0
+        for rid, arrival in sub:
+            st = server.poll(rid)
+            lat.append(st.doneMs - st.submitMs)
+            rays += st.rays
+            t_last = max(t_last, st.doneMs)
+            t_first = st.submitMs if t_first is None else min(t_first, st.submitMs)
+            server.release(rid)
+        lat.sort()
+        span_ms = t_last - t_first
+        return {"requests": len(sub), "p50_ms": round(lat[len(lat) // 2], 3),
+                "p99_ms": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 3),
+                "rays": int(rays), "span_s": round(span_ms / 1e3, 3), "Mrays_s": round(rays / span_ms / 1e3, 1)}
+
+    results = {}
+    for rate in [float(x) for x in args.rates.split(",")]:
+        reqs = make_requests(rate, args.duration, int(rate))
+        row = {}
+        for mode in ("continuous", "serial"):
+            server = Server(memory_budget=120 << 30, render_slots=4, serial=(mode == "serial"))
+            ids = [server.add_scene(sc) for sc in scenes]
+            row[mode] = run(server, ids, reqs)
+            server.close()
+        results[str(int(rate))] = row
+    line = {"workload": "serve", "metric": METRIC, "unit": "Mrays/s",
+            "scenes_triangles": [int(len(s.tri_verts)) for s, _ in built], "scene_build_s": round(build_s, 1),
+            "budget_bytes": 120 << 30, "arrivals_s": args.duration, "rates": results}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     world, rank, local = dist_setup(args.gpus)
     if args.impl == "reference":
         run_reference(args, world, rank)
-    else:
+    elif args.workload == "frame":
         run_ours(args, world, rank, local)
+    else:
+        {"batch": run_batch, "large": run_large, "serve": run_serve}[args.workload](args)
 
 
 if __name__ == "__main__":

@@ -296,19 +296,94 @@ phe_status phe_renderer_read(const phe_renderer* renderer, int which, void* host
 /* Rays cast by the last frame: primary, primary shadow, bounce, bounce shadow. Synchronises `stream`. */
 phe_status phe_renderer_ray_counts(const phe_renderer* renderer, uint64_t counts[4], void* stream);
 
+/* Frame pipeline: fused = 1 (the default) runs traversal and shading in one kernel per bounce (5
+ * kernels); 0 splits them (7 kernels: primary trace, primary shade, primary shadow, bounce trace, bounce
+ * shade, bounce shadow, resolve + TAA) so the persistent traversal kernels refill idle lanes with new
+ * rays when fewer than `refill` (0..32, default 28) lanes of a warp are still busy. */
+phe_status phe_renderer_set_pipeline(phe_renderer* renderer, int fused, int refill);
 /* Per-kernel timing with CUDA events on the render stream (direct launches; ignored while a graph is
- * replayed). Enabling resets the totals. kernel_times returns the summed milliseconds of the 5 frame
- * kernels (primary, primary shadow, bounce, bounce shadow, resolve + TAA) and the frames timed. */
+ * replayed). Enabling resets the totals. kernel_times returns the summed milliseconds per frame kernel
+ * (in launch order, `numKernels` of them) and the number of frames timed. */
 phe_status phe_renderer_set_kernel_timing(phe_renderer* renderer, int enable);
 /* Bytes copied host -> device per frame (the frame parameter block: camera, jitter, lights). */
 uint32_t phe_renderer_frame_param_bytes(void);
-phe_status phe_renderer_kernel_times(phe_renderer* renderer, double msTotal[5], uint32_t* frames);
+phe_status phe_renderer_kernel_times(phe_renderer* renderer, double msTotal[8], uint32_t* numKernels, uint32_t* frames);
+
+/* Ray totals per pass summed over the frames since the last reset (device counters): reset clears them
+ * on `stream`; totals_async copies the 4 totals (primary, primary shadow, bounce, bounce shadow) to
+ * host memory on `stream` (pinned memory for a truly asynchronous copy). */
+phe_status phe_renderer_reset_ray_totals(phe_renderer* renderer, void* stream);
+phe_status phe_renderer_ray_totals_async(const phe_renderer* renderer, uint64_t* hostTotals4, void* stream);
 
 /* TAA resolve alone (taa.frag:25-71) on device float4 buffers; velocity and prevVelocity are float2
  * uv velocities (NULL = static), roughness float (NULL = 0). */
 phe_status phe_taa_resolve(uint32_t resX, uint32_t resY, const float* cur, const float* hist, const float* velocity,
                            const float* prevVelocity, const float* roughness, float* outColor, float* outHist,
                            void* stream);
+
+/* ---------------------------------------------------------------------------------------------
+ * Serving (no reference counterpart): continuous batching of ray-query and render requests against
+ * device-resident scenes. A scheduler thread admits requests in arrival order while they fit the
+ * device-memory budget (resident scenes count against it), the in-flight limit and, for renders, a
+ * free render slot. Admitted ray queries whose rays are on the device join the next wave, ONE batched
+ * persistent launch over all of them; requests arriving meanwhile join the following wave. Renders
+ * run their spp frames (wavefront frame + TAA with Halton jitter) on their slot's own stream, so they
+ * overlap each other and the query waves. Results go straight to the caller's host buffers (pinned
+ * memory gives truly asynchronous copies). `serial` = 1 is the baseline: one request at a time, plain
+ * per-request launches, each waited for.
+ * ------------------------------------------------------------------------------------------- */
+#define PHE_REQ_CLOSEST 0
+#define PHE_REQ_ANY 1
+#define PHE_REQ_RENDER 2
+typedef struct phe_server phe_server;
+typedef struct phe_server_config {
+	uint64_t memoryBudget;     /* device bytes scenes + in-flight requests may hold (default 120 GiB) */
+	uint32_t maxInFlight;      /* admitted requests at once (default 256) */
+	uint32_t renderSlots;      /* concurrent renders, each with its own frame buffers (default 4) */
+	uint32_t maxRenderPixels;  /* largest render (default 1920*1080; width <= 1920) */
+	uint32_t maxLights;        /* lights per render (default 4, at most 8) */
+	int32_t serial;            /* 1 = serial baseline */
+	uint32_t pad;
+} phe_server_config;
+typedef struct phe_request {
+	uint32_t kind;             /* PHE_REQ_* */
+	uint32_t scene;            /* id from phe_server_add_scene */
+	uint32_t numRays;          /* queries */
+	uint32_t spp;              /* renders: frames accumulated through TAA */
+	const phe_ray_in* rays;    /* queries: host rays */
+	void* out;                 /* host: phe_ray_hit[numRays] (closest), uint8_t[numRays] (any), float4[resX*resY] (render) */
+	uint32_t resX, resY;       /* renders: multiples of 8 */
+	uint32_t numLights, pad;
+	phe_camera_def cam;
+	float camPos[3];
+	float pad2;
+	const phe_sphere_light* lights; /* host, copied at submit */
+	uint64_t seed;
+} phe_request;
+typedef struct phe_request_stats {
+	double submitMs, admitMs, doneMs; /* milliseconds since the server was created */
+	uint64_t rays;                    /* rays cast for the request */
+	phe_status status;
+	uint32_t pad;
+} phe_request_stats;
+typedef struct phe_server_stats {
+	uint64_t waves, raysCompleted, bytesInUse;
+	uint32_t pending, inFlight;
+} phe_server_stats;
+void phe_server_default_config(phe_server_config* config);
+phe_status phe_server_create(const phe_server_config* config, phe_server** out);
+/* Registers a resident scene (the server does not own it); returns its id. */
+phe_status phe_server_add_scene(phe_server* server, const phe_scene* scene, uint32_t* sceneId);
+/* Queues a request (never blocks on the GPU). PHE_ERR_BUDGET if it alone cannot fit the budget. */
+phe_status phe_server_submit(phe_server* server, const phe_request* request, uint64_t* requestId);
+/* PHE_OK with stats when done, PHE_ERR_NOT_READY while running. */
+phe_status phe_server_poll(phe_server* server, uint64_t requestId, phe_request_stats* stats);
+phe_status phe_server_wait(phe_server* server, uint64_t requestId, phe_request_stats* stats);
+phe_status phe_server_drain(phe_server* server);
+/* Forgets a completed request. */
+phe_status phe_server_release(phe_server* server, uint64_t requestId);
+phe_status phe_server_get_stats(phe_server* server, phe_server_stats* stats);
+phe_status phe_server_destroy(phe_server* server);
 
 #ifdef __cplusplus
 }

@@ -17,17 +17,11 @@
 #include <mutex>
 #include <vector>
 
+#include "batch.cuh"
 #include "runtime.cuh"
 #include "traverse.cuh"
 
 namespace phe_gb300 {
-
-struct BatchItemDev {
-	uint32_t scene, kind, count, base;
-	const phe_ray_in* rays;
-	void* out;
-};
-static_assert(sizeof(BatchItemDev) == 32, "BatchItemDev is 32 bytes");
 
 struct BatchTableDev {
 	const BatchItemDev* items;
@@ -96,6 +90,22 @@ static phe_status launch_batch_kernel(const BatchTableDev& t, int blocksPerSM, i
 	batch_kernel<BLOCK><<<grid, BLOCK, 0, stream>>>(t, counter, status);
 	PHE_CUDA_TRY(cudaGetLastError(), "batch_kernel launch");
 	return PHE_OK;
+}
+
+phe_status launch_batch_table(const BatchItemDev* items, uint32_t numItems, uint32_t totalPadded,
+                              const DeviceScene* scenes, uint32_t* counter, uint32_t* status, int blockSize,
+                              int blocksPerSM, cudaStream_t stream)
+{
+	DeviceInfo* d = nullptr;
+	phe_status st = device_info(&d);
+	if (st) return st;
+	if (totalPadded == 0) return PHE_OK;
+	BatchTableDev t{items, scenes, numItems, totalPadded};
+	switch (blockSize) {
+	case 64: return launch_batch_kernel<64>(t, blocksPerSM, d->numSMs, counter, status, stream, nullptr);
+	case 256: return launch_batch_kernel<256>(t, blocksPerSM, d->numSMs, counter, status, stream, nullptr);
+	default: return launch_batch_kernel<128>(t, blocksPerSM, d->numSMs, counter, status, stream, nullptr);
+	}
 }
 
 } // namespace phe_gb300

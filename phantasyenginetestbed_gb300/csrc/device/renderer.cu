@@ -21,7 +21,10 @@ struct phe_renderer {
 	FrameBuffers fb{};
 	void* allocation = nullptr;
 	FrameParamsDev* dParams = nullptr;
-	FrameParamsDev* hParams = nullptr;   // pinned staging
+	FrameParamsDev* hParams = nullptr;   // pinned staging ring of kParamSlots
+	cudaEvent_t paramEvents[8] = {};     // last copy out of each staging slot
+	uint32_t paramSlot = 0;
+	size_t capacityP = 0, capacityL = 0; // frame buffers are kept while a resolution fits
 	phe_camera_def cam{};
 	float camPos[3] = {0, 0, 0};
 	float jitter[2] = {0, 0};
@@ -32,14 +35,18 @@ struct phe_renderer {
 	cudaGraphExec_t graphExec = nullptr;
 	cudaStream_t graphStream = nullptr;  // stream the graph was captured for (graphs relaunch on any stream)
 	bool cameraSet = false;
+	bool fused = true;                     // traversal and shading fused in one kernel per bounce
+	int refill = 28;                       // lane-refill threshold of the persistent traversal kernels
 	bool timing = false;                   // record events around each kernel (direct launches only)
 	cudaEvent_t events[kFrameKernels + 1] = {};
 	double kernelMs[kFrameKernels] = {};   // accumulated since timing was enabled
+	int timedKernels = 0;
 	uint32_t timedFrames = 0;
 	bool pendingTimes = false;
 };
 
 static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+static const uint32_t kParamSlots = 8;
 
 static void free_buffers(phe_renderer* r)
 {
@@ -48,13 +55,27 @@ static void free_buffers(phe_renderer* r)
 	if (r->allocation) cudaFree(r->allocation);
 	r->allocation = nullptr;
 	std::memset(&r->fb, 0, sizeof(r->fb));
+	r->capacityP = r->capacityL = 0;
 }
 
 static phe_status allocate(phe_renderer* r, uint32_t resX, uint32_t resY, uint32_t numLights)
 {
-	free_buffers(r);
 	const size_t P = (size_t)resX * resY;
-	const size_t LP = P * (numLights ? numLights : 1);
+	const size_t L = numLights ? numLights : 1;
+	if (r->allocation && P <= r->capacityP && L <= r->capacityL) {
+		// Keep the buffers: every stride is computed from the current resolution at launch time. A
+		// captured graph holds launch shapes for the old resolution, so it is rebuilt.
+		if ((resX != r->resX || resY != r->resY) && r->graphExec) {
+			cudaGraphExecDestroy(r->graphExec);
+			r->graphExec = nullptr;
+		}
+		r->resX = resX;
+		r->resY = resY;
+		r->numLights = (uint32_t)L;
+		return PHE_OK;
+	}
+	free_buffers(r);
+	const size_t LP = P * L;
 	size_t sizes[] = {
 		2 * LP * sizeof(float4),      // contrib
 		2 * LP,                       // inLight
@@ -69,6 +90,9 @@ static phe_status allocate(phe_renderer* r, uint32_t resX, uint32_t resY, uint32
 		P * sizeof(float4),           // history[1]
 		P * sizeof(float4),           // color
 		kNumCounters * sizeof(uint32_t),
+		P * sizeof(phe_ray_hit),      // primaryHits
+		P * sizeof(phe_ray_hit),      // bounceHits
+		4 * sizeof(unsigned long long), // rayTotals
 	};
 	size_t total = 0;
 	for (size_t s : sizes) total += align256(s);
@@ -91,7 +115,13 @@ static phe_status allocate(phe_renderer* r, uint32_t resX, uint32_t resY, uint32
 	fb.history[1] = (float4*)take(10);
 	fb.color = (float4*)take(11);
 	fb.counters = (uint32_t*)take(12);
+	fb.primaryHits = (phe_ray_hit*)take(13);
+	fb.bounceHits = (phe_ray_hit*)take(14);
+	fb.rayTotals = (unsigned long long*)take(15);
 	fb.capacityLP = (uint32_t)LP;
+	fb.refill = r->refill;
+	r->capacityP = P;
+	r->capacityL = L;
 	r->allocation = base;
 	r->resX = resX;
 	r->resY = resY;
@@ -105,8 +135,8 @@ static phe_status allocate(phe_renderer* r, uint32_t resX, uint32_t resY, uint32
 static phe_status collect_times(phe_renderer* r)
 {
 	if (!r->pendingTimes) return PHE_OK;
-	PHE_CUDA_TRY(cudaEventSynchronize(r->events[kFrameKernels]), "wait for timed frame");
-	for (int i = 0; i < kFrameKernels; i++) {
+	PHE_CUDA_TRY(cudaEventSynchronize(r->events[r->timedKernels]), "wait for timed frame");
+	for (int i = 0; i < r->timedKernels; i++) {
 		float ms = 0.0f;
 		PHE_CUDA_TRY(cudaEventElapsedTime(&ms, r->events[i], r->events[i + 1]), "kernel time");
 		r->kernelMs[i] += ms;
@@ -128,15 +158,49 @@ extern "C" phe_status phe_renderer_set_kernel_timing(phe_renderer* r, int enable
 	return PHE_OK;
 }
 
-extern "C" phe_status phe_renderer_kernel_times(phe_renderer* r, double msTotal[5], uint32_t* frames)
+extern "C" phe_status phe_renderer_kernel_times(phe_renderer* r, double msTotal[8], uint32_t* numKernels, uint32_t* frames)
 {
-	if (!r || !msTotal || !frames) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_kernel_times: null argument");
+	if (!r || !msTotal || !frames || !numKernels)
+		return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_kernel_times: null argument");
 	phe_status st = collect_times(r);
 	if (st) return st;
-	for (int i = 0; i < kFrameKernels; i++) msTotal[i] = r->kernelMs[i];
+	for (int i = 0; i < 8; i++) msTotal[i] = i < kFrameKernels ? r->kernelMs[i] : 0.0;
+	*numKernels = (uint32_t)(r->fused ? kFusedFrameKernels : kFrameKernels);
 	*frames = r->timedFrames;
 	return PHE_OK;
 }
+
+extern "C" phe_status phe_renderer_set_pipeline(phe_renderer* r, int fused, int refill)
+{
+	if (!r) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_set_pipeline: null renderer");
+	if (refill < 0 || refill > 32) return fail(PHE_ERR_INVALID_ARGUMENT, "refill threshold must be in [0, 32]");
+	r->fused = fused != 0;
+	r->refill = refill;
+	r->fb.refill = refill;
+	if (r->graphExec) {
+		cudaGraphExecDestroy(r->graphExec);
+		r->graphExec = nullptr;
+	}
+	r->pendingTimes = false;
+	r->timedFrames = 0;
+	for (int i = 0; i < kFrameKernels; i++) r->kernelMs[i] = 0.0;
+	return PHE_OK;
+}
+
+namespace phe_gb300 {
+phe_status renderer_reserve(phe_renderer* r, uint64_t pixels, uint32_t lights)
+{
+	if (!r || pixels == 0) return fail(PHE_ERR_INVALID_ARGUMENT, "renderer_reserve: bad arguments");
+	if (pixels * kMaxLights * 2 >= 0xFFFFFFFFull) return fail(PHE_ERR_TOO_LARGE, "renderer_reserve: too many pixels");
+	if (r->allocation && pixels <= r->capacityP && lights <= r->capacityL) return PHE_OK;
+	// A 8-pixel-wide frame of the requested size: allocate() only uses the pixel and light counts.
+	uint32_t resY = (uint32_t)((pixels + 7) / 8);
+	phe_status st = allocate(r, 8, resY, lights);
+	if (st) return st;
+	r->resX = r->resY = 0;   // no target resolution chosen yet
+	return PHE_OK;
+}
+} // namespace phe_gb300
 
 extern "C" phe_status phe_renderer_create(phe_renderer** out)
 {
@@ -147,13 +211,16 @@ extern "C" phe_status phe_renderer_create(phe_renderer** out)
 	if (st) return st;
 	phe_renderer* r = new phe_renderer();
 	cudaError_t e = cudaMalloc(&r->dParams, sizeof(FrameParamsDev));
-	if (e == cudaSuccess) e = cudaMallocHost(&r->hParams, sizeof(FrameParamsDev));
+	if (e == cudaSuccess) e = cudaMallocHost(&r->hParams, sizeof(FrameParamsDev) * kParamSlots);
+	for (uint32_t i = 0; i < kParamSlots && e == cudaSuccess; i++)
+		e = cudaEventCreateWithFlags(&r->paramEvents[i], cudaEventDisableTiming);
 	if (e != cudaSuccess) {
 		if (r->dParams) cudaFree(r->dParams);
+		if (r->hParams) cudaFreeHost(r->hParams);
 		delete r;
 		return cuda_fail(e, "allocate frame parameters");
 	}
-	std::memset(r->hParams, 0, sizeof(FrameParamsDev));
+	std::memset(r->hParams, 0, sizeof(FrameParamsDev) * kParamSlots);
 	*out = r;
 	return PHE_OK;
 }
@@ -164,6 +231,8 @@ extern "C" phe_status phe_renderer_destroy(phe_renderer* r)
 	cudaDeviceSynchronize();
 	for (int i = 0; i <= kFrameKernels; i++)
 		if (r->events[i]) cudaEventDestroy(r->events[i]);
+	for (uint32_t i = 0; i < kParamSlots; i++)
+		if (r->paramEvents[i]) cudaEventDestroy(r->paramEvents[i]);
 	free_buffers(r);
 	cudaFree(r->dParams);
 	cudaFreeHost(r->hParams);
@@ -245,6 +314,22 @@ extern "C" phe_status phe_renderer_reset_taa(phe_renderer* r, void* stream)
 	return PHE_OK;
 }
 
+extern "C" phe_status phe_renderer_reset_ray_totals(phe_renderer* r, void* stream)
+{
+	if (!r || !r->allocation) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_reset_ray_totals: no frame buffers");
+	PHE_CUDA_TRY(cudaMemsetAsync(r->fb.rayTotals, 0, 4 * sizeof(unsigned long long), (cudaStream_t)stream),
+	             "reset ray totals");
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_renderer_ray_totals_async(const phe_renderer* r, uint64_t* hostTotals4, void* stream)
+{
+	if (!r || !r->allocation || !hostTotals4) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_ray_totals_async: no frame");
+	PHE_CUDA_TRY(cudaMemcpyAsync(hostTotals4, r->fb.rayTotals, 4 * sizeof(uint64_t), cudaMemcpyDeviceToHost,
+	                             (cudaStream_t)stream), "read ray totals");
+	return PHE_OK;
+}
+
 extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_light* lights, uint32_t numLights, void* stream)
 {
 	if (!r) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_render: null renderer");
@@ -261,9 +346,11 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 		phe_status st = allocate(r, r->resX, r->resY, L);
 		if (st) return st;
 	}
-	FrameParamsDev& fp = *r->hParams;
-	// The pinned staging buffer is rewritten below: wait until the previous frame's copy has read it.
-	PHE_CUDA_TRY(cudaStreamSynchronize(s), "wait for previous frame parameters");
+	// Pinned staging ring: a slot is rewritten only after its previous copy has been consumed.
+	uint32_t slot = r->paramSlot;
+	r->paramSlot = (slot + 1) % kParamSlots;
+	PHE_CUDA_TRY(cudaEventSynchronize(r->paramEvents[slot]), "wait for a free parameter slot");
+	FrameParamsDev& fp = r->hParams[slot];
 	fp.cam = r->cam;
 	fp.jitter[0] = r->jitter[0];
 	fp.jitter[1] = r->jitter[1];
@@ -277,8 +364,9 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 	fp.seed = r->seed;
 	std::memset(fp.lights, 0, sizeof(fp.lights));
 	if (numLights) std::memcpy(fp.lights, lights, sizeof(phe_sphere_light) * numLights);
-	PHE_CUDA_TRY(cudaMemcpyAsync(r->dParams, r->hParams, sizeof(FrameParamsDev), cudaMemcpyHostToDevice, s),
+	PHE_CUDA_TRY(cudaMemcpyAsync(r->dParams, &fp, sizeof(FrameParamsDev), cudaMemcpyHostToDevice, s),
 	             "upload frame parameters");
+	PHE_CUDA_TRY(cudaEventRecord(r->paramEvents[slot], s), "record parameter slot");
 	if (r->useGraph) {
 		if (!r->graphExec) {
 			phe_status pst = prepare_frame();
@@ -289,7 +377,7 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 			cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
 			phe_status st = PHE_OK;
 			if (e == cudaSuccess) {
-				st = launch_frame(r->scene, r->dParams, r->fb, r->resX, r->resY, cap);
+				st = launch_frame(r->scene, r->dParams, r->fb, r->resX, r->resY, cap, nullptr, r->fused);
 				e = cudaStreamEndCapture(cap, &g);
 			}
 			cudaStreamDestroy(cap);
@@ -304,10 +392,11 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 		phe_status st;
 		if (r->timing) {
 			if ((st = collect_times(r))) return st;
-			st = launch_frame(r->scene, r->dParams, r->fb, r->resX, r->resY, s, r->events);
+			r->timedKernels = r->fused ? kFusedFrameKernels : kFrameKernels;
+			st = launch_frame(r->scene, r->dParams, r->fb, r->resX, r->resY, s, r->events, r->fused);
 			r->pendingTimes = true;
 		} else {
-			st = launch_frame(r->scene, r->dParams, r->fb, r->resX, r->resY, s);
+			st = launch_frame(r->scene, r->dParams, r->fb, r->resX, r->resY, s, nullptr, r->fused);
 		}
 		if (st) return st;
 	}

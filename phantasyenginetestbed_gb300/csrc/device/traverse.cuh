@@ -167,3 +167,144 @@ __device__ __forceinline__ void store_hit(phe_ray_hit* __restrict__ hits, uint32
 }
 
 } // namespace phe_gb300
+
+namespace phe_gb300 {
+
+// ------------------------------------------------------------------------------------------------
+// Persistent traversal with lane refill (Aila & Laine 2009, "persistent while-while" with dynamic ray
+// fetch; the reference does the same with a threshold of 20 lanes, RayCastKernel.cu:225-393). Every
+// lane keeps its own ray state across outer iterations; when fewer than `refill` lanes of a warp are
+// still traversing, the warp leaves the traversal loop, idle lanes take new rays (one atomic per warp)
+// and traversal resumes. Divergent incoherent rays then keep more lanes busy than with a fixed
+// 32-ray batch per warp.
+//
+// Source: `RayState load(uint32_t i)` for i < n. Sink: `void store(uint32_t i, const RayState&, const
+// HitRecord&)`, called once per ray when its traversal ends.
+// ------------------------------------------------------------------------------------------------
+template <bool ANY, bool SAFE>
+__device__ __forceinline__ void trace_step(const float4* __restrict__ nodes, const float4* __restrict__ tris,
+                                           const RayState& r, HitRecord& hit, int32_t* stack, int& sp,
+                                           int32_t& nodeAddr, int32_t& leafAddr, uint32_t& err)
+{
+	while (nodeAddr >= 0 && nodeAddr != kSentinel) {
+		const float4* np = nodes + 4 * (size_t)nodeAddr;
+		float4 b0 = __ldg(np), b1 = __ldg(np + 1), b2 = __ldg(np + 2);
+		int4 ix = __ldg(reinterpret_cast<const int4*>(np + 3));
+		float tIn0, tIn1;
+		bool v0 = visit_box<SAFE>(r, b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, hit.t, tIn0);
+		bool v1 = visit_box<SAFE>(r, b1.z, b1.w, b2.x, b2.y, b2.z, b2.w, hit.t, tIn1);
+		if (!v0 && !v1) {
+			nodeAddr = stack[sp--];
+		} else {
+			nodeAddr = v0 ? ix.x : ix.y;
+			if (v0 && v1) {
+				int32_t other = ix.y;
+				if (!ANY && tIn1 < tIn0) {
+					other = ix.x;
+					nodeAddr = ix.y;
+				}
+				if (sp >= kStackSize - 1) {
+					err |= kErrStackOverflow;
+					nodeAddr = kSentinel;
+					leafAddr = 0;
+					return;
+				}
+				stack[++sp] = other;
+			}
+		}
+		if (nodeAddr < 0 && leafAddr >= 0) {
+			leafAddr = nodeAddr;
+			nodeAddr = stack[sp--];
+		}
+		if (!__any_sync(__activemask(), leafAddr >= 0)) break;
+	}
+	while (leafAddr < 0) {
+		int32_t slot = ~leafAddr;
+		for (;;) {
+			const float4* tp = tris + 3 * (size_t)slot;
+			float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+			float t, u, v;
+			if (intersect_tri(a, b, c, r.o, r.d, t, u, v) && r.tMin <= t && t < hit.t) {
+				hit.slot = (uint32_t)slot;
+				hit.t = t;
+				hit.u = u;
+				hit.v = v;
+				if (ANY) {
+					nodeAddr = kSentinel;
+					leafAddr = 0;
+					return;
+				}
+			}
+			if (a.w < 0.0f) break;
+			slot++;
+		}
+		leafAddr = nodeAddr;
+		if (nodeAddr < 0) nodeAddr = stack[sp--];
+	}
+}
+
+template <bool ANY, class Source, class Sink>
+__device__ __forceinline__ uint32_t persistent_trace(const float4* __restrict__ nodes, const float4* __restrict__ tris,
+                                                     const Source& src, const Sink& sink, uint32_t n,
+                                                     uint32_t* __restrict__ counter, int refill)
+{
+	const uint32_t lane = threadIdx.x & 31u;
+	const uint32_t below = (1u << lane) - 1u;
+	int32_t stack[kStackSize];
+	int sp = 0;
+	int32_t nodeAddr = kSentinel, leafAddr = 0;
+	RayState r;
+	HitRecord h;
+	h.slot = ~0u;
+	h.t = 0.0f;
+	h.u = h.v = 0.0f;
+	r.safe = true;
+	uint32_t rayIdx = 0, err = 0;
+	bool hasRay = false, exhausted = false;
+	for (;;) {
+		bool need = !hasRay && !exhausted;
+		uint32_t needMask = __ballot_sync(0xFFFFFFFFu, need);
+		if (needMask) {
+			uint32_t leader = (uint32_t)__ffs(needMask) - 1u;
+			uint32_t base = 0;
+			if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(needMask));
+			base = __shfl_sync(0xFFFFFFFFu, base, leader);
+			if (need) {
+				rayIdx = base + (uint32_t)__popc(needMask & below);
+				if (rayIdx < n) {
+					r = src.load(rayIdx);
+					h = empty_hit(r);
+					sp = 0;
+					stack[0] = kSentinel;
+					nodeAddr = 0;
+					leafAddr = 0;
+					hasRay = true;
+				} else {
+					exhausted = true;
+				}
+			}
+		}
+		if (!__any_sync(0xFFFFFFFFu, hasRay)) break;
+		if (hasRay) {
+			if (r.safe) {
+				while (nodeAddr != kSentinel) {
+					trace_step<ANY, true>(nodes, tris, r, h, stack, sp, nodeAddr, leafAddr, err);
+					if (__popc(__activemask()) < refill) break;
+				}
+			} else {
+				while (nodeAddr != kSentinel) {
+					trace_step<ANY, false>(nodes, tris, r, h, stack, sp, nodeAddr, leafAddr, err);
+					if (__popc(__activemask()) < refill) break;
+				}
+			}
+			if (nodeAddr == kSentinel) {
+				sink.store(rayIdx, r, h);
+				hasRay = false;
+			}
+		}
+		__syncwarp();
+	}
+	return err;
+}
+
+} // namespace phe_gb300

@@ -230,6 +230,179 @@ __global__ void __launch_bounds__(kWaveBlock) bounce_kernel(DeviceScene s, const
 	}
 }
 
+// ------------------------------------------------------------------------------------------------
+// Split pipeline: traversal kernels (persistent, lane refill, no shading state in registers) and
+// shading kernels (one thread per hit, full warps) communicate through 16-byte hit records.
+// ------------------------------------------------------------------------------------------------
+
+__device__ __forceinline__ void tile_pixel(uint32_t i, uint32_t W, uint32_t& x, uint32_t& y)
+{
+	uint32_t tile = i >> 6, within = i & 63u, tilesX = W >> 3;
+	x = (tile % tilesX) * 8u + (within & 7u);
+	y = (tile / tilesX) * 8u + (within >> 3);
+}
+
+struct CameraSource {
+	const FrameParamsDev* fp;
+	__device__ __forceinline__ RayState load(uint32_t i) const
+	{
+		uint32_t x, y;
+		tile_pixel(i, fp->resX, x, y);
+		RayState r;
+		f3 d = primary_dir(fp->cam, x, y, fp->resX, fp->resY, fp->jitter[0], fp->jitter[1]);
+		r.o = mk3(fp->cam.origin[0], fp->cam.origin[1], fp->cam.origin[2]);
+		r.d = d;
+		r.tMin = 0.0001f;
+		r.tMax = 3.402823466e+38f;
+		r.inv = mk3(__frcp_rn(d.x), __frcp_rn(d.y), __frcp_rn(d.z));
+		r.safe = isfinite(r.inv.x) && isfinite(r.inv.y) && isfinite(r.inv.z) && isfinite(d.x) && isfinite(d.y) &&
+		         isfinite(d.z) && isfinite(r.o.x) && isfinite(r.o.y) && isfinite(r.o.z);
+		return r;
+	}
+};
+
+struct ArraySource {
+	const phe_ray_in* rays;
+	__device__ __forceinline__ RayState load(uint32_t i) const { return load_ray(rays, i); }
+};
+
+struct HitSink {
+	phe_ray_hit* hits;
+	__device__ __forceinline__ void store(uint32_t i, const RayState& r, const HitRecord& h) const { store_hit(hits, i, r, h); }
+};
+
+struct VisibilitySink {
+	uint8_t* inLight;
+	const uint32_t* slots;
+	__device__ __forceinline__ void store(uint32_t i, const RayState&, const HitRecord& h) const
+	{
+		inLight[slots ? __ldg(slots + i) : i] = h.slot == ~0u ? 1 : 0;
+	}
+};
+
+__global__ void __launch_bounds__(kWaveBlock) primary_trace_kernel(DeviceScene s, const FrameParamsDev* __restrict__ fpp,
+                                                                   FrameBuffers fb, uint32_t* __restrict__ status)
+{
+	uint32_t err = persistent_trace<false>(s.nodes, s.tris, CameraSource{fpp}, HitSink{fb.primaryHits}, fpp->numPixels,
+	                                       fb.counters + kCtrWork0, fb.refill);
+	if (err) atomicOr(status, err);
+}
+
+__global__ void __launch_bounds__(kWaveBlock) any_refill_kernel(DeviceScene s, const phe_ray_in* __restrict__ rays,
+                                                                const uint32_t* __restrict__ slots,
+                                                                const uint32_t* __restrict__ count,
+                                                                uint8_t* __restrict__ inLight, uint32_t* __restrict__ work,
+                                                                int refill, uint32_t* __restrict__ status)
+{
+	uint32_t err = persistent_trace<true>(s.nodes, s.tris, ArraySource{rays}, VisibilitySink{inLight, slots}, *count,
+	                                      work, refill);
+	if (err) atomicOr(status, err);
+}
+
+__global__ void __launch_bounds__(kWaveBlock) bounce_trace_kernel(DeviceScene s, FrameBuffers fb, uint32_t* __restrict__ status)
+{
+	uint32_t err = persistent_trace<false>(s.nodes, s.tris, ArraySource{fb.bounceRays}, HitSink{fb.bounceHits},
+	                                       fb.counters[kCtrBounce], fb.counters + kCtrWork1, fb.refill);
+	if (err) atomicOr(status, err);
+}
+
+__global__ void __launch_bounds__(kWaveBlock) primary_shade_kernel(DeviceScene s, const FrameParamsDev* __restrict__ fpp,
+                                                                   FrameBuffers fb)
+{
+	const FrameParamsDev& fp = *fpp;
+	const uint32_t P = fp.numPixels, W = fp.resX, L = fp.numLights;
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;; i += gridDim.x * blockDim.x) {
+		bool active = i < P;
+		if (!__any_sync(0xFFFFFFFFu, active)) break;
+		uint32_t x = 0, y = 0, pid = 0;
+		float4 hv = make_float4(__uint_as_float(~0u), 0.0f, 0.0f, 0.0f);
+		if (active) {
+			tile_pixel(i, W, x, y);
+			pid = y * W + x;
+			hv = reinterpret_cast<const float4*>(fb.primaryHits)[i];
+		}
+		uint32_t slot = __float_as_uint(hv.x);
+		bool hit = active && slot != ~0u;
+		HitInfo hi;
+		DevPcg rng;
+		f3 toCamera = mk3(0.0f, 0.0f, 0.0f);
+		f3 camPos = mk3(fp.camPos[0], fp.camPos[1], fp.camPos[2]);
+		if (hit) {
+			f3 o = mk3(fp.cam.origin[0], fp.cam.origin[1], fp.cam.origin[2]);
+			f3 d = primary_dir(fp.cam, x, y, W, fp.resY, fp.jitter[0], fp.jitter[1]);
+			hi = interpret_hit(s.datas, s.materials, o, d, slot, hv.y, hv.z, hv.w);
+			pixel_stream(rng, fp.seed, fp.frame, pid, 0);
+			toCamera = normalize3(sub3(camPos, hi.pos));
+		} else {
+			hi.pos = hi.normal = hi.albedo = mk3(0.0f, 0.0f, 0.0f);
+			hi.alpha = hi.roughness = hi.metallic = 0.0f;
+		}
+		if (active) fb.roughness[pid] = hit ? hi.roughness : 0.0f;
+		shade_all_lights(fp, fb, 0, hit, hi, mk3(1.0f, 1.0f, 1.0f), toCamera, rng, pid);
+		float btMin = 0.001f;
+		f3 thr = mk3(0.0f, 0.0f, 0.0f), bdir = mk3(0.0f, 0.0f, 0.0f);
+		if (hit) bdir = sample_bounce(hi, camPos, rng, btMin, thr);
+		uint32_t q = warp_append(fb.counters + kCtrBounce, hit, 0xFFFFFFFFu);
+		if (hit) {
+			store_ray(fb.bounceRays, q, hi.pos, btMin, bdir, 3.402823466e+38f);
+			fb.bouncePixel[q] = pid;
+			fb.bounceThroughput[q] = make_float4(thr.x, thr.y, thr.z, 0.0f);
+		} else if (active) {
+			for (uint32_t l = 0; l < L; l++) {
+				fb.contrib[(size_t)l * P + pid] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+				fb.inLight[(size_t)l * P + pid] = 1;
+				fb.contrib[(size_t)(L + l) * P + pid] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+				fb.inLight[(size_t)(L + l) * P + pid] = 1;
+			}
+		}
+	}
+}
+
+__global__ void __launch_bounds__(kWaveBlock) bounce_shade_kernel(DeviceScene s, const FrameParamsDev* __restrict__ fpp,
+                                                                  FrameBuffers fb)
+{
+	const FrameParamsDev& fp = *fpp;
+	const uint32_t P = fp.numPixels, L = fp.numLights;
+	const uint32_t n = fb.counters[kCtrBounce];
+	for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;; i += gridDim.x * blockDim.x) {
+		bool active = i < n;
+		if (!__any_sync(0xFFFFFFFFu, active)) break;
+		uint32_t pid = 0, slot = ~0u;
+		f3 thr = mk3(0.0f, 0.0f, 0.0f), o = thr, d = thr;
+		float4 hv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+		if (active) {
+			pid = fb.bouncePixel[i];
+			float4 t4 = fb.bounceThroughput[i];
+			thr = mk3(t4.x, t4.y, t4.z);
+			hv = reinterpret_cast<const float4*>(fb.bounceHits)[i];
+			slot = __float_as_uint(hv.x);
+			const float4* rp = reinterpret_cast<const float4*>(fb.bounceRays + i);
+			float4 a = rp[0], b = rp[1];
+			o = mk3(a.x, a.y, a.z);
+			d = mk3(b.x, b.y, b.z);
+		}
+		bool hit = active && slot != ~0u;
+		HitInfo hi;
+		DevPcg rng;
+		f3 toCamera = mk3(0.0f, 0.0f, 0.0f);
+		if (hit) {
+			hi = interpret_hit(s.datas, s.materials, o, d, slot, hv.y, hv.z, hv.w);
+			pixel_stream(rng, fp.seed, fp.frame, pid, 1);
+			toCamera = mk3(-d.x, -d.y, -d.z);
+		} else {
+			hi.pos = hi.normal = hi.albedo = mk3(0.0f, 0.0f, 0.0f);
+			hi.alpha = hi.roughness = hi.metallic = 0.0f;
+		}
+		shade_all_lights(fp, fb, 1, hit, hi, thr, toCamera, rng, pid);
+		if (active && !hit) {
+			for (uint32_t l = 0; l < L; l++) {
+				fb.contrib[(size_t)(L + l) * P + pid] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+				fb.inLight[(size_t)(L + l) * P + pid] = 1;
+			}
+		}
+	}
+}
+
 // TAA (taa.frag:25-71) with the history fetched in pixel space: (x + 0.5) - velocity * res.
 __device__ __forceinline__ float glsl_mix(float a, float b, float t)
 {
@@ -304,6 +477,12 @@ __global__ void resolve_taa_kernel(const FrameParamsDev* __restrict__ fpp, Frame
 	if (x >= fp.resX || y >= fp.resY) return;
 	const uint32_t P = fp.numPixels, L = fp.numLights;
 	uint32_t pid = y * fp.resX + x;
+	if (pid == 0) {
+		atomicAdd(&fb.rayTotals[0], (unsigned long long)P);
+		atomicAdd(&fb.rayTotals[1], (unsigned long long)fb.counters[kCtrShadow0]);
+		atomicAdd(&fb.rayTotals[2], (unsigned long long)fb.counters[kCtrBounce]);
+		atomicAdd(&fb.rayTotals[3], (unsigned long long)fb.counters[kCtrShadow1]);
+	}
 	f3 acc = mk3(0.0f, 0.0f, 0.0f);
 	for (uint32_t k = 0; k < 2 * L; k++) {
 		size_t slot = (size_t)k * P + pid;
@@ -340,16 +519,32 @@ __global__ void taa_kernel(uint32_t W, uint32_t H, const float4* __restrict__ cu
 // Launch sequence of one frame
 // ------------------------------------------------------------------------------------------------
 
-static int g_waveBlocksPerSM[3] = {0, 0, 0};
+enum { kGridPrimary = 0, kGridAnyQueue, kGridBounce, kGridPrimaryTrace, kGridAnyRefill, kGridBounceTrace,
+       kGridPrimaryShade, kGridBounceShade, kGridCount };
+static int g_waveBlocksPerSM[kGridCount] = {};
 
-static phe_status wave_grid(int which, const void* kernel, int* grid)
+static const void* wave_kernel(int which)
+{
+	switch (which) {
+	case kGridPrimary: return (const void*)primary_kernel;
+	case kGridAnyQueue: return (const void*)any_queue_kernel;
+	case kGridBounce: return (const void*)bounce_kernel;
+	case kGridPrimaryTrace: return (const void*)primary_trace_kernel;
+	case kGridAnyRefill: return (const void*)any_refill_kernel;
+	case kGridBounceTrace: return (const void*)bounce_trace_kernel;
+	case kGridPrimaryShade: return (const void*)primary_shade_kernel;
+	default: return (const void*)bounce_shade_kernel;
+	}
+}
+
+static phe_status wave_grid(int which, int* grid)
 {
 	DeviceInfo* d = nullptr;
 	phe_status st = device_info(&d);
 	if (st) return st;
 	if (g_waveBlocksPerSM[which] == 0) {
 		int b = 0;
-		PHE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, kWaveBlock, 0), "occupancy");
+		PHE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, wave_kernel(which), kWaveBlock, 0), "occupancy");
 		g_waveBlocksPerSM[which] = b > 0 ? b : 1;
 	}
 	*grid = g_waveBlocksPerSM[which] * d->numSMs;
@@ -359,38 +554,63 @@ static phe_status wave_grid(int which, const void* kernel, int* grid)
 phe_status prepare_frame()
 {
 	int g;
-	phe_status st;
-	if ((st = wave_grid(0, (const void*)primary_kernel, &g))) return st;
-	if ((st = wave_grid(1, (const void*)any_queue_kernel, &g))) return st;
-	return wave_grid(2, (const void*)bounce_kernel, &g);
+	for (int k = 0; k < kGridCount; k++) {
+		phe_status st = wave_grid(k, &g);
+		if (st) return st;
+	}
+	return PHE_OK;
 }
 
 phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, const FrameBuffers& fb, uint32_t resX,
-                        uint32_t resY, cudaStream_t stream, cudaEvent_t* ev)
+                        uint32_t resY, cudaStream_t stream, cudaEvent_t* ev, bool fused)
 {
 	phe_status st;
-	int g0 = 0, g1 = 0, g2 = 0;
-	if ((st = wave_grid(0, (const void*)primary_kernel, &g0))) return st;
-	if ((st = wave_grid(1, (const void*)any_queue_kernel, &g1))) return st;
-	if ((st = wave_grid(2, (const void*)bounce_kernel, &g2))) return st;
+	int g[kGridCount];
+	for (int k = 0; k < kGridCount; k++)
+		if ((st = wave_grid(k, &g[k]))) return st;
 	PHE_CUDA_TRY(cudaMemsetAsync(fb.counters, 0, sizeof(uint32_t) * kNumCounters, stream), "clear frame counters");
-	auto mark = [&](int i) { if (ev) cudaEventRecord(ev[i], stream); };
-	mark(0);
-	primary_kernel<<<g0, kWaveBlock, 0, stream>>>(scene->dev, dParams, fb, scene->status);
-	mark(1);
-	any_queue_kernel<<<g1, kWaveBlock, 0, stream>>>(scene->dev, fb.shadowRays, fb.shadowSlots, fb.counters + kCtrShadow0,
-	                                                fb.inLight, fb.counters + kCtrWork2, scene->status);
-	mark(2);
-	bounce_kernel<<<g2, kWaveBlock, 0, stream>>>(scene->dev, dParams, fb, scene->status);
-	mark(3);
-	any_queue_kernel<<<g1, kWaveBlock, 0, stream>>>(scene->dev, fb.shadowRays + fb.capacityLP,
-	                                                fb.shadowSlots + fb.capacityLP, fb.counters + kCtrShadow1, fb.inLight,
-	                                                fb.counters + kCtrWork3, scene->status);
-	mark(4);
+	int e = 0;
+	auto mark = [&]() { if (ev) cudaEventRecord(ev[e++], stream); };
 	dim3 block(16, 8);
 	dim3 grid((resX + 15) / 16, (resY + 7) / 8);
+	mark();
+	if (fused) {
+		primary_kernel<<<g[kGridPrimary], kWaveBlock, 0, stream>>>(scene->dev, dParams, fb, scene->status);
+		mark();
+		any_queue_kernel<<<g[kGridAnyQueue], kWaveBlock, 0, stream>>>(scene->dev, fb.shadowRays, fb.shadowSlots,
+		                                                               fb.counters + kCtrShadow0, fb.inLight,
+		                                                               fb.counters + kCtrWork2, scene->status);
+		mark();
+		bounce_kernel<<<g[kGridBounce], kWaveBlock, 0, stream>>>(scene->dev, dParams, fb, scene->status);
+		mark();
+		any_queue_kernel<<<g[kGridAnyQueue], kWaveBlock, 0, stream>>>(scene->dev, fb.shadowRays + fb.capacityLP,
+		                                                               fb.shadowSlots + fb.capacityLP,
+		                                                               fb.counters + kCtrShadow1, fb.inLight,
+		                                                               fb.counters + kCtrWork3, scene->status);
+		mark();
+	} else {
+		primary_trace_kernel<<<g[kGridPrimaryTrace], kWaveBlock, 0, stream>>>(scene->dev, dParams, fb, scene->status);
+		mark();
+		primary_shade_kernel<<<g[kGridPrimaryShade], kWaveBlock, 0, stream>>>(scene->dev, dParams, fb);
+		mark();
+		any_refill_kernel<<<g[kGridAnyRefill], kWaveBlock, 0, stream>>>(scene->dev, fb.shadowRays, fb.shadowSlots,
+		                                                                 fb.counters + kCtrShadow0, fb.inLight,
+		                                                                 fb.counters + kCtrWork2, fb.refill,
+		                                                                 scene->status);
+		mark();
+		bounce_trace_kernel<<<g[kGridBounceTrace], kWaveBlock, 0, stream>>>(scene->dev, fb, scene->status);
+		mark();
+		bounce_shade_kernel<<<g[kGridBounceShade], kWaveBlock, 0, stream>>>(scene->dev, dParams, fb);
+		mark();
+		any_refill_kernel<<<g[kGridAnyRefill], kWaveBlock, 0, stream>>>(scene->dev, fb.shadowRays + fb.capacityLP,
+		                                                                 fb.shadowSlots + fb.capacityLP,
+		                                                                 fb.counters + kCtrShadow1, fb.inLight,
+		                                                                 fb.counters + kCtrWork3, fb.refill,
+		                                                                 scene->status);
+		mark();
+	}
 	resolve_taa_kernel<<<grid, block, 0, stream>>>(dParams, fb);
-	mark(5);
+	mark();
 	PHE_CUDA_TRY(cudaGetLastError(), "frame kernel launch");
 	return PHE_OK;
 }

@@ -50,14 +50,26 @@ struct FrameBuffers {
 	float4* color;            // [P] TAA output
 	uint32_t* counters;       // [kNumCounters]
 	uint32_t capacityLP;      // L * P
+	phe_ray_hit* primaryHits; // [P] closest hits of the primary rays, in 8x8-tile ray order
+	phe_ray_hit* bounceHits;  // [P] closest hits of the bounce queue
+	unsigned long long* rayTotals; // [4] rays cast per pass, summed over frames until reset
+	int refill;               // lane-refill threshold of the persistent traversal kernels
 };
+
+// Allocates a renderer's frame buffers for up to `pixels` pixels and `lights` lights at once, so that
+// later resolutions within that capacity reuse them (no allocation per request).
+phe_status renderer_reserve(phe_renderer* r, uint64_t pixels, uint32_t lights);
 
 // Resolves launch shapes (occupancy queries); call before capturing a frame into a graph.
 phe_status prepare_frame();
-// Number of kernels in a frame (primary, primary any-hit, bounce, bounce any-hit, resolve + TAA).
-constexpr int kFrameKernels = 5;
-// `events` (optional, kFrameKernels + 1 entries) are recorded on `stream` around each kernel.
+// Kernels of one frame: primary trace, primary shade, primary any-hit, bounce trace, bounce shade,
+// bounce any-hit, resolve + TAA (kFrameKernels); the fused pipeline has five (primary and bounce
+// trace+shade fused).
+constexpr int kFrameKernels = 7;
+constexpr int kFusedFrameKernels = 5;
+// `events` (optional, kernels + 1 entries) are recorded on `stream` around each kernel. `fused`
+// selects the pipeline with traversal and shading in one kernel.
 phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, const FrameBuffers& fb, uint32_t resX,
-                        uint32_t resY, cudaStream_t stream, cudaEvent_t* events = nullptr);
+                        uint32_t resY, cudaStream_t stream, cudaEvent_t* events = nullptr, bool fused = false);
 
 } // namespace phe_gb300

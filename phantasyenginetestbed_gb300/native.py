@@ -76,6 +76,28 @@ class BatchTuningRow(C.Structure):
     _fields_ = [("params", BatchParams), ("ms", C.c_float)]
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("memoryBudget", C.c_uint64), ("maxInFlight", C.c_uint32), ("renderSlots", C.c_uint32),
+                ("maxRenderPixels", C.c_uint32), ("maxLights", C.c_uint32), ("serial", C.c_int32), ("pad", C.c_uint32)]
+
+
+class Request(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("scene", C.c_uint32), ("numRays", C.c_uint32), ("spp", C.c_uint32),
+                ("rays", C.c_void_p), ("out", C.c_void_p), ("resX", C.c_uint32), ("resY", C.c_uint32),
+                ("numLights", C.c_uint32), ("pad", C.c_uint32), ("cam", CameraDef), ("camPos", C.c_float * 3),
+                ("pad2", C.c_float), ("lights", C.c_void_p), ("seed", C.c_uint64)]
+
+
+class RequestStats(C.Structure):
+    _fields_ = [("submitMs", C.c_double), ("admitMs", C.c_double), ("doneMs", C.c_double), ("rays", C.c_uint64),
+                ("status", C.c_int), ("pad", C.c_uint32)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("waves", C.c_uint64), ("raysCompleted", C.c_uint64), ("bytesInUse", C.c_uint64),
+                ("pending", C.c_uint32), ("inFlight", C.c_uint32)]
+
+
 class PheError(RuntimeError):
     def __init__(self, status: int, where: str, text: str):
         super().__init__(f"{where}: status {status}: {text}")
@@ -128,7 +150,8 @@ SIGNATURES: dict[str, tuple] = {
     "phe_renderer_ray_counts": (_I32, [_VP, C.POINTER(C.c_uint64), _VP]),
     "phe_renderer_set_kernel_timing": (_I32, [_VP, _I32]),
     "phe_renderer_frame_param_bytes": (_U32, []),
-    "phe_renderer_kernel_times": (_I32, [_VP, C.POINTER(C.c_double), C.POINTER(_U32)]),
+    "phe_renderer_kernel_times": (_I32, [_VP, C.POINTER(C.c_double), C.POINTER(_U32), C.POINTER(_U32)]),
+    "phe_renderer_set_pipeline": (_I32, [_VP, _I32, _I32]),
     "phe_batch_default_params": (None, [C.POINTER(BatchParams)]),
     "phe_batch_create": (_I32, [C.POINTER(_VP), _U32, C.POINTER(BatchItem), _U32, C.POINTER(BatchParams), C.POINTER(_VP)]),
     "phe_batch_update": (_I32, [_VP, C.POINTER(BatchItem), _U32]),
@@ -139,6 +162,18 @@ SIGNATURES: dict[str, tuple] = {
                                   C.POINTER(BatchTuningRow), _U32, C.POINTER(_U32)]),
     "phe_batch_destroy": (_I32, [_VP]),
     "phe_batch_cast_noalloc": (_I32, [C.POINTER(_VP), _U32, C.POINTER(BatchItem), _U32, _VP]),
+    "phe_renderer_reset_ray_totals": (_I32, [_VP, _VP]),
+    "phe_renderer_ray_totals_async": (_I32, [_VP, C.POINTER(C.c_uint64), _VP]),
+    "phe_server_default_config": (None, [C.POINTER(ServerConfig)]),
+    "phe_server_create": (_I32, [C.POINTER(ServerConfig), C.POINTER(_VP)]),
+    "phe_server_add_scene": (_I32, [_VP, _VP, C.POINTER(_U32)]),
+    "phe_server_submit": (_I32, [_VP, C.POINTER(Request), C.POINTER(C.c_uint64)]),
+    "phe_server_poll": (_I32, [_VP, C.c_uint64, C.POINTER(RequestStats)]),
+    "phe_server_wait": (_I32, [_VP, C.c_uint64, C.POINTER(RequestStats)]),
+    "phe_server_drain": (_I32, [_VP]),
+    "phe_server_release": (_I32, [_VP, C.c_uint64]),
+    "phe_server_get_stats": (_I32, [_VP, C.POINTER(ServerStats)]),
+    "phe_server_destroy": (_I32, [_VP]),
     "phe_taa_resolve": (_I32, [_U32, _U32, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
 }
 

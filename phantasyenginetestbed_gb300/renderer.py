@@ -93,11 +93,15 @@ class CudaTracerRenderer:
         check(lib().phe_renderer_set_kernel_timing(self.handle, 1 if enable else 0), "phe_renderer_set_kernel_timing")
 
     def kernel_times(self):
-        """(summed ms per frame kernel, frames timed)."""
-        ms = (C.c_double * 5)()
-        n = C.c_uint32()
-        check(lib().phe_renderer_kernel_times(self.handle, ms, C.byref(n)), "phe_renderer_kernel_times")
-        return np.array(list(ms)), int(n.value)
+        """(summed ms per frame kernel in launch order, frames timed)."""
+        ms = (C.c_double * 8)()
+        k, n = C.c_uint32(), C.c_uint32()
+        check(lib().phe_renderer_kernel_times(self.handle, ms, C.byref(k), C.byref(n)), "phe_renderer_kernel_times")
+        return np.array(list(ms)[:k.value]), int(n.value)
+
+    def set_pipeline(self, fused: bool = True, refill: int = 28) -> None:
+        """fused: traversal + shading in one kernel per bounce; refill: lane-refill threshold (0..32)."""
+        check(lib().phe_renderer_set_pipeline(self.handle, 1 if fused else 0, refill), "phe_renderer_set_pipeline")
 
     def close(self) -> None:
         if getattr(self, "handle", None):

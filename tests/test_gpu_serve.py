@@ -1,0 +1,138 @@
+"""Serving loop: continuous batching of ray-query and render requests. Each result is identical alone
+and in the mix; ray queries match the oracle; renders match the renderer object; admission respects
+the memory budget; the serial baseline gives the same results."""
+import math
+
+import numpy as np
+import pytest
+
+import phantasyenginetestbed_gb300 as P
+from phantasyenginetestbed_gb300.renderer import READ_COLOR, CudaTracerRenderer, make_lights
+from phantasyenginetestbed_gb300.serve import REQ_ANY, REQ_CLOSEST, REQ_RENDER, Server, pinned
+from oracle import oracle as O
+from tests.helpers import C1_CAM, cam_struct, random_rays
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def scenes():
+    out = []
+    for args in [(32, 20, True, 71), (64, 60, False, 72)]:
+        s = P.generate_scene(*args)
+        b = P.build_sbvh(s.tri_verts)
+        out.append((s, b, P.Scene(b.nodes, b.verts, b.slot_datas(s.datas), s.materials)))
+    return out
+
+
+def _requests(scenes, seed):
+    rng = np.random.default_rng(seed)
+    reqs = []
+    for i in range(14):
+        si = i % 2
+        s = scenes[si][0]
+        if i % 3 == 2:
+            res = (int(rng.choice([64, 96, 128])), int(rng.choice([48, 64, 96])))
+            k = s.scale
+            cam_pos = (0.5 * k, -0.3 * k, 0.6 * k)
+            cam = O.camera_def(cam_pos, C1_CAM["dir"], C1_CAM["up"], math.radians(60), res)
+            lights = make_lights(np.array([[0.5, 0.5, 2.0], [0.2, 0.8, 1.0]], np.float32)[: 1 + i % 2] * np.float32(k),
+                                 range_=1000.0 * k)
+            reqs.append(("render", si, dict(res=res, spp=1 + i % 3, cam=cam, cam_pos=cam_pos, lights=lights, seed=100 + i)))
+        else:
+            n = int(rng.integers(1, 20000))
+            rays = random_rays(n, [0, 0, 0.02], [s.scale, s.scale, 0.4 * s.scale], seed * 100 + i)
+            kind = REQ_ANY if i % 4 == 1 else REQ_CLOSEST
+            if kind == REQ_ANY:
+                rays["tMax"] = np.float32(0.4 * s.scale)
+            reqs.append(("rays", si, dict(rays=rays, kind=kind)))
+    return reqs
+
+
+def _submit(server, ids, req):
+    kind, si, a = req
+    if kind == "render":
+        out = pinned((a["res"][1], a["res"][0], 4), np.float32)
+        rid = server.submit_render(ids[si], a["res"], a["spp"], cam_struct(a["cam"]), a["cam_pos"], a["lights"], a["seed"], out)
+    else:
+        rays = pinned(len(a["rays"]), P.RAY_IN_DTYPE)
+        rays[:] = a["rays"]
+        out = pinned(len(rays) * (1 if a["kind"] == REQ_ANY else 16), np.uint8)
+        rid = server.submit_rays(ids[si], rays, out, a["kind"])
+    return rid, out
+
+
+def test_each_result_is_the_same_alone_and_in_the_mix(scenes):
+    server = Server(render_slots=3)
+    ids = [server.add_scene(x[2]) for x in scenes]
+    reqs = _requests(scenes, 1)
+    alone = []
+    for q in reqs:
+        rid, out = _submit(server, ids, q)
+        st = server.wait(rid)
+        assert st.status == 0 and st.rays > 0
+        alone.append(out.copy())
+    waves_before = server.stats()["waves"]
+    mixed = [_submit(server, ids, q) for q in reqs]   # all in flight together
+    server.drain()
+    waves = server.stats()["waves"] - waves_before
+    for (rid, out), a in zip(mixed, alone):
+        st = server.poll(rid)
+        assert st is not None and st.status == 0
+        assert np.array_equal(out.view(np.uint8), a.view(np.uint8))
+    assert waves < len([q for q in reqs if q[0] == "rays"])  # queries shared waves
+    # ray queries against the oracle, renders against the renderer object
+    for (kind, si, a), res in zip(reqs, alone):
+        s, b, sc = scenes[si]
+        if kind == "rays":
+            if a["kind"] == REQ_ANY:
+                assert np.array_equal(res, O.any_rays(b.nodes, b.verts, a["rays"]))
+            else:
+                rep = O.compare_closest(res.view(P.RAY_HIT_DTYPE), O.cast_rays(b.nodes, b.verts, a["rays"]), a["rays"],
+                                        b.slot_to_tri, b.verts)
+                assert rep["ok"], rep
+        else:
+            r = CudaTracerRenderer()
+            r.setStaticScene(sc)
+            r.setTargetResolution(a["res"])
+            r.set_seed(a["seed"], 0)
+            r.resetTAA()
+            for f in range(a["spp"]):
+                r.set_camera_def(cam_struct(a["cam"]), a["cam_pos"], P.halton_jitter(f))
+                r.render(a["lights"])
+            assert np.array_equal(r.read(READ_COLOR), res)
+    server.close()
+
+
+def test_budget_admission_and_serial_baseline(scenes):
+    sc_bytes = sum(x[2].device_bytes() for x in scenes)
+    # room for the scenes plus about two 20K-ray queries at a time
+    server = Server(memory_budget=sc_bytes + 2 * 20000 * 48 + 4096, render_slots=1)
+    ids = [server.add_scene(x[2]) for x in scenes]
+    s = scenes[0][0]
+    big = pinned(200000, P.RAY_IN_DTYPE)
+    big[:] = random_rays(200000, [0, 0, 0.02], [s.scale, s.scale, 0.4 * s.scale], 3)
+    with pytest.raises(P.PheError) as e:
+        server.submit_rays(ids[0], big, pinned(200000 * 16, np.uint8))
+    assert e.value.status == 5   # PHE_ERR_BUDGET
+    queries = []
+    for i in range(8):
+        rays = pinned(20000, P.RAY_IN_DTYPE)
+        rays[:] = random_rays(20000, [0, 0, 0.02], [s.scale, s.scale, 0.4 * s.scale], 10 + i)
+        out = pinned(20000 * 16, np.uint8)
+        queries.append((server.submit_rays(ids[0], rays, out), rays, out))
+    server.drain()
+    b = scenes[0][1]
+    for rid, rays, out in queries:
+        assert server.poll(rid).status == 0
+        rep = O.compare_closest(out.view(P.RAY_HIT_DTYPE), O.cast_rays(b.nodes, b.verts, rays), rays, b.slot_to_tri, b.verts)
+        assert rep["ok"], rep
+    server.close()
+    # the serial baseline returns the same bytes
+    serial = Server(serial=True, render_slots=1)
+    ids = [serial.add_scene(x[2]) for x in scenes]
+    for rid, rays, out in queries[:3]:
+        out2 = pinned(len(rays) * 16, np.uint8)
+        serial.wait(serial.submit_rays(ids[0], rays, out2))
+        assert np.array_equal(out2, out)
+    serial.close()

@@ -39,10 +39,11 @@ def _compare(gpu, ref, what):
     return d.max()
 
 
-@pytest.mark.parametrize("graph", [False, True])
-def test_frame_matches_oracle_small(graph):
+@pytest.mark.parametrize("graph,fused,refill", [(False, False, 20), (True, False, 0), (True, False, 32), (False, True, 20)])
+def test_frame_matches_oracle_small(graph, fused, refill):
     res = (320, 184)
     s, b, datas, scene, cam, cam_pos, lights, r = _setup("c2_256_2000", res, [(0.5, 0.5, 2.0), (0.1, 0.9, 1.0)], graph)
+    r.set_pipeline(fused=fused, refill=refill)
     r.set_seed(1234, 0)
     r.resetTAA()
     jit = P.halton_jitter(3)
