@@ -37,9 +37,9 @@ RES = (1920, 1080)
 SEED = 2024
 CAM_DIR = (0.0, 0.8, -0.6)
 CAM_UP = (0.0, 0.6, 0.8)
-KERNELS = ["primary_trace", "primary_shade", "primary_shadow", "bounce_trace", "bounce_shade", "bounce_shadow",
-           "resolve_taa"]
-KERNELS_FUSED = ["primary", "primary_shadow", "bounce", "bounce_shadow", "resolve_taa"]
+KERNELS = ["primary_trace", "primary_shade", "primary_shadow", "bounce_bin", "bounce_trace", "bounce_shade",
+           "bounce_shadow", "resolve_taa"]
+KERNELS_FUSED = ["primary", "primary_shadow", "bounce_bin", "bounce", "bounce_shadow", "resolve_taa"]
 # traversal kernel -> the pass whose rays it casts
 TRACE_PASS = {"primary_trace": "primary", "primary": "primary", "primary_shadow": "primary_shadow",
               "bounce_trace": "bounce", "bounce": "bounce", "bounce_shadow": "bounce_shadow"}
@@ -55,8 +55,9 @@ def parse():
     ap.add_argument("--pipeline", choices=["fused", "split"], default="fused",
                     help="fused: traversal + shading in one kernel per bounce (5 kernels); split: 7 kernels")
     ap.add_argument("--refill", type=int, default=28, help="lane-refill threshold of the split pipeline")
+    ap.add_argument("--sort-window", type=int, default=0, help="bin bounce rays by octant in windows of N (0 = off)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["frame", "batch", "large", "serve"], default="frame",
+    ap.add_argument("--workload", choices=["frame", "plain", "batch", "large", "serve"], default="frame",
                     help="frame (default, the headline): 1080p wavefront frame; batch: 64 uneven batches over 4 "
                          "scenes in one launch vs 64 plain launches; large: 8.6M-triangle scene, 4096x4096, 4 "
                          "lights; serve: Poisson request arrivals through the serving loop")
@@ -216,7 +217,7 @@ def run_ours(args, world, rank, local):
     s, b, cam_pos, lights, build_s = frame_inputs()
     scene = P.Scene(b.nodes, b.verts, b.slot_datas(s.datas), s.materials)
     r = CudaTracerRenderer(use_graph=not args.no_graph)
-    r.set_pipeline(fused=args.pipeline == "fused", refill=args.refill)
+    r.set_pipeline(fused=args.pipeline == "fused", refill=args.refill, sort_window=args.sort_window)
     r.setStaticScene(scene)
     r.setTargetResolution(RES)
     r.set_seed(SEED, 0)
@@ -343,7 +344,7 @@ def run_ours(args, world, rank, local):
                    "bvh_slots": int(len(b.verts)), "sbvh_build_s": round(build_s, 2), "lights": 1,
                    "rays_per_frame": round(rays_per_frame, 1), "rays_by_pass": {k: round(v, 1) for k, v in stage_rays.items()},
                    "cuda_graph": not args.no_graph, "pipeline": args.pipeline,
-                   "refill_threshold": args.refill, "l2": "flushed before every timed frame (512 MiB write)",
+                   "refill_threshold": args.refill, "sort_window": args.sort_window, "l2": "flushed before every timed frame (512 MiB write)",
                    "parallelism": f"replicas x{world}"},
         "latency_ms": {"p50": round(lat[len(lat) // 2], 4), "p99": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 4)},
         "passes": per_kernel,
@@ -406,6 +407,51 @@ def _timed(fn, steps, stream, flush=None):
         ev[k][1].record(stream)
     torch.cuda.synchronize()
     return [a.elapsed_time(b) for a, b in ev]
+
+
+def run_plain(args):
+    """The plain closest-hit configuration: 512x512 pinhole primary rays on the 9,392-triangle scene
+    (64x64-cell heightfield + 100 axis-aligned cubes), through phe_cast_closest (persistent),
+    phe_cast_closest_plain (one ray per thread) and phe_cast_any, with the CPU castRay restatement on
+    all host cores beside it. Each step is one launch over all rays; L2 flushed before each."""
+    import torch
+    import phantasyenginetestbed_gb300 as P
+    torch.cuda.set_device(0)
+    stream = torch.cuda.current_stream()
+    s, b, build_s = _scene_with_bvh("c1_64_100")
+    scene = P.Scene(b.nodes, b.verts)
+    res = (512, 512)
+    n = res[0] * res[1]
+    cam = P.camera_def((0.5, -0.3, 0.6), CAM_DIR, CAM_UP, 60.0, res)
+    rays = torch.empty(n * 32, dtype=torch.uint8, device="cuda")
+    P.gen_primary_rays(rays, cam, res, order=1)
+    hits = torch.empty(n * 16, dtype=torch.uint8, device="cuda")
+    vis = torch.empty(n, dtype=torch.uint8, device="cuda")
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    out = {}
+    for name, fn in (("closest_persistent", lambda: P.cast_closest(scene, rays, hits, n, stream=stream)),
+                     ("closest_plain", lambda: P.cast_closest_plain(scene, rays, hits, n, stream=stream)),
+                     ("any", lambda: P.cast_any(scene, rays, vis, n, stream=stream))):
+        for _ in range(args.warmup):
+            fn()
+        t = statistics.median(_timed(fn, args.steps, stream, flush))
+        out[name] = {"ms": round(t, 4), "Mrays_s": round(n / t / 1e3, 1)}
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        host_rays = rays.cpu().numpy().view(P.RAY_IN_DTYPE)
+        O.cast_rays(b.nodes, b.verts, host_rays)
+        t0, reps = time.perf_counter(), 0
+        while time.perf_counter() - t0 < 5.0:
+            O.cast_rays(b.nodes, b.verts, host_rays)
+            reps += 1
+        el = time.perf_counter() - t0
+        cpu = {"value": round(n * reps / el / 1e6, 2), "unit": "Mrays/s", "cores": O.threads(), "kind": "port",
+               "sample": f"{reps} passes over the 512x512 primary rays (~5 s)"}
+    line = {"workload": "plain", "metric": METRIC, "unit": "Mrays/s", "rays": n, "triangles": int(len(s.tri_verts)),
+            "bvh_nodes": int(len(b.nodes)), "bvh_slots": int(len(b.verts)), "launches": out, "cpu_baseline": cpu,
+            "l2": "flushed before every timed launch"}
+    print(json.dumps(line), flush=True)
 
 
 def run_batch(args):
@@ -584,13 +630,13 @@ def run_serve(args):
                 reqs.append((t, "rays", si, n, REQ_CLOSEST if r.random() < 0.7 else REQ_ANY))
         return reqs
 
-    def run(server, ids, reqs):
+    def run(server, ids, reqs, burst=False):
         cams = {}
         start = time.perf_counter() + 0.05
         sub = []
         for j, q in enumerate(reqs):
             dt = start + q[0] - time.perf_counter()
-            if dt > 0:
+            if dt > 0 and not burst:
                 time.sleep(dt)
             arrival = (start + q[0])
             if q[1] == "render":
@@ -606,9 +652,10 @@ def run_serve(args):
                 rid = server.submit_rays(ids[q[2]], pools[q[2]][: q[3]], out_ring[j % 8], q[4])
             sub.append((rid, arrival))
         server.drain()
-        lat, rays, t_first, t_last = [], 0, None, 0.0
+        lat, rays, t_first, t_last, errors = [], 0, None, 0.0, 0
         for rid, arrival in sub:
             st = server.poll(rid)
+            errors += st.status != 0
             lat.append(st.doneMs - st.submitMs)
             rays += st.rays
             t_last = max(t_last, st.doneMs)
@@ -616,7 +663,7 @@ def run_serve(args):
             server.release(rid)
         lat.sort()
         span_ms = t_last - t_first
-        return {"requests": len(sub), "p50_ms": round(lat[len(lat) // 2], 3),
+        return {"requests": len(sub), "errors": int(errors), "p50_ms": round(lat[len(lat) // 2], 3),
                 "p99_ms": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 3),
                 "rays": int(rays), "span_s": round(span_ms / 1e3, 3), "Mrays_s": round(rays / span_ms / 1e3, 1)}
 
@@ -630,6 +677,16 @@ def run_serve(args):
             row[mode] = run(server, ids, reqs)
             server.close()
         results[str(int(rate))] = row
+    # Saturation: the highest rate's requests all submitted at once (makespan throughput).
+    burst = {}
+    reqs = make_requests(max(float(x) for x in args.rates.split(",")), args.duration, 99)
+    for mode in ("continuous", "serial"):
+        server = Server(memory_budget=120 << 30, render_slots=4, serial=(mode == "serial"))
+        ids = [server.add_scene(sc) for sc in scenes]
+        burst[mode] = run(server, ids, reqs, burst=True)
+        server.close()
+    burst["speedup"] = round(burst["continuous"]["Mrays_s"] / max(burst["serial"]["Mrays_s"], 1e-9), 3)
+    results["burst"] = burst
     line = {"workload": "serve", "metric": METRIC, "unit": "Mrays/s",
             "scenes_triangles": [int(len(s.tri_verts)) for s, _ in built], "scene_build_s": round(build_s, 1),
             "budget_bytes": 120 << 30, "arrivals_s": args.duration, "rates": results}
@@ -644,7 +701,7 @@ def main():
     elif args.workload == "frame":
         run_ours(args, world, rank, local)
     else:
-        {"batch": run_batch, "large": run_large, "serve": run_serve}[args.workload](args)
+        {"plain": run_plain, "batch": run_batch, "large": run_large, "serve": run_serve}[args.workload](args)
 
 
 if __name__ == "__main__":

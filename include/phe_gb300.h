@@ -296,11 +296,14 @@ phe_status phe_renderer_read(const phe_renderer* renderer, int which, void* host
 /* Rays cast by the last frame: primary, primary shadow, bounce, bounce shadow. Synchronises `stream`. */
 phe_status phe_renderer_ray_counts(const phe_renderer* renderer, uint64_t counts[4], void* stream);
 
-/* Frame pipeline: fused = 1 (the default) runs traversal and shading in one kernel per bounce (5
- * kernels); 0 splits them (7 kernels: primary trace, primary shade, primary shadow, bounce trace, bounce
+/* Frame pipeline: fused = 1 (the default) runs traversal and shading in one kernel per bounce (6
+ * kernels: primary, primary shadow, bounce binning, bounce, bounce shadow, resolve + TAA); 0 splits
+ * them (8 kernels: primary trace, primary shade, primary shadow, bounce binning, bounce trace, bounce
  * shade, bounce shadow, resolve + TAA) so the persistent traversal kernels refill idle lanes with new
- * rays when fewer than `refill` (0..32, default 28) lanes of a warp are still busy. */
-phe_status phe_renderer_set_pipeline(phe_renderer* renderer, int fused, int refill);
+ * rays when fewer than `refill` (0..32, default 28) lanes of a warp are still busy. sortWindow (0 or
+ * a multiple of 256 up to 4096; default 0) bins the bounce rays by direction octant within windows of
+ * that many queue entries before they are traced. */
+phe_status phe_renderer_set_pipeline(phe_renderer* renderer, int fused, int refill, int sortWindow);
 /* Per-kernel timing with CUDA events on the render stream (direct launches; ignored while a graph is
  * replayed). Enabling resets the totals. kernel_times returns the summed milliseconds per frame kernel
  * (in launch order, `numKernels` of them) and the number of frames timed. */

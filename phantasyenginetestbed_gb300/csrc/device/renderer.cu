@@ -37,6 +37,7 @@ struct phe_renderer {
 	bool cameraSet = false;
 	bool fused = true;                     // traversal and shading fused in one kernel per bounce
 	int refill = 28;                       // lane-refill threshold of the persistent traversal kernels
+	int sortWindow = 0;                    // bounce-ray binning window (0 = off)
 	bool timing = false;                   // record events around each kernel (direct launches only)
 	cudaEvent_t events[kFrameKernels + 1] = {};
 	double kernelMs[kFrameKernels] = {};   // accumulated since timing was enabled
@@ -93,6 +94,7 @@ static phe_status allocate(phe_renderer* r, uint32_t resX, uint32_t resY, uint32
 		P * sizeof(phe_ray_hit),      // primaryHits
 		P * sizeof(phe_ray_hit),      // bounceHits
 		4 * sizeof(unsigned long long), // rayTotals
+		P * sizeof(uint32_t),         // bouncePerm
 	};
 	size_t total = 0;
 	for (size_t s : sizes) total += align256(s);
@@ -118,6 +120,8 @@ static phe_status allocate(phe_renderer* r, uint32_t resX, uint32_t resY, uint32
 	fb.primaryHits = (phe_ray_hit*)take(13);
 	fb.bounceHits = (phe_ray_hit*)take(14);
 	fb.rayTotals = (unsigned long long*)take(15);
+	fb.bouncePerm = (uint32_t*)take(16);
+	fb.sortWindow = r->sortWindow;
 	fb.capacityLP = (uint32_t)LP;
 	fb.refill = r->refill;
 	r->capacityP = P;
@@ -170,13 +174,17 @@ extern "C" phe_status phe_renderer_kernel_times(phe_renderer* r, double msTotal[
 	return PHE_OK;
 }
 
-extern "C" phe_status phe_renderer_set_pipeline(phe_renderer* r, int fused, int refill)
+extern "C" phe_status phe_renderer_set_pipeline(phe_renderer* r, int fused, int refill, int sortWindow)
 {
 	if (!r) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_set_pipeline: null renderer");
 	if (refill < 0 || refill > 32) return fail(PHE_ERR_INVALID_ARGUMENT, "refill threshold must be in [0, 32]");
+	if (sortWindow != 0 && (sortWindow < 256 || sortWindow > 4096 || sortWindow % 256))
+		return fail(PHE_ERR_INVALID_ARGUMENT, "sort window must be 0 or a multiple of 256 in [256, 4096]");
 	r->fused = fused != 0;
 	r->refill = refill;
 	r->fb.refill = refill;
+	r->sortWindow = sortWindow;
+	r->fb.sortWindow = sortWindow;
 	if (r->graphExec) {
 		cudaGraphExecDestroy(r->graphExec);
 		r->graphExec = nullptr;

@@ -20,6 +20,7 @@
 #include <cstring>
 #include <deque>
 #include <mutex>
+#include <string>
 #include <thread>
 #include <unordered_map>
 #include <vector>
@@ -55,8 +56,8 @@ struct Request {
 	void* dMem = nullptr;           // query: rays then results
 	cudaEvent_t done = nullptr;
 	int slot = -1;                  // render slot
-	uint64_t* totals = nullptr;     // pinned, 4 per render request
 	uint64_t rays = 0;
+	std::string error;              // message of a failed request (set on the scheduler thread)
 };
 
 struct RenderSlot {
@@ -134,6 +135,7 @@ cudaEvent_t take_event(phe_server* s)
 void finish(phe_server* s, Request* r, phe_status st)
 {
 	r->status = st;
+	if (st != PHE_OK) r->error = phe_last_error();
 	r->tDone = now_ms(s->t0);
 	r->state = kDone;
 	s->bytesInUse -= r->bytes;
@@ -207,6 +209,7 @@ phe_status issue_render(phe_server* s, Request* r, RenderSlot& slot)
 	phe_renderer* R = slot.renderer;
 	cudaStream_t st = slot.stream;
 	phe_status ps;
+	if ((ps = phe_renderer_set_static_scene(R, s->scenes[d.scene]))) return ps;
 	if ((ps = phe_renderer_set_target_resolution(R, d.resX, d.resY))) return ps;
 	if ((ps = phe_renderer_set_seed(R, d.seed, 0))) return ps;
 	if ((ps = phe_renderer_reset_taa(R, st))) return ps;
@@ -523,7 +526,8 @@ extern "C" phe_status phe_server_wait(phe_server* s, uint64_t id, phe_request_st
 	Request* r = it->second;
 	s->cvDone.wait(lock, [&] { return r->state == kDone; });
 	fill_stats(r, out);
-	return r->status;
+	if (r->status != PHE_OK) return fail(r->status, "request %llu failed: %s", (unsigned long long)id, r->error.c_str());
+	return PHE_OK;
 }
 
 extern "C" phe_status phe_server_drain(phe_server* s)

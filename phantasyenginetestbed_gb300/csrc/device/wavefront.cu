@@ -178,6 +178,74 @@ __global__ void __launch_bounds__(kWaveBlock) any_queue_kernel(DeviceScene s, co
 	}
 }
 
+// Bins the bounce queue by direction octant (sign bits of dir.xyz) inside windows of fb.sortWindow
+// consecutive entries: a deterministic counting sort per window, so warps of the bounce pass trace
+// rays of one octant from one neighbourhood of the image. Writes fb.bouncePerm.
+constexpr int kBinBlock = 256;
+constexpr int kMaxSortWindow = 4096;
+
+__global__ void __launch_bounds__(kBinBlock) bin_bounce_kernel(FrameBuffers fb)
+{
+	const int W = fb.sortWindow;
+	if (W <= 0) return;
+	const uint32_t n = fb.counters[kCtrBounce];
+	const int per = W / kBinBlock;   // entries per thread (W is a multiple of kBinBlock, <= kMaxSortWindow)
+	__shared__ uint32_t cnt[8][kBinBlock];
+	__shared__ uint32_t bucketBase[8];
+	const int t = threadIdx.x;
+	for (uint32_t w0 = blockIdx.x * (uint32_t)W; w0 < n; w0 += gridDim.x * (uint32_t)W) {
+		uint32_t c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+		uint8_t keys[kMaxSortWindow / kBinBlock];
+		for (int k = 0; k < per; k++) {
+			uint32_t i = w0 + (uint32_t)(t * per + k);
+			uint8_t key = 0xFF;
+			if (i < n) {
+				float4 d = reinterpret_cast<const float4*>(fb.bounceRays + i)[1];
+				key = (uint8_t)((d.x < 0.0f ? 1 : 0) | (d.y < 0.0f ? 2 : 0) | (d.z < 0.0f ? 4 : 0));
+				c[key]++;
+			}
+			keys[k] = key;
+		}
+		for (int b = 0; b < 8; b++) cnt[b][t] = c[b];
+		__syncthreads();
+		// Exclusive scan of each bucket's per-thread counts: warp b scans bucket b (8 warps).
+		const int warp = t >> 5, lane = t & 31;
+		if (warp < 8) {
+			uint32_t local[kBinBlock / 32];
+			uint32_t sum = 0;
+			for (int j = 0; j < kBinBlock / 32; j++) {
+				local[j] = sum;
+				sum += cnt[warp][lane * (kBinBlock / 32) + j];
+			}
+			uint32_t incl = sum;
+			for (int o = 1; o < 32; o <<= 1) {
+				uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
+				if (lane >= o) incl += v;
+			}
+			uint32_t excl = incl - sum;
+			for (int j = 0; j < kBinBlock / 32; j++) cnt[warp][lane * (kBinBlock / 32) + j] = excl + local[j];
+			if (lane == 31) bucketBase[warp] = incl;   // bucket total for now
+		}
+		__syncthreads();
+		if (t == 0) {
+			uint32_t acc = 0;
+			for (int b = 0; b < 8; b++) {
+				uint32_t tot = bucketBase[b];
+				bucketBase[b] = acc;
+				acc += tot;
+			}
+		}
+		__syncthreads();
+		uint32_t rank[8];
+		for (int b = 0; b < 8; b++) rank[b] = bucketBase[b] + cnt[b][t];
+		for (int k = 0; k < per; k++) {
+			uint8_t key = keys[k];
+			if (key != 0xFF) fb.bouncePerm[w0 + rank[key]++] = w0 + (uint32_t)(t * per + k);
+		}
+		__syncthreads();
+	}
+}
+
 __global__ void __launch_bounds__(kWaveBlock) bounce_kernel(DeviceScene s, const FrameParamsDev* __restrict__ fpp,
                                                             FrameBuffers fb, uint32_t* __restrict__ status)
 {
@@ -198,9 +266,10 @@ __global__ void __launch_bounds__(kWaveBlock) bounce_kernel(DeviceScene s, const
 		uint32_t pid = 0;
 		f3 thr = mk3(0.0f, 0.0f, 0.0f);
 		if (active) {
-			r = load_ray(fb.bounceRays, i);
-			pid = fb.bouncePixel[i];
-			float4 t4 = fb.bounceThroughput[i];
+			uint32_t j = fb.sortWindow > 0 ? fb.bouncePerm[i] : i;
+			r = load_ray(fb.bounceRays, j);
+			pid = fb.bouncePixel[j];
+			float4 t4 = fb.bounceThroughput[j];
 			thr = mk3(t4.x, t4.y, t4.z);
 			h = empty_hit(r);
 			uint32_t err = trace<false>(s.nodes, s.tris, r, h);
@@ -263,7 +332,8 @@ struct CameraSource {
 
 struct ArraySource {
 	const phe_ray_in* rays;
-	__device__ __forceinline__ RayState load(uint32_t i) const { return load_ray(rays, i); }
+	const uint32_t* perm;   // optional: ray i of the pass is rays[perm[i]]
+	__device__ __forceinline__ RayState load(uint32_t i) const { return load_ray(rays, perm ? __ldg(perm + i) : i); }
 };
 
 struct HitSink {
@@ -294,14 +364,15 @@ __global__ void __launch_bounds__(kWaveBlock) any_refill_kernel(DeviceScene s, c
                                                                 uint8_t* __restrict__ inLight, uint32_t* __restrict__ work,
                                                                 int refill, uint32_t* __restrict__ status)
 {
-	uint32_t err = persistent_trace<true>(s.nodes, s.tris, ArraySource{rays}, VisibilitySink{inLight, slots}, *count,
+	uint32_t err = persistent_trace<true>(s.nodes, s.tris, ArraySource{rays, nullptr}, VisibilitySink{inLight, slots}, *count,
 	                                      work, refill);
 	if (err) atomicOr(status, err);
 }
 
 __global__ void __launch_bounds__(kWaveBlock) bounce_trace_kernel(DeviceScene s, FrameBuffers fb, uint32_t* __restrict__ status)
 {
-	uint32_t err = persistent_trace<false>(s.nodes, s.tris, ArraySource{fb.bounceRays}, HitSink{fb.bounceHits},
+	uint32_t err = persistent_trace<false>(s.nodes, s.tris, ArraySource{fb.bounceRays, fb.sortWindow > 0 ? fb.bouncePerm : nullptr},
+	                                       HitSink{fb.bounceHits},
 	                                       fb.counters[kCtrBounce], fb.counters + kCtrWork1, fb.refill);
 	if (err) atomicOr(status, err);
 }
@@ -371,12 +442,13 @@ __global__ void __launch_bounds__(kWaveBlock) bounce_shade_kernel(DeviceScene s,
 		f3 thr = mk3(0.0f, 0.0f, 0.0f), o = thr, d = thr;
 		float4 hv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 		if (active) {
-			pid = fb.bouncePixel[i];
-			float4 t4 = fb.bounceThroughput[i];
+			uint32_t j = fb.sortWindow > 0 ? fb.bouncePerm[i] : i;
+			pid = fb.bouncePixel[j];
+			float4 t4 = fb.bounceThroughput[j];
 			thr = mk3(t4.x, t4.y, t4.z);
 			hv = reinterpret_cast<const float4*>(fb.bounceHits)[i];
 			slot = __float_as_uint(hv.x);
-			const float4* rp = reinterpret_cast<const float4*>(fb.bounceRays + i);
+			const float4* rp = reinterpret_cast<const float4*>(fb.bounceRays + j);
 			float4 a = rp[0], b = rp[1];
 			o = mk3(a.x, a.y, a.z);
 			d = mk3(b.x, b.y, b.z);
@@ -573,6 +645,9 @@ phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, c
 	auto mark = [&]() { if (ev) cudaEventRecord(ev[e++], stream); };
 	dim3 block(16, 8);
 	dim3 grid((resX + 15) / 16, (resY + 7) / 8);
+	DeviceInfo* dinfo = nullptr;
+	if ((st = device_info(&dinfo))) return st;
+	int binGrid = dinfo->numSMs * 4;
 	mark();
 	if (fused) {
 		primary_kernel<<<g[kGridPrimary], kWaveBlock, 0, stream>>>(scene->dev, dParams, fb, scene->status);
@@ -580,6 +655,8 @@ phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, c
 		any_queue_kernel<<<g[kGridAnyQueue], kWaveBlock, 0, stream>>>(scene->dev, fb.shadowRays, fb.shadowSlots,
 		                                                               fb.counters + kCtrShadow0, fb.inLight,
 		                                                               fb.counters + kCtrWork2, scene->status);
+		mark();
+		bin_bounce_kernel<<<binGrid, kBinBlock, 0, stream>>>(fb);
 		mark();
 		bounce_kernel<<<g[kGridBounce], kWaveBlock, 0, stream>>>(scene->dev, dParams, fb, scene->status);
 		mark();
@@ -597,6 +674,8 @@ phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, c
 		                                                                 fb.counters + kCtrShadow0, fb.inLight,
 		                                                                 fb.counters + kCtrWork2, fb.refill,
 		                                                                 scene->status);
+		mark();
+		bin_bounce_kernel<<<binGrid, kBinBlock, 0, stream>>>(fb);
 		mark();
 		bounce_trace_kernel<<<g[kGridBounceTrace], kWaveBlock, 0, stream>>>(scene->dev, fb, scene->status);
 		mark();

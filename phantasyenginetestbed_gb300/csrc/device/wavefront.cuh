@@ -53,7 +53,10 @@ struct FrameBuffers {
 	phe_ray_hit* primaryHits; // [P] closest hits of the primary rays, in 8x8-tile ray order
 	phe_ray_hit* bounceHits;  // [P] closest hits of the bounce queue
 	unsigned long long* rayTotals; // [4] rays cast per pass, summed over frames until reset
+	uint32_t* bouncePerm;     // [P] bounce-queue order after binning by direction octant
 	int refill;               // lane-refill threshold of the persistent traversal kernels
+	int sortWindow;           // bounce rays are binned by direction octant within windows of this
+	                          // many queue entries (0 = queue order)
 };
 
 // Allocates a renderer's frame buffers for up to `pixels` pixels and `lights` lights at once, so that
@@ -62,11 +65,12 @@ phe_status renderer_reserve(phe_renderer* r, uint64_t pixels, uint32_t lights);
 
 // Resolves launch shapes (occupancy queries); call before capturing a frame into a graph.
 phe_status prepare_frame();
-// Kernels of one frame: primary trace, primary shade, primary any-hit, bounce trace, bounce shade,
-// bounce any-hit, resolve + TAA (kFrameKernels); the fused pipeline has five (primary and bounce
-// trace+shade fused).
-constexpr int kFrameKernels = 7;
-constexpr int kFusedFrameKernels = 5;
+// Kernels of one frame: primary trace, primary shade, primary any-hit, bounce binning, bounce trace,
+// bounce shade, bounce any-hit, resolve + TAA (kFrameKernels); the fused pipeline has six (primary
+// and bounce trace+shade fused). The binning kernel is launched even when sortWindow is 0 (it then
+// returns at once) so every frame has the same launch sequence.
+constexpr int kFrameKernels = 8;
+constexpr int kFusedFrameKernels = 6;
 // `events` (optional, kernels + 1 entries) are recorded on `stream` around each kernel. `fused`
 // selects the pipeline with traversal and shading in one kernel.
 phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, const FrameBuffers& fb, uint32_t resX,

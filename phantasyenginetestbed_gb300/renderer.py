@@ -99,9 +99,11 @@ class CudaTracerRenderer:
         check(lib().phe_renderer_kernel_times(self.handle, ms, C.byref(k), C.byref(n)), "phe_renderer_kernel_times")
         return np.array(list(ms)[:k.value]), int(n.value)
 
-    def set_pipeline(self, fused: bool = True, refill: int = 28) -> None:
-        """fused: traversal + shading in one kernel per bounce; refill: lane-refill threshold (0..32)."""
-        check(lib().phe_renderer_set_pipeline(self.handle, 1 if fused else 0, refill), "phe_renderer_set_pipeline")
+    def set_pipeline(self, fused: bool = True, refill: int = 28, sort_window: int = 0) -> None:
+        """fused: traversal + shading in one kernel per bounce; refill: lane-refill threshold (0..32);
+        sort_window: bin bounce rays by direction octant within windows of this many rays (0 = off)."""
+        check(lib().phe_renderer_set_pipeline(self.handle, 1 if fused else 0, refill, sort_window),
+              "phe_renderer_set_pipeline")
 
     def close(self) -> None:
         if getattr(self, "handle", None):

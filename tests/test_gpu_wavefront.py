@@ -39,11 +39,12 @@ def _compare(gpu, ref, what):
     return d.max()
 
 
-@pytest.mark.parametrize("graph,fused,refill", [(False, False, 20), (True, False, 0), (True, False, 32), (False, True, 20)])
-def test_frame_matches_oracle_small(graph, fused, refill):
+@pytest.mark.parametrize("graph,fused,refill,window", [(False, False, 20, 0), (True, False, 0, 1024), (True, False, 32, 256),
+                                                      (False, True, 20, 0), (True, True, 20, 4096)])
+def test_frame_matches_oracle_small(graph, fused, refill, window):
     res = (320, 184)
     s, b, datas, scene, cam, cam_pos, lights, r = _setup("c2_256_2000", res, [(0.5, 0.5, 2.0), (0.1, 0.9, 1.0)], graph)
-    r.set_pipeline(fused=fused, refill=refill)
+    r.set_pipeline(fused=fused, refill=refill, sort_window=window)
     r.set_seed(1234, 0)
     r.resetTAA()
     jit = P.halton_jitter(3)
