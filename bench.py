@@ -63,6 +63,8 @@ def parse():
                          "lights; serve: Poisson request arrivals through the serving loop")
     ap.add_argument("--rates", default="200,500,1000", help="serve: arrival rates (requests/s)")
     ap.add_argument("--duration", type=float, default=2.0, help="serve: seconds of arrivals per rate")
+    ap.add_argument("--render-slots", type=int, default=8, help="serve: concurrent render requests")
+    ap.add_argument("--batch-window-us", type=int, default=0, help="serve: wave batching window")
     return ap.parse_args()
 
 
@@ -127,6 +129,21 @@ class ClockSampler:
         if not sm:
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
         return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def aggregate_over_ranks(rays_this_rank: float, ms_this_rank: float, dist=None, device=None):
+    """Whole-job throughput of replicas: rays summed over ranks / the slowest rank's time (ms).
+    Returns (total rays, max ms, Mrays/s)."""
+    if dist is None or not dist.is_initialized() or dist.get_world_size() == 1:
+        return rays_this_rank, ms_this_rank, rays_this_rank / (ms_this_rank / 1e3) / 1e6
+    import torch
+    t = torch.tensor([float(rays_this_rank), float(ms_this_rank)], dtype=torch.float64, device=device)
+    rays = t[:1].clone()
+    ms = t[1:].clone()
+    dist.all_reduce(rays, op=dist.ReduceOp.SUM)
+    dist.all_reduce(ms, op=dist.ReduceOp.MAX)
+    r, m = float(rays.item()), float(ms.item())
+    return r, m, r / (m / 1e3) / 1e6
 
 
 def frame_inputs():
@@ -252,10 +269,6 @@ def run_ours(args, world, rank, local):
         dist.barrier()
     per = [a.elapsed_time(e) for a, e in zip(starts, ends)]
     total_ms = sum(per)
-    if dist:
-        t = torch.tensor([total_ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        total_ms = float(t.item())
     # Rays cast by the timed frames: the frames are deterministic, so replaying them with the same
     # seed and frame indices and reading the queue counters after each gives the exact counts.
     r.set_seed(SEED, first)
@@ -264,7 +277,8 @@ def run_ours(args, world, rank, local):
         frame(first + k)
         counts += r.ray_counts(stream=stream).astype(np.int64)
     rays_per_frame = int(counts.sum()) / args.steps
-    value = rays_per_frame * args.steps * world / (total_ms / 1e3) / 1e6
+    _, total_ms, value = aggregate_over_ranks(rays_per_frame * args.steps, total_ms, dist,
+                                              torch.device("cuda", local) if dist else None)
 
     # Per-kernel durations (CUDA events on the render stream, direct launches) for the roofline.
     r.set_graph(False)
@@ -302,6 +316,8 @@ def run_ours(args, world, rank, local):
     stage_rays = dict(zip(["primary", "primary_shadow", "bounce", "bounce_shadow"], (counts / args.steps).tolist()))
     per_kernel = {}
     names = KERNELS_FUSED if args.pipeline == "fused" else KERNELS
+    if args.sort_window == 0:
+        names = [k for k in names if k != "bounce_bin"]
     for i, name in enumerate(names):
         entry = {"ms": round(float(avg_kernel_ms[i]), 4)}
         if name in TRACE_PASS:
@@ -568,7 +584,7 @@ def run_large(args):
     avg = kms / frames
     counts = counts / steps
     frame_ms = float(avg.sum())
-    names = KERNELS_FUSED
+    names = [k for k in KERNELS_FUSED if k != "bounce_bin"]
     passes = {}
     for i, nm in enumerate(names):
         e = {"ms": round(float(avg[i]), 3)}
@@ -672,7 +688,8 @@ def run_serve(args):
         reqs = make_requests(rate, args.duration, int(rate))
         row = {}
         for mode in ("continuous", "serial"):
-            server = Server(memory_budget=120 << 30, render_slots=4, serial=(mode == "serial"))
+            server = Server(memory_budget=120 << 30, render_slots=args.render_slots, serial=(mode == "serial"),
+                            batch_window_us=args.batch_window_us)
             ids = [server.add_scene(sc) for sc in scenes]
             row[mode] = run(server, ids, reqs)
             server.close()
@@ -681,7 +698,8 @@ def run_serve(args):
     burst = {}
     reqs = make_requests(max(float(x) for x in args.rates.split(",")), args.duration, 99)
     for mode in ("continuous", "serial"):
-        server = Server(memory_budget=120 << 30, render_slots=4, serial=(mode == "serial"))
+        server = Server(memory_budget=120 << 30, render_slots=args.render_slots, serial=(mode == "serial"),
+                        batch_window_us=args.batch_window_us)
         ids = [server.add_scene(sc) for sc in scenes]
         burst[mode] = run(server, ids, reqs, burst=True)
         server.close()
@@ -689,7 +707,8 @@ def run_serve(args):
     results["burst"] = burst
     line = {"workload": "serve", "metric": METRIC, "unit": "Mrays/s",
             "scenes_triangles": [int(len(s.tri_verts)) for s, _ in built], "scene_build_s": round(build_s, 1),
-            "budget_bytes": 120 << 30, "arrivals_s": args.duration, "rates": results}
+            "budget_bytes": 120 << 30, "arrivals_s": args.duration, "render_slots": args.render_slots,
+            "batch_window_us": args.batch_window_us, "rates": results}
     print(json.dumps(line), flush=True)
 
 

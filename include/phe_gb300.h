@@ -346,7 +346,8 @@ typedef struct phe_server_config {
 	uint32_t maxRenderPixels;  /* largest render (default 1920*1080; width <= 1920) */
 	uint32_t maxLights;        /* lights per render (default 4, at most 8) */
 	int32_t serial;            /* 1 = serial baseline */
-	uint32_t pad;
+	uint32_t batchWindowUs;    /* a wave waits up to this long after its first query was admitted to
+	                              gather more (0 = launch as soon as a wave slot is free) */
 } phe_server_config;
 typedef struct phe_request {
 	uint32_t kind;             /* PHE_REQ_* */

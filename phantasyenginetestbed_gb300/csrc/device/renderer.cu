@@ -169,7 +169,7 @@ extern "C" phe_status phe_renderer_kernel_times(phe_renderer* r, double msTotal[
 	phe_status st = collect_times(r);
 	if (st) return st;
 	for (int i = 0; i < 8; i++) msTotal[i] = i < kFrameKernels ? r->kernelMs[i] : 0.0;
-	*numKernels = (uint32_t)(r->fused ? kFusedFrameKernels : kFrameKernels);
+	*numKernels = (uint32_t)((r->fused ? kFusedFrameKernels : kFrameKernels) - (r->sortWindow > 0 ? 0 : 1));
 	*frames = r->timedFrames;
 	return PHE_OK;
 }
@@ -400,7 +400,7 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 		phe_status st;
 		if (r->timing) {
 			if ((st = collect_times(r))) return st;
-			r->timedKernels = r->fused ? kFusedFrameKernels : kFrameKernels;
+			r->timedKernels = (r->fused ? kFusedFrameKernels : kFrameKernels) - (r->sortWindow > 0 ? 0 : 1);
 			st = launch_frame(r->scene, r->dParams, r->fb, r->resX, r->resY, s, r->events, r->fused);
 			r->pendingTimes = true;
 		} else {

@@ -343,8 +343,14 @@ void worker_loop(phe_server* s)
 				progress = true;
 			}
 
-			// 3. a wave over the admitted queries when a wave slot is free
-			if (!s->admitted.empty())
+			// 3. a wave over the admitted queries when a wave slot is free and the batching window of
+			//    the oldest admitted query has passed (or the wave is full, or nothing else is coming)
+			bool waveReady = !s->admitted.empty();
+			if (waveReady && s->cfg.batchWindowUs > 0 && s->admitted.size() < kMaxWaveItems) {
+				double waited = now_ms(s->t0) - s->admitted.front()->tAdmit;
+				waveReady = waited * 1000.0 >= (double)s->cfg.batchWindowUs;
+			}
+			if (waveReady)
 				for (Wave& w : s->waves)
 					if (!w.busy) {
 						phe_status ps = launch_wave(s, w);
@@ -378,6 +384,7 @@ extern "C" void phe_server_default_config(phe_server_config* c)
 	c->maxRenderPixels = 1920 * 1080;
 	c->maxLights = 4;
 	c->serial = 0;
+	c->batchWindowUs = 0;
 }
 
 extern "C" phe_status phe_server_create(const phe_server_config* cfg, phe_server** out)

@@ -656,8 +656,10 @@ phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, c
 		                                                               fb.counters + kCtrShadow0, fb.inLight,
 		                                                               fb.counters + kCtrWork2, scene->status);
 		mark();
-		bin_bounce_kernel<<<binGrid, kBinBlock, 0, stream>>>(fb);
-		mark();
+		if (fb.sortWindow > 0) {
+			bin_bounce_kernel<<<binGrid, kBinBlock, 0, stream>>>(fb);
+			mark();
+		}
 		bounce_kernel<<<g[kGridBounce], kWaveBlock, 0, stream>>>(scene->dev, dParams, fb, scene->status);
 		mark();
 		any_queue_kernel<<<g[kGridAnyQueue], kWaveBlock, 0, stream>>>(scene->dev, fb.shadowRays + fb.capacityLP,
@@ -675,8 +677,10 @@ phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, c
 		                                                                 fb.counters + kCtrWork2, fb.refill,
 		                                                                 scene->status);
 		mark();
-		bin_bounce_kernel<<<binGrid, kBinBlock, 0, stream>>>(fb);
-		mark();
+		if (fb.sortWindow > 0) {
+			bin_bounce_kernel<<<binGrid, kBinBlock, 0, stream>>>(fb);
+			mark();
+		}
 		bounce_trace_kernel<<<g[kGridBounceTrace], kWaveBlock, 0, stream>>>(scene->dev, fb, scene->status);
 		mark();
 		bounce_shade_kernel<<<g[kGridBounceShade], kWaveBlock, 0, stream>>>(scene->dev, dParams, fb);

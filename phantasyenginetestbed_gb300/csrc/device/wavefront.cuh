@@ -67,8 +67,8 @@ phe_status renderer_reserve(phe_renderer* r, uint64_t pixels, uint32_t lights);
 phe_status prepare_frame();
 // Kernels of one frame: primary trace, primary shade, primary any-hit, bounce binning, bounce trace,
 // bounce shade, bounce any-hit, resolve + TAA (kFrameKernels); the fused pipeline has six (primary
-// and bounce trace+shade fused). The binning kernel is launched even when sortWindow is 0 (it then
-// returns at once) so every frame has the same launch sequence.
+// and bounce trace+shade fused). The binning kernel is launched only when sortWindow > 0, so the
+// frame has one kernel less without binning.
 constexpr int kFrameKernels = 8;
 constexpr int kFusedFrameKernels = 6;
 // `events` (optional, kernels + 1 entries) are recorded on `stream` around each kernel. `fused`

@@ -78,7 +78,8 @@ class BatchTuningRow(C.Structure):
 
 class ServerConfig(C.Structure):
     _fields_ = [("memoryBudget", C.c_uint64), ("maxInFlight", C.c_uint32), ("renderSlots", C.c_uint32),
-                ("maxRenderPixels", C.c_uint32), ("maxLights", C.c_uint32), ("serial", C.c_int32), ("pad", C.c_uint32)]
+                ("maxRenderPixels", C.c_uint32), ("maxLights", C.c_uint32), ("serial", C.c_int32),
+                ("batchWindowUs", C.c_uint32)]
 
 
 class Request(C.Structure):

@@ -27,7 +27,7 @@ _PINNED: dict = {}
 
 class Server:
     def __init__(self, memory_budget=120 << 30, max_in_flight=256, render_slots=4, max_render_pixels=1920 * 1080,
-                 max_lights=4, serial=False):
+                 max_lights=4, serial=False, batch_window_us=0):
         cfg = _n.ServerConfig()
         lib().phe_server_default_config(C.byref(cfg))
         cfg.memoryBudget = memory_budget
@@ -36,6 +36,7 @@ class Server:
         cfg.maxRenderPixels = max_render_pixels
         cfg.maxLights = max_lights
         cfg.serial = 1 if serial else 0
+        cfg.batchWindowUs = batch_window_us
         h = C.c_void_p()
         check(lib().phe_server_create(C.byref(cfg), C.byref(h)), "phe_server_create")
         self.handle = h

@@ -202,3 +202,31 @@ def test_invalid_scene_and_arguments_are_rejected():
     scene = P.Scene(b.nodes, b.verts)
     with pytest.raises(P.PheError):
         P.cast_closest(scene, None, device_empty(4, P.RAY_HIT_DTYPE), 4)
+
+
+@pytest.mark.parametrize("T", [1, 2, 3, 5, 8, 13, 32, 64])
+def test_small_scenes_every_ray_vs_brute_force(T):
+    """Exhaustive small cases: 1..64 random triangles (some sharing edges, some degenerate), 4096 rays
+    from all around; GPU closest hit vs brute force over the triangles, GPU any hit vs the oracle."""
+    rng = np.random.default_rng(T)
+    tv = rng.uniform(0, 1, (T, 9)).astype(np.float32)
+    if T >= 3:
+        tv[1, 0:3], tv[1, 3:6] = tv[0, 0:3], tv[0, 6:9]     # shared edge
+        tv[2, 6:9] = tv[2, 0:3]                               # degenerate (zero area)
+    b = P.build_sbvh(tv)
+    scene = P.Scene(b.nodes, b.verts)
+    rays = random_rays(4096, [-0.5, -0.5, -0.5], [1.5, 1.5, 1.5], 100 + T)
+    aim = rng.uniform(0.2, 0.8, (4096, 3)).astype(np.float32)
+    d = aim - rays["origin"]
+    rays["dir"] = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    tris = np.zeros(T, P.TRI_VERTS_DTYPE)
+    tris["v0"][:, :3], tris["v1"][:, :3], tris["v2"][:, :3] = tv[:, 0:3], tv[:, 3:6], tv[:, 6:9]
+    bf = O.brute_closest(tris, rays, mode=O.MODE_GPU)
+    gpu = _gpu_closest(scene, rays)
+    gpu_orig = gpu.copy()
+    hit = gpu["triangleIndex"] != 0xFFFFFFFF
+    gpu_orig["triangleIndex"][hit] = b.slot_to_tri[gpu["triangleIndex"][hit]]
+    rep = O.compare_closest(gpu_orig, bf, rays, np.arange(T, dtype=np.uint32), tris)
+    _check(rep, len(rays))
+    assert hit.mean() > 0.05
+    assert np.array_equal(_gpu_any(scene, rays), O.any_rays(b.nodes, b.verts, rays))

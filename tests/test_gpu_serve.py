@@ -49,21 +49,29 @@ def _requests(scenes, seed):
     return reqs
 
 
-def _submit(server, ids, req):
+def _prepare(req):
+    """Pinned host buffers of a request (allocated before submission so that submits are quick)."""
     kind, si, a = req
     if kind == "render":
-        out = pinned((a["res"][1], a["res"][0], 4), np.float32)
+        return None, pinned((a["res"][1], a["res"][0], 4), np.float32)
+    rays = pinned(len(a["rays"]), P.RAY_IN_DTYPE)
+    rays[:] = a["rays"]
+    return rays, pinned(len(rays) * (1 if a["kind"] == REQ_ANY else 16), np.uint8)
+
+
+def _submit(server, ids, req, bufs=None):
+    kind, si, a = req
+    rays, out = bufs if bufs is not None else _prepare(req)
+    if kind == "render":
         rid = server.submit_render(ids[si], a["res"], a["spp"], cam_struct(a["cam"]), a["cam_pos"], a["lights"], a["seed"], out)
     else:
-        rays = pinned(len(a["rays"]), P.RAY_IN_DTYPE)
-        rays[:] = a["rays"]
-        out = pinned(len(rays) * (1 if a["kind"] == REQ_ANY else 16), np.uint8)
         rid = server.submit_rays(ids[si], rays, out, a["kind"])
     return rid, out
 
 
 def test_each_result_is_the_same_alone_and_in_the_mix(scenes):
-    server = Server(render_slots=3)
+    # a 200 ms batching window: the queries submitted together below all join one wave
+    server = Server(render_slots=3, batch_window_us=200000)
     ids = [server.add_scene(x[2]) for x in scenes]
     reqs = _requests(scenes, 1)
     alone = []
@@ -73,14 +81,15 @@ def test_each_result_is_the_same_alone_and_in_the_mix(scenes):
         assert st.status == 0 and st.rays > 0
         alone.append(out.copy())
     waves_before = server.stats()["waves"]
-    mixed = [_submit(server, ids, q) for q in reqs]   # all in flight together
+    bufs = [_prepare(q) for q in reqs]
+    mixed = [_submit(server, ids, q, bb) for q, bb in zip(reqs, bufs)]   # all in flight together
     server.drain()
     waves = server.stats()["waves"] - waves_before
+    assert waves == 1   # every query of the mix went into one batched launch
     for (rid, out), a in zip(mixed, alone):
         st = server.poll(rid)
         assert st is not None and st.status == 0
         assert np.array_equal(out.view(np.uint8), a.view(np.uint8))
-    assert waves < len([q for q in reqs if q[0] == "rays"])  # queries shared waves
     # ray queries against the oracle, renders against the renderer object
     for (kind, si, a), res in zip(reqs, alone):
         s, b, sc = scenes[si]
