@@ -445,13 +445,16 @@ def run_plain(args):
     vis = torch.empty(n, dtype=torch.uint8, device="cuda")
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
     out = {}
-    for name, fn in (("closest_persistent", lambda: P.cast_closest(scene, rays, hits, n, stream=stream)),
-                     ("closest_plain", lambda: P.cast_closest_plain(scene, rays, hits, n, stream=stream)),
-                     ("any", lambda: P.cast_any(scene, rays, vis, n, stream=stream))):
-        for _ in range(args.warmup):
-            fn()
-        t = statistics.median(_timed(fn, args.steps, stream, flush))
-        out[name] = {"ms": round(t, 4), "Mrays_s": round(n / t / 1e3, 1)}
+    for layout, lname in ((0, "binary"), (1, "wide4")):
+        scene.set_layout(layout)
+        for name, fn in (("closest_persistent", lambda: P.cast_closest(scene, rays, hits, n, stream=stream)),
+                         ("closest_plain", lambda: P.cast_closest_plain(scene, rays, hits, n, stream=stream)),
+                         ("any", lambda: P.cast_any(scene, rays, vis, n, stream=stream))):
+            for _ in range(args.warmup):
+                fn()
+            t = statistics.median(_timed(fn, args.steps, stream, flush))
+            out[f"{name}_{lname}"] = {"ms": round(t, 4), "Mrays_s": round(n / t / 1e3, 1)}
+    scene.set_layout(0)
     cpu = None
     if not args.no_cpu_baseline:
         from oracle import oracle as O
@@ -509,7 +512,8 @@ def run_batch(args):
     batch = Batch(scenes, items, use_graph=False)
     best, best_ms, table = batch.autotune(repeats=3)
     save_tuning(ROOT / "profiles" / "batch_autotune.json", best, best_ms, table)
-    batch.set_params(block_size=best["blockSize"], blocks_per_sm=best["blocksPerSM"], order=best["order"], use_graph=True)
+    batch.set_params(block_size=best["blockSize"], blocks_per_sm=best["blocksPerSM"], order=best["order"], use_graph=True,
+                     layout=best["layout"])
     for _ in range(args.warmup):
         batch.launch(stream)
     t_batched = _timed(lambda: batch.launch(stream), args.steps, stream, flush)
@@ -544,7 +548,8 @@ def run_batch(args):
             "plain_64_launches": {"ms": round(mp, 4), "Mrays_s": round(total / mp / 1e3, 1)},
             "plain_64_launches_synchronised": {"ms": round(ms_sync, 4), "Mrays_s": round(total / ms_sync / 1e3, 1)},
             "speedup_vs_plain": round(mp / mb, 3), "speedup_vs_synchronised": round(ms_sync / mb, 3),
-            "autotune_candidates": len(table), "l2": "flushed before every timed step"}
+            "autotune_candidates": len(table), "layouts_tried": sorted({r["layout"] for r in table}),
+            "l2": "flushed before every timed step"}
     print(json.dumps(line), flush=True)
 
 

@@ -194,6 +194,17 @@ phe_status phe_cast_any(const phe_scene* scene, const phe_ray_in* rays, uint8_t*
 phe_status phe_gen_primary_rays(phe_ray_in* rays, const phe_camera_def* cam, uint32_t resX, uint32_t resY,
                                 float jitterX, float jitterY, int order, void* stream);
 
+/* Node layout used by every kernel on this scene. PHE_LAYOUT_BINARY (default): the reference's 2-wide
+ * nodes. PHE_LAYOUT_WIDE4: the same tree collapsed to 4-wide 128-byte nodes (child bounds in SoA
+ * float4s), built at upload when every grandchild box lies inside its parent box; it visits exactly
+ * the leaves the binary traversal visits (the rounded slab test is monotone in the bounds), so results
+ * are the same, and it is faster for small coherent launches, slower for large incoherent ones.
+ * Rays with a non-finite 1/dir always use the binary nodes. Kernels read the layout when launched. */
+#define PHE_LAYOUT_BINARY 0
+#define PHE_LAYOUT_WIDE4 1
+phe_status phe_scene_set_layout(phe_scene* scene, int layout);
+phe_status phe_scene_get_layout(const phe_scene* scene, int* layout, int* wideAvailable);
+
 /* OR of error bits raised by kernels on this scene (1 = traversal stack overflow; never set for a
  * scene that passed validation). Synchronous. */
 phe_status phe_scene_status(const phe_scene* scene, uint32_t* bits);
@@ -221,6 +232,8 @@ typedef struct phe_batch_params {
 	int32_t blocksPerSM;     /* resident blocks per SM (0 = occupancy limit) */
 	int32_t order;           /* PHE_BATCH_ORDER_* */
 	int32_t useGraph;        /* 1 = replay from a CUDA graph captured on first launch */
+	int32_t layout;          /* PHE_LAYOUT_* for every scene of the batch (wide only where available) */
+	int32_t pad;
 } phe_batch_params;
 typedef struct phe_batch_tuning_row { phe_batch_params params; float ms; } phe_batch_tuning_row;
 void phe_batch_default_params(phe_batch_params* params);
@@ -233,7 +246,7 @@ phe_status phe_batch_set_params(phe_batch* batch, const phe_batch_params* params
 /* One persistent launch over every item, asynchronous on `stream`. */
 phe_status phe_batch_launch(phe_batch* batch, void* stream);
 phe_status phe_batch_info(const phe_batch* batch, uint64_t* totalRays, uint32_t* paddedRays);
-/* Times every candidate (block size x batch order x occupancy) `repeats` times on this batch with
+/* Times every candidate (block size x batch order x occupancy x node layout) `repeats` times on this batch with
  * CUDA events on `stream`, sets the fastest on the batch and returns it; `rows` (optional) receives
  * every candidate's time. Synchronous. */
 phe_status phe_batch_autotune(phe_batch* batch, int repeats, void* stream, phe_batch_params* best, float* bestMs,
@@ -317,6 +330,12 @@ phe_status phe_renderer_kernel_times(phe_renderer* renderer, double msTotal[8], 
  * host memory on `stream` (pinned memory for a truly asynchronous copy). */
 phe_status phe_renderer_reset_ray_totals(phe_renderer* renderer, void* stream);
 phe_status phe_renderer_ray_totals_async(const phe_renderer* renderer, uint64_t* hostTotals4, void* stream);
+
+/* Display post-process for image dumps (gamma_correction.frag:20-74: Uncharted 2 tonemap, then
+ * pow(rgb, 1/gamma)) of a linear float4 image into `display` (float4) and/or `rgba8` (4 bytes per
+ * pixel, rounded from [0, 1]); either output may be NULL. */
+phe_status phe_postprocess(uint32_t resX, uint32_t resY, const float* linear, float gamma, float* display, uint8_t* rgba8,
+                           void* stream);
 
 /* TAA resolve alone (taa.frag:25-71) on device float4 buffers; velocity and prevVelocity are float2
  * uv velocities (NULL = static), roughness float (NULL = 0). */

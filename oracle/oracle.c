@@ -734,3 +734,27 @@ void oracle_halton_jitter(uint32_t i, float out[2])
 	out[0] = (float)r - 0.5f;
 	out[1] = (float)r3 - 0.5f;
 }
+
+/* ---------------------------------------------------------------------------------------------
+ * Display post-process (gamma_correction.frag:20-74)
+ * ------------------------------------------------------------------------------------------- */
+
+static float u2_tonemap(float x)
+{
+	const float A = 0.25f, B = 0.25f, C = 0.105f, D = 0.20f, E = 0.025f, F = 0.25f;
+	return (x * (A * x + C * B) + D * E) / (x * (A * x + B) + D * F) - E / F;
+}
+
+void oracle_postprocess(uint32_t n, const float* linear, float gamma, float* display)
+{
+	const float W = 11.2f, BLACK_CRUSH = 0.0015f, exposureBias = 2.0f;
+	float invGamma = 1.0f / gamma;
+	float white = u2_tonemap(W);
+	for (uint32_t i = 0; i < n; i++) {
+		for (int k = 0; k < 3; k++) {
+			float x = exposureBias * fmaxf(0.0f, linear[4 * (size_t)i + k] - BLACK_CRUSH);
+			display[4 * (size_t)i + k] = powf(u2_tonemap(x) / white, invGamma);
+		}
+		display[4 * (size_t)i + 3] = linear[4 * (size_t)i + 3];
+	}
+}

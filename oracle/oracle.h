@@ -124,6 +124,10 @@ int oracle_render_frame(const or_node* nodes, const or_tri* tris, const or_tri_d
 void oracle_taa(uint32_t resX, uint32_t resY, const float* cur, const float* hist, const float* velocity,
                 const float* prevVelocity, const float* roughness, float* outColor, float* outHist);
 
+/* Display post-process (gamma_correction.frag:20-74): Uncharted 2 tonemap then pow(rgb, 1/gamma), on
+ * n float4 pixels; alpha passes through. */
+void oracle_postprocess(uint32_t n, const float* linear, float gamma, float* display);
+
 /* Halton(2,3) jitter table entry i - 0.5 (GameScreen.cpp:21-39). */
 void oracle_halton_jitter(uint32_t i, float out[2]);
 

@@ -69,6 +69,8 @@ def lib():
         L.oracle_render_frame.argtypes = [V, V, V, C.POINTER(FrameParams), V, V, V, V, V, C.c_int]
         L.oracle_taa.argtypes = [C.c_uint32, C.c_uint32, V, V, V, V, V, V, V]
         L.oracle_taa.restype = None
+        L.oracle_postprocess.argtypes = [C.c_uint32, V, C.c_float, V]
+        L.oracle_postprocess.restype = None
         L.oracle_halton_jitter.argtypes = [C.c_uint32, V]
         L.oracle_halton_jitter.restype = None
         L.oracle_sincos_2pi.argtypes = [C.c_float, V, V]
@@ -276,3 +278,10 @@ def compare_closest(test_hits, oracle_hits, rays, slot_to_tri, verts, rel_t=1e-6
         "bad_ties": bad_ties, "miss_t_mismatch": miss_vals.tolist(),
         "ok": len(flip) == 0 and len(bad_vals) == 0 and len(bad_ties) == 0 and len(miss_vals) == 0,
     }
+
+
+def postprocess(linear, gamma=2.2):
+    lin = np.ascontiguousarray(linear, np.float32)
+    out = np.empty_like(lin)
+    lib().oracle_postprocess(lin.size // 4, _p(lin), gamma, _p(out))
+    return out

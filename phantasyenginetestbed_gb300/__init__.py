@@ -154,6 +154,15 @@ class Scene:
             return cls(bvh.nodes, bvh.verts)
         return cls(bvh.nodes, bvh.verts, bvh.slot_datas(scene.datas), scene.materials)
 
+    def set_layout(self, layout: int) -> None:
+        """0 = binary nodes (default), 1 = 4-wide nodes (same results; see phe_scene_set_layout)."""
+        check(lib().phe_scene_set_layout(self.handle, layout), "phe_scene_set_layout")
+
+    def layout(self):
+        lay, avail = C.c_int(), C.c_int()
+        check(lib().phe_scene_get_layout(self.handle, C.byref(lay), C.byref(avail)), "phe_scene_get_layout")
+        return int(lay.value), bool(avail.value)
+
     def device_bytes(self) -> int:
         b = C.c_uint64()
         check(lib().phe_scene_device_bytes(self.handle, C.byref(b)), "phe_scene_device_bytes")

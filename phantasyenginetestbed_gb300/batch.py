@@ -20,12 +20,12 @@ def _stream(stream):
 
 
 class Batch:
-    def __init__(self, scenes, items, block_size=128, blocks_per_sm=0, order=ORDER_GIVEN, use_graph=True):
+    def __init__(self, scenes, items, block_size=128, blocks_per_sm=0, order=ORDER_GIVEN, use_graph=True, layout=0):
         """scenes: list of Scene; items: list of (scene index, kind, count, device rays, device out)."""
         self.scenes = list(scenes)
         arr = (C.c_void_p * len(scenes))(*[s.handle.value for s in scenes])
         self._items = self._table(items)
-        p = _n.BatchParams(block_size, blocks_per_sm, order, 1 if use_graph else 0)
+        p = _n.BatchParams(block_size, blocks_per_sm, order, 1 if use_graph else 0, layout, 0)
         h = C.c_void_p()
         check(lib().phe_batch_create(arr, len(scenes), self._items, len(items), C.byref(p), C.byref(h)), "phe_batch_create")
         self.handle = h
@@ -41,8 +41,8 @@ class Batch:
         self._items = self._table(items)
         check(lib().phe_batch_update(self.handle, self._items, len(items)), "phe_batch_update")
 
-    def set_params(self, block_size=128, blocks_per_sm=0, order=ORDER_GIVEN, use_graph=True) -> None:
-        p = _n.BatchParams(block_size, blocks_per_sm, order, 1 if use_graph else 0)
+    def set_params(self, block_size=128, blocks_per_sm=0, order=ORDER_GIVEN, use_graph=True, layout=0) -> None:
+        p = _n.BatchParams(block_size, blocks_per_sm, order, 1 if use_graph else 0, layout, 0)
         check(lib().phe_batch_set_params(self.handle, C.byref(p)), "phe_batch_set_params")
 
     def launch(self, stream=None) -> None:
@@ -62,7 +62,7 @@ class Batch:
         check(lib().phe_batch_autotune(self.handle, repeats, _stream(stream), C.byref(best), C.byref(ms), rows, 64,
                                        C.byref(n)), "phe_batch_autotune")
         as_dict = lambda p: {"blockSize": p.blockSize, "blocksPerSM": p.blocksPerSM, "order": p.order,
-                             "useGraph": p.useGraph}
+                             "useGraph": p.useGraph, "layout": p.layout}
         table = [dict(as_dict(rows[i].params), ms=rows[i].ms) for i in range(min(n.value, 64))]
         return as_dict(best), float(ms.value), table
 

@@ -60,10 +60,10 @@ __global__ void __launch_bounds__(BLOCK) batch_kernel(BatchTableDev t, uint32_t*
 			HitRecord h = empty_hit(r);
 			uint32_t err;
 			if (item.kind == 0) {
-				err = trace<false>(s.nodes, s.tris, r, h);
+				err = trace<false>(s, r, h);
 				store_hit((phe_ray_hit*)item.out, i, r, h);
 			} else {
-				err = trace<true>(s.nodes, s.tris, r, h);
+				err = trace<true>(s, r, h);
 				((uint8_t*)item.out)[i] = h.slot == ~0u ? 1 : 0;
 			}
 			if (err) atomicOr(status, err);
@@ -138,6 +138,7 @@ extern "C" void phe_batch_default_params(phe_batch_params* p)
 	p->blocksPerSM = 0;
 	p->order = PHE_BATCH_ORDER_GIVEN;
 	p->useGraph = 1;
+	p->layout = PHE_LAYOUT_BINARY;
 }
 
 static phe_status upload_table(phe_batch* b)
@@ -174,6 +175,14 @@ static phe_status upload_table(phe_batch* b)
 	b->totalPadded = base;
 	b->totalRays = total;
 	PHE_CUDA_TRY(cudaMemcpy(b->dItems, dev.data(), n * sizeof(BatchItemDev), cudaMemcpyHostToDevice), "upload batch table");
+	std::vector<DeviceScene> st(b->sceneHandles.size());
+	for (size_t i = 0; i < st.size(); i++) {
+		st[i] = b->sceneHandles[i]->dev;
+		st[i].nodes4 = b->params.layout == PHE_LAYOUT_WIDE4 ? b->sceneHandles[i]->nodes4 : nullptr;
+	}
+	if (!st.empty())
+		PHE_CUDA_TRY(cudaMemcpy(b->dScenes, st.data(), st.size() * sizeof(DeviceScene), cudaMemcpyHostToDevice),
+		             "upload scene table");
 	if (b->graph) {
 		cudaGraphExecDestroy(b->graph);
 		b->graph = nullptr;
@@ -347,6 +356,7 @@ extern "C" phe_status phe_batch_autotune(phe_batch* b, int repeats, void* stream
 	const int blocks[] = {64, 128, 256};
 	const int orders[] = {PHE_BATCH_ORDER_GIVEN, PHE_BATCH_ORDER_LARGEST_FIRST};
 	const int occFrac[] = {4, 3, 2};  // quarters of the occupancy limit: 4/4, 3/4, 2/4
+	const int layouts[] = {PHE_LAYOUT_BINARY, PHE_LAYOUT_WIDE4};
 	cudaEvent_t e0, e1;
 	PHE_CUDA_TRY(cudaEventCreate(&e0), "cudaEventCreate");
 	PHE_CUDA_TRY(cudaEventCreate(&e1), "cudaEventCreate");
@@ -361,12 +371,14 @@ extern "C" phe_status phe_batch_autotune(phe_batch* b, int repeats, void* stream
 		else if (bs == 128) launch_batch_kernel<128>(t, 0, 1, nullptr, nullptr, nullptr, &occ);
 		else launch_batch_kernel<256>(t, 0, 1, nullptr, nullptr, nullptr, &occ);
 		for (int ord : orders)
-			for (int q : occFrac) {
+			for (int q : occFrac)
+				for (int lay : layouts) {
 				phe_batch_params p = saved;
 				p.blockSize = bs;
 				p.order = ord;
 				p.blocksPerSM = std::max(1, occ * q / 4);
 				p.useGraph = 0;
+				p.layout = lay;
 				b->params = p;
 				if ((st = upload_table(b))) goto done;
 				if ((st = batch_enqueue(b, s))) goto done;  // warm-up

@@ -23,17 +23,29 @@ namespace phe_gb300 {
 //        changes no result bit. endMarker is -1 on the last slot of each leaf, else 0.
 // ------------------------------------------------------------------------------------------------
 
+// nodes4 (optional): the same tree collapsed to 4-wide nodes, 128 B each — 6 float4 of child bounds
+//        in SoA order (lo.x[4], lo.y[4], lo.z[4], hi.x[4], hi.y[4], hi.z[4]), one int4 of child refs
+//        (4-wide node index >= 0, leaf ~firstSlot < 0, kEmptyChild for an unused slot) and one float4
+//        of padding. Every child box is a box of the binary tree (a grandchild when the binary child
+//        is inner), and it is built only when each grandchild box lies inside its parent box, so the
+//        4-wide test of a grandchild passes only if the skipped binary test of its parent would pass.
 struct DeviceScene {
 	const float4* nodes;
 	const float4* tris;
 	const phe_triangle_data* datas;
 	const phe_material* materials;
 	uint32_t numNodes, numSlots, numMaterials, maxDepth;
+	const float4* nodes4;
+	uint32_t numNodes4, maxDepth4;
 };
+
+constexpr int32_t kEmptyChild = 0x7FFFFFFE;
 
 // Traversal stack depth: leaves of a valid scene are at most 64 levels deep, and a node pushes at
 // most one entry per inner level, plus the sentinel.
 constexpr int kStackSize = 68;
+// 4-wide traversal: a node pushes up to 3 entries; a binary tree of depth <= 64 collapses to <= 32 levels.
+constexpr int kStackSize4 = 100;
 constexpr int32_t kSentinel = 0x7FFFFFFF;
 
 // Error bits written to the per-launch status word.

@@ -24,7 +24,7 @@ __global__ void __launch_bounds__(kPlainBlock) closest_plain_kernel(DeviceScene 
 	if (i >= n) return;
 	RayState r = load_ray(rays, i);
 	HitRecord h = empty_hit(r);
-	uint32_t err = trace<false>(s.nodes, s.tris, r, h);
+	uint32_t err = trace<false>(s, r, h);
 	if (err) atomicOr(status, err);
 	store_hit(hits, i, r, h);
 }
@@ -47,7 +47,7 @@ __global__ void __launch_bounds__(kPersistentBlock) closest_persistent_kernel(De
 		if (i < n) {
 			RayState r = load_ray(rays, i);
 			HitRecord h = empty_hit(r);
-			uint32_t err = trace<false>(s.nodes, s.tris, r, h);
+			uint32_t err = trace<false>(s, r, h);
 			if (err) atomicOr(status, err);
 			store_hit(hits, i, r, h);
 		}
@@ -72,7 +72,7 @@ __global__ void __launch_bounds__(kPersistentBlock) any_persistent_kernel(Device
 		if (i < n) {
 			RayState r = load_ray(rays, i);
 			HitRecord h = empty_hit(r);
-			uint32_t err = trace<true>(s.nodes, s.tris, r, h);
+			uint32_t err = trace<true>(s, r, h);
 			if (err) atomicOr(status, err);
 			uint32_t o = scatter ? __ldg(scatter + i) : i;
 			inLight[o] = h.slot == ~0u ? 1 : 0;

@@ -9,7 +9,8 @@
 #include "common.cuh"
 
 struct phe_scene {
-	phe_gb300::DeviceScene dev;
+	phe_gb300::DeviceScene dev;         // dev.nodes4 is set only while the 4-wide layout is selected
+	const float4* nodes4 = nullptr;     // 4-wide nodes, when the tree allows them (else null)
 	void* allocation = nullptr;   // one cudaMalloc holding nodes, tris, datas, materials
 	uint64_t bytes = 0;
 	uint32_t* status = nullptr;   // device word: OR of error bits raised by kernels on this scene

@@ -3,6 +3,7 @@
 // (cuda_ray_tracer/CudaTracerRenderer.cpp:251-315), which uploaded the arrays unchanged into linear
 // texture objects.
 
+#include <algorithm>
 #include <atomic>
 #include <cstring>
 #include <mutex>
@@ -62,6 +63,87 @@ static_assert(sizeof(phe_ray_in) == 32, "RayIn is 32 bytes");
 static_assert(sizeof(phe_ray_hit) == 16, "RayHit is 16 bytes");
 
 static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+namespace {
+
+struct ChildRef {
+	float box[6];   // lo.xyz, hi.xyz
+	int32_t ref;    // binary inner node index (>= 0) or ~firstSlot (< 0)
+};
+
+ChildRef binary_child(const std::vector<float4>& dn, uint32_t node, int c)
+{
+	const float* f = reinterpret_cast<const float*>(&dn[(size_t)node * 4]);
+	const int32_t* iv = reinterpret_cast<const int32_t*>(&dn[(size_t)node * 4 + 3]);
+	ChildRef r;
+	for (int k = 0; k < 6; k++) r.box[k] = f[6 * c + k];
+	r.ref = iv[c];
+	return r;
+}
+
+bool contains(const float* outer, const float* inner)
+{
+	return inner[0] >= outer[0] && inner[1] >= outer[1] && inner[2] >= outer[2] && inner[3] <= outer[3] &&
+	       inner[4] <= outer[4] && inner[5] <= outer[5];
+}
+
+// Collapses the binary tree (traversal layout `dn`) into 4-wide nodes: a binary node's inner children
+// are replaced by their own two children. Returns false (and builds nothing) when some grandchild box
+// is not inside its parent box, where skipping the parent test could change the traversal.
+bool collapse4(const std::vector<float4>& dn, std::vector<float4>& out, uint32_t& depth4)
+{
+	out.clear();
+	depth4 = 0;
+	struct Item { uint32_t binary, index4, depth; };
+	std::vector<Item> work;
+	out.resize(8);
+	work.push_back({0, 0, 1});
+	while (!work.empty()) {
+		Item it = work.back();
+		work.pop_back();
+		depth4 = std::max(depth4, it.depth);
+		ChildRef kids[4];
+		int n = 0;
+		for (int c = 0; c < 2; c++) {
+			ChildRef ch = binary_child(dn, it.binary, c);
+			if (ch.ref >= 0) {
+				for (int g = 0; g < 2; g++) {
+					ChildRef gc = binary_child(dn, (uint32_t)ch.ref, g);
+					if (!contains(ch.box, gc.box)) return false;
+					kids[n++] = gc;
+				}
+			} else {
+				kids[n++] = ch;
+			}
+		}
+		float lanes[6][4];
+		int32_t refs[4];
+		for (int k = 0; k < 4; k++) {
+			if (k < n) {
+				for (int j = 0; j < 6; j++) lanes[j][k] = kids[k].box[j];
+				if (kids[k].ref >= 0) {
+					uint32_t child4 = (uint32_t)(out.size() / 8);
+					out.resize(out.size() + 8);
+					work.push_back({(uint32_t)kids[k].ref, child4, it.depth + 1});
+					refs[k] = (int32_t)child4;
+				} else {
+					refs[k] = kids[k].ref;
+				}
+			} else {
+				for (int j = 0; j < 6; j++) lanes[j][k] = 0.0f;
+				refs[k] = kEmptyChild;
+			}
+		}
+		float4* q = &out[(size_t)it.index4 * 8];
+		for (int j = 0; j < 6; j++) q[j] = make_float4(lanes[j][0], lanes[j][1], lanes[j][2], lanes[j][3]);
+		int4 rv = make_int4(refs[0], refs[1], refs[2], refs[3]);
+		std::memcpy(&q[6], &rv, sizeof(rv));
+		q[7] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+	}
+	return true;
+}
+
+} // namespace
 
 extern "C" phe_status phe_scene_create(const phe_bvh_node* nodes, uint32_t numNodes, const phe_triangle_vertices* verts,
                                        const phe_triangle_data* datas, uint32_t numSlots, const phe_material* materials,
@@ -165,24 +247,33 @@ extern "C" phe_status phe_scene_create(const phe_bvh_node* nodes, uint32_t numNo
 		}
 	}
 
+	std::vector<float4> dn4;
+	uint32_t depth4 = 0;
+	bool wide = collapse4(dn, dn4, depth4);
+	if (!wide) dn4.clear();
+
 	size_t nodeBytes = align256(dn.size() * sizeof(float4));
+	size_t node4Bytes = align256(dn4.size() * sizeof(float4));
 	size_t triBytes = align256(dt.size() * sizeof(float4));
 	size_t dataBytes = align256(hd.size() * sizeof(phe_triangle_data));
 	size_t matBytes = align256(hm.size() * sizeof(phe_material));
 	size_t statusBytes = 256;
-	size_t total = nodeBytes + triBytes + dataBytes + matBytes + statusBytes;
+	size_t total = nodeBytes + node4Bytes + triBytes + dataBytes + matBytes + statusBytes;
 	char* base = nullptr;
 	cudaError_t e = cudaMalloc(&base, total);
 	if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(scene)");
 	auto cleanup = [&](phe_status st) { cudaFree(base); return st; };
 	char* p = base;
 	float4* dNodes = (float4*)p; p += nodeBytes;
+	float4* dNodes4 = dn4.empty() ? nullptr : (float4*)p; p += node4Bytes;
 	float4* dTris = (float4*)p; p += triBytes;
 	phe_triangle_data* dDatas = hd.empty() ? nullptr : (phe_triangle_data*)p; p += dataBytes;
 	phe_material* dMats = hm.empty() ? nullptr : (phe_material*)p; p += matBytes;
 	uint32_t* dStatus = (uint32_t*)p;
 	if ((e = cudaMemcpy(dNodes, dn.data(), dn.size() * sizeof(float4), cudaMemcpyHostToDevice)) != cudaSuccess)
 		return cleanup(cuda_fail(e, "upload nodes"));
+	if (dNodes4 && (e = cudaMemcpy(dNodes4, dn4.data(), dn4.size() * sizeof(float4), cudaMemcpyHostToDevice)) != cudaSuccess)
+		return cleanup(cuda_fail(e, "upload 4-wide nodes"));
 	if ((e = cudaMemcpy(dTris, dt.data(), dt.size() * sizeof(float4), cudaMemcpyHostToDevice)) != cudaSuccess)
 		return cleanup(cuda_fail(e, "upload triangles"));
 	if (dDatas && (e = cudaMemcpy(dDatas, hd.data(), hd.size() * sizeof(phe_triangle_data), cudaMemcpyHostToDevice)) != cudaSuccess)
@@ -200,6 +291,10 @@ extern "C" phe_status phe_scene_create(const phe_bvh_node* nodes, uint32_t numNo
 	sc->dev.numSlots = numSlots;
 	sc->dev.numMaterials = (uint32_t)hm.size();
 	sc->dev.maxDepth = maxDepth;
+	sc->dev.nodes4 = nullptr;   // binary layout unless phe_scene_set_layout selects the 4-wide one
+	sc->nodes4 = dNodes4;
+	sc->dev.numNodes4 = (uint32_t)(dn4.size() / 8);
+	sc->dev.maxDepth4 = depth4;
 	sc->allocation = base;
 	sc->bytes = total;
 	sc->status = dStatus;
@@ -228,5 +323,27 @@ extern "C" phe_status phe_scene_status(const phe_scene* scene, uint32_t* bits)
 {
 	if (!scene || !bits) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_scene_status: null argument");
 	PHE_CUDA_TRY(cudaMemcpy(bits, scene->status, sizeof(uint32_t), cudaMemcpyDeviceToHost), "read scene status");
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_scene_set_layout(phe_scene* scene, int layout)
+{
+	if (!scene) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_scene_set_layout: null scene");
+	if (layout == PHE_LAYOUT_BINARY) {
+		scene->dev.nodes4 = nullptr;
+		return PHE_OK;
+	}
+	if (layout != PHE_LAYOUT_WIDE4) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_scene_set_layout: unknown layout %d", layout);
+	if (!scene->nodes4)
+		return fail(PHE_ERR_INVALID_SCENE, "phe_scene_set_layout: this tree has child boxes outside their parent box");
+	scene->dev.nodes4 = scene->nodes4;
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_scene_get_layout(const phe_scene* scene, int* layout, int* wideAvailable)
+{
+	if (!scene) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_scene_get_layout: null scene");
+	if (layout) *layout = scene->dev.nodes4 ? PHE_LAYOUT_WIDE4 : PHE_LAYOUT_BINARY;
+	if (wideAvailable) *wideAvailable = scene->nodes4 ? 1 : 0;
 	return PHE_OK;
 }

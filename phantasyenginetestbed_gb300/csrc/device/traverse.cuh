@@ -150,12 +150,121 @@ __device__ __forceinline__ HitRecord empty_hit(const RayState& r)
 	return h;
 }
 
-template <bool ANY>
-__device__ __forceinline__ uint32_t trace(const float4* __restrict__ nodes, const float4* __restrict__ tris,
-                                          const RayState& r, HitRecord& hit)
+// Compare-and-swap of (key, payload) pairs for the near-first order of a 4-wide node.
+__device__ __forceinline__ void cswap(float& ka, int32_t& pa, float& kb, int32_t& pb)
 {
-	if (r.safe) return traverse<true, ANY>(nodes, tris, r, hit);
-	return traverse<false, ANY>(nodes, tris, r, hit);
+	bool sw = kb < ka;
+	float k = sw ? kb : ka;
+	int32_t q = sw ? pb : pa;
+	kb = sw ? ka : kb;
+	pb = sw ? pa : pb;
+	ka = k;
+	pa = q;
+}
+
+// Traversal of the 4-wide layout (DeviceScene::nodes4) for rays whose 1/dir is finite. The four
+// child boxes of a node are tested with the same arithmetic as the binary traversal; hit children
+// are visited nearest first (closest hit) and the others pushed. A child box lies inside the binary
+// box it replaces and the rounded slab test is monotone in the box bounds, so a child passes here
+// only if the skipped binary test would pass too: the set of reachable leaves is the binary one.
+template <bool ANY>
+__device__ __forceinline__ uint32_t traverse4(const float4* __restrict__ nodes4, const float4* __restrict__ tris,
+                                              const RayState& r, HitRecord& hit)
+{
+	int32_t stack[kStackSize4];
+	int sp = 0;
+	stack[0] = kSentinel;
+	int32_t nodeAddr = 0;
+	int32_t leafAddr = 0;
+	uint32_t err = 0;
+	const float INF = __int_as_float(0x7f800000);
+
+	while (nodeAddr != kSentinel) {
+		while (nodeAddr >= 0 && nodeAddr != kSentinel) {
+			const float4* np = nodes4 + 8 * (size_t)nodeAddr;
+			float4 lx = __ldg(np), ly = __ldg(np + 1), lz = __ldg(np + 2);
+			float4 hx = __ldg(np + 3), hy = __ldg(np + 4), hz = __ldg(np + 5);
+			int4 ref = __ldg(reinterpret_cast<const int4*>(np + 6));
+			float t0, t1, t2, t3;
+			bool v0 = visit_box<true>(r, lx.x, ly.x, lz.x, hx.x, hy.x, hz.x, hit.t, t0) && ref.x != kEmptyChild;
+			bool v1 = visit_box<true>(r, lx.y, ly.y, lz.y, hx.y, hy.y, hz.y, hit.t, t1) && ref.y != kEmptyChild;
+			bool v2 = visit_box<true>(r, lx.z, ly.z, lz.z, hx.z, hy.z, hz.z, hit.t, t2) && ref.z != kEmptyChild;
+			bool v3 = visit_box<true>(r, lx.w, ly.w, lz.w, hx.w, hy.w, hz.w, hit.t, t3) && ref.w != kEmptyChild;
+			int nhit = (int)v0 + (int)v1 + (int)v2 + (int)v3;
+			if (nhit == 0) {
+				nodeAddr = stack[sp--];
+			} else {
+				float k0 = v0 ? t0 : INF, k1 = v1 ? t1 : INF, k2 = v2 ? t2 : INF, k3 = v3 ? t3 : INF;
+				int32_t c0 = ref.x, c1 = ref.y, c2 = ref.z, c3 = ref.w;
+				if (ANY) {
+					// no order needed: compact the hit children to the front
+					if (!v0) { k0 = k1; c0 = c1; k1 = k2; c1 = c2; k2 = k3; c2 = c3; v0 = v1; v1 = v2; v2 = v3; }
+					if (!v0) { k0 = k1; c0 = c1; k1 = k2; c1 = c2; v0 = v1; v1 = v2; }
+					if (!v0) { c0 = c1; }
+					if (nhit > 1 && !v1) { c1 = c2; c2 = c3; v1 = v2; }
+					if (nhit > 1 && !v1) { c1 = c2; }
+					if (nhit > 2 && !v2) { c2 = c3; }
+				} else {
+					cswap(k0, c0, k1, c1);
+					cswap(k2, c2, k3, c3);
+					cswap(k0, c0, k2, c2);
+					cswap(k1, c1, k3, c3);
+					cswap(k1, c1, k2, c2);
+				}
+				if (sp + 3 >= kStackSize4 - 1) {
+					err |= kErrStackOverflow;
+					nodeAddr = kSentinel;
+					leafAddr = 0;
+					break;
+				}
+				if (nhit > 3) stack[++sp] = c3;
+				if (nhit > 2) stack[++sp] = c2;
+				if (nhit > 1) stack[++sp] = c1;
+				nodeAddr = c0;
+			}
+			if (nodeAddr < 0 && leafAddr >= 0) {
+				leafAddr = nodeAddr;
+				nodeAddr = stack[sp--];
+			}
+			if (!__any_sync(__activemask(), leafAddr >= 0)) break;
+		}
+
+		while (leafAddr < 0) {
+			int32_t slot = ~leafAddr;
+			for (;;) {
+				const float4* tp = tris + 3 * (size_t)slot;
+				float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+				float t, u, v;
+				if (intersect_tri(a, b, c, r.o, r.d, t, u, v) && r.tMin <= t && t < hit.t) {
+					hit.slot = (uint32_t)slot;
+					hit.t = t;
+					hit.u = u;
+					hit.v = v;
+					if (ANY) {
+						nodeAddr = kSentinel;
+						leafAddr = 0;
+						break;
+					}
+				}
+				if (a.w < 0.0f) break;
+				slot++;
+			}
+			if (ANY && nodeAddr == kSentinel && leafAddr == 0) break;
+			leafAddr = nodeAddr;
+			if (nodeAddr < 0) nodeAddr = stack[sp--];
+		}
+	}
+	return err;
+}
+
+template <bool ANY>
+__device__ __forceinline__ uint32_t trace(const DeviceScene& s, const RayState& r, HitRecord& hit)
+{
+	if (r.safe) {
+		if (s.nodes4) return traverse4<ANY>(s.nodes4, s.tris, r, hit);
+		return traverse<true, ANY>(s.nodes, s.tris, r, hit);
+	}
+	return traverse<false, ANY>(s.nodes, s.tris, r, hit);
 }
 
 __device__ __forceinline__ void store_hit(phe_ray_hit* __restrict__ hits, uint32_t i, const RayState& r, const HitRecord& h)

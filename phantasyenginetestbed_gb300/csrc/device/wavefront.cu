@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(kWaveBlock) primary_kernel(DeviceScene s, cons
 			r.safe = isfinite(r.inv.x) && isfinite(r.inv.y) && isfinite(r.inv.z) && isfinite(d.x) && isfinite(d.y) &&
 			         isfinite(d.z) && isfinite(r.o.x) && isfinite(r.o.y) && isfinite(r.o.z);
 			h = empty_hit(r);
-			uint32_t err = trace<false>(s.nodes, s.tris, r, h);
+			uint32_t err = trace<false>(s, r, h);
 			if (err) atomicOr(status, err);
 		}
 		__syncwarp();
@@ -170,7 +170,7 @@ __global__ void __launch_bounds__(kWaveBlock) any_queue_kernel(DeviceScene s, co
 		if (i < n) {
 			RayState r = load_ray(rays, i);
 			HitRecord h = empty_hit(r);
-			uint32_t err = trace<true>(s.nodes, s.tris, r, h);
+			uint32_t err = trace<true>(s, r, h);
 			if (err) atomicOr(status, err);
 			inLight[__ldg(slots + i)] = h.slot == ~0u ? 1 : 0;
 		}
@@ -272,7 +272,7 @@ __global__ void __launch_bounds__(kWaveBlock) bounce_kernel(DeviceScene s, const
 			float4 t4 = fb.bounceThroughput[j];
 			thr = mk3(t4.x, t4.y, t4.z);
 			h = empty_hit(r);
-			uint32_t err = trace<false>(s.nodes, s.tris, r, h);
+			uint32_t err = trace<false>(s, r, h);
 			if (err) atomicOr(status, err);
 		}
 		__syncwarp();

@@ -27,6 +27,8 @@ PHE_ERR_NO_DEVICE = 10
 
 PTR_HOST = 0
 PTR_DEVICE = 1
+LAYOUT_BINARY = 0
+LAYOUT_WIDE4 = 1
 
 # numpy views of the reference layouts
 NODE_DTYPE = np.dtype([("fData", "<f4", (12,)), ("iData", "<i4", (4,))])            # phe::BVHNode, 64 B
@@ -69,7 +71,8 @@ class BatchItem(C.Structure):
 
 
 class BatchParams(C.Structure):
-    _fields_ = [("blockSize", C.c_int32), ("blocksPerSM", C.c_int32), ("order", C.c_int32), ("useGraph", C.c_int32)]
+    _fields_ = [("blockSize", C.c_int32), ("blocksPerSM", C.c_int32), ("order", C.c_int32), ("useGraph", C.c_int32),
+                ("layout", C.c_int32), ("pad", C.c_int32)]
 
 
 class BatchTuningRow(C.Structure):
@@ -136,6 +139,8 @@ SIGNATURES: dict[str, tuple] = {
     "phe_cast_any": (_I32, [_VP, _VP, _VP, _U32, _VP, _VP]),
     "phe_gen_primary_rays": (_I32, [_VP, C.POINTER(CameraDef), _U32, _U32, _F, _F, _I32, _VP]),
     "phe_scene_status": (_I32, [_VP, C.POINTER(_U32)]),
+    "phe_scene_set_layout": (_I32, [_VP, _I32]),
+    "phe_scene_get_layout": (_I32, [_VP, C.POINTER(_I32), C.POINTER(_I32)]),
     "phe_renderer_create": (_I32, [C.POINTER(_VP)]),
     "phe_renderer_destroy": (_I32, [_VP]),
     "phe_renderer_set_static_scene": (_I32, [_VP, _VP]),
@@ -175,6 +180,7 @@ SIGNATURES: dict[str, tuple] = {
     "phe_server_release": (_I32, [_VP, C.c_uint64]),
     "phe_server_get_stats": (_I32, [_VP, C.POINTER(ServerStats)]),
     "phe_server_destroy": (_I32, [_VP]),
+    "phe_postprocess": (_I32, [_U32, _U32, _VP, _F, _VP, _VP, _VP]),
     "phe_taa_resolve": (_I32, [_U32, _U32, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
 }
 

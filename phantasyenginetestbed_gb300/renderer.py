@@ -133,3 +133,17 @@ def taa_resolve(res, cur, hist, out_color, out_hist, velocity=None, prev_velocit
     """TAA resolve on device buffers (phe_taa_resolve)."""
     check(lib().phe_taa_resolve(int(res[0]), int(res[1]), ptr(cur), ptr(hist), ptr(velocity), ptr(prev_velocity),
                                 ptr(roughness), ptr(out_color), ptr(out_hist), _stream(stream)), "phe_taa_resolve")
+
+
+def postprocess(res, linear, display=None, rgba8=None, gamma=2.2, stream=None):
+    """Uncharted 2 tonemap + gamma on device buffers (phe_postprocess)."""
+    check(lib().phe_postprocess(int(res[0]), int(res[1]), ptr(linear), C.c_float(gamma), ptr(display), ptr(rgba8),
+                                _stream(stream)), "phe_postprocess")
+
+
+def write_ppm(path, rgba8: np.ndarray) -> None:
+    """Writes an (H, W, 4) uint8 image as binary PPM, top row first (the renderer's row 0 is the bottom)."""
+    h, w = rgba8.shape[:2]
+    with open(path, "wb") as f:
+        f.write(b"P6\n%d %d\n255\n" % (w, h))
+        f.write(np.ascontiguousarray(rgba8[::-1, :, :3]).tobytes())

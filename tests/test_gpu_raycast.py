@@ -230,3 +230,27 @@ def test_small_scenes_every_ray_vs_brute_force(T):
     _check(rep, len(rays))
     assert hit.mean() > 0.05
     assert np.array_equal(_gpu_any(scene, rays), O.any_rays(b.nodes, b.verts, rays))
+
+
+def test_wide_layout_gives_the_binary_results():
+    """The 4-wide node layout visits the leaves the binary layout visits: closest hits (same slots
+    except documented near-ties) and any hits identical, on coherent, incoherent and axis-aligned rays."""
+    s, b = built_scene("c2_256_2000")
+    scene = P.Scene(b.nodes, b.verts)
+    lay, avail = scene.layout()
+    assert lay == 0 and avail
+    k = s.scale
+    cam = O.camera_def((0.5 * k, -0.3 * k, 0.6 * k), C1_CAM["dir"], C1_CAM["up"], math.radians(60), (640, 360))
+    rays = np.concatenate([O.gen_primary(cam, (640, 360)), random_rays(100000, [0, 0, 0.02], [k, k, 0.3 * k], 9)])
+    axes = np.array([[1, 0, 0], [0, 1, 0], [0, 0, -1]], np.float32)
+    rays["dir"][::7] = axes[np.arange(len(rays[::7])) % 3]
+    binary = _gpu_closest(scene, rays)
+    binary_any = _gpu_any(scene, rays)
+    scene.set_layout(1)
+    assert scene.layout() == (1, True)
+    for kind in ("persistent", "plain"):
+        wide = _gpu_closest(scene, rays, kind)
+        _check(O.compare_closest(wide, binary, rays, b.slot_to_tri, b.verts), len(rays))
+    assert np.array_equal(_gpu_any(scene, rays), binary_any)
+    orc = O.cast_rays(b.nodes, b.verts, rays)
+    _check(O.compare_closest(_gpu_closest(scene, rays), orc, rays, b.slot_to_tri, b.verts), len(rays))

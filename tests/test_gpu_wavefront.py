@@ -123,3 +123,25 @@ def test_renderer_rejects_bad_configuration():
         r.setTargetResolution((100, 64))   # not a multiple of 8
     with pytest.raises(P.PheError):
         r.render(make_lights([(0, 0, 1)]))  # no scene, no resolution
+
+
+def test_postprocess_matches_oracle_and_writes_an_image(tmp_path):
+    import torch
+    from phantasyenginetestbed_gb300.renderer import postprocess, write_ppm
+    rng = np.random.default_rng(8)
+    W, H = 64, 40
+    lin = rng.uniform(0, 3, (H, W, 4)).astype(np.float32)
+    lin[0, :5, :3] = [[0, 0, 0], [0.0015, 0.0015, 0.0015], [1e-3, 0, 2], [100, 50, 1e4], [0.5, 0.5, 0.5]]
+    d_lin = to_device(lin)
+    d_disp = device_empty(W * H, np.dtype((np.float32, 4)))
+    d_rgba = device_empty(W * H * 4, np.uint8)
+    postprocess((W, H), d_lin, d_disp, d_rgba)
+    torch.cuda.synchronize()
+    disp = from_device(d_disp, np.float32).reshape(H, W, 4)
+    ref = O.postprocess(lin)
+    assert np.abs(disp - ref).max() <= TOL          # powf on both sides: a few ulp apart at most
+    rgba = from_device(d_rgba, np.uint8).reshape(H, W, 4)
+    want = np.rint(np.clip(ref, 0, 1) * 255).astype(np.int32)
+    assert np.abs(rgba.astype(np.int32) - want).max() <= 1
+    write_ppm(tmp_path / "frame.ppm", rgba)
+    assert (tmp_path / "frame.ppm").stat().st_size == len(b"P6\n64 40\n255\n") + W * H * 3
