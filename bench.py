@@ -56,6 +56,8 @@ def parse():
                     help="fused: traversal + shading in one kernel per bounce (5 kernels); split: 7 kernels")
     ap.add_argument("--refill", type=int, default=28, help="lane-refill threshold of the split pipeline")
     ap.add_argument("--sort-window", type=int, default=0, help="bin bounce rays by octant in windows of N (0 = off)")
+    ap.add_argument("--serial-passes", action="store_true",
+                    help="run the primary shadow pass after the bounce pass instead of beside it")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", choices=["frame", "plain", "batch", "large", "serve"], default="frame",
                     help="frame (default, the headline): 1080p wavefront frame; batch: 64 uneven batches over 4 "
@@ -235,6 +237,7 @@ def run_ours(args, world, rank, local):
     scene = P.Scene(b.nodes, b.verts, b.slot_datas(s.datas), s.materials)
     r = CudaTracerRenderer(use_graph=not args.no_graph)
     r.set_pipeline(fused=args.pipeline == "fused", refill=args.refill, sort_window=args.sort_window)
+    r.set_concurrent(not args.serial_passes)
     r.setStaticScene(scene)
     r.setTargetResolution(RES)
     r.set_seed(SEED, 0)
@@ -360,7 +363,8 @@ def run_ours(args, world, rank, local):
                    "bvh_slots": int(len(b.verts)), "sbvh_build_s": round(build_s, 2), "lights": 1,
                    "rays_per_frame": round(rays_per_frame, 1), "rays_by_pass": {k: round(v, 1) for k, v in stage_rays.items()},
                    "cuda_graph": not args.no_graph, "pipeline": args.pipeline,
-                   "refill_threshold": args.refill, "sort_window": args.sort_window, "l2": "flushed before every timed frame (512 MiB write)",
+                   "refill_threshold": args.refill, "sort_window": args.sort_window,
+                   "concurrent_shadow_pass": args.pipeline == "fused" and not args.serial_passes, "l2": "flushed before every timed frame (512 MiB write)",
                    "parallelism": f"replicas x{world}"},
         "latency_ms": {"p50": round(lat[len(lat) // 2], 4), "p99": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 4)},
         "passes": per_kernel,

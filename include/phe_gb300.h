@@ -317,6 +317,11 @@ phe_status phe_renderer_ray_counts(const phe_renderer* renderer, uint64_t counts
  * a multiple of 256 up to 4096; default 0) bins the bounce rays by direction octant within windows of
  * that many queue entries before they are traced. */
 phe_status phe_renderer_set_pipeline(phe_renderer* renderer, int fused, int refill, int sortWindow);
+/* Concurrent passes (default 1): with the fused pipeline, the primary shadow pass runs on a second
+ * stream of the renderer beside the bounce pass (both read only the primary pass's queues; in a
+ * captured graph they are parallel branches). 0 runs every kernel in order on the render stream.
+ * Results are the same either way. Frames timed per kernel always run in order. */
+phe_status phe_renderer_set_concurrent(phe_renderer* renderer, int concurrent);
 /* Per-kernel timing with CUDA events on the render stream (direct launches; ignored while a graph is
  * replayed). Enabling resets the totals. kernel_times returns the summed milliseconds per frame kernel
  * (in launch order, `numKernels` of them) and the number of frames timed. */

@@ -44,6 +44,8 @@ struct phe_renderer {
 	int timedKernels = 0;
 	uint32_t timedFrames = 0;
 	bool pendingTimes = false;
+	FrameStreams streams;                  // side stream for the concurrent shadow pass
+	bool concurrent = true;
 };
 
 static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -195,6 +197,17 @@ extern "C" phe_status phe_renderer_set_pipeline(phe_renderer* r, int fused, int 
 	return PHE_OK;
 }
 
+extern "C" phe_status phe_renderer_set_concurrent(phe_renderer* r, int concurrent)
+{
+	if (!r) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_set_concurrent: null renderer");
+	if ((concurrent != 0) != r->concurrent && r->graphExec) {
+		cudaGraphExecDestroy(r->graphExec);
+		r->graphExec = nullptr;
+	}
+	r->concurrent = concurrent != 0;
+	return PHE_OK;
+}
+
 namespace phe_gb300 {
 phe_status renderer_reserve(phe_renderer* r, uint64_t pixels, uint32_t lights)
 {
@@ -229,6 +242,13 @@ extern "C" phe_status phe_renderer_create(phe_renderer** out)
 		return cuda_fail(e, "allocate frame parameters");
 	}
 	std::memset(r->hParams, 0, sizeof(FrameParamsDev) * kParamSlots);
+	if (cudaStreamCreateWithFlags(&r->streams.side, cudaStreamNonBlocking) != cudaSuccess ||
+	    cudaEventCreateWithFlags(&r->streams.fork, cudaEventDisableTiming) != cudaSuccess ||
+	    cudaEventCreateWithFlags(&r->streams.join, cudaEventDisableTiming) != cudaSuccess) {
+		cudaError_t e2 = cudaGetLastError();
+		phe_renderer_destroy(r);
+		return cuda_fail(e2, "create renderer streams");
+	}
 	*out = r;
 	return PHE_OK;
 }
@@ -241,6 +261,9 @@ extern "C" phe_status phe_renderer_destroy(phe_renderer* r)
 		if (r->events[i]) cudaEventDestroy(r->events[i]);
 	for (uint32_t i = 0; i < kParamSlots; i++)
 		if (r->paramEvents[i]) cudaEventDestroy(r->paramEvents[i]);
+	if (r->streams.side) cudaStreamDestroy(r->streams.side);
+	if (r->streams.fork) cudaEventDestroy(r->streams.fork);
+	if (r->streams.join) cudaEventDestroy(r->streams.join);
 	free_buffers(r);
 	cudaFree(r->dParams);
 	cudaFreeHost(r->hParams);
@@ -385,7 +408,8 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 			cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
 			phe_status st = PHE_OK;
 			if (e == cudaSuccess) {
-				st = launch_frame(r->scene, r->dParams, r->fb, r->resX, r->resY, cap, nullptr, r->fused);
+				st = launch_frame(r->scene, r->dParams, r->fb, r->resX, r->resY, cap, nullptr, r->fused,
+				                  r->concurrent ? &r->streams : nullptr);
 				e = cudaStreamEndCapture(cap, &g);
 			}
 			cudaStreamDestroy(cap);
@@ -404,7 +428,8 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 			st = launch_frame(r->scene, r->dParams, r->fb, r->resX, r->resY, s, r->events, r->fused);
 			r->pendingTimes = true;
 		} else {
-			st = launch_frame(r->scene, r->dParams, r->fb, r->resX, r->resY, s, nullptr, r->fused);
+			st = launch_frame(r->scene, r->dParams, r->fb, r->resX, r->resY, s, nullptr, r->fused,
+			                  r->concurrent ? &r->streams : nullptr);
 		}
 		if (st) return st;
 	}

@@ -634,8 +634,10 @@ phe_status prepare_frame()
 }
 
 phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, const FrameBuffers& fb, uint32_t resX,
-                        uint32_t resY, cudaStream_t stream, cudaEvent_t* ev, bool fused)
+                        uint32_t resY, cudaStream_t stream, cudaEvent_t* ev, bool fused, const FrameStreams* streams)
 {
+	// Timed frames keep one stream so that the per-kernel events measure one kernel each.
+	const bool concurrent = streams && streams->side && !ev;
 	phe_status st;
 	int g[kGridCount];
 	for (int k = 0; k < kGridCount; k++)
@@ -652,9 +654,16 @@ phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, c
 	if (fused) {
 		primary_kernel<<<g[kGridPrimary], kWaveBlock, 0, stream>>>(scene->dev, dParams, fb, scene->status);
 		mark();
-		any_queue_kernel<<<g[kGridAnyQueue], kWaveBlock, 0, stream>>>(scene->dev, fb.shadowRays, fb.shadowSlots,
-		                                                               fb.counters + kCtrShadow0, fb.inLight,
-		                                                               fb.counters + kCtrWork2, scene->status);
+		cudaStream_t shadowStream = stream;
+		if (concurrent) {
+			PHE_CUDA_TRY(cudaEventRecord(streams->fork, stream), "fork frame");
+			PHE_CUDA_TRY(cudaStreamWaitEvent(streams->side, streams->fork, 0), "fork frame");
+			shadowStream = streams->side;
+		}
+		any_queue_kernel<<<g[kGridAnyQueue], kWaveBlock, 0, shadowStream>>>(scene->dev, fb.shadowRays, fb.shadowSlots,
+		                                                                     fb.counters + kCtrShadow0, fb.inLight,
+		                                                                     fb.counters + kCtrWork2, scene->status);
+		if (concurrent) PHE_CUDA_TRY(cudaEventRecord(streams->join, shadowStream), "join frame");
 		mark();
 		if (fb.sortWindow > 0) {
 			bin_bounce_kernel<<<binGrid, kBinBlock, 0, stream>>>(fb);
@@ -692,6 +701,7 @@ phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, c
 		                                                                 scene->status);
 		mark();
 	}
+	if (concurrent && fused) PHE_CUDA_TRY(cudaStreamWaitEvent(stream, streams->join, 0), "join frame");
 	resolve_taa_kernel<<<grid, block, 0, stream>>>(dParams, fb);
 	mark();
 	PHE_CUDA_TRY(cudaGetLastError(), "frame kernel launch");

@@ -73,7 +73,15 @@ constexpr int kFrameKernels = 8;
 constexpr int kFusedFrameKernels = 6;
 // `events` (optional, kernels + 1 entries) are recorded on `stream` around each kernel. `fused`
 // selects the pipeline with traversal and shading in one kernel.
+// `side` (optional, with `fork`/`join` events) runs the primary shadow pass concurrently with the bounce
+// pass: both only need the primary pass's queues, and the second persistent kernel fills the first one's
+// tail. In a captured graph this becomes two parallel branches.
+struct FrameStreams {
+	cudaStream_t side = nullptr;
+	cudaEvent_t fork = nullptr, join = nullptr;
+};
 phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, const FrameBuffers& fb, uint32_t resX,
-                        uint32_t resY, cudaStream_t stream, cudaEvent_t* events = nullptr, bool fused = false);
+                        uint32_t resY, cudaStream_t stream, cudaEvent_t* events = nullptr, bool fused = false,
+                        const FrameStreams* streams = nullptr);
 
 } // namespace phe_gb300

@@ -105,6 +105,10 @@ class CudaTracerRenderer:
         check(lib().phe_renderer_set_pipeline(self.handle, 1 if fused else 0, refill, sort_window),
               "phe_renderer_set_pipeline")
 
+    def set_concurrent(self, concurrent: bool = True) -> None:
+        """Run the primary shadow pass beside the bounce pass on a second stream (same results)."""
+        check(lib().phe_renderer_set_concurrent(self.handle, 1 if concurrent else 0), "phe_renderer_set_concurrent")
+
     def close(self) -> None:
         if getattr(self, "handle", None):
             check(lib().phe_renderer_destroy(self.handle), "phe_renderer_destroy")

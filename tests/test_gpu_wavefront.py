@@ -61,6 +61,26 @@ def test_frame_matches_oracle_small(graph, fused, refill, window):
     assert raw[..., :3].max() > 0.01 and (raw[..., :3] > 0).mean() > 0.2
 
 
+@pytest.mark.parametrize("graph", [False, True])
+def test_concurrent_shadow_pass_gives_the_serial_frame(graph):
+    """The primary shadow pass beside the bounce pass (second stream / parallel graph branch) writes the
+    same bytes as the in-order pipeline, frame after frame (TAA history included)."""
+    res = (256, 160)
+    s, b, datas, scene, cam, cam_pos, lights, r = _setup("c2_256_2000", res, [(0.5, 0.5, 2.0), (0.9, 0.2, 1.5)], graph)
+    out = {}
+    for conc in (False, True):
+        r.set_concurrent(conc)
+        r.set_seed(77, 0)
+        r.resetTAA()
+        for f in range(3):
+            r.set_camera_def(cam_struct(cam), cam_pos, P.halton_jitter(f))
+            r.render(lights)
+        out[conc] = (r.read(READ_RAW), r.read(READ_HISTORY), r.ray_counts())
+    assert np.array_equal(out[False][0], out[True][0])
+    assert np.array_equal(out[False][1], out[True][1])
+    assert np.array_equal(out[False][2], out[True][2])
+
+
 def test_frame_full_resolution_and_taa_sequence():
     """The wavefront-frame configuration: 1920x1080, point light at (0.5, 0.5, 2.0) * scale, 8 frames
     with Halton(2,3) jitter and the TAA resolve on an FP32 RGBA history."""
