@@ -41,7 +41,7 @@ __device__ __forceinline__ uint32_t find_item(const BatchItemDev* __restrict__ i
 	return lo;
 }
 
-template <int BLOCK>
+template <int BLOCK, bool WIDE>
 __global__ void __launch_bounds__(BLOCK) batch_kernel(BatchTableDev t, uint32_t* __restrict__ counter,
                                                       uint32_t* __restrict__ status)
 {
@@ -60,10 +60,10 @@ __global__ void __launch_bounds__(BLOCK) batch_kernel(BatchTableDev t, uint32_t*
 			HitRecord h = empty_hit(r);
 			uint32_t err;
 			if (item.kind == 0) {
-				err = trace<false>(s, r, h);
+				err = trace<false, WIDE>(s, r, h);
 				store_hit((phe_ray_hit*)item.out, i, r, h);
 			} else {
-				err = trace<true>(s, r, h);
+				err = trace<true, WIDE>(s, r, h);
 				((uint8_t*)item.out)[i] = h.slot == ~0u ? 1 : 0;
 			}
 			if (err) atomicOr(status, err);
@@ -72,12 +72,14 @@ __global__ void __launch_bounds__(BLOCK) batch_kernel(BatchTableDev t, uint32_t*
 	}
 }
 
+// `wide` selects the instantiation with the 4-wide traversal (for scene tables holding 4-wide scenes).
 template <int BLOCK>
-static phe_status launch_batch_kernel(const BatchTableDev& t, int blocksPerSM, int numSMs, uint32_t* counter,
+static phe_status launch_batch_kernel(const BatchTableDev& t, bool wide, int blocksPerSM, int numSMs, uint32_t* counter,
                                       uint32_t* status, cudaStream_t stream, int* occupancyOut)
 {
+	auto kernel = wide ? batch_kernel<BLOCK, true> : batch_kernel<BLOCK, false>;
 	int maxB = 0;
-	PHE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxB, batch_kernel<BLOCK>, BLOCK, 0), "occupancy");
+	PHE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxB, kernel, BLOCK, 0), "occupancy");
 	if (occupancyOut) {
 		*occupancyOut = maxB;
 		return PHE_OK;
@@ -87,14 +89,14 @@ static phe_status launch_batch_kernel(const BatchTableDev& t, int blocksPerSM, i
 	uint32_t grid = (uint32_t)(b * numSMs);
 	uint32_t need = (t.totalPadded + BLOCK - 1) / BLOCK;
 	if (grid > need) grid = need > 0 ? need : 1;
-	batch_kernel<BLOCK><<<grid, BLOCK, 0, stream>>>(t, counter, status);
+	kernel<<<grid, BLOCK, 0, stream>>>(t, counter, status);
 	PHE_CUDA_TRY(cudaGetLastError(), "batch_kernel launch");
 	return PHE_OK;
 }
 
 phe_status launch_batch_table(const BatchItemDev* items, uint32_t numItems, uint32_t totalPadded,
                               const DeviceScene* scenes, uint32_t* counter, uint32_t* status, int blockSize,
-                              int blocksPerSM, cudaStream_t stream)
+                              int blocksPerSM, cudaStream_t stream, bool wide)
 {
 	DeviceInfo* d = nullptr;
 	phe_status st = device_info(&d);
@@ -102,9 +104,9 @@ phe_status launch_batch_table(const BatchItemDev* items, uint32_t numItems, uint
 	if (totalPadded == 0) return PHE_OK;
 	BatchTableDev t{items, scenes, numItems, totalPadded};
 	switch (blockSize) {
-	case 64: return launch_batch_kernel<64>(t, blocksPerSM, d->numSMs, counter, status, stream, nullptr);
-	case 256: return launch_batch_kernel<256>(t, blocksPerSM, d->numSMs, counter, status, stream, nullptr);
-	default: return launch_batch_kernel<128>(t, blocksPerSM, d->numSMs, counter, status, stream, nullptr);
+	case 64: return launch_batch_kernel<64>(t, wide, blocksPerSM, d->numSMs, counter, status, stream, nullptr);
+	case 256: return launch_batch_kernel<256>(t, wide, blocksPerSM, d->numSMs, counter, status, stream, nullptr);
+	default: return launch_batch_kernel<128>(t, wide, blocksPerSM, d->numSMs, counter, status, stream, nullptr);
 	}
 }
 
@@ -271,10 +273,11 @@ static phe_status batch_enqueue(phe_batch* b, cudaStream_t stream)
 	BatchTableDev t{b->dItems, b->dScenes, (uint32_t)b->items.size(), b->totalPadded};
 	PHE_CUDA_TRY(cudaMemsetAsync(b->dCounter, 0, sizeof(uint32_t), stream), "clear batch counter");
 	if (b->totalPadded == 0) return PHE_OK;
+	const bool wide = b->params.layout == PHE_LAYOUT_WIDE4;
 	switch (b->params.blockSize) {
-	case 64: return launch_batch_kernel<64>(t, b->params.blocksPerSM, d->numSMs, b->dCounter, b->dStatus, stream, nullptr);
-	case 256: return launch_batch_kernel<256>(t, b->params.blocksPerSM, d->numSMs, b->dCounter, b->dStatus, stream, nullptr);
-	case 128: return launch_batch_kernel<128>(t, b->params.blocksPerSM, d->numSMs, b->dCounter, b->dStatus, stream, nullptr);
+	case 64: return launch_batch_kernel<64>(t, wide, b->params.blocksPerSM, d->numSMs, b->dCounter, b->dStatus, stream, nullptr);
+	case 256: return launch_batch_kernel<256>(t, wide, b->params.blocksPerSM, d->numSMs, b->dCounter, b->dStatus, stream, nullptr);
+	case 128: return launch_batch_kernel<128>(t, wide, b->params.blocksPerSM, d->numSMs, b->dCounter, b->dStatus, stream, nullptr);
 	default: return fail(PHE_ERR_INVALID_ARGUMENT, "batch block size must be 64, 128 or 256");
 	}
 }
@@ -288,10 +291,11 @@ extern "C" phe_status phe_batch_launch(phe_batch* b, void* stream)
 		// Resolve occupancy outside capture.
 		int occ = 0;
 		BatchTableDev t{};
+		const bool wide = b->params.layout == PHE_LAYOUT_WIDE4;
 		switch (b->params.blockSize) {
-		case 64: launch_batch_kernel<64>(t, 0, 1, nullptr, nullptr, nullptr, &occ); break;
-		case 256: launch_batch_kernel<256>(t, 0, 1, nullptr, nullptr, nullptr, &occ); break;
-		default: launch_batch_kernel<128>(t, 0, 1, nullptr, nullptr, nullptr, &occ); break;
+		case 64: launch_batch_kernel<64>(t, wide, 0, 1, nullptr, nullptr, nullptr, &occ); break;
+		case 256: launch_batch_kernel<256>(t, wide, 0, 1, nullptr, nullptr, nullptr, &occ); break;
+		default: launch_batch_kernel<128>(t, wide, 0, 1, nullptr, nullptr, nullptr, &occ); break;
 		}
 		cudaStream_t cap = nullptr;
 		PHE_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), "create capture stream");
@@ -367,9 +371,9 @@ extern "C" phe_status phe_batch_autotune(phe_batch* b, int repeats, void* stream
 	for (int bs : blocks) {
 		int occ = 0;
 		BatchTableDev t{};
-		if (bs == 64) launch_batch_kernel<64>(t, 0, 1, nullptr, nullptr, nullptr, &occ);
-		else if (bs == 128) launch_batch_kernel<128>(t, 0, 1, nullptr, nullptr, nullptr, &occ);
-		else launch_batch_kernel<256>(t, 0, 1, nullptr, nullptr, nullptr, &occ);
+		if (bs == 64) launch_batch_kernel<64>(t, false, 0, 1, nullptr, nullptr, nullptr, &occ);
+		else if (bs == 128) launch_batch_kernel<128>(t, false, 0, 1, nullptr, nullptr, nullptr, &occ);
+		else launch_batch_kernel<256>(t, false, 0, 1, nullptr, nullptr, nullptr, &occ);
 		for (int ord : orders)
 			for (int q : occFrac)
 				for (int lay : layouts) {
@@ -506,7 +510,11 @@ extern "C" phe_status phe_batch_cast_noalloc(const phe_scene* const* scenes, uin
 		if (next > 0xFFFFFFF0ull) return fail(PHE_ERR_TOO_LARGE, "phe_batch_cast_noalloc: more than 2^32 rays");
 		base = (uint32_t)next;
 	}
-	for (uint32_t i = 0; i < numScenes; i++) sceneTable[i] = scenes[i]->dev;
+	bool wide = false;
+	for (uint32_t i = 0; i < numScenes; i++) {
+		sceneTable[i] = scenes[i]->dev;
+		wide = wide || scenes[i]->dev.nodes4 != nullptr;
+	}
 	BatchItemDev* dItems = (BatchItemDev*)scratch;
 	DeviceScene* dScenes = (DeviceScene*)(scratch + kNoAllocItemsBytes);
 	uint32_t* dCounter = (uint32_t*)(scratch + kNoAllocItemsBytes + kNoAllocScenesBytes);
@@ -522,12 +530,13 @@ extern "C" phe_status phe_batch_cast_noalloc(const phe_scene* const* scenes, uin
 	int dev = 0, numSMs = 0, perSM = 0;
 	PHE_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
 	PHE_CUDA_TRY(cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, dev), "SM count");
-	PHE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, batch_kernel<128>, 128, 0), "occupancy");
+	auto kernel = wide ? batch_kernel<128, true> : batch_kernel<128, false>;
+	PHE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kernel, 128, 0), "occupancy");
 	uint32_t grid = (uint32_t)(perSM > 0 ? perSM : 1) * (uint32_t)numSMs;
 	uint32_t need = (base + 127u) / 128u;
 	if (grid > need) grid = need;
 	BatchTableDev t{dItems, dScenes, numItems, base};
-	batch_kernel<128><<<grid, 128, 0, s>>>(t, dCounter, dStatus);
+	kernel<<<grid, 128, 0, s>>>(t, dCounter, dStatus);
 	PHE_CUDA_TRY(cudaGetLastError(), "batch_kernel launch (no-alloc)");
 	return PHE_OK;
 }

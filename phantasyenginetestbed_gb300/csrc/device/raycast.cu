@@ -16,6 +16,7 @@ namespace phe_gb300 {
 constexpr int kPlainBlock = 128;
 constexpr int kPersistentBlock = 128;
 
+template <bool WIDE>
 __global__ void __launch_bounds__(kPlainBlock) closest_plain_kernel(DeviceScene s, const phe_ray_in* __restrict__ rays,
                                                                     phe_ray_hit* __restrict__ hits, uint32_t n,
                                                                     uint32_t* __restrict__ status)
@@ -24,13 +25,14 @@ __global__ void __launch_bounds__(kPlainBlock) closest_plain_kernel(DeviceScene 
 	if (i >= n) return;
 	RayState r = load_ray(rays, i);
 	HitRecord h = empty_hit(r);
-	uint32_t err = trace<false>(s, r, h);
+	uint32_t err = trace<false, WIDE>(s, r, h);
 	if (err) atomicOr(status, err);
 	store_hit(hits, i, r, h);
 }
 
 // Persistent warps: each warp takes 32 consecutive rays per atomic fetch (one atomic per warp,
 // lane 0 fetches and broadcasts) until the batch is exhausted.
+template <bool WIDE>
 __global__ void __launch_bounds__(kPersistentBlock) closest_persistent_kernel(DeviceScene s,
                                                                               const phe_ray_in* __restrict__ rays,
                                                                               phe_ray_hit* __restrict__ hits, uint32_t n,
@@ -47,7 +49,7 @@ __global__ void __launch_bounds__(kPersistentBlock) closest_persistent_kernel(De
 		if (i < n) {
 			RayState r = load_ray(rays, i);
 			HitRecord h = empty_hit(r);
-			uint32_t err = trace<false>(s, r, h);
+			uint32_t err = trace<false, WIDE>(s, r, h);
 			if (err) atomicOr(status, err);
 			store_hit(hits, i, r, h);
 		}
@@ -55,6 +57,7 @@ __global__ void __launch_bounds__(kPersistentBlock) closest_persistent_kernel(De
 	}
 }
 
+template <bool WIDE>
 __global__ void __launch_bounds__(kPersistentBlock) any_persistent_kernel(DeviceScene s,
                                                                           const phe_ray_in* __restrict__ rays,
                                                                           uint8_t* __restrict__ inLight,
@@ -72,7 +75,7 @@ __global__ void __launch_bounds__(kPersistentBlock) any_persistent_kernel(Device
 		if (i < n) {
 			RayState r = load_ray(rays, i);
 			HitRecord h = empty_hit(r);
-			uint32_t err = trace<true>(s, r, h);
+			uint32_t err = trace<true, WIDE>(s, r, h);
 			if (err) atomicOr(status, err);
 			uint32_t o = scatter ? __ldg(scatter + i) : i;
 			inLight[o] = h.slot == ~0u ? 1 : 0;
@@ -81,7 +84,7 @@ __global__ void __launch_bounds__(kPersistentBlock) any_persistent_kernel(Device
 	}
 }
 
-static int g_persistentBlocksPerSM[2] = {0, 0};
+static int g_persistentBlocksPerSM[4] = {0, 0, 0, 0};   // [closest, any] x [binary, wide]
 
 static phe_status persistent_grid(int which, const void* kernel, int* grid)
 {
@@ -117,7 +120,8 @@ extern "C" phe_status phe_cast_closest_plain(const phe_scene* scene, const phe_r
 	if (((uintptr_t)hits & 15u) != 0) return fail(PHE_ERR_INVALID_ARGUMENT, "hit buffer must be 16-byte aligned");
 	if (n == 0) return PHE_OK;
 	uint32_t grid = (n + kPlainBlock - 1) / kPlainBlock;
-	closest_plain_kernel<<<grid, kPlainBlock, 0, (cudaStream_t)stream>>>(scene->dev, rays, hits, n, scene->status);
+	auto kernel = scene->dev.nodes4 ? closest_plain_kernel<true> : closest_plain_kernel<false>;
+	kernel<<<grid, kPlainBlock, 0, (cudaStream_t)stream>>>(scene->dev, rays, hits, n, scene->status);
 	PHE_CUDA_TRY(cudaGetLastError(), "closest_plain_kernel launch");
 	return PHE_OK;
 }
@@ -129,14 +133,15 @@ extern "C" phe_status phe_cast_closest(const phe_scene* scene, const phe_ray_in*
 	if (st) return st;
 	if (((uintptr_t)hits & 15u) != 0) return fail(PHE_ERR_INVALID_ARGUMENT, "hit buffer must be 16-byte aligned");
 	if (n == 0) return PHE_OK;
+	const bool wide = scene->dev.nodes4 != nullptr;
+	auto kernel = wide ? closest_persistent_kernel<true> : closest_persistent_kernel<false>;
 	int grid = 0;
-	if ((st = persistent_grid(0, (const void*)closest_persistent_kernel, &grid))) return st;
+	if ((st = persistent_grid(wide ? 2 : 0, (const void*)kernel, &grid))) return st;
 	uint32_t maxGrid = (n + kPersistentBlock - 1) / kPersistentBlock;
 	if ((uint32_t)grid > maxGrid) grid = (int)maxGrid;
 	uint32_t* counter = nullptr;
 	if ((st = acquire_counter((cudaStream_t)stream, &counter))) return st;
-	closest_persistent_kernel<<<grid, kPersistentBlock, 0, (cudaStream_t)stream>>>(scene->dev, rays, hits, n, counter,
-	                                                                               scene->status);
+	kernel<<<grid, kPersistentBlock, 0, (cudaStream_t)stream>>>(scene->dev, rays, hits, n, counter, scene->status);
 	PHE_CUDA_TRY(cudaGetLastError(), "closest_persistent_kernel launch");
 	return PHE_OK;
 }
@@ -147,14 +152,16 @@ extern "C" phe_status phe_cast_any(const phe_scene* scene, const phe_ray_in* ray
 	phe_status st = check_cast_args(scene, rays, inLight);
 	if (st) return st;
 	if (n == 0) return PHE_OK;
+	const bool wide = scene->dev.nodes4 != nullptr;
+	auto kernel = wide ? any_persistent_kernel<true> : any_persistent_kernel<false>;
 	int grid = 0;
-	if ((st = persistent_grid(1, (const void*)any_persistent_kernel, &grid))) return st;
+	if ((st = persistent_grid(wide ? 3 : 1, (const void*)kernel, &grid))) return st;
 	uint32_t maxGrid = (n + kPersistentBlock - 1) / kPersistentBlock;
 	if ((uint32_t)grid > maxGrid) grid = (int)maxGrid;
 	uint32_t* counter = nullptr;
 	if ((st = acquire_counter((cudaStream_t)stream, &counter))) return st;
-	any_persistent_kernel<<<grid, kPersistentBlock, 0, (cudaStream_t)stream>>>(scene->dev, rays, inLight, scatter, n,
-	                                                                           counter, scene->status);
+	kernel<<<grid, kPersistentBlock, 0, (cudaStream_t)stream>>>(scene->dev, rays, inLight, scatter, n, counter,
+	                                                        scene->status);
 	PHE_CUDA_TRY(cudaGetLastError(), "any_persistent_kernel launch");
 	return PHE_OK;
 }

@@ -33,6 +33,7 @@ struct phe_renderer {
 	uint32_t parity = 0;
 	int useGraph = 0;
 	cudaGraphExec_t graphExec = nullptr;
+	const float4* graphNodes4 = nullptr;   // scene layout the graph was captured with
 	cudaStream_t graphStream = nullptr;  // stream the graph was captured for (graphs relaunch on any stream)
 	bool cameraSet = false;
 	bool fused = true;                     // traversal and shading fused in one kernel per bounce
@@ -399,6 +400,10 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 	             "upload frame parameters");
 	PHE_CUDA_TRY(cudaEventRecord(r->paramEvents[slot], s), "record parameter slot");
 	if (r->useGraph) {
+		if (r->graphExec && r->graphNodes4 != r->scene->dev.nodes4) {   // layout switched since capture
+			cudaGraphExecDestroy(r->graphExec);
+			r->graphExec = nullptr;
+		}
 		if (!r->graphExec) {
 			phe_status pst = prepare_frame();
 			if (pst) return pst;
@@ -418,6 +423,7 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 			e = cudaGraphInstantiate(&r->graphExec, g, 0);
 			cudaGraphDestroy(g);
 			if (e != cudaSuccess) return cuda_fail(e, "instantiate frame graph");
+			r->graphNodes4 = r->scene->dev.nodes4;
 		}
 		PHE_CUDA_TRY(cudaGraphLaunch(r->graphExec, s), "launch frame graph");
 	} else {

@@ -107,6 +107,7 @@ struct phe_server {
 	uint64_t bytesInUse = 0;
 	bool stop = false;
 	bool sceneTableDirty = true;
+	bool wideScenes = false;               // some resident scene has its 4-wide layout selected
 
 	cudaStream_t waveStream = nullptr;
 	Wave waves[kWaveRing];
@@ -180,7 +181,8 @@ phe_status launch_wave(phe_server* s, Wave& w)
 	PHE_CUDA_TRY(cudaMemcpyAsync(w.devItems, w.hostItems, n * sizeof(BatchItemDev), cudaMemcpyHostToDevice, st),
 	             "upload wave table");
 	PHE_CUDA_TRY(cudaMemsetAsync(w.counter, 0, 2 * sizeof(uint32_t), st), "clear wave counter");
-	phe_status ps = launch_batch_table(w.devItems, n, base, s->dScenes, w.counter, w.counter + 1, 128, 0, st);
+	phe_status ps = launch_batch_table(w.devItems, n, base, s->dScenes, w.counter, w.counter + 1, 128, 0, st,
+	                                   s->wideScenes);
 	if (ps) return ps;
 	for (uint32_t i = 0; i < n; i++) {
 		Request* r = s->admitted[i];
@@ -237,7 +239,11 @@ phe_status issue_render(phe_server* s, Request* r, RenderSlot& slot)
 void upload_scene_table(phe_server* s)
 {
 	std::vector<DeviceScene> t;
-	for (const phe_scene* sc : s->scenes) t.push_back(sc->dev);
+	s->wideScenes = false;
+	for (const phe_scene* sc : s->scenes) {
+		t.push_back(sc->dev);
+		s->wideScenes = s->wideScenes || sc->dev.nodes4 != nullptr;
+	}
 	if (!t.empty()) cudaMemcpy(s->dScenes, t.data(), t.size() * sizeof(DeviceScene), cudaMemcpyHostToDevice);
 	s->sceneTableDirty = false;
 }

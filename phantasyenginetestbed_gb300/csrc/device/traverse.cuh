@@ -257,11 +257,16 @@ __device__ __forceinline__ uint32_t traverse4(const float4* __restrict__ nodes4,
 	return err;
 }
 
-template <bool ANY>
+// WIDE = false compiles the binary traversal only; kernels are instantiated for both layouts and
+// the host launches the WIDE one only for scenes whose 4-wide layout is selected, so binary
+// launches carry neither the 4-wide code nor its larger stack.
+template <bool ANY, bool WIDE = false>
 __device__ __forceinline__ uint32_t trace(const DeviceScene& s, const RayState& r, HitRecord& hit)
 {
 	if (r.safe) {
-		if (s.nodes4) return traverse4<ANY>(s.nodes4, s.tris, r, hit);
+		if constexpr (WIDE) {
+			if (s.nodes4) return traverse4<ANY>(s.nodes4, s.tris, r, hit);
+		}
 		return traverse<true, ANY>(s.nodes, s.tris, r, hit);
 	}
 	return traverse<false, ANY>(s.nodes, s.tris, r, hit);

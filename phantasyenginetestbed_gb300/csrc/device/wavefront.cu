@@ -82,6 +82,7 @@ __device__ __forceinline__ void shade_all_lights(const FrameParamsDev& fp, const
 	}
 }
 
+template <bool WIDE>
 __global__ void __launch_bounds__(kWaveBlock) primary_kernel(DeviceScene s, const FrameParamsDev* __restrict__ fpp,
                                                              FrameBuffers fb, uint32_t* __restrict__ status)
 {
@@ -114,7 +115,7 @@ __global__ void __launch_bounds__(kWaveBlock) primary_kernel(DeviceScene s, cons
 			r.safe = isfinite(r.inv.x) && isfinite(r.inv.y) && isfinite(r.inv.z) && isfinite(d.x) && isfinite(d.y) &&
 			         isfinite(d.z) && isfinite(r.o.x) && isfinite(r.o.y) && isfinite(r.o.z);
 			h = empty_hit(r);
-			uint32_t err = trace<false>(s, r, h);
+			uint32_t err = trace<false, WIDE>(s, r, h);
 			if (err) atomicOr(status, err);
 		}
 		__syncwarp();
@@ -155,6 +156,7 @@ __global__ void __launch_bounds__(kWaveBlock) primary_kernel(DeviceScene s, cons
 	}
 }
 
+template <bool WIDE>
 __global__ void __launch_bounds__(kWaveBlock) any_queue_kernel(DeviceScene s, const phe_ray_in* __restrict__ rays,
                                                                const uint32_t* __restrict__ slots,
                                                                const uint32_t* __restrict__ count, uint8_t* __restrict__ inLight,
@@ -170,7 +172,7 @@ __global__ void __launch_bounds__(kWaveBlock) any_queue_kernel(DeviceScene s, co
 		if (i < n) {
 			RayState r = load_ray(rays, i);
 			HitRecord h = empty_hit(r);
-			uint32_t err = trace<true>(s, r, h);
+			uint32_t err = trace<true, WIDE>(s, r, h);
 			if (err) atomicOr(status, err);
 			inLight[__ldg(slots + i)] = h.slot == ~0u ? 1 : 0;
 		}
@@ -246,6 +248,7 @@ __global__ void __launch_bounds__(kBinBlock) bin_bounce_kernel(FrameBuffers fb)
 	}
 }
 
+template <bool WIDE>
 __global__ void __launch_bounds__(kWaveBlock) bounce_kernel(DeviceScene s, const FrameParamsDev* __restrict__ fpp,
                                                             FrameBuffers fb, uint32_t* __restrict__ status)
 {
@@ -272,7 +275,7 @@ __global__ void __launch_bounds__(kWaveBlock) bounce_kernel(DeviceScene s, const
 			float4 t4 = fb.bounceThroughput[j];
 			thr = mk3(t4.x, t4.y, t4.z);
 			h = empty_hit(r);
-			uint32_t err = trace<false>(s, r, h);
+			uint32_t err = trace<false, WIDE>(s, r, h);
 			if (err) atomicOr(status, err);
 		}
 		__syncwarp();
@@ -591,16 +594,20 @@ __global__ void taa_kernel(uint32_t W, uint32_t H, const float4* __restrict__ cu
 // Launch sequence of one frame
 // ------------------------------------------------------------------------------------------------
 
+// The last three are the 4-wide instantiations of the fused kernels.
 enum { kGridPrimary = 0, kGridAnyQueue, kGridBounce, kGridPrimaryTrace, kGridAnyRefill, kGridBounceTrace,
-       kGridPrimaryShade, kGridBounceShade, kGridCount };
+       kGridPrimaryShade, kGridBounceShade, kGridPrimaryWide, kGridAnyQueueWide, kGridBounceWide, kGridCount };
 static int g_waveBlocksPerSM[kGridCount] = {};
 
 static const void* wave_kernel(int which)
 {
 	switch (which) {
-	case kGridPrimary: return (const void*)primary_kernel;
-	case kGridAnyQueue: return (const void*)any_queue_kernel;
-	case kGridBounce: return (const void*)bounce_kernel;
+	case kGridPrimary: return (const void*)primary_kernel<false>;
+	case kGridAnyQueue: return (const void*)any_queue_kernel<false>;
+	case kGridBounce: return (const void*)bounce_kernel<false>;
+	case kGridPrimaryWide: return (const void*)primary_kernel<true>;
+	case kGridAnyQueueWide: return (const void*)any_queue_kernel<true>;
+	case kGridBounceWide: return (const void*)bounce_kernel<true>;
 	case kGridPrimaryTrace: return (const void*)primary_trace_kernel;
 	case kGridAnyRefill: return (const void*)any_refill_kernel;
 	case kGridBounceTrace: return (const void*)bounce_trace_kernel;
@@ -652,7 +659,14 @@ phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, c
 	int binGrid = dinfo->numSMs * 4;
 	mark();
 	if (fused) {
-		primary_kernel<<<g[kGridPrimary], kWaveBlock, 0, stream>>>(scene->dev, dParams, fb, scene->status);
+		const bool wide = scene->dev.nodes4 != nullptr;
+		auto primary = wide ? primary_kernel<true> : primary_kernel<false>;
+		auto anyQueue = wide ? any_queue_kernel<true> : any_queue_kernel<false>;
+		auto bounce = wide ? bounce_kernel<true> : bounce_kernel<false>;
+		const int gPrimary = g[wide ? kGridPrimaryWide : kGridPrimary];
+		const int gAny = g[wide ? kGridAnyQueueWide : kGridAnyQueue];
+		const int gBounce = g[wide ? kGridBounceWide : kGridBounce];
+		primary<<<gPrimary, kWaveBlock, 0, stream>>>(scene->dev, dParams, fb, scene->status);
 		mark();
 		cudaStream_t shadowStream = stream;
 		if (concurrent) {
@@ -660,21 +674,20 @@ phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, c
 			PHE_CUDA_TRY(cudaStreamWaitEvent(streams->side, streams->fork, 0), "fork frame");
 			shadowStream = streams->side;
 		}
-		any_queue_kernel<<<g[kGridAnyQueue], kWaveBlock, 0, shadowStream>>>(scene->dev, fb.shadowRays, fb.shadowSlots,
-		                                                                     fb.counters + kCtrShadow0, fb.inLight,
-		                                                                     fb.counters + kCtrWork2, scene->status);
+		anyQueue<<<gAny, kWaveBlock, 0, shadowStream>>>(scene->dev, fb.shadowRays, fb.shadowSlots,
+		                                                 fb.counters + kCtrShadow0, fb.inLight, fb.counters + kCtrWork2,
+		                                                 scene->status);
 		if (concurrent) PHE_CUDA_TRY(cudaEventRecord(streams->join, shadowStream), "join frame");
 		mark();
 		if (fb.sortWindow > 0) {
 			bin_bounce_kernel<<<binGrid, kBinBlock, 0, stream>>>(fb);
 			mark();
 		}
-		bounce_kernel<<<g[kGridBounce], kWaveBlock, 0, stream>>>(scene->dev, dParams, fb, scene->status);
+		bounce<<<gBounce, kWaveBlock, 0, stream>>>(scene->dev, dParams, fb, scene->status);
 		mark();
-		any_queue_kernel<<<g[kGridAnyQueue], kWaveBlock, 0, stream>>>(scene->dev, fb.shadowRays + fb.capacityLP,
-		                                                               fb.shadowSlots + fb.capacityLP,
-		                                                               fb.counters + kCtrShadow1, fb.inLight,
-		                                                               fb.counters + kCtrWork3, scene->status);
+		anyQueue<<<gAny, kWaveBlock, 0, stream>>>(scene->dev, fb.shadowRays + fb.capacityLP, fb.shadowSlots + fb.capacityLP,
+		                                           fb.counters + kCtrShadow1, fb.inLight, fb.counters + kCtrWork3,
+		                                           scene->status);
 		mark();
 	} else {
 		primary_trace_kernel<<<g[kGridPrimaryTrace], kWaveBlock, 0, stream>>>(scene->dev, dParams, fb, scene->status);

@@ -81,6 +81,25 @@ def test_concurrent_shadow_pass_gives_the_serial_frame(graph):
     assert np.array_equal(out[False][2], out[True][2])
 
 
+@pytest.mark.parametrize("graph", [False, True])
+def test_wide_layout_frame_gives_the_binary_frame(graph):
+    """Switching the scene to 4-wide nodes between frames (graph re-captured) renders the same frame."""
+    res = (256, 160)
+    s, b, datas, scene, cam, cam_pos, lights, r = _setup("c2_256_2000", res, [(0.5, 0.5, 2.0)], graph)
+    out = []
+    for layout in (0, 1, 0):
+        scene.set_layout(layout)
+        r.set_seed(5, 0)
+        r.resetTAA()
+        for f in range(2):
+            r.set_camera_def(cam_struct(cam), cam_pos, P.halton_jitter(f))
+            r.render(lights)
+        out.append((r.read(READ_RAW), r.ray_counts()))
+    for raw, counts in out[1:]:
+        _compare(raw, out[0][0], "4-wide vs binary frame")     # same hits up to documented near-ties
+        assert np.abs(counts.astype(np.int64) - out[0][1].astype(np.int64)).max() <= 2
+
+
 def test_frame_full_resolution_and_taa_sequence():
     """The wavefront-frame configuration: 1920x1080, point light at (0.5, 0.5, 2.0) * scale, 8 frames
     with Halton(2,3) jitter and the TAA resolve on an FP32 RGBA history."""
