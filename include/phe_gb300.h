@@ -306,6 +306,14 @@ phe_status phe_renderer_result(const phe_renderer* renderer, phe_render_result* 
  * 3 = roughness: 4 bytes per pixel). Synchronises `stream`. The headless stand-in for reading the
  * GL result texture. */
 phe_status phe_renderer_read(const phe_renderer* renderer, int which, void* hostDst, void* stream);
+/* Asynchronous read-back for frame pipelines: snapshots the buffer into one of two device staging
+ * slots on `stream` (so the next frames may overwrite it) and copies the snapshot to `hostDst` on the
+ * renderer's copy stream, overlapping the frames queued after it. Returns at once. `hostDst` must be
+ * pinned for the copy to be asynchronous, and holds the image once phe_renderer_read_wait returns (or
+ * two read_async calls later, whose snapshot waits for this copy). */
+phe_status phe_renderer_read_async(phe_renderer* renderer, int which, void* hostDst, void* stream);
+/* Waits until every read_async copy issued so far has landed in host memory. */
+phe_status phe_renderer_read_wait(phe_renderer* renderer);
 /* Rays cast by the last frame: primary, primary shadow, bounce, bounce shadow. Synchronises `stream`. */
 phe_status phe_renderer_ray_counts(const phe_renderer* renderer, uint64_t counts[4], void* stream);
 

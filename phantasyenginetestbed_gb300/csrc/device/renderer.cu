@@ -47,6 +47,13 @@ struct phe_renderer {
 	bool pendingTimes = false;
 	FrameStreams streams;                  // side stream for the concurrent shadow pass
 	bool concurrent = true;
+	// Asynchronous read-back: two device staging slots copied to the host on copyStream.
+	cudaStream_t copyStream = nullptr;
+	void* staging[2] = {nullptr, nullptr};
+	size_t stagingBytes = 0;
+	cudaEvent_t snapEvents[2] = {}, doneEvents[2] = {};
+	bool readPending[2] = {false, false};
+	uint32_t readSlot = 0;
 };
 
 static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -262,6 +269,12 @@ extern "C" phe_status phe_renderer_destroy(phe_renderer* r)
 		if (r->events[i]) cudaEventDestroy(r->events[i]);
 	for (uint32_t i = 0; i < kParamSlots; i++)
 		if (r->paramEvents[i]) cudaEventDestroy(r->paramEvents[i]);
+	for (int i = 0; i < 2; i++) {
+		if (r->staging[i]) cudaFree(r->staging[i]);
+		if (r->snapEvents[i]) cudaEventDestroy(r->snapEvents[i]);
+		if (r->doneEvents[i]) cudaEventDestroy(r->doneEvents[i]);
+	}
+	if (r->copyStream) cudaStreamDestroy(r->copyStream);
 	if (r->streams.side) cudaStreamDestroy(r->streams.side);
 	if (r->streams.fork) cudaEventDestroy(r->streams.fork);
 	if (r->streams.join) cudaEventDestroy(r->streams.join);
@@ -469,21 +482,77 @@ extern "C" phe_status phe_renderer_ray_counts(const phe_renderer* r, uint64_t co
 	return PHE_OK;
 }
 
+static phe_status read_source(const phe_renderer* r, int which, const void** src, size_t* bytes)
+{
+	size_t P = (size_t)r->resX * r->resY;
+	*bytes = P * sizeof(float4);
+	switch (which) {
+	case 0: *src = r->fb.color; break;
+	case 1: *src = r->fb.history[r->parity]; break;
+	case 2: *src = r->fb.rawColor; break;
+	case 3: *src = r->fb.roughness; *bytes = P * sizeof(float); break;
+	default: return fail(PHE_ERR_INVALID_ARGUMENT, "renderer read: which must be 0..3");
+	}
+	return PHE_OK;
+}
+
 extern "C" phe_status phe_renderer_read(const phe_renderer* r, int which, void* hostDst, void* stream)
 {
 	if (!r || !hostDst || !r->allocation) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_read: no frame");
-	size_t P = (size_t)r->resX * r->resY;
 	const void* src = nullptr;
-	size_t bytes = P * sizeof(float4);
-	switch (which) {
-	case 0: src = r->fb.color; break;
-	case 1: src = r->fb.history[r->parity]; break;
-	case 2: src = r->fb.rawColor; break;
-	case 3: src = r->fb.roughness; bytes = P * sizeof(float); break;
-	default: return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_read: which must be 0..3");
-	}
+	size_t bytes = 0;
+	phe_status st = read_source(r, which, &src, &bytes);
+	if (st) return st;
 	PHE_CUDA_TRY(cudaMemcpyAsync(hostDst, src, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)stream), "read result");
 	PHE_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream), "read result");
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_renderer_read_async(phe_renderer* r, int which, void* hostDst, void* stream)
+{
+	if (!r || !hostDst || !r->allocation) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_read_async: no frame");
+	const void* src = nullptr;
+	size_t bytes = 0;
+	phe_status st = read_source(r, which, &src, &bytes);
+	if (st) return st;
+	cudaStream_t s = (cudaStream_t)stream;
+	if (!r->copyStream) {
+		PHE_CUDA_TRY(cudaStreamCreateWithFlags(&r->copyStream, cudaStreamNonBlocking), "create copy stream");
+		for (int i = 0; i < 2; i++) {
+			PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->snapEvents[i], cudaEventDisableTiming), "create read event");
+			PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->doneEvents[i], cudaEventDisableTiming), "create read event");
+		}
+	}
+	if (bytes > r->stagingBytes) {   // grow both slots once no copy uses them
+		if ((st = phe_renderer_read_wait(r))) return st;
+		for (int i = 0; i < 2; i++) {
+			if (r->staging[i]) cudaFree(r->staging[i]);
+			r->staging[i] = nullptr;
+		}
+		r->stagingBytes = 0;
+		for (int i = 0; i < 2; i++) PHE_CUDA_TRY(cudaMalloc(&r->staging[i], bytes), "allocate read-back staging");
+		r->stagingBytes = bytes;
+	}
+	const uint32_t k = r->readSlot;
+	r->readSlot ^= 1u;
+	if (r->readPending[k]) PHE_CUDA_TRY(cudaStreamWaitEvent(s, r->doneEvents[k], 0), "wait for staging slot");
+	PHE_CUDA_TRY(cudaMemcpyAsync(r->staging[k], src, bytes, cudaMemcpyDeviceToDevice, s), "snapshot result");
+	PHE_CUDA_TRY(cudaEventRecord(r->snapEvents[k], s), "record snapshot");
+	PHE_CUDA_TRY(cudaStreamWaitEvent(r->copyStream, r->snapEvents[k], 0), "order read-back");
+	PHE_CUDA_TRY(cudaMemcpyAsync(hostDst, r->staging[k], bytes, cudaMemcpyDeviceToHost, r->copyStream), "read result");
+	PHE_CUDA_TRY(cudaEventRecord(r->doneEvents[k], r->copyStream), "record read-back");
+	r->readPending[k] = true;
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_renderer_read_wait(phe_renderer* r)
+{
+	if (!r) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_read_wait: null renderer");
+	for (int i = 0; i < 2; i++)
+		if (r->readPending[i]) {
+			PHE_CUDA_TRY(cudaEventSynchronize(r->doneEvents[i]), "wait for read-back");
+			r->readPending[i] = false;
+		}
 	return PHE_OK;
 }
 

@@ -84,6 +84,17 @@ class CudaTracerRenderer:
         check(lib().phe_renderer_read(self.handle, which, ptr(out), _stream(stream)), "phe_renderer_read")
         return out
 
+    def read_async(self, out: np.ndarray, which: int = READ_COLOR, stream=None) -> None:
+        """Queue a read-back into `out` (pinned for overlap); the image is there after read_wait()."""
+        W, H = self.res
+        need = W * H * (4 if which == READ_ROUGHNESS else 16)
+        if out.nbytes < need or not out.flags.c_contiguous:
+            raise ValueError(f"read_async: need a contiguous buffer of {need} bytes")
+        check(lib().phe_renderer_read_async(self.handle, which, ptr(out), _stream(stream)), "phe_renderer_read_async")
+
+    def read_wait(self) -> None:
+        check(lib().phe_renderer_read_wait(self.handle), "phe_renderer_read_wait")
+
     def ray_counts(self, stream=None) -> np.ndarray:
         c = (C.c_uint64 * 4)()
         check(lib().phe_renderer_ray_counts(self.handle, c, _stream(stream)), "phe_renderer_ray_counts")
