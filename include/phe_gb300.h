@@ -74,9 +74,25 @@ typedef struct phe_sphere_light {
 	float pos[3]; float radius; float range; float strength[3]; int32_t staticShadows;
 } phe_sphere_light;
 
-/* Material values read at a hit (rendering/Material.hpp:17-55 without textures):
- * albedo rgb + alpha, roughness, metallic. */
-typedef struct phe_material { float albedo[4]; float roughness; float metallic; float pad[2]; } phe_material;
+/* Material (rendering/Material.hpp:17-55, byte-identical to the reference's Material: iData, fData1,
+ * fData2): texture indices of albedo, roughness and metallic (-1 = none; the fourth is unused),
+ * albedo rgba, roughness, metallic, two unused floats. A texture replaces its constant. */
+typedef struct phe_material {
+	int32_t texIndex[4];
+	float albedo[4];
+	float roughness;
+	float metallic;
+	float pad[2];
+} phe_material;
+
+/* A texture in the reference's RawImage form (rendering/RawImage.hpp:21-28): 8-bit channels, 1, 2 or
+ * 4 bytes per pixel, rows `pitch` bytes apart starting with row 0 (texel y = 0). Host memory. */
+typedef struct phe_texture {
+	const uint8_t* data;
+	int32_t width, height;   /* 1 .. 65536 */
+	uint32_t bytesPerPixel;  /* 1, 2 or 4 */
+	uint32_t pitch;          /* >= width * bytesPerPixel */
+} phe_texture;
 
 /* ---------------------------------------------------------------------------------------------
  * Library
@@ -167,6 +183,16 @@ typedef struct phe_scene phe_scene;
 phe_status phe_scene_create(const phe_bvh_node* nodes, uint32_t numNodes, const phe_triangle_vertices* verts,
                             const phe_triangle_data* datas, uint32_t numSlots, const phe_material* materials,
                             uint32_t numMaterials, int where, phe_scene** out);
+/* setMaterialsAndTextures (CudaTracerRenderer.cpp:192-239): replaces the scene's materials and
+ * textures (host arrays). Every materialIndex of the scene's triangle data must be < numMaterials, every
+ * texture index -1 or < numTextures, and albedo textures must have 4 bytes per pixel. Sampling follows
+ * the reference's texture objects (CudaBindlessTexture.cpp:66-72: normalized coordinates, wrap, nearest
+ * texel): texel i = floor(frac(u) * width) (i = width wraps to 0; NaN -> 0), j likewise with v and height;
+ * albedo rgb = powf(byte / 255, 2.2) (InterpretRayHitKernel.cu:41-47) from a table of the correctly
+ * rounded values, alpha = byte / 255; roughness and metallic = first byte / 255. Synchronous: waits for
+ * the device to finish work that may still read the old arrays. */
+phe_status phe_scene_set_materials_and_textures(phe_scene* scene, const phe_material* materials, uint32_t numMaterials,
+                                                const phe_texture* textures, uint32_t numTextures);
 phe_status phe_scene_destroy(phe_scene* scene);
 /* Device bytes held by the scene. */
 phe_status phe_scene_device_bytes(const phe_scene* scene, uint64_t* bytes);

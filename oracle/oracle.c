@@ -451,22 +451,58 @@ static v3 sample_ggx(float r1, float r2, float a, v3 reflection, v3 surfaceNorma
  * Wavefront frame
  * ------------------------------------------------------------------------------------------- */
 
-typedef struct { v3 pos, normal; const or_material* mat; } hit_info;
+/* Surface values at a hit: albedo rgb + alpha, roughness, metallic (constants or texels). */
+typedef struct { float albedo[4]; float roughness; float metallic; } or_surface;
+typedef struct { v3 pos, normal; or_surface surf; } hit_info;
 
-static hit_info interpret(const or_tri_data* datas, const or_material* mats, const or_ray* r, const or_hit* h)
+uint32_t oracle_texel_coord(float c, int32_t n)
 {
-	/* retrieveTriData (InterpretRayHitKernel.cu:13-37) */
+	float f = c - floorf(c);
+	if (!(f >= 0.0f)) return 0u;
+	uint32_t i = (uint32_t)(f * (float)n);
+	return i >= (uint32_t)n ? 0u : i;
+}
+
+void oracle_srgb_table(float out[256])
+{
+	for (int b = 0; b < 256; b++) out[b] = (float)pow((double)((float)b / 255.0f), (double)2.2f);
+}
+
+static const uint8_t* texel_at(const or_texture* t, float u, float v)
+{
+	uint32_t i = oracle_texel_coord(u, t->width), jj = oracle_texel_coord(v, t->height);
+	return t->data + (size_t)jj * t->pitch + (size_t)i * t->bytesPerPixel;
+}
+
+static hit_info interpret(const or_tri_data* datas, const or_frame_params* fp, const float* srgb, const or_ray* r,
+                          const or_hit* h)
+{
+	/* retrieveTriData + material lookup (InterpretRayHitKernel.cu:13-37, 60-121) */
 	hit_info hi;
 	const or_tri_data* d = &datas[h->tri];
 	hi.pos = add(ld3(r->o), muls(ld3(r->d), h->t));
 	v3 n0 = ld3(d->n0), n1 = ld3(d->n1), n2 = ld3(d->n2);
 	hi.normal = normalize3(add(add(n0, muls(sub(n1, n0), h->u)), muls(sub(n2, n0), h->v)));
-	hi.mat = &mats[d->materialIndex];
+	const or_material* m = &fp->materials[d->materialIndex];
+	for (int k = 0; k < 4; k++) hi.surf.albedo[k] = m->albedo[k];
+	hi.surf.roughness = m->roughness;
+	hi.surf.metallic = m->metallic;
+	if (m->texIndex[0] >= 0 || m->texIndex[1] >= 0 || m->texIndex[2] >= 0) {
+		float tu = (d->uv0[0] + (d->uv1[0] - d->uv0[0]) * h->u) + (d->uv2[0] - d->uv0[0]) * h->v;
+		float tv = (d->uv0[1] + (d->uv1[1] - d->uv0[1]) * h->u) + (d->uv2[1] - d->uv0[1]) * h->v;
+		if (m->texIndex[0] >= 0) {
+			const uint8_t* c = texel_at(&fp->textures[m->texIndex[0]], tu, tv);
+			for (int k = 0; k < 3; k++) hi.surf.albedo[k] = srgb[c[k]];
+			hi.surf.albedo[3] = (float)c[3] / 255.0f;
+		}
+		if (m->texIndex[1] >= 0) hi.surf.roughness = (float)*texel_at(&fp->textures[m->texIndex[1]], tu, tv) / 255.0f;
+		if (m->texIndex[2] >= 0) hi.surf.metallic = (float)*texel_at(&fp->textures[m->texIndex[2]], tu, tv) / 255.0f;
+	}
 	return hi;
 }
 
 /* shadeHit (MaterialKernel.cu:49-112) for one light: contribution and, when cast, the shadow ray. */
-static int shade_light(const or_light* light, v3 mask, v3 normal, v3 toCamera, v3 pos, const or_material* m,
+static int shade_light(const or_light* light, v3 mask, v3 normal, v3 toCamera, v3 pos, const or_surface* m,
                        or_pcg* rng, float contrib[3], or_ray* shadowRay)
 {
 	v3 lp = ld3(light->pos);
@@ -504,6 +540,7 @@ static int shade_light(const or_light* light, v3 mask, v3 normal, v3 toCamera, v
 typedef struct {
 	const or_node* nodes; const or_tri* tris; const or_tri_data* datas; const or_frame_params* fp;
 	const or_hit* primaryHits; float* color; float* roughnessOut;
+	float srgb[256];
 	atomic_uint next; atomic_ullong counts[4]; atomic_ullong work[8]; atomic_int overflows;
 } frame_job;
 
@@ -535,8 +572,8 @@ static void frame_pixel(frame_job* j, uint32_t x, uint32_t y)
 	else if (cast1(j, &pr, &ph, 0)) atomic_fetch_add(&j->overflows, 1);
 	if (ph.tri == ~0u) goto done;
 	{
-		hit_info hi = interpret(j->datas, fp->materials, &pr, &ph);
-		if (j->roughnessOut) j->roughnessOut[pid] = hi.mat->roughness;
+		hit_info hi = interpret(j->datas, fp, j->srgb, &pr, &ph);
+		if (j->roughnessOut) j->roughnessOut[pid] = hi.surf.roughness;
 		or_pcg rng;
 		oracle_pixel_stream(&rng, fp->seed, fp->frame, pid, 0);
 		v3 toCamera = normalize3(sub(ld3(fp->camPos), hi.pos));
@@ -545,7 +582,7 @@ static void frame_pixel(frame_job* j, uint32_t x, uint32_t y)
 			float c[3];
 			or_ray sr;
 			int inLight = 1;
-			if (shade_light(&fp->lights[li], mk(1.0f, 1.0f, 1.0f), hi.normal, toCamera, hi.pos, hi.mat, &rng, c, &sr)) {
+			if (shade_light(&fp->lights[li], mk(1.0f, 1.0f, 1.0f), hi.normal, toCamera, hi.pos, &hi.surf, &rng, c, &sr)) {
 				or_hit sh;
 				counts[1]++;
 				if (cast1(j, &sr, &sh, 1)) atomic_fetch_add(&j->overflows, 1);
@@ -562,7 +599,7 @@ static void frame_pixel(frame_job* j, uint32_t x, uint32_t y)
 		br.tmin = 0.001f;
 		br.tmax = FLT_MAX;
 		v3 bdir;
-		const or_material* m = hi.mat;
+		const or_surface* m = &hi.surf;
 		v3 alb = ld3(m->albedo);
 		v3 fromCamera = normalize3(sub(hi.pos, ld3(fp->camPos)));
 		if (m->albedo[3] > 0.5f) {
@@ -588,7 +625,7 @@ static void frame_pixel(frame_job* j, uint32_t x, uint32_t y)
 		or_hit bh;
 		if (cast1(j, &br, &bh, 2)) atomic_fetch_add(&j->overflows, 1);
 		if (bh.tri != ~0u) {
-			hit_info bi = interpret(j->datas, fp->materials, &br, &bh);
+			hit_info bi = interpret(j->datas, fp, j->srgb, &br, &bh);
 			or_pcg rng2;
 			oracle_pixel_stream(&rng2, fp->seed, fp->frame, pid, 1);
 			v3 toCam2 = mk(-br.d[0], -br.d[1], -br.d[2]);
@@ -596,7 +633,7 @@ static void frame_pixel(frame_job* j, uint32_t x, uint32_t y)
 				float c[3];
 				or_ray sr;
 				int inLight = 1;
-				if (shade_light(&fp->lights[li], throughput, bi.normal, toCam2, bi.pos, bi.mat, &rng2, c, &sr)) {
+				if (shade_light(&fp->lights[li], throughput, bi.normal, toCam2, bi.pos, &bi.surf, &rng2, c, &sr)) {
 					or_hit sh;
 					counts[3]++;
 					if (cast1(j, &sr, &sh, 3)) atomic_fetch_add(&j->overflows, 1);
@@ -631,6 +668,7 @@ int oracle_render_frame(const or_node* nodes, const or_tri* tris, const or_tri_d
 	memset(&j, 0, sizeof(j));
 	j.nodes = nodes; j.tris = tris; j.datas = datas; j.fp = fp; j.primaryHits = primaryHits;
 	j.color = color; j.roughnessOut = roughnessOut;
+	oracle_srgb_table(j.srgb);
 	atomic_init(&j.next, 0u);
 	for (int i = 0; i < 4; i++) atomic_init(&j.counts[i], 0ull);
 	for (int i = 0; i < 8; i++) atomic_init(&j.work[i], 0ull);

@@ -33,8 +33,11 @@ typedef struct { uint32_t tri; float t, u, v; } or_hit;
 typedef struct { float origin[3], dir[3], dX[3], dY[3]; } or_camera;
 /* SphereLight (level/SphereLight.hpp:13-26) as used by the shading code. */
 typedef struct { float pos[3]; float radius; float range; float strength[3]; int32_t staticShadows; } or_light;
-/* Material values used by shading: albedo rgb + alpha, roughness, metallic. */
-typedef struct { float albedo[4]; float roughness; float metallic; float pad[2]; } or_material;
+/* Material (rendering/Material.hpp:17-55): texture indices (albedo, roughness, metallic, unused;
+ * -1 = none), albedo rgba, roughness, metallic, two unused floats. */
+typedef struct { int32_t texIndex[4]; float albedo[4]; float roughness; float metallic; float pad[2]; } or_material;
+/* Texture (RawImage, rendering/RawImage.hpp:21-28): 8-bit channels, rows `pitch` bytes apart. */
+typedef struct { const uint8_t* data; int32_t width, height; uint32_t bytesPerPixel, pitch; } or_texture;
 
 /* Semantics of the accept rule.
  * OR_MODE_REFERENCE_CPU: castRay (BVHTraversal.hpp:37-128): accept t < closest && tMin <= t <= tMax.
@@ -112,12 +115,20 @@ typedef struct {
 	const or_light* lights; uint32_t numLights;
 	const or_material* materials;
 	uint64_t seed; uint32_t frame;
+	const or_texture* textures; uint32_t numTextures;
 } or_frame_params;
 /* `rayCounts` (optional, 4): rays cast per stage (primary, primary shadow, bounce, bounce shadow);
  * `workSums` (optional, 8): castDebugRay's nodesVisited and triangleIntersectionTests summed per stage. */
 int oracle_render_frame(const or_node* nodes, const or_tri* tris, const or_tri_data* datas,
                         const or_frame_params* fp, const or_hit* primaryHits, float* color, float* roughnessOut,
                         uint64_t* rayCounts, uint64_t* workSums, int threads);
+
+/* Nearest-texel index along one axis for a normalized coordinate with wrap addressing (the
+ * reference's texture objects, CudaBindlessTexture.cpp:66-72): floor(frac(c) * n), with n wrapping
+ * to 0 and a NaN or infinite coordinate giving 0. */
+uint32_t oracle_texel_coord(float c, int32_t n);
+/* powf(b / 255, 2.2) (InterpretRayHitKernel.cu:41-47), correctly rounded, for b = 0..255. */
+void oracle_srgb_table(float out[256]);
 
 /* TAA resolve (resources/shaders/taa.frag:25-71) on row-major float4 buffers. velocity and
  * prevVelocity are float2 uv-velocities (NULL = zero). History alpha holds the sample count. */

@@ -32,7 +32,33 @@ LIGHT_DTYPE = np.dtype([("pos", "<f4", (3,)), ("radius", "<f4"), ("range", "<f4"
 class FrameParams(C.Structure):
     _fields_ = [("resX", C.c_uint32), ("resY", C.c_uint32), ("cam", C.c_float * 12), ("jitter", C.c_float * 2),
                 ("camPos", C.c_float * 3), ("lights", C.c_void_p), ("numLights", C.c_uint32),
-                ("materials", C.c_void_p), ("seed", C.c_uint64), ("frame", C.c_uint32)]
+                ("materials", C.c_void_p), ("seed", C.c_uint64), ("frame", C.c_uint32),
+                ("textures", C.c_void_p), ("numTextures", C.c_uint32)]
+
+
+class Texture(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("width", C.c_int32), ("height", C.c_int32), ("bytesPerPixel", C.c_uint32),
+                ("pitch", C.c_uint32)]
+
+
+def textures_array(textures):
+    """ctypes array of or_texture over (H, W, C) uint8 images (the images must stay alive)."""
+    arr = (Texture * max(1, len(textures)))()
+    for k, img in enumerate(textures):
+        img3 = img.reshape(img.shape[0], img.shape[1], -1)
+        assert img3.dtype == np.uint8 and img3.flags.c_contiguous
+        arr[k] = Texture(img3.ctypes.data, img3.shape[1], img3.shape[0], img3.shape[2], img3.shape[1] * img3.shape[2])
+    return arr
+
+
+def texel_coord(c, n):
+    return int(lib().oracle_texel_coord(C.c_float(c), n))
+
+
+def srgb_table():
+    out = np.empty(256, np.float32)
+    lib().oracle_srgb_table(_p(out))
+    return out
 
 
 def build() -> None:
@@ -75,6 +101,10 @@ def lib():
         L.oracle_halton_jitter.restype = None
         L.oracle_sincos_2pi.argtypes = [C.c_float, V, V]
         L.oracle_sincos_2pi.restype = None
+        L.oracle_texel_coord.argtypes = [C.c_float, C.c_int32]
+        L.oracle_texel_coord.restype = C.c_uint32
+        L.oracle_srgb_table.argtypes = [V]
+        L.oracle_srgb_table.restype = None
         L.oracle_pixel_stream.argtypes = [V, C.c_uint64, C.c_uint32, C.c_uint32, C.c_uint32]
         L.oracle_pixel_stream.restype = None
         L.oracle_pcg_uniform.argtypes = [V]
@@ -174,9 +204,10 @@ def sincos_2pi(r):
 
 
 def render_frame(nodes, verts, slot_datas, materials, lights, cam12, res, jitter, cam_pos, seed, frame,
-                 primary_hits=None, nthreads=None, work=None):
+                 primary_hits=None, nthreads=None, work=None, textures=()):
     """Oracle frame: (color (H, W, 4), roughness (H, W), ray counts per stage). `work` (optional
-    uint64 array of 8) receives nodesVisited / triangle tests summed per stage."""
+    uint64 array of 8) receives nodesVisited / triangle tests summed per stage; `textures` are
+    (H, W, C) uint8 images indexed by the materials' texture indices."""
     fp = FrameParams()
     fp.resX, fp.resY = res
     fp.cam[:] = [float(x) for x in cam12]
@@ -188,6 +219,9 @@ def render_frame(nodes, verts, slot_datas, materials, lights, cam12, res, jitter
     fp.materials = materials.ctypes.data
     fp.seed = seed
     fp.frame = frame
+    tex = textures_array(textures)
+    fp.textures = C.addressof(tex)
+    fp.numTextures = len(textures)
     color = np.empty((res[1], res[0], 4), np.float32)
     rough = np.empty((res[1], res[0]), np.float32)
     counts = np.zeros(4, np.uint64)

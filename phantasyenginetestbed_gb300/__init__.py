@@ -154,6 +154,20 @@ class Scene:
             return cls(bvh.nodes, bvh.verts)
         return cls(bvh.nodes, bvh.verts, bvh.slot_datas(scene.datas), scene.materials)
 
+    def setMaterialsAndTextures(self, materials: np.ndarray, textures=()) -> None:
+        """setMaterialsAndTextures (CudaTracerRenderer.cpp:192-239): `materials` MATERIAL_DTYPE,
+        `textures` (H, W[, C]) uint8 images with C in {1, 2, 4} (RawImage rows, row 0 first)."""
+        materials = np.ascontiguousarray(materials)
+        assert materials.dtype == MATERIAL_DTYPE
+        imgs = [np.ascontiguousarray(t, np.uint8) for t in textures]
+        arr = (_n.Texture * max(1, len(imgs)))()
+        for k, img in enumerate(imgs):
+            img3 = img.reshape(img.shape[0], img.shape[1], -1)
+            arr[k] = _n.Texture(img3.ctypes.data, img3.shape[1], img3.shape[0], img3.shape[2],
+                                img3.shape[1] * img3.shape[2])
+        check(lib().phe_scene_set_materials_and_textures(self.handle, ptr(materials), len(materials), arr, len(imgs)),
+              "phe_scene_set_materials_and_textures")
+
     def set_layout(self, layout: int) -> None:
         """0 = binary nodes (default), 1 = 4-wide nodes (same results; see phe_scene_set_layout)."""
         check(lib().phe_scene_set_layout(self.handle, layout), "phe_scene_set_layout")

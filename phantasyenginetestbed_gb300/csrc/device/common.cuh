@@ -29,6 +29,15 @@ namespace phe_gb300 {
 //        of padding. Every child box is a box of the binary tree (a grandchild when the binary child
 //        is inner), and it is built only when each grandchild box lies inside its parent box, so the
 //        4-wide test of a grandchild passes only if the skipped binary test of its parent would pass.
+// Textures of a scene: texels of texture k start at texels + offset (rows rowBytes apart, tightly
+// packed); srgb[b] = powf(b / 255, 2.2) correctly rounded.
+struct DeviceTexture {
+	uint64_t offset;
+	int32_t width, height;
+	uint32_t bytesPerPixel, rowBytes;
+};
+static_assert(sizeof(DeviceTexture) == 24, "DeviceTexture is 24 bytes");
+
 struct DeviceScene {
 	const float4* nodes;
 	const float4* tris;
@@ -37,7 +46,12 @@ struct DeviceScene {
 	uint32_t numNodes, numSlots, numMaterials, maxDepth;
 	const float4* nodes4;
 	uint32_t numNodes4, maxDepth4;
+	const DeviceTexture* textures;
+	const uint8_t* texels;
+	const float* srgb;
+	uint32_t numTextures, pad;
 };
+static_assert(sizeof(DeviceScene) == 96, "DeviceScene is 96 bytes");
 
 constexpr int32_t kEmptyChild = 0x7FFFFFFE;
 

@@ -33,7 +33,7 @@ struct phe_renderer {
 	uint32_t parity = 0;
 	int useGraph = 0;
 	cudaGraphExec_t graphExec = nullptr;
-	const float4* graphNodes4 = nullptr;   // scene layout the graph was captured with
+	uint64_t graphGeneration = 0;          // scene generation the graph was captured with
 	cudaStream_t graphStream = nullptr;  // stream the graph was captured for (graphs relaunch on any stream)
 	bool cameraSet = false;
 	bool fused = true;                     // traversal and shading fused in one kernel per bounce
@@ -288,8 +288,8 @@ extern "C" phe_status phe_renderer_destroy(phe_renderer* r)
 extern "C" phe_status phe_renderer_set_static_scene(phe_renderer* r, const phe_scene* scene)
 {
 	if (!r || !scene) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_set_static_scene: null argument");
-	if (!scene->dev.datas || !scene->dev.materials)
-		return fail(PHE_ERR_INVALID_SCENE, "rendering needs a scene created with triangle data and materials");
+	if (!scene->dev.datas)
+		return fail(PHE_ERR_INVALID_SCENE, "rendering needs a scene created with triangle data");
 	r->scene = scene;
 	if (r->graphExec) cudaGraphExecDestroy(r->graphExec);
 	r->graphExec = nullptr;
@@ -381,6 +381,8 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 	if (!r->scene) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_render: no static scene");
 	if (!r->resX) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_render: no target resolution");
 	if (!r->cameraSet) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_render: no camera");
+	if (!r->scene->dev.materials)
+		return fail(PHE_ERR_INVALID_SCENE, "phe_renderer_render: the scene has no materials");
 	if (numLights > kMaxLights) return fail(PHE_ERR_TOO_LARGE, "at most %u lights", kMaxLights);
 	if (numLights && !lights) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_render: lights is null");
 	cudaStream_t s = (cudaStream_t)stream;
@@ -413,7 +415,7 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 	             "upload frame parameters");
 	PHE_CUDA_TRY(cudaEventRecord(r->paramEvents[slot], s), "record parameter slot");
 	if (r->useGraph) {
-		if (r->graphExec && r->graphNodes4 != r->scene->dev.nodes4) {   // layout switched since capture
+		if (r->graphExec && r->graphGeneration != r->scene->generation) {   // scene arrays or layout changed
 			cudaGraphExecDestroy(r->graphExec);
 			r->graphExec = nullptr;
 		}
@@ -436,7 +438,7 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 			e = cudaGraphInstantiate(&r->graphExec, g, 0);
 			cudaGraphDestroy(g);
 			if (e != cudaSuccess) return cuda_fail(e, "instantiate frame graph");
-			r->graphNodes4 = r->scene->dev.nodes4;
+			r->graphGeneration = r->scene->generation;
 		}
 		PHE_CUDA_TRY(cudaGraphLaunch(r->graphExec, s), "launch frame graph");
 	} else {

@@ -11,8 +11,11 @@
 struct phe_scene {
 	phe_gb300::DeviceScene dev;         // dev.nodes4 is set only while the 4-wide layout is selected
 	const float4* nodes4 = nullptr;     // 4-wide nodes, when the tree allows them (else null)
-	void* allocation = nullptr;   // one cudaMalloc holding nodes, tris, datas, materials
-	uint64_t bytes = 0;
+	void* allocation = nullptr;   // one cudaMalloc holding nodes, 4-wide nodes, tris, datas, status
+	void* shading = nullptr;      // one cudaMalloc holding materials, texture table, sRGB table, texels
+	uint64_t bytes = 0, shadingBytes = 0;
+	uint64_t generation = 0;      // bumped whenever `dev` changes (layout, materials): graphs re-capture
+	int64_t maxMaterialIndex = -1; // largest materialIndex of the triangle data (-1 without data)
 	uint32_t* status = nullptr;   // device word: OR of error bits raised by kernels on this scene
 	int device = 0;
 };

@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -143,6 +144,89 @@ bool collapse4(const std::vector<float4>& dn, std::vector<float4>& out, uint32_t
 	return true;
 }
 
+// Materials and textures (setMaterialsAndTextures, CudaTracerRenderer.cpp:192-239).
+phe_status check_materials(const phe_material* mats, uint32_t numMats, const phe_texture* tex, uint32_t numTex)
+{
+	for (uint32_t t = 0; t < numTex; t++) {
+		const phe_texture& x = tex[t];
+		if (!x.data) return fail(PHE_ERR_INVALID_ARGUMENT, "texture %u: null data", t);
+		if (x.width < 1 || x.height < 1 || x.width > 65536 || x.height > 65536)
+			return fail(PHE_ERR_INVALID_ARGUMENT, "texture %u: size %dx%d outside 1..65536", t, x.width, x.height);
+		if (x.bytesPerPixel != 1 && x.bytesPerPixel != 2 && x.bytesPerPixel != 4)
+			return fail(PHE_ERR_INVALID_ARGUMENT, "texture %u: %u bytes per pixel (1, 2 or 4)", t, x.bytesPerPixel);
+		if ((uint64_t)x.pitch < (uint64_t)x.width * x.bytesPerPixel)
+			return fail(PHE_ERR_INVALID_ARGUMENT, "texture %u: pitch %u < width x bytes per pixel", t, x.pitch);
+	}
+	for (uint32_t m = 0; m < numMats; m++)
+		for (int k = 0; k < 3; k++) {
+			int32_t ti = mats[m].texIndex[k];
+			if (ti < -1 || ti >= (int32_t)numTex)
+				return fail(PHE_ERR_INVALID_SCENE, "material %u: texture index %d with %u textures", m, ti, numTex);
+			if (k == 0 && ti >= 0 && tex[ti].bytesPerPixel != 4)
+				return fail(PHE_ERR_INVALID_SCENE, "material %u: albedo texture %d needs 4 bytes per pixel", m, ti);
+		}
+	return PHE_OK;
+}
+
+// One allocation: materials | texture table | sRGB table | texels (each texture 16-byte aligned, rows
+// packed). Replaces the scene's previous one once the device is idle.
+phe_status upload_shading(phe_scene* sc, const phe_material* mats, uint32_t numMats, const phe_texture* tex,
+                          uint32_t numTex)
+{
+	const size_t matBytes = align256((size_t)numMats * sizeof(phe_material));
+	const size_t tableBytes = align256((size_t)numTex * sizeof(DeviceTexture));
+	const size_t srgbBytes = align256(256 * sizeof(float));
+	std::vector<DeviceTexture> table(numTex);
+	uint64_t texelBytes = 0;
+	for (uint32_t t = 0; t < numTex; t++) {
+		DeviceTexture& d = table[t];
+		d.width = tex[t].width;
+		d.height = tex[t].height;
+		d.bytesPerPixel = tex[t].bytesPerPixel;
+		d.rowBytes = (uint32_t)tex[t].width * tex[t].bytesPerPixel;
+		d.offset = texelBytes;
+		texelBytes += ((uint64_t)d.rowBytes * (uint64_t)d.height + 15u) & ~uint64_t(15);
+	}
+	const size_t total = matBytes + tableBytes + srgbBytes + (size_t)texelBytes;
+	std::vector<uint8_t> host;
+	try {
+		host.assign(total, 0);
+	} catch (const std::bad_alloc&) {
+		return fail(PHE_ERR_OUT_OF_MEMORY, "materials and textures: host staging allocation failed");
+	}
+	if (numMats) std::memcpy(host.data(), mats, (size_t)numMats * sizeof(phe_material));
+	if (numTex) std::memcpy(host.data() + matBytes, table.data(), (size_t)numTex * sizeof(DeviceTexture));
+	float* srgb = reinterpret_cast<float*>(host.data() + matBytes + tableBytes);
+	for (int b = 0; b < 256; b++) srgb[b] = (float)std::pow((double)((float)b / 255.0f), (double)2.2f);
+	uint8_t* texels = host.data() + matBytes + tableBytes + srgbBytes;
+	for (uint32_t t = 0; t < numTex; t++)
+		for (int32_t y = 0; y < tex[t].height; y++)
+			std::memcpy(texels + table[t].offset + (uint64_t)y * table[t].rowBytes,
+			            tex[t].data + (uint64_t)y * tex[t].pitch, table[t].rowBytes);
+	char* base = nullptr;
+	PHE_CUDA_TRY(cudaMalloc(&base, total), "cudaMalloc(materials and textures)");
+	cudaError_t e = cudaMemcpy(base, host.data(), total, cudaMemcpyHostToDevice);
+	if (e != cudaSuccess) {
+		cudaFree(base);
+		return cuda_fail(e, "upload materials and textures");
+	}
+	if (sc->shading) {
+		// Frames or casts queued on any stream may still read the old arrays.
+		cudaDeviceSynchronize();
+		cudaFree(sc->shading);
+	}
+	sc->shading = base;
+	sc->shadingBytes = total;
+	sc->dev.materials = numMats ? reinterpret_cast<const phe_material*>(base) : nullptr;
+	sc->dev.numMaterials = numMats;
+	sc->dev.textures = numTex ? reinterpret_cast<const DeviceTexture*>(base + matBytes) : nullptr;
+	sc->dev.srgb = reinterpret_cast<const float*>(base + matBytes + tableBytes);
+	sc->dev.texels = reinterpret_cast<const uint8_t*>(base + matBytes + tableBytes + srgbBytes);
+	sc->dev.numTextures = numTex;
+	sc->generation++;
+	return PHE_OK;
+}
+
 } // namespace
 
 extern "C" phe_status phe_scene_create(const phe_bvh_node* nodes, uint32_t numNodes, const phe_triangle_vertices* verts,
@@ -183,11 +267,12 @@ extern "C" phe_status phe_scene_create(const phe_bvh_node* nodes, uint32_t numNo
 	uint32_t maxDepth = 0;
 	s = phe_bvh_validate(hn.data(), numNodes, numSlots, &maxDepth);
 	if (s) return s;
-	if (!hd.empty() && !hm.empty())
-		for (uint32_t i = 0; i < numSlots; i++)
-			if (hd[i].materialIndex >= numMaterials)
-				return fail(PHE_ERR_INVALID_SCENE, "slot %u: materialIndex %u >= %u materials", i, hd[i].materialIndex,
-				            numMaterials);
+	int64_t maxMaterialIndex = -1;
+	for (const phe_triangle_data& d : hd) maxMaterialIndex = std::max<int64_t>(maxMaterialIndex, d.materialIndex);
+	if (!hm.empty() && maxMaterialIndex >= (int64_t)numMaterials)
+		return fail(PHE_ERR_INVALID_SCENE, "materialIndex %lld >= %u materials", (long long)maxMaterialIndex,
+		            numMaterials);
+	if ((s = check_materials(hm.data(), (uint32_t)hm.size(), nullptr, 0))) return s;
 
 	// Traversal layout: child indices normalised (leaf = ~first), leaf end markers rewritten from
 	// the counts so that leaf loops always stop inside the slot array, triangles as (p0, e1, e2).
@@ -256,9 +341,8 @@ extern "C" phe_status phe_scene_create(const phe_bvh_node* nodes, uint32_t numNo
 	size_t node4Bytes = align256(dn4.size() * sizeof(float4));
 	size_t triBytes = align256(dt.size() * sizeof(float4));
 	size_t dataBytes = align256(hd.size() * sizeof(phe_triangle_data));
-	size_t matBytes = align256(hm.size() * sizeof(phe_material));
 	size_t statusBytes = 256;
-	size_t total = nodeBytes + node4Bytes + triBytes + dataBytes + matBytes + statusBytes;
+	size_t total = nodeBytes + node4Bytes + triBytes + dataBytes + statusBytes;
 	char* base = nullptr;
 	cudaError_t e = cudaMalloc(&base, total);
 	if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(scene)");
@@ -268,7 +352,6 @@ extern "C" phe_status phe_scene_create(const phe_bvh_node* nodes, uint32_t numNo
 	float4* dNodes4 = dn4.empty() ? nullptr : (float4*)p; p += node4Bytes;
 	float4* dTris = (float4*)p; p += triBytes;
 	phe_triangle_data* dDatas = hd.empty() ? nullptr : (phe_triangle_data*)p; p += dataBytes;
-	phe_material* dMats = hm.empty() ? nullptr : (phe_material*)p; p += matBytes;
 	uint32_t* dStatus = (uint32_t*)p;
 	if ((e = cudaMemcpy(dNodes, dn.data(), dn.size() * sizeof(float4), cudaMemcpyHostToDevice)) != cudaSuccess)
 		return cleanup(cuda_fail(e, "upload nodes"));
@@ -278,19 +361,22 @@ extern "C" phe_status phe_scene_create(const phe_bvh_node* nodes, uint32_t numNo
 		return cleanup(cuda_fail(e, "upload triangles"));
 	if (dDatas && (e = cudaMemcpy(dDatas, hd.data(), hd.size() * sizeof(phe_triangle_data), cudaMemcpyHostToDevice)) != cudaSuccess)
 		return cleanup(cuda_fail(e, "upload triangle data"));
-	if (dMats && (e = cudaMemcpy(dMats, hm.data(), hm.size() * sizeof(phe_material), cudaMemcpyHostToDevice)) != cudaSuccess)
-		return cleanup(cuda_fail(e, "upload materials"));
 	if ((e = cudaMemset(dStatus, 0, statusBytes)) != cudaSuccess) return cleanup(cuda_fail(e, "clear status"));
 
 	phe_scene* sc = new phe_scene();
 	sc->dev.nodes = dNodes;
 	sc->dev.tris = dTris;
 	sc->dev.datas = dDatas;
-	sc->dev.materials = dMats;
+	sc->dev.materials = nullptr;
 	sc->dev.numNodes = numNodes;
 	sc->dev.numSlots = numSlots;
-	sc->dev.numMaterials = (uint32_t)hm.size();
+	sc->dev.numMaterials = 0;
 	sc->dev.maxDepth = maxDepth;
+	sc->dev.textures = nullptr;
+	sc->dev.texels = nullptr;
+	sc->dev.srgb = nullptr;
+	sc->dev.numTextures = 0;
+	sc->maxMaterialIndex = maxMaterialIndex;
 	sc->dev.nodes4 = nullptr;   // binary layout unless phe_scene_set_layout selects the 4-wide one
 	sc->nodes4 = dNodes4;
 	sc->dev.numNodes4 = (uint32_t)(dn4.size() / 8);
@@ -299,13 +385,33 @@ extern "C" phe_status phe_scene_create(const phe_bvh_node* nodes, uint32_t numNo
 	sc->bytes = total;
 	sc->status = dStatus;
 	sc->device = dinfo->device;
+	if (!hm.empty() && (s = upload_shading(sc, hm.data(), (uint32_t)hm.size(), nullptr, 0))) {
+		phe_scene_destroy(sc);
+		return s;
+	}
 	*out = sc;
 	return PHE_OK;
+}
+
+extern "C" phe_status phe_scene_set_materials_and_textures(phe_scene* scene, const phe_material* materials,
+                                                           uint32_t numMaterials, const phe_texture* textures,
+                                                           uint32_t numTextures)
+{
+	if (!scene) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_scene_set_materials_and_textures: null scene");
+	if ((!materials && numMaterials) || (!textures && numTextures))
+		return fail(PHE_ERR_INVALID_ARGUMENT, "phe_scene_set_materials_and_textures: null array");
+	if (scene->maxMaterialIndex >= (int64_t)numMaterials)
+		return fail(PHE_ERR_INVALID_SCENE, "materialIndex %lld >= %u materials", (long long)scene->maxMaterialIndex,
+		            numMaterials);
+	phe_status s = check_materials(materials, numMaterials, textures, numTextures);
+	if (s) return s;
+	return upload_shading(scene, materials, numMaterials, textures, numTextures);
 }
 
 extern "C" phe_status phe_scene_destroy(phe_scene* scene)
 {
 	if (!scene) return PHE_OK;
+	if (scene->shading) cudaFree(scene->shading);
 	cudaError_t e = cudaFree(scene->allocation);
 	delete scene;
 	if (e != cudaSuccess) return cuda_fail(e, "cudaFree(scene)");
@@ -315,7 +421,7 @@ extern "C" phe_status phe_scene_destroy(phe_scene* scene)
 extern "C" phe_status phe_scene_device_bytes(const phe_scene* scene, uint64_t* bytes)
 {
 	if (!scene || !bytes) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_scene_device_bytes: null argument");
-	*bytes = scene->bytes;
+	*bytes = scene->bytes + scene->shadingBytes;
 	return PHE_OK;
 }
 
@@ -330,12 +436,14 @@ extern "C" phe_status phe_scene_set_layout(phe_scene* scene, int layout)
 {
 	if (!scene) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_scene_set_layout: null scene");
 	if (layout == PHE_LAYOUT_BINARY) {
+		if (scene->dev.nodes4) scene->generation++;
 		scene->dev.nodes4 = nullptr;
 		return PHE_OK;
 	}
 	if (layout != PHE_LAYOUT_WIDE4) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_scene_set_layout: unknown layout %d", layout);
 	if (!scene->nodes4)
 		return fail(PHE_ERR_INVALID_SCENE, "phe_scene_set_layout: this tree has child boxes outside their parent box");
+	if (scene->dev.nodes4 != scene->nodes4) scene->generation++;
 	scene->dev.nodes4 = scene->nodes4;
 	return PHE_OK;
 }

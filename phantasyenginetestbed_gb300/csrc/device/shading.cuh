@@ -76,22 +76,58 @@ struct HitInfo {
 	float alpha, roughness, metallic;
 };
 
-__device__ __forceinline__ HitInfo interpret_hit(const phe_triangle_data* __restrict__ datas,
-                                                 const phe_material* __restrict__ mats, f3 o, f3 d, uint32_t slot,
-                                                 float t, float u, float v)
+// Nearest texel index along one axis of a normalized, wrapping texture coordinate (the reference's
+// texture objects, CudaBindlessTexture.cpp:66-72): floor(frac(c) * n), n wrapping to 0, NaN to 0.
+__device__ __forceinline__ uint32_t texel_coord(float c, int32_t n)
 {
-	const phe_triangle_data& td = datas[slot];
+	float f = __fsub_rn(c, floorf(c));
+	if (!(f >= 0.0f)) return 0u;   // NaN or infinite coordinate
+	uint32_t i = (uint32_t)__fmul_rn(f, (float)n);
+	return i >= (uint32_t)n ? 0u : i;
+}
+
+// Address of texel (u, v) of texture `ti` (validated on upload: ti < numTextures).
+__device__ __forceinline__ const uint8_t* texel(const DeviceScene& s, int32_t ti, float u, float v)
+{
+	const DeviceTexture t = s.textures[ti];
+	uint32_t i = texel_coord(u, t.width), j = texel_coord(v, t.height);
+	return s.texels + t.offset + (uint64_t)j * t.rowBytes + (uint64_t)i * t.bytesPerPixel;
+}
+
+// retrieveTriData + the material part of interpretRayHitKernel (InterpretRayHitKernel.cu:13-37,
+// 60-121): position, interpolated normal and uv, material constants or texels.
+__device__ __forceinline__ HitInfo interpret_hit(const DeviceScene& s, f3 o, f3 d, uint32_t slot, float t, float u,
+                                                 float v)
+{
+	const phe_triangle_data& td = s.datas[slot];
 	HitInfo hi;
 	hi.pos = add3(o, muls3(d, t));
 	f3 n0 = mk3(td.n0[0], td.n0[1], td.n0[2]);
 	f3 n1 = mk3(td.n1[0], td.n1[1], td.n1[2]);
 	f3 n2 = mk3(td.n2[0], td.n2[1], td.n2[2]);
 	hi.normal = normalize3(add3(add3(n0, muls3(sub3(n1, n0), u)), muls3(sub3(n2, n0), v)));
-	const phe_material& m = mats[td.materialIndex];
-	hi.albedo = mk3(m.albedo[0], m.albedo[1], m.albedo[2]);
-	hi.alpha = m.albedo[3];
-	hi.roughness = m.roughness;
-	hi.metallic = m.metallic;
+	const uint32_t mi = td.materialIndex;
+	const int4 tix = __ldg(reinterpret_cast<const int4*>(s.materials + mi));
+	const float4 alb = __ldg(reinterpret_cast<const float4*>(s.materials + mi) + 1);
+	const float4 rm = __ldg(reinterpret_cast<const float4*>(s.materials + mi) + 2);
+	hi.albedo = mk3(alb.x, alb.y, alb.z);
+	hi.alpha = alb.w;
+	hi.roughness = rm.x;
+	hi.metallic = rm.y;
+	if ((tix.x & tix.y & tix.z) >= 0) {   // some texture index is set (indices are -1 or >= 0)
+		// uv = uv0 + (uv1 - uv0) * u + (uv2 - uv0) * v, left to right
+		float tu = __fadd_rn(__fadd_rn(td.uv0[0], __fmul_rn(__fsub_rn(td.uv1[0], td.uv0[0]), u)),
+		                     __fmul_rn(__fsub_rn(td.uv2[0], td.uv0[0]), v));
+		float tv = __fadd_rn(__fadd_rn(td.uv0[1], __fmul_rn(__fsub_rn(td.uv1[1], td.uv0[1]), u)),
+		                     __fmul_rn(__fsub_rn(td.uv2[1], td.uv0[1]), v));
+		if (tix.x >= 0) {
+			uchar4 c = __ldg(reinterpret_cast<const uchar4*>(texel(s, tix.x, tu, tv)));
+			hi.albedo = mk3(__ldg(s.srgb + c.x), __ldg(s.srgb + c.y), __ldg(s.srgb + c.z));
+			hi.alpha = __fdiv_rn((float)c.w, 255.0f);
+		}
+		if (tix.y >= 0) hi.roughness = __fdiv_rn((float)__ldg(texel(s, tix.y, tu, tv)), 255.0f);
+		if (tix.z >= 0) hi.metallic = __fdiv_rn((float)__ldg(texel(s, tix.z, tu, tv)), 255.0f);
+	}
 	return hi;
 }
 

@@ -125,7 +125,7 @@ __global__ void __launch_bounds__(kWaveBlock) primary_kernel(DeviceScene s, cons
 		f3 toCamera = mk3(0.0f, 0.0f, 0.0f);
 		f3 camPos = mk3(fp.camPos[0], fp.camPos[1], fp.camPos[2]);
 		if (hit) {
-			hi = interpret_hit(s.datas, s.materials, r.o, r.d, h.slot, h.t, h.u, h.v);
+			hi = interpret_hit(s, r.o, r.d, h.slot, h.t, h.u, h.v);
 			pixel_stream(rng, fp.seed, fp.frame, pid, 0);
 			toCamera = normalize3(sub3(camPos, hi.pos));
 		} else {
@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(kWaveBlock) bounce_kernel(DeviceScene s, const
 		DevPcg rng;
 		f3 toCamera = mk3(0.0f, 0.0f, 0.0f);
 		if (hit) {
-			hi = interpret_hit(s.datas, s.materials, r.o, r.d, h.slot, h.t, h.u, h.v);
+			hi = interpret_hit(s, r.o, r.d, h.slot, h.t, h.u, h.v);
 			pixel_stream(rng, fp.seed, fp.frame, pid, 1);
 			toCamera = mk3(-r.d.x, -r.d.y, -r.d.z);
 		} else {
@@ -404,7 +404,7 @@ __global__ void __launch_bounds__(kWaveBlock) primary_shade_kernel(DeviceScene s
 		if (hit) {
 			f3 o = mk3(fp.cam.origin[0], fp.cam.origin[1], fp.cam.origin[2]);
 			f3 d = primary_dir(fp.cam, x, y, W, fp.resY, fp.jitter[0], fp.jitter[1]);
-			hi = interpret_hit(s.datas, s.materials, o, d, slot, hv.y, hv.z, hv.w);
+			hi = interpret_hit(s, o, d, slot, hv.y, hv.z, hv.w);
 			pixel_stream(rng, fp.seed, fp.frame, pid, 0);
 			toCamera = normalize3(sub3(camPos, hi.pos));
 		} else {
@@ -461,7 +461,7 @@ __global__ void __launch_bounds__(kWaveBlock) bounce_shade_kernel(DeviceScene s,
 		DevPcg rng;
 		f3 toCamera = mk3(0.0f, 0.0f, 0.0f);
 		if (hit) {
-			hi = interpret_hit(s.datas, s.materials, o, d, slot, hv.y, hv.z, hv.w);
+			hi = interpret_hit(s, o, d, slot, hv.y, hv.z, hv.w);
 			pixel_stream(rng, fp.seed, fp.frame, pid, 1);
 			toCamera = mk3(-d.x, -d.y, -d.z);
 		} else {

@@ -100,6 +100,7 @@ struct Writer {
 		if (mats) {
 			phe_material& m = mats[index];
 			std::memset(&m, 0, sizeof(m));
+			for (int k = 0; k < 4; k++) m.texIndex[k] = -1;
 			for (int k = 0; k < 3; k++) m.albedo[k] = 0.2f + 0.6f * matRng->uniform();
 			m.albedo[3] = 1.0f;
 			m.roughness = 1.0f;

@@ -38,16 +38,23 @@ TRI_DATA_DTYPE = np.dtype([("n0", "<f4", (3,)), ("n1", "<f4", (3,)), ("n2", "<f4
                            ("materialIndex", "<u4")])                                 # 64 B
 RAY_IN_DTYPE = np.dtype([("origin", "<f4", (3,)), ("tMin", "<f4"), ("dir", "<f4", (3,)), ("tMax", "<f4")])  # 32 B
 RAY_HIT_DTYPE = np.dtype([("triangleIndex", "<u4"), ("t", "<f4"), ("u", "<f4"), ("v", "<f4")])  # 16 B
-MATERIAL_DTYPE = np.dtype([("albedo", "<f4", (4,)), ("roughness", "<f4"), ("metallic", "<f4"), ("pad", "<f4", (2,))])
+MATERIAL_DTYPE = np.dtype([("texIndex", "<i4", (4,)), ("albedo", "<f4", (4,)), ("roughness", "<f4"), ("metallic", "<f4"),
+                           ("pad", "<f4", (2,))])
 LIGHT_DTYPE = np.dtype([("pos", "<f4", (3,)), ("radius", "<f4"), ("range", "<f4"), ("strength", "<f4", (3,)),
                         ("staticShadows", "<i4")])
 assert NODE_DTYPE.itemsize == 64 and TRI_VERTS_DTYPE.itemsize == 48 and TRI_DATA_DTYPE.itemsize == 64
-assert RAY_IN_DTYPE.itemsize == 32 and RAY_HIT_DTYPE.itemsize == 16 and MATERIAL_DTYPE.itemsize == 32
+assert RAY_IN_DTYPE.itemsize == 32 and RAY_HIT_DTYPE.itemsize == 16 and MATERIAL_DTYPE.itemsize == 48
 assert LIGHT_DTYPE.itemsize == 36
 
 
 class CameraDef(C.Structure):
     _fields_ = [("origin", C.c_float * 3), ("dir", C.c_float * 3), ("dX", C.c_float * 3), ("dY", C.c_float * 3)]
+
+
+class Texture(C.Structure):
+    """phe_texture: a RawImage-like host image (8-bit channels)."""
+    _fields_ = [("data", C.c_void_p), ("width", C.c_int32), ("height", C.c_int32), ("bytesPerPixel", C.c_uint32),
+                ("pitch", C.c_uint32)]
 
 
 class SceneRecipe(C.Structure):
@@ -132,6 +139,7 @@ SIGNATURES: dict[str, tuple] = {
     "phe_generate_camera_def": (None, [_PF, _PF, _PF, _F, _F, _F, C.POINTER(CameraDef)]),
     "phe_halton_jitter": (None, [_U32, _PF]),
     "phe_scene_create": (_I32, [_VP, _U32, _VP, _VP, _U32, _VP, _U32, _I32, C.POINTER(_VP)]),
+    "phe_scene_set_materials_and_textures": (_I32, [_VP, _VP, _U32, C.POINTER(Texture), _U32]),
     "phe_scene_destroy": (_I32, [_VP]),
     "phe_scene_device_bytes": (_I32, [_VP, C.POINTER(C.c_uint64)]),
     "phe_cast_closest": (_I32, [_VP, _VP, _VP, _U32, _VP]),

@@ -52,7 +52,7 @@ def test_camera_and_jitter_match_reference_fixture():
     assert np.array_equal(cam, g["cam"])
     pc = P.camera_def(C1_CAM["pos"], C1_CAM["dir"], C1_CAM["up"], 60.0, C1_CAM["res"])
     assert np.array_equal(P.camera_def_array(pc), g["cam"])
-    table = np.load("tests/golden/ref_halton.npy") if False else load_halton()
+    table = load_halton()
     for i in range(16):
         assert np.array_equal(O.halton_jitter(i), table[i] - np.float32(0.5))
         assert P.halton_jitter(i) == tuple(float(x) for x in table[i] - np.float32(0.5))
@@ -144,3 +144,56 @@ def test_sincos_accuracy_and_pcg_reference_stream():
     L.oracle_pcg_seed(C.addressof(st), 42, 54)
     got = [L.oracle_pcg_next(C.addressof(st)) for _ in range(6)]
     assert got == [0xa15c02b7, 0x7b47f409, 0xba1d3330, 0x83d2f293, 0xbfa4784b, 0xcbed606e]
+
+
+def test_texel_sampling_rule_and_srgb_table():
+    """Nearest-texel rule of the reference's texture objects (normalized coordinates, wrap):
+    floor(frac(c) * n) with n wrapping to 0; the sRGB table is powf(b / 255, 2.2) correctly rounded."""
+    n = 4
+    cases = {0.0: 0, 0.2499: 0, 0.25: 1, 0.999: 3, 1.0: 0, 1.3: 1, -0.25: 3, -1.0: 0, 7.75: 3,
+             float("nan"): 0, float("inf"): 0, float("-inf"): 0}
+    for c, want in cases.items():
+        assert O.texel_coord(c, n) == want, c
+    # frac of a tiny negative coordinate rounds to 1.0f: that texel wraps to 0
+    assert O.texel_coord(-1e-9, 37) == 0
+    for c in np.random.default_rng(5).uniform(-3, 3, 2000).astype(np.float32):
+        f = np.float32(c) - np.floor(np.float32(c))
+        want = int(np.float32(f) * np.float32(37))
+        assert O.texel_coord(float(c), 37) == (0 if want >= 37 else want)
+    t = O.srgb_table()
+    assert t[0] == 0.0 and t[255] == 1.0 and np.all(np.diff(t) > 0)
+    exact = (np.arange(256, dtype=np.float32) / np.float32(255)).astype(np.float64) ** np.float64(np.float32(2.2))
+    assert np.array_equal(t, exact.astype(np.float32))
+
+
+def test_oracle_constant_textures_equal_material_constants():
+    """A texture whose every texel encodes a material's constants renders the frame of the constants:
+    albedo rgb = sRGB table entry, alpha 255 -> 1, roughness 255 -> 1, metallic 0 -> 0."""
+    s = P.generate_scene(24, 20, True, 7)
+    b = P.build_sbvh(s.tri_verts)
+    datas = s.datas.copy()
+    for name in ("uv0", "uv1", "uv2"):
+        datas[name] = np.random.default_rng(1).uniform(-2, 2, (len(datas), 2))
+    slot_datas = b.slot_datas(datas)
+    srgb = O.srgb_table()
+    mats = s.materials.copy()
+    mats["albedo"][:, :3] = srgb[77]
+    mats["texIndex"][:] = -1
+    tex = [np.full((5, 7, 4), 77, np.uint8), np.full((3, 3), 255, np.uint8), np.zeros((2, 2, 2), np.uint8)]
+    tex[0][..., 3] = 255
+    textured = mats.copy()
+    textured["texIndex"][:] = [0, 1, 2, -1]
+    textured["albedo"][:] = 0.5
+    textured["roughness"] = 0.25
+    textured["metallic"] = 0.75
+    k = s.scale
+    res = (64, 48)
+    cam_pos = (0.5 * k, -0.3 * k, 0.6 * k)
+    cam = O.camera_def(cam_pos, C1_CAM["dir"], C1_CAM["up"], math.radians(60), res)
+    from phantasyenginetestbed_gb300.renderer import make_lights
+    lights = make_lights(np.array([(0.5, 0.5, 2.0)], np.float32) * np.float32(k), range_=1000.0 * k)
+    a = O.render_frame(b.nodes, b.verts, slot_datas, mats, lights, cam, res, (0.0, 0.0), cam_pos, 3, 0)
+    t = O.render_frame(b.nodes, b.verts, slot_datas, textured, lights, cam, res, (0.0, 0.0), cam_pos, 3, 0,
+                       textures=tex)
+    assert np.array_equal(a[0], t[0]) and np.array_equal(a[1], t[1]) and np.array_equal(a[2], t[2])
+    assert a[0][..., :3].max() > 0.01
