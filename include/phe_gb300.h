@@ -281,7 +281,7 @@ phe_status phe_batch_destroy(phe_batch* batch);
 /* The batched launch without any device allocation (no counterpart in the reference). For callers
  * that manage all device memory themselves and cannot let a library call cudaMalloc (an engine's
  * renderer or a plugin host with its own allocator and memory budget; cudaMalloc may also wait for
- * the whole device). The descriptor table, scene table and work counter live in a fixed 9,984-byte
+ * the whole device). The descriptor table, scene table and work counter live in a fixed 11,520-byte
  * array inside the library (per GPU, until exit) instead of device memory the call allocates.
  * At most 256 batch items and 32 scenes per call (PHE_ERR_TOO_LARGE beyond). All calls share the
  * array: calls whose GPU work overlaps race, so serialise them on one stream. The first call on a

@@ -433,7 +433,7 @@ done:
 // output buffers as usual.
 //
 // Limits and sharing rules:
-//   * at most kNoAllocMaxItems batches and kNoAllocMaxScenes scenes per call (9,984 bytes of scratch,
+//   * at most kNoAllocMaxItems batches and kNoAllocMaxScenes scenes per call (11,520 bytes of scratch,
 //     held by every GPU that loads the library until the process exits); larger calls fail with
 //     PHE_ERR_TOO_LARGE;
 //   * every call uses the same array and leaves its table there; the counter and status word are
@@ -448,9 +448,10 @@ namespace phe_gb300 {
 constexpr uint32_t kNoAllocMaxItems = 256;
 constexpr uint32_t kNoAllocMaxScenes = 32;
 constexpr size_t kNoAllocItemsBytes = kNoAllocMaxItems * sizeof(BatchItemDev);          // 8192
-constexpr size_t kNoAllocScenesBytes = kNoAllocMaxScenes * sizeof(DeviceScene);         // 1536
+constexpr size_t kNoAllocScenesBytes = kNoAllocMaxScenes * sizeof(DeviceScene);         // 3072
 constexpr size_t kNoAllocScratchBytes = kNoAllocItemsBytes + kNoAllocScenesBytes + 256; // + counter, status
 static_assert(sizeof(DeviceScene) % 16 == 0, "scene table entries stay 16-byte aligned");
+static_assert(kNoAllocScratchBytes == 11520, "the documented scratch size");
 
 static __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocScratchBytes];
 
