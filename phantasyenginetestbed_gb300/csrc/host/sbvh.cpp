@@ -15,6 +15,7 @@
 // slot vertices copy the input triangle with .w = 0 except -1 on each leaf's last slot.
 
 #include <algorithm>
+#include <array>
 #include <atomic>
 #include <cmath>
 #include <cstring>
@@ -32,6 +33,13 @@ constexpr int kSpatialBins = 32;
 constexpr int kObjectBins = 128;
 constexpr size_t kExactSweepMax = 1024;
 constexpr size_t kParallelMin = 16384;
+// Nodes with at least kChunkedMin references bin and partition them in contiguous chunks of at
+// least kChunkMin on threads from the free pool (the top levels of the tree, where too few subtrees
+// exist to keep the threads busy). Binning merges boxes by min/max and counts by addition, and
+// partitions concatenate the chunks in order, so the tree is the same for any thread count.
+constexpr size_t kChunkedMin = 1u << 18;
+constexpr size_t kChunkMin = 1u << 16;
+constexpr int kMaxChunks = 64;
 
 struct AABB {
 	float lo[3] = {INFINITY, INFINITY, INFINITY};
@@ -75,6 +83,41 @@ struct Builder {
 	phe_sbvh_params params;
 	float minOverlap = 0.0f;
 	std::atomic<int> freeThreads{0};
+
+	// Splits [0, n) into contiguous chunks, one per thread taken from the free pool plus the calling
+	// thread, and runs fn(chunk, begin, end) on each. Returns the number of chunks (>= 1).
+	static size_t maxChunks(size_t n) { return n >= kChunkedMin ? std::min<size_t>(kMaxChunks, n / kChunkMin) : 1; }
+
+	template <class F>
+	int chunked(size_t n, F&& fn)
+	{
+		int want = (int)maxChunks(n);
+		int extra = 0;
+		while (extra + 1 < want) {
+			int f = freeThreads.load();
+			if (f <= 0) break;
+			if (freeThreads.compare_exchange_weak(f, f - 1)) extra++;
+		}
+		const int chunks = extra + 1;
+		auto range = [&](int c, size_t& b, size_t& e) {
+			b = n * (size_t)c / (size_t)chunks;
+			e = n * (size_t)(c + 1) / (size_t)chunks;
+		};
+		std::vector<std::thread> pool;
+		pool.reserve((size_t)extra);
+		for (int c = 1; c < chunks; c++)
+			pool.emplace_back([&, c]() {
+				size_t b, e;
+				range(c, b, e);
+				fn(c, b, e);
+			});
+		size_t b0, e0;
+		range(0, b0, e0);
+		fn(0, b0, e0);
+		for (std::thread& t : pool) t.join();
+		freeThreads.fetch_add(extra);
+		return chunks;
+	}
 
 	void clipTriangle(const Ref& ref, int dim, float pos, AABB& left, AABB& right) const
 	{
@@ -142,22 +185,53 @@ struct Builder {
 		return best;
 	}
 
-	ObjectSplit binnedObjectSplit(const std::vector<Ref>& refs, float nodeSAH) const
+	ObjectSplit binnedObjectSplit(const std::vector<Ref>& refs, float nodeSAH)
 	{
 		ObjectSplit best;
 		size_t n = refs.size();
+		// Centroid ranges of the three axes, then the bins of the three axes, each in one chunked pass.
+		struct Range { float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY}; };
+		std::vector<Range> ranges(maxChunks(n));
+		int chunks = chunked(n, [&](int c, size_t b, size_t e) {
+			Range& rg = ranges[(size_t)c];
+			for (size_t i = b; i < e; i++)
+				for (int a = 0; a < 3; a++) {
+					float v = refs[i].centroid2(a);
+					rg.lo[a] = std::min(rg.lo[a], v);
+					rg.hi[a] = std::max(rg.hi[a], v);
+				}
+		});
+		float cmins[3], scales[3];
+		bool active[3];
+		for (int a = 0; a < 3; a++) {
+			float lo = INFINITY, hi = -INFINITY;
+			for (int c = 0; c < chunks; c++) { lo = std::min(lo, ranges[(size_t)c].lo[a]); hi = std::max(hi, ranges[(size_t)c].hi[a]); }
+			active[a] = hi > lo;
+			cmins[a] = lo;
+			scales[a] = active[a] ? (float)kObjectBins / (hi - lo) : 0.0f;
+		}
+		struct Bins { AABB box[3][kObjectBins]; size_t cnt[3][kObjectBins] = {}; };
+		std::vector<Bins> partial(maxChunks(n));
+		chunks = chunked(n, [&](int c, size_t b, size_t e) {
+			Bins& pb = partial[(size_t)c];
+			for (size_t i = b; i < e; i++)
+				for (int a = 0; a < 3; a++) {
+					if (!active[a]) continue;
+					int k = std::min(kObjectBins - 1, (int)((refs[i].centroid2(a) - cmins[a]) * scales[a]));
+					pb.box[a][k].grow(refs[i].box);
+					pb.cnt[a][k]++;
+				}
+		});
 		for (int axis = 0; axis < 3; axis++) {
-			float cmin = INFINITY, cmax = -INFINITY;
-			for (const Ref& r : refs) { float c = r.centroid2(axis); cmin = std::min(cmin, c); cmax = std::max(cmax, c); }
-			if (!(cmax > cmin)) continue;
-			float scale = (float)kObjectBins / (cmax - cmin);
+			if (!active[axis]) continue;
+			const float cmin = cmins[axis], scale = scales[axis];
 			AABB bins[kObjectBins];
 			size_t cnt[kObjectBins] = {};
-			for (const Ref& r : refs) {
-				int b = std::min(kObjectBins - 1, (int)((r.centroid2(axis) - cmin) * scale));
-				bins[b].grow(r.box);
-				cnt[b]++;
-			}
+			for (int c = 0; c < chunks; c++)
+				for (int k = 0; k < kObjectBins; k++) {
+					bins[k].grow(partial[(size_t)c].box[axis][k]);
+					cnt[k] += partial[(size_t)c].cnt[axis][k];
+				}
 			AABB rboxes[kObjectBins];
 			size_t rcnt[kObjectBins];
 			AABB rb;
@@ -181,8 +255,22 @@ struct Builder {
 		return best;
 	}
 
+	// Concatenates per-chunk vectors in chunk order.
+	static void concat(std::vector<std::vector<Ref>>& parts, int chunks, std::vector<Ref>& out)
+	{
+		if (chunks == 1) {
+			out.swap(parts[0]);
+			return;
+		}
+		size_t total = 0;
+		for (int c = 0; c < chunks; c++) total += parts[(size_t)c].size();
+		out.clear();
+		out.reserve(total);
+		for (int c = 0; c < chunks; c++) out.insert(out.end(), parts[(size_t)c].begin(), parts[(size_t)c].end());
+	}
+
 	void performObjectSplit(std::vector<Ref>& refs, const ObjectSplit& s, std::vector<Ref>& left,
-	                        std::vector<Ref>& right) const
+	                        std::vector<Ref>& right)
 	{
 		left.clear();
 		right.clear();
@@ -192,16 +280,22 @@ struct Builder {
 			left.assign(refs.begin(), refs.begin() + (ptrdiff_t)s.numLeft);
 			right.assign(refs.begin() + (ptrdiff_t)s.numLeft, refs.end());
 		} else {
-			for (const Ref& r : refs) {
-				int b = std::min(kObjectBins - 1, (int)((r.centroid2(s.axis) - s.cmin) * s.cscale));
-				(b < s.binSplit ? left : right).push_back(r);
-			}
+			const size_t mc = maxChunks(refs.size());
+			std::vector<std::vector<Ref>> lp(mc), rp(mc);
+			int chunks = chunked(refs.size(), [&](int c, size_t b, size_t e) {
+				for (size_t i = b; i < e; i++) {
+					int k = std::min(kObjectBins - 1, (int)((refs[i].centroid2(s.axis) - s.cmin) * s.cscale));
+					(k < s.binSplit ? lp : rp)[(size_t)c].push_back(refs[i]);
+				}
+			});
+			concat(lp, chunks, left);
+			concat(rp, chunks, right);
 		}
 	}
 
 	struct SpatialSplit { float sah = INFINITY; int dim = -1; float pos = 0.0f; };
 
-	SpatialSplit findSpatialSplit(const std::vector<Ref>& refs, const AABB& box, float nodeSAH) const
+	SpatialSplit findSpatialSplit(const std::vector<Ref>& refs, const AABB& box, float nodeSAH)
 	{
 		SpatialSplit best;
 		float origin[3], binSize[3], inv[3];
@@ -213,23 +307,34 @@ struct Builder {
 		struct Bin { AABB box; uint32_t enter = 0, exit = 0; };
 		for (int dim = 0; dim < 3; dim++) {
 			if (!(binSize[dim] > 0.0f) || !std::isfinite(inv[dim])) continue;
-			Bin bins[kSpatialBins];
-			for (const Ref& r : refs) {
-				int first = (int)((r.box.lo[dim] - origin[dim]) * inv[dim]);
-				first = std::min(kSpatialBins - 1, std::max(0, first));
-				int last = (int)((r.box.hi[dim] - origin[dim]) * inv[dim]);
-				last = std::min(kSpatialBins - 1, std::max(first, last));
-				Ref cur = r;
-				for (int i = first; i < last; i++) {
-					AABB l, rr;
-					clipTriangle(cur, dim, origin[dim] + binSize[dim] * (float)(i + 1), l, rr);
-					bins[i].box.grow(l);
-					cur.box = rr;
+			std::vector<std::array<Bin, kSpatialBins>> partial(maxChunks(refs.size()));
+			int chunks = chunked(refs.size(), [&](int c, size_t b, size_t e) {
+				Bin* pb = partial[(size_t)c].data();
+				for (size_t j = b; j < e; j++) {
+					const Ref& r = refs[j];
+					int first = (int)((r.box.lo[dim] - origin[dim]) * inv[dim]);
+					first = std::min(kSpatialBins - 1, std::max(0, first));
+					int last = (int)((r.box.hi[dim] - origin[dim]) * inv[dim]);
+					last = std::min(kSpatialBins - 1, std::max(first, last));
+					Ref cur = r;
+					for (int i = first; i < last; i++) {
+						AABB l, rr;
+						clipTriangle(cur, dim, origin[dim] + binSize[dim] * (float)(i + 1), l, rr);
+						pb[i].box.grow(l);
+						cur.box = rr;
+					}
+					pb[last].box.grow(cur.box);
+					pb[first].enter++;
+					pb[last].exit++;
 				}
-				bins[last].box.grow(cur.box);
-				bins[first].enter++;
-				bins[last].exit++;
-			}
+			});
+			Bin bins[kSpatialBins];
+			for (int c = 0; c < chunks; c++)
+				for (int i = 0; i < kSpatialBins; i++) {
+					bins[i].box.grow(partial[(size_t)c][(size_t)i].box);
+					bins[i].enter += partial[(size_t)c][(size_t)i].enter;
+					bins[i].exit += partial[(size_t)c][(size_t)i].exit;
+				}
 			AABB rboxes[kSpatialBins];
 			AABB rb;
 			for (int i = kSpatialBins - 1; i > 0; i--) { rb.grow(bins[i].box); rboxes[i - 1] = rb; }
@@ -247,18 +352,30 @@ struct Builder {
 	}
 
 	void performSpatialSplit(const std::vector<Ref>& refs, const SpatialSplit& s, std::vector<Ref>& left,
-	                         std::vector<Ref>& right, AABB& lbox, AABB& rbox) const
+	                         std::vector<Ref>& right, AABB& lbox, AABB& rbox)
 	{
-		left.clear();
-		right.clear();
 		lbox = AABB();
 		rbox = AABB();
+		// References entirely on one side keep their order; the straddling ones are decided after, in order.
+		const size_t mc = maxChunks(refs.size());
+		std::vector<std::vector<Ref>> lp(mc), rp(mc), sp(mc);
+		std::vector<AABB> lb(mc), rb(mc);
+		int chunks = chunked(refs.size(), [&](int c, size_t b, size_t e) {
+			for (size_t i = b; i < e; i++) {
+				const Ref& r = refs[i];
+				if (r.box.hi[s.dim] <= s.pos) { lp[(size_t)c].push_back(r); lb[(size_t)c].grow(r.box); }
+				else if (r.box.lo[s.dim] >= s.pos) { rp[(size_t)c].push_back(r); rb[(size_t)c].grow(r.box); }
+				else sp[(size_t)c].push_back(r);
+			}
+		});
+		concat(lp, chunks, left);
+		concat(rp, chunks, right);
+		std::vector<Ref> straddleRefs;
+		concat(sp, chunks, straddleRefs);
+		for (int c = 0; c < chunks; c++) { lbox.grow(lb[(size_t)c]); rbox.grow(rb[(size_t)c]); }
 		std::vector<const Ref*> straddle;
-		for (const Ref& r : refs) {
-			if (r.box.hi[s.dim] <= s.pos) { left.push_back(r); lbox.grow(r.box); }
-			else if (r.box.lo[s.dim] >= s.pos) { right.push_back(r); rbox.grow(r.box); }
-			else straddle.push_back(&r);
-		}
+		straddle.reserve(straddleRefs.size());
+		for (const Ref& r : straddleRefs) straddle.push_back(&r);
 		// Reference unsplitting: keep a straddling reference whole on one side when that is cheaper
 		// than duplicating it.
 		for (const Ref* rp : straddle) {
