@@ -375,6 +375,13 @@ phe_status phe_renderer_ray_totals_async(const phe_renderer* renderer, uint64_t*
  * pixel, rounded from [0, 1]); either output may be NULL. */
 phe_status phe_postprocess(uint32_t resX, uint32_t resY, const float* linear, float gamma, float* display, uint8_t* rgba8,
                            void* stream);
+/* Display scaling pass (resources/shaders/scaling.frag:19-35, drawn by GameScreen.cpp:268-273): resamples
+ * the rendered region (the first viewportW x viewportH texels of a srcW x srcH float4 image) to dstW x dstH.
+ * Each destination pixel averages four GL_LINEAR, clamp-to-edge taps at +-1/4 destination pixel around
+ * its centre (uv = (x + 0.5) / dstW, (y + 0.5) / dstH; coord = uv * viewport / src); alpha = 1. Writes
+ * float4 `dst` and/or 8-bit RGBA `dstRgba8` (either may be NULL). Asynchronous on `stream`. */
+phe_status phe_scale(uint32_t srcW, uint32_t srcH, const float* src, uint32_t viewportW, uint32_t viewportH,
+                     uint32_t dstW, uint32_t dstH, float* dst, uint8_t* dstRgba8, void* stream);
 
 /* TAA resolve alone (taa.frag:25-71) on device float4 buffers; velocity and prevVelocity are float2
  * uv velocities (NULL = static), roughness float (NULL = 0). */

@@ -783,6 +783,29 @@ static float u2_tonemap(float x)
 	return (x * (A * x + C * B) + D * E) / (x * (A * x + B) + D * F) - E / F;
 }
 
+void oracle_scale(uint32_t srcW, uint32_t srcH, const float* src, uint32_t vpW, uint32_t vpH, uint32_t dstW,
+                  uint32_t dstH, float* dst)
+{
+	/* scaling.frag:19-35 */
+	const float dw = (float)dstW, dh = (float)dstH, sw = (float)srcW, sh = (float)srcH;
+	const float ox = (1.0f / dw) * 0.25f, oy = (1.0f / dh) * 0.25f;
+	const float sx[4] = {-ox, ox, -ox, ox}, sy[4] = {-oy, -oy, oy, oy};
+	for (uint32_t y = 0; y < dstH; y++)
+		for (uint32_t x = 0; x < dstW; x++) {
+			float u = ((float)x + 0.5f) / dw, v = ((float)y + 0.5f) / dh;
+			float cx = (u * (float)vpW) / sw, cy = (v * (float)vpH) / sh;
+			float acc[3] = {0.0f, 0.0f, 0.0f};
+			for (int k = 0; k < 4; k++) {
+				float t[4];
+				bilinear(src, srcW, srcH, 4, (cx + sx[k]) * sw, (cy + sy[k]) * sh, t);
+				for (int c = 0; c < 3; c++) acc[c] = k == 0 ? t[c] : acc[c] + t[c];
+			}
+			float* o = &dst[4 * ((size_t)y * dstW + x)];
+			for (int c = 0; c < 3; c++) o[c] = acc[c] / 4.0f;
+			o[3] = 1.0f;
+		}
+}
+
 void oracle_postprocess(uint32_t n, const float* linear, float gamma, float* display)
 {
 	const float W = 11.2f, BLACK_CRUSH = 0.0015f, exposureBias = 2.0f;

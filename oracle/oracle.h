@@ -137,6 +137,10 @@ void oracle_taa(uint32_t resX, uint32_t resY, const float* cur, const float* his
 
 /* Display post-process (gamma_correction.frag:20-74): Uncharted 2 tonemap then pow(rgb, 1/gamma), on
  * n float4 pixels; alpha passes through. */
+/* Display scaling pass (scaling.frag:19-35): the viewport part of a float4 source resampled to the
+ * destination by averaging four GL_LINEAR clamp-to-edge taps at +-1/4 destination pixel. */
+void oracle_scale(uint32_t srcW, uint32_t srcH, const float* src, uint32_t vpW, uint32_t vpH, uint32_t dstW,
+                  uint32_t dstH, float* dst);
 void oracle_postprocess(uint32_t n, const float* linear, float gamma, float* display);
 
 /* Halton(2,3) jitter table entry i - 0.5 (GameScreen.cpp:21-39). */

@@ -51,6 +51,16 @@ def textures_array(textures):
     return arr
 
 
+def scale(src, dst_res, viewport=None):
+    """scaling.frag restated: (H, W, 4) float32 source -> (dstH, dstW, 4)."""
+    src = np.ascontiguousarray(src, np.float32)
+    H, W = src.shape[:2]
+    vw, vh = viewport or (W, H)
+    out = np.empty((dst_res[1], dst_res[0], 4), np.float32)
+    lib().oracle_scale(W, H, _p(src), vw, vh, dst_res[0], dst_res[1], _p(out))
+    return out
+
+
 def texel_coord(c, n):
     return int(lib().oracle_texel_coord(C.c_float(c), n))
 
@@ -101,6 +111,8 @@ def lib():
         L.oracle_halton_jitter.restype = None
         L.oracle_sincos_2pi.argtypes = [C.c_float, V, V]
         L.oracle_sincos_2pi.restype = None
+        L.oracle_scale.argtypes = [C.c_uint32, C.c_uint32, V, C.c_uint32, C.c_uint32, C.c_uint32, C.c_uint32, V]
+        L.oracle_scale.restype = None
         L.oracle_texel_coord.argtypes = [C.c_float, C.c_int32]
         L.oracle_texel_coord.restype = C.c_uint32
         L.oracle_srgb_table.argtypes = [V]

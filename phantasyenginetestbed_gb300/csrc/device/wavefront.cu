@@ -23,6 +23,7 @@
 
 #include "raygen.cuh"
 #include "runtime.cuh"
+#include "sampling.cuh"
 #include "shading.cuh"
 #include "traverse.cuh"
 #include "wavefront.cuh"
@@ -484,30 +485,6 @@ __global__ void __launch_bounds__(kWaveBlock) bounce_shade_kernel(DeviceScene s,
 }
 
 // TAA (taa.frag:25-71) with the history fetched in pixel space: (x + 0.5) - velocity * res.
-__device__ __forceinline__ float glsl_mix(float a, float b, float t)
-{
-	return __fadd_rn(__fmul_rn(a, __fsub_rn(1.0f, t)), __fmul_rn(b, t));
-}
-
-template <int CH>
-__device__ __forceinline__ void bilinear(const float* tex, uint32_t W, uint32_t H, float px, float py, float* out)
-{
-	float fx = __fsub_rn(px, 0.5f), fy = __fsub_rn(py, 0.5f);
-	float x0f = floorf(fx), y0f = floorf(fy);
-	float ax = __fsub_rn(fx, x0f), ay = __fsub_rn(fy, y0f);
-	long x0 = (long)x0f, y0 = (long)y0f, x1 = x0 + 1, y1 = y0 + 1;
-	long Wm = (long)W - 1, Hm = (long)H - 1;
-	x0 = x0 < 0 ? 0 : (x0 > Wm ? Wm : x0);
-	x1 = x1 < 0 ? 0 : (x1 > Wm ? Wm : x1);
-	y0 = y0 < 0 ? 0 : (y0 > Hm ? Hm : y0);
-	y1 = y1 < 0 ? 0 : (y1 > Hm ? Hm : y1);
-	for (int c = 0; c < CH; c++) {
-		float t00 = tex[((size_t)y0 * W + x0) * CH + c], t10 = tex[((size_t)y0 * W + x1) * CH + c];
-		float t01 = tex[((size_t)y1 * W + x0) * CH + c], t11 = tex[((size_t)y1 * W + x1) * CH + c];
-		out[c] = glsl_mix(glsl_mix(t00, t10, ax), glsl_mix(t01, t11, ax), ay);
-	}
-}
-
 __device__ __forceinline__ void taa_pixel(uint32_t x, uint32_t y, uint32_t W, uint32_t H, float4 cur,
                                           const float4* __restrict__ hist, const float2* __restrict__ vel,
                                           const float2* __restrict__ prevVel, float roughness, float4& outColor,

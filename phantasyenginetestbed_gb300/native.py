@@ -192,6 +192,7 @@ SIGNATURES: dict[str, tuple] = {
     "phe_server_get_stats": (_I32, [_VP, C.POINTER(ServerStats)]),
     "phe_server_destroy": (_I32, [_VP]),
     "phe_postprocess": (_I32, [_U32, _U32, _VP, _F, _VP, _VP, _VP]),
+    "phe_scale": (_I32, [_U32, _U32, _VP, _U32, _U32, _U32, _U32, _VP, _VP, _VP]),
     "phe_taa_resolve": (_I32, [_U32, _U32, _VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
 }
 

@@ -156,6 +156,14 @@ def postprocess(res, linear, display=None, rgba8=None, gamma=2.2, stream=None):
                                 _stream(stream)), "phe_postprocess")
 
 
+def scale(src_res, src, dst_res, dst=None, rgba8=None, viewport=None, stream=None):
+    """Display scaling pass (scaling.frag) on device buffers (phe_scale): the `viewport` part of the
+    float4 `src` image resampled to `dst_res`."""
+    vw, vh = viewport or src_res
+    check(lib().phe_scale(int(src_res[0]), int(src_res[1]), ptr(src), int(vw), int(vh), int(dst_res[0]),
+                          int(dst_res[1]), ptr(dst), ptr(rgba8), _stream(stream)), "phe_scale")
+
+
 def write_ppm(path, rgba8: np.ndarray) -> None:
     """Writes an (H, W, 4) uint8 image as binary PPM, top row first (the renderer's row 0 is the bottom)."""
     h, w = rgba8.shape[:2]

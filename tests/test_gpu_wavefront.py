@@ -132,6 +132,27 @@ def test_async_read_back_matches_the_blocking_read():
         r.read_async(np.empty(10, np.float32))
 
 
+@pytest.mark.parametrize("src,dst,viewport", [((320, 184), (1280, 720), None), ((1920, 1080), (1280, 720), None),
+                                               ((333, 201), (333, 201), None), ((320, 184), (640, 400), (300, 150)),
+                                               ((64, 40), (7, 3), None)])
+def test_scaling_pass_matches_oracle(src, dst, viewport):
+    import torch
+    from phantasyenginetestbed_gb300.renderer import scale
+    rng = np.random.default_rng(src[0] + dst[0])
+    img = rng.uniform(0, 1.2, (src[1], src[0], 4)).astype(np.float32)
+    d_src = to_device(img)
+    d_dst = device_empty(dst[0] * dst[1], np.dtype((np.float32, 4)))
+    d_rgba = device_empty(dst[0] * dst[1] * 4, np.uint8)
+    scale(src, d_src, dst, d_dst, d_rgba, viewport=viewport)
+    torch.cuda.synchronize()
+    got = from_device(d_dst, np.float32).reshape(dst[1], dst[0], 4)
+    ref = O.scale(img, dst, viewport)
+    assert np.array_equal(got, ref)
+    rgba = from_device(d_rgba, np.uint8).reshape(dst[1], dst[0], 4)
+    assert np.array_equal(rgba[..., :3], np.rint(np.clip(ref[..., :3], 0, 1) * 255).astype(np.uint8))
+    assert np.all(rgba[..., 3] == 255)
+
+
 def test_frame_full_resolution_and_taa_sequence():
     """The wavefront-frame configuration: 1920x1080, point light at (0.5, 0.5, 2.0) * scale, 8 frames
     with Halton(2,3) jitter and the TAA resolve on an FP32 RGBA history."""

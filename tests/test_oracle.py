@@ -197,3 +197,29 @@ def test_oracle_constant_textures_equal_material_constants():
                        textures=tex)
     assert np.array_equal(a[0], t[0]) and np.array_equal(a[1], t[1]) and np.array_equal(a[2], t[2])
     assert a[0][..., :3].max() > 0.01
+
+
+def test_oracle_scaling_pass_reproduces_linear_images():
+    """Bilinear taps reproduce an affine image exactly away from the clamped border, and the four
+    symmetric taps average to the value at the destination pixel's mapped centre."""
+    W, H = 64, 40
+    yy, xx = np.mgrid[0:H, 0:W].astype(np.float64)
+    img = np.zeros((H, W, 4), np.float32)
+    img[..., 0] = 0.01 * (xx + 0.5) + 0.002 * (yy + 0.5)
+    img[..., 1] = 0.5
+    img[..., 2] = 0.03 * (yy + 0.5)
+    for dst in ((96, 60), (32, 20), (64, 40)):
+        out = O.scale(img, dst)
+        dy, dx = np.mgrid[0:dst[1], 0:dst[0]].astype(np.float64)
+        cx = (dx + 0.5) / dst[0] * W
+        cy = (dy + 0.5) / dst[1] * H
+        inner = (cx > 1.5) & (cx < W - 1.5) & (cy > 1.5) & (cy < H - 1.5)
+        want_r = 0.01 * cx + 0.002 * cy
+        assert np.abs(out[..., 0] - want_r)[inner].max() < 1e-5
+        assert np.abs(out[..., 2] - 0.03 * cy)[inner].max() < 1e-5
+        assert np.all(out[..., 1] == np.float32(0.5)) and np.all(out[..., 3] == 1.0)
+    # a viewport of the lower-left 32 x 20 texels stretched over the destination: taps reach at most one
+    # texel past it (clamping happens only at the texture edge, as in GL)
+    out = O.scale(img, (64, 40), viewport=(32, 20))
+    assert out[..., 0].max() <= img[:21, :33, 0].max() + 1e-6
+    assert out[..., 0].max() > img[:20, :32, 0].max() - 0.02
