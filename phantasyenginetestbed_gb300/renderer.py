@@ -39,10 +39,21 @@ class CudaTracerRenderer:
         self.handle = h
         self.res = (0, 0)
         self.scene = None
+        self._materials = None
         if use_graph:
             self.set_graph(True)
 
+    def setMaterialsAndTextures(self, materials, textures=()) -> None:
+        """BaseRenderer::setMaterialsAndTextures (CudaTracerRenderer.cpp:192-239). The reference calls it
+        before setStaticScene; the arrays belong to the device scene here, so they are applied to the
+        current scene now and to each scene given to setStaticScene later."""
+        self._materials = (materials, list(textures))
+        if self.scene is not None:
+            self.scene.setMaterialsAndTextures(materials, textures)
+
     def setStaticScene(self, scene) -> None:
+        if self._materials is not None:
+            scene.setMaterialsAndTextures(*self._materials)
         check(lib().phe_renderer_set_static_scene(self.handle, scene.handle), "phe_renderer_set_static_scene")
         self.scene = scene
 

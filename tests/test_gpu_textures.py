@@ -121,3 +121,26 @@ def test_invalid_materials_and_textures_are_refused():
         scene.setMaterialsAndTextures(s.materials, [np.zeros((4, 4, 3), np.uint8)])
     scene.setMaterialsAndTextures(mats, textures)                # the valid set still loads
     assert scene.device_bytes() > 0
+
+
+def test_renderer_level_materials_call_order():
+    """The reference's order (GameScreen.cpp:86-87): setMaterialsAndTextures, then setStaticScene."""
+    s, datas, mats, textures = _textured_scene(13)
+    b = P.build_sbvh(s.tri_verts)
+    slot_datas = b.slot_datas(datas)
+    scene = P.Scene(b.nodes, b.verts, slot_datas)          # no materials yet
+    k = s.scale
+    res = (96, 64)
+    cam_pos = (0.5 * k, -0.3 * k, 0.6 * k)
+    cam = O.camera_def(cam_pos, C1_CAM["dir"], C1_CAM["up"], math.radians(60), res)
+    lights = make_lights(np.array([(0.5, 0.5, 2.0)], np.float32) * np.float32(k), range_=1000.0 * k)
+    r = CudaTracerRenderer()
+    r.setMaterialsAndTextures(mats, textures)
+    r.setStaticScene(scene)
+    r.setTargetResolution(res)
+    r.set_seed(21, 0)
+    r.resetTAA()
+    raw, rough, counts = _render(r, cam, cam_pos, lights)
+    ref, ref_rough, ref_counts = _oracle(b, slot_datas, mats, lights, cam, res, cam_pos, textures)
+    _compare(raw, ref, "renderer-level materials")
+    assert np.array_equal(rough, ref_rough)
