@@ -48,7 +48,8 @@ TRACE_PASS = {"primary_trace": "primary", "primary": "primary", "primary_shadow"
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--steps", type=int, default=1000,
+                    help="frames timed (default: about one second of frames, so the clock sampler sees the load)")
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-graph", action="store_true")
