@@ -652,9 +652,10 @@ static void* frame_worker(void* arg)
 {
 	frame_job* j = (frame_job*)arg;
 	uint32_t W = j->fp->resX, H = j->fp->resY;
+	uint32_t end = j->fp->rowEnd && j->fp->rowEnd < H ? j->fp->rowEnd : H;
 	for (;;) {
-		uint32_t row = atomic_fetch_add(&j->next, 1u);
-		if (row >= H) break;
+		uint32_t row = j->fp->rowBegin + atomic_fetch_add(&j->next, 1u);
+		if (row >= end) break;
 		for (uint32_t x = 0; x < W; x++) frame_pixel(j, x, row);
 	}
 	return NULL;

@@ -116,6 +116,7 @@ typedef struct {
 	const or_material* materials;
 	uint64_t seed; uint32_t frame;
 	const or_texture* textures; uint32_t numTextures;
+	uint32_t rowBegin, rowEnd;  /* rows rendered: [rowBegin, rowEnd), rowEnd = 0 meaning resY */
 } or_frame_params;
 /* `rayCounts` (optional, 4): rays cast per stage (primary, primary shadow, bounce, bounce shadow);
  * `workSums` (optional, 8): castDebugRay's nodesVisited and triangleIntersectionTests summed per stage. */

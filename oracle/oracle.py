@@ -33,7 +33,8 @@ class FrameParams(C.Structure):
     _fields_ = [("resX", C.c_uint32), ("resY", C.c_uint32), ("cam", C.c_float * 12), ("jitter", C.c_float * 2),
                 ("camPos", C.c_float * 3), ("lights", C.c_void_p), ("numLights", C.c_uint32),
                 ("materials", C.c_void_p), ("seed", C.c_uint64), ("frame", C.c_uint32),
-                ("textures", C.c_void_p), ("numTextures", C.c_uint32)]
+                ("textures", C.c_void_p), ("numTextures", C.c_uint32), ("rowBegin", C.c_uint32),
+                ("rowEnd", C.c_uint32)]
 
 
 class Texture(C.Structure):
@@ -216,10 +217,11 @@ def sincos_2pi(r):
 
 
 def render_frame(nodes, verts, slot_datas, materials, lights, cam12, res, jitter, cam_pos, seed, frame,
-                 primary_hits=None, nthreads=None, work=None, textures=()):
+                 primary_hits=None, nthreads=None, work=None, textures=(), rows=None):
     """Oracle frame: (color (H, W, 4), roughness (H, W), ray counts per stage). `work` (optional
     uint64 array of 8) receives nodesVisited / triangle tests summed per stage; `textures` are
-    (H, W, C) uint8 images indexed by the materials' texture indices."""
+    (H, W, C) uint8 images indexed by the materials' texture indices; `rows` = (begin, end) renders
+    only those rows (the rest of the image is left unset, the counts cover those rows)."""
     fp = FrameParams()
     fp.resX, fp.resY = res
     fp.cam[:] = [float(x) for x in cam12]
@@ -234,6 +236,8 @@ def render_frame(nodes, verts, slot_datas, materials, lights, cam12, res, jitter
     tex = textures_array(textures)
     fp.textures = C.addressof(tex)
     fp.numTextures = len(textures)
+    if rows is not None:
+        fp.rowBegin, fp.rowEnd = int(rows[0]), int(rows[1])
     color = np.empty((res[1], res[0], 4), np.float32)
     rough = np.empty((res[1], res[0]), np.float32)
     counts = np.zeros(4, np.uint64)
