@@ -198,8 +198,11 @@ phe_status phe_scene_destroy(phe_scene* scene);
 phe_status phe_scene_device_bytes(const phe_scene* scene, uint64_t* bytes);
 
 /* ---------------------------------------------------------------------------------------------
- * Ray casting (the hot path). Rays and results are device arrays of n entries.
+ * Ray casting (the hot path). Rays and results are device arrays of n entries. The persistent
+ * launches (phe_cast_closest, phe_cast_any, batches) take at most PHE_MAX_PERSISTENT_RAYS rays
+ * (PHE_ERR_TOO_LARGE above it).
  * ------------------------------------------------------------------------------------------- */
+#define PHE_MAX_PERSISTENT_RAYS 0xFC000000u
 
 /* Closest hit, persistent warps with dynamic ray fetch (replaces launchRayCastKernel,
  * RayCastKernel.cu:806-839). */

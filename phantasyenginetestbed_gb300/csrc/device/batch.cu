@@ -170,7 +170,8 @@ static phe_status upload_table(phe_batch* b)
 		dev[k].rays = it.rays;
 		dev[k].out = it.out;
 		uint64_t next = (uint64_t)base + ((uint64_t)it.count + 31u) / 32u * 32u;
-		if (next > 0xFFFFFFF0ull) return fail(PHE_ERR_TOO_LARGE, "batch: more than 2^32 rays in one launch");
+		if (next > kMaxPersistentRays)
+			return fail(PHE_ERR_TOO_LARGE, "batch: more than %u rays (padded) in one launch", kMaxPersistentRays);
 		base = (uint32_t)next;
 		total += it.count;
 	}
@@ -508,7 +509,8 @@ extern "C" phe_status phe_batch_cast_noalloc(const phe_scene* const* scenes, uin
 		table[k].rays = items[k].rays;
 		table[k].out = items[k].out;
 		uint64_t next = (uint64_t)base + ((uint64_t)items[k].count + 31u) / 32u * 32u;
-		if (next > 0xFFFFFFF0ull) return fail(PHE_ERR_TOO_LARGE, "phe_batch_cast_noalloc: more than 2^32 rays");
+		if (next > kMaxPersistentRays)
+			return fail(PHE_ERR_TOO_LARGE, "phe_batch_cast_noalloc: more than %u rays (padded)", kMaxPersistentRays);
 		base = (uint32_t)next;
 	}
 	bool wide = false;

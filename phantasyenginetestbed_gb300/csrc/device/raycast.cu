@@ -133,6 +133,7 @@ extern "C" phe_status phe_cast_closest(const phe_scene* scene, const phe_ray_in*
 	if (st) return st;
 	if (((uintptr_t)hits & 15u) != 0) return fail(PHE_ERR_INVALID_ARGUMENT, "hit buffer must be 16-byte aligned");
 	if (n == 0) return PHE_OK;
+	if (n > kMaxPersistentRays) return fail(PHE_ERR_TOO_LARGE, "phe_cast_closest: at most %u rays per launch", kMaxPersistentRays);
 	const bool wide = scene->dev.nodes4 != nullptr;
 	auto kernel = wide ? closest_persistent_kernel<true> : closest_persistent_kernel<false>;
 	int grid = 0;
@@ -152,6 +153,7 @@ extern "C" phe_status phe_cast_any(const phe_scene* scene, const phe_ray_in* ray
 	phe_status st = check_cast_args(scene, rays, inLight);
 	if (st) return st;
 	if (n == 0) return PHE_OK;
+	if (n > kMaxPersistentRays) return fail(PHE_ERR_TOO_LARGE, "phe_cast_any: at most %u rays per launch", kMaxPersistentRays);
 	const bool wide = scene->dev.nodes4 != nullptr;
 	auto kernel = wide ? any_persistent_kernel<true> : any_persistent_kernel<false>;
 	int grid = 0;

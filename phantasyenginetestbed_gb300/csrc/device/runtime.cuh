@@ -30,6 +30,9 @@ struct DeviceInfo {
 };
 
 constexpr uint32_t kCounterPool = 4096;
+// Largest ray count of one persistent launch. Every resident warp fetches 32 rays past the end before
+// it stops, so the 32-bit work counter needs headroom above the count (2^26 covers 2M resident warps).
+constexpr uint32_t kMaxPersistentRays = PHE_MAX_PERSISTENT_RAYS;
 
 // Returns the runtime state of the current device, initialising it on first use.
 phe_status device_info(DeviceInfo** out);

@@ -485,6 +485,16 @@ __global__ void __launch_bounds__(kWaveBlock) bounce_shade_kernel(DeviceScene s,
 }
 
 // TAA (taa.frag:25-71) with the history fetched in pixel space: (x + 0.5) - velocity * res.
+// The blend of taa.frag:62-70: n' = n * trust + 1, out = mix(cur, hist, 1 - 1/n'), alpha n'.
+__device__ __forceinline__ void taa_blend(float4 cur, float4 h, float trust, float4& outColor, float4& outHist)
+{
+	float newSamples = __fadd_rn(__fmul_rn(h.w, trust), 1.0f);
+	float blend = __fsub_rn(1.0f, __fdiv_rn(1.0f, newSamples));
+	outHist = make_float4(glsl_mix(cur.x, h.x, blend), glsl_mix(cur.y, h.y, blend), glsl_mix(cur.z, h.z, blend),
+	                      newSamples);
+	outColor = make_float4(outHist.x, outHist.y, outHist.z, 1.0f);
+}
+
 __device__ __forceinline__ void taa_pixel(uint32_t x, uint32_t y, uint32_t W, uint32_t H, float4 cur,
                                           const float4* __restrict__ hist, const float2* __restrict__ vel,
                                           const float2* __restrict__ prevVel, float roughness, float4& outColor,
@@ -512,18 +522,15 @@ __device__ __forceinline__ void taa_pixel(uint32_t x, uint32_t y, uint32_t W, ui
 	float velocityDistrust = fminf(1.0f, __fmul_rn(1.2f, __fsqrt_rn(fabsf(__fsub_rn(lp, lh)))));
 	float roughnessDistrust = glsl_mix(3.0f, 1.0f, roughness);
 	float trust = clampf(__fsub_rn(1.0f, __fmul_rn(roughnessDistrust, velocityDistrust)), 0.0f, 1.0f);
-	float h4[4];
+	float4 h;
 	if (still) {
-		float4 t = hist[p];
-		h4[0] = t.x; h4[1] = t.y; h4[2] = t.z; h4[3] = t.w;
+		h = hist[p];
 	} else {
+		float h4[4];
 		bilinear<4>(reinterpret_cast<const float*>(hist), W, H, hx, hy, h4);
+		h = make_float4(h4[0], h4[1], h4[2], h4[3]);
 	}
-	float newSamples = __fadd_rn(__fmul_rn(h4[3], trust), 1.0f);
-	float blend = __fsub_rn(1.0f, __fdiv_rn(1.0f, newSamples));
-	outHist = make_float4(glsl_mix(cur.x, h4[0], blend), glsl_mix(cur.y, h4[1], blend), glsl_mix(cur.z, h4[2], blend),
-	                      newSamples);
-	outColor = make_float4(outHist.x, outHist.y, outHist.z, 1.0f);
+	taa_blend(cur, h, trust, outColor, outHist);
 }
 
 __global__ void resolve_taa_kernel(const FrameParamsDev* __restrict__ fpp, FrameBuffers fb)
@@ -540,22 +547,25 @@ __global__ void resolve_taa_kernel(const FrameParamsDev* __restrict__ fpp, Frame
 		atomicAdd(&fb.rayTotals[2], (unsigned long long)fb.counters[kCtrBounce]);
 		atomicAdd(&fb.rayTotals[3], (unsigned long long)fb.counters[kCtrShadow1]);
 	}
+	// Every load this pixel needs is issued before the first store (the stores could alias them for
+	// the compiler). With zero velocity the history texel is the pixel itself and both velocity
+	// lengths are 0, so velocityDistrust = 0 and trust = clamp(1 - roughnessDistrust * 0).
+	const float4 h = __ldg(fb.history[fp.parity] + pid);
+	const float rough = __ldg(fb.roughness + pid);
+	uint8_t lit[2 * kMaxLights];
+	for (uint32_t k = 0; k < 2 * L; k++) lit[k] = __ldg(fb.inLight + (size_t)k * P + pid);
 	f3 acc = mk3(0.0f, 0.0f, 0.0f);
-	for (uint32_t k = 0; k < 2 * L; k++) {
-		size_t slot = (size_t)k * P + pid;
-		if (fb.inLight[slot]) {
-			float4 c = fb.contrib[slot];
+	for (uint32_t k = 0; k < 2 * L; k++)
+		if (lit[k]) {
+			float4 c = __ldg(fb.contrib + (size_t)k * P + pid);
 			acc = add3(acc, mk3(c.x, c.y, c.z));
 		}
-	}
 	float4 cur = make_float4(acc.x, acc.y, acc.z, 1.0f);
-	fb.rawColor[pid] = cur;
-	const float4* hin = fb.history[fp.parity];
-	float4* hout = fb.history[fp.parity ^ 1u];
 	float4 oc, oh;
-	taa_pixel(x, y, fp.resX, fp.resY, cur, hin, nullptr, nullptr, fb.roughness[pid], oc, oh);
+	taa_blend(cur, h, clampf(__fsub_rn(1.0f, __fmul_rn(glsl_mix(3.0f, 1.0f, rough), 0.0f)), 0.0f, 1.0f), oc, oh);
+	fb.rawColor[pid] = cur;
 	fb.color[pid] = oc;
-	hout[pid] = oh;
+	fb.history[fp.parity ^ 1u][pid] = oh;
 }
 
 __global__ void taa_kernel(uint32_t W, uint32_t H, const float4* __restrict__ cur, const float4* __restrict__ hist,

@@ -183,3 +183,15 @@ def test_scene_generator_shapes():
     assert a.min() >= 0.2 and a.max() <= 0.8
     n = s.datas["n0"]
     assert np.allclose(np.linalg.norm(n, axis=1), 1, atol=1e-6)
+
+
+def test_persistent_launch_size_limit_is_checked_before_any_device_work():
+    """n above PHE_MAX_PERSISTENT_RAYS is refused on the host, before the scene or the device is
+    touched (the handles below are never dereferenced)."""
+    import ctypes as C
+    from phantasyenginetestbed_gb300 import native
+    L = native.lib()
+    fake = C.c_void_p(0x1000)
+    assert L.phe_cast_closest(fake, fake, fake, 0xFC000001, None) == 8
+    assert L.phe_cast_any(fake, fake, fake, 0xFFFFFFFF, None, None) == 8
+    assert "rays per launch" in L.phe_last_error().decode()
