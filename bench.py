@@ -58,8 +58,9 @@ def parse():
                     help="fused: traversal + shading in one kernel per bounce (5 kernels); split: 7 kernels")
     ap.add_argument("--refill", type=int, default=28, help="lane-refill threshold of the split pipeline")
     ap.add_argument("--sort-window", type=int, default=0, help="bin bounce rays by octant in windows of N (0 = off)")
-    ap.add_argument("--serial-passes", action="store_true",
-                    help="run the primary shadow pass after the bounce pass instead of beside it")
+    ap.add_argument("--shadows", choices=["merged", "beside", "in-order"], default="merged",
+                    help="shadow-pass schedule: one pass over both queues after the bounce pass (default), the "
+                         "primary shadow pass beside the bounce pass, or each after its own pass")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--workload", choices=["frame", "plain", "batch", "large", "serve"], default="frame",
                     help="frame (default, the headline): 1080p wavefront frame; batch: 64 uneven batches over 4 "
@@ -249,7 +250,7 @@ def run_ours(args, world, rank, local):
     scene = P.Scene(b.nodes, b.verts, b.slot_datas(s.datas), s.materials)
     r = CudaTracerRenderer(use_graph=not args.no_graph)
     r.set_pipeline(fused=args.pipeline == "fused", refill=args.refill, sort_window=args.sort_window)
-    r.set_concurrent(not args.serial_passes)
+    r.set_shadow_schedule({"in-order": 0, "beside": 1, "merged": 2}[args.shadows])
     r.setStaticScene(scene)
     r.setTargetResolution(RES)
     r.set_seed(SEED, 0)
@@ -341,20 +342,33 @@ def run_ours(args, world, rank, local):
     stage_rays = dict(zip(["primary", "primary_shadow", "bounce", "bounce_shadow"], (counts / args.steps).tolist()))
     per_kernel = {}
     names = KERNELS_FUSED if args.pipeline == "fused" else KERNELS
+    if args.pipeline == "fused" and args.shadows == "merged":
+        names = ["primary", "bounce_bin", "bounce", "shadows", "resolve_taa"]
     if args.sort_window == 0:
         names = [k for k in names if k != "bounce_bin"]
+
+    def pass_bytes(pas):
+        w = work[pas]
+        return io[pas] + 64 * w["n_node"] + 48 * w["n_tri"]
+
     for i, name in enumerate(names):
         entry = {"ms": round(float(avg_kernel_ms[i]), 4)}
-        if name in TRACE_PASS:
+        if name == "shadows":   # both shadow queues in one launch
+            n = stage_rays["primary_shadow"] + stage_rays["bounce_shadow"]
+            bytes_per_ray = (stage_rays["primary_shadow"] * pass_bytes("primary_shadow") +
+                             stage_rays["bounce_shadow"] * pass_bytes("bounce_shadow")) / n
+            entry.update({"rays": round(n, 1), "Mrays_s": round(n / (avg_kernel_ms[i] / 1e3) / 1e6, 1),
+                          "alg_bytes_per_ray": round(bytes_per_ray, 1),
+                          "GB_s": round(n * bytes_per_ray / (avg_kernel_ms[i] / 1e3) / 1e9, 1)})
+        elif name in TRACE_PASS:
             pas = TRACE_PASS[name]
             n = stage_rays[pas]
-            w = work[pas]
-            bytes_per_ray = io[pas] + 64 * w["n_node"] + 48 * w["n_tri"]
+            bytes_per_ray = pass_bytes(pas)
             entry.update({"rays": round(n, 1), "Mrays_s": round(n / (avg_kernel_ms[i] / 1e3) / 1e6, 1),
                           "alg_bytes_per_ray": round(bytes_per_ray, 1),
                           "GB_s": round(n * bytes_per_ray / (avg_kernel_ms[i] / 1e3) / 1e9, 1)})
         per_kernel[name] = entry
-    dominant = max((k for k in names if k in TRACE_PASS), key=lambda k: per_kernel[k]["ms"])
+    dominant = max((k for k in names if "rays" in per_kernel[k]), key=lambda k: per_kernel[k]["ms"])
     peaks_path = ROOT / "MEASURED_PEAKS.json"
     if peaks_path.exists():
         peak = float(json.loads(peaks_path.read_text())["hbm_gbs"])
@@ -386,7 +400,7 @@ def run_ours(args, world, rank, local):
                    "rays_per_frame": round(rays_per_frame, 1), "rays_by_pass": {k: round(v, 1) for k, v in stage_rays.items()},
                    "cuda_graph": not args.no_graph, "pipeline": args.pipeline,
                    "refill_threshold": args.refill, "sort_window": args.sort_window,
-                   "concurrent_shadow_pass": args.pipeline == "fused" and not args.serial_passes, "l2": "flushed before every timed frame (512 MiB write)",
+                   "shadow_schedule": args.shadows if args.pipeline == "fused" else "in-order", "l2": "flushed before every timed frame (512 MiB write)",
                    "parallelism": f"replicas x{world}"},
         "latency_ms": {"p50": round(lat[len(lat) // 2], 4), "p99": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 4)},
         "passes": per_kernel,
@@ -618,11 +632,15 @@ def run_large(args):
     avg = kms / frames
     counts = counts / steps
     frame_ms = float(avg.sum())
-    names = [k for k in KERNELS_FUSED if k != "bounce_bin"]
+    names = ["primary", "bounce", "shadows", "resolve_taa"]   # the default (merged) shadow schedule
     passes = {}
     for i, nm in enumerate(names):
         e = {"ms": round(float(avg[i]), 3)}
-        if nm in TRACE_PASS:
+        if nm == "shadows":
+            n = counts[1] + counts[3]
+            e.update({"rays": int(n), "Mrays_s": round(n / avg[i] / 1e3, 1),
+                      "primary_shadow_rays": int(counts[1]), "bounce_shadow_rays": int(counts[3])})
+        elif nm in TRACE_PASS:
             n = counts[["primary", "primary_shadow", "bounce", "bounce_shadow"].index(TRACE_PASS[nm])]
             e.update({"rays": int(n), "Mrays_s": round(n / avg[i] / 1e3, 1)})
         passes[nm] = e

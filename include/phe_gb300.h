@@ -354,11 +354,16 @@ phe_status phe_renderer_ray_counts(const phe_renderer* renderer, uint64_t counts
  * a multiple of 256 up to 4096; default 0) bins the bounce rays by direction octant within windows of
  * that many queue entries before they are traced. */
 phe_status phe_renderer_set_pipeline(phe_renderer* renderer, int fused, int refill, int sortWindow);
-/* Concurrent passes (default 1): with the fused pipeline, the primary shadow pass runs on a second
- * stream of the renderer beside the bounce pass (both read only the primary pass's queues; in a
- * captured graph they are parallel branches). 0 runs every kernel in order on the render stream.
- * Results are the same either way. Frames timed per kernel always run in order. */
-phe_status phe_renderer_set_concurrent(phe_renderer* renderer, int concurrent);
+/* Schedule of the two shadow (any-hit) passes of the fused pipeline; every schedule gives the same
+ * bytes. IN_ORDER: primary shadows after the primary pass, bounce shadows after the bounce pass.
+ * BESIDE_BOUNCE: the primary shadow pass on a second stream of the renderer beside the bounce pass
+ * (two parallel graph branches). MERGED (default): one any-hit pass over both queues after the bounce
+ * pass, bounce shadows first, so that the short bounce-shadow queue is not a launch of its own that
+ * is mostly tail. Frames timed per kernel run BESIDE_BOUNCE in order. */
+#define PHE_SHADOWS_IN_ORDER 0
+#define PHE_SHADOWS_BESIDE_BOUNCE 1
+#define PHE_SHADOWS_MERGED 2
+phe_status phe_renderer_set_shadow_schedule(phe_renderer* renderer, int schedule);
 /* Per-kernel timing with CUDA events on the render stream (direct launches; ignored while a graph is
  * replayed). Enabling resets the totals. kernel_times returns the summed milliseconds per frame kernel
  * (in launch order, `numKernels` of them) and the number of frames timed. */

@@ -45,8 +45,8 @@ struct phe_renderer {
 	int timedKernels = 0;
 	uint32_t timedFrames = 0;
 	bool pendingTimes = false;
-	FrameStreams streams;                  // side stream for the concurrent shadow pass
-	bool concurrent = true;
+	FrameStreams streams;                  // second stream for PHE_SHADOWS_BESIDE_BOUNCE
+	int shadowSchedule = PHE_SHADOWS_MERGED;
 	// Asynchronous read-back: two device staging slots copied to the host on copyStream.
 	cudaStream_t copyStream = nullptr;
 	void* staging[2] = {nullptr, nullptr};
@@ -179,7 +179,7 @@ extern "C" phe_status phe_renderer_kernel_times(phe_renderer* r, double msTotal[
 	phe_status st = collect_times(r);
 	if (st) return st;
 	for (int i = 0; i < 8; i++) msTotal[i] = i < kFrameKernels ? r->kernelMs[i] : 0.0;
-	*numKernels = (uint32_t)((r->fused ? kFusedFrameKernels : kFrameKernels) - (r->sortWindow > 0 ? 0 : 1));
+	*numKernels = (uint32_t)frame_kernels(r->fused, r->shadowSchedule, r->sortWindow);
 	*frames = r->timedFrames;
 	return PHE_OK;
 }
@@ -205,14 +205,19 @@ extern "C" phe_status phe_renderer_set_pipeline(phe_renderer* r, int fused, int 
 	return PHE_OK;
 }
 
-extern "C" phe_status phe_renderer_set_concurrent(phe_renderer* r, int concurrent)
+extern "C" phe_status phe_renderer_set_shadow_schedule(phe_renderer* r, int schedule)
 {
-	if (!r) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_set_concurrent: null renderer");
-	if ((concurrent != 0) != r->concurrent && r->graphExec) {
+	if (!r) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_set_shadow_schedule: null renderer");
+	if (schedule != PHE_SHADOWS_IN_ORDER && schedule != PHE_SHADOWS_BESIDE_BOUNCE && schedule != PHE_SHADOWS_MERGED)
+		return fail(PHE_ERR_INVALID_ARGUMENT, "unknown shadow schedule %d", schedule);
+	if (schedule != r->shadowSchedule && r->graphExec) {
 		cudaGraphExecDestroy(r->graphExec);
 		r->graphExec = nullptr;
 	}
-	r->concurrent = concurrent != 0;
+	r->shadowSchedule = schedule;
+	r->pendingTimes = false;
+	r->timedFrames = 0;
+	for (int i = 0; i < kFrameKernels; i++) r->kernelMs[i] = 0.0;
 	return PHE_OK;
 }
 
@@ -429,7 +434,7 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 			phe_status st = PHE_OK;
 			if (e == cudaSuccess) {
 				st = launch_frame(r->scene, r->dParams, r->fb, r->resX, r->resY, cap, nullptr, r->fused,
-				                  r->concurrent ? &r->streams : nullptr);
+				                  r->shadowSchedule, &r->streams);
 				e = cudaStreamEndCapture(cap, &g);
 			}
 			cudaStreamDestroy(cap);
@@ -445,12 +450,13 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 		phe_status st;
 		if (r->timing) {
 			if ((st = collect_times(r))) return st;
-			r->timedKernels = (r->fused ? kFusedFrameKernels : kFrameKernels) - (r->sortWindow > 0 ? 0 : 1);
-			st = launch_frame(r->scene, r->dParams, r->fb, r->resX, r->resY, s, r->events, r->fused);
+			r->timedKernels = frame_kernels(r->fused, r->shadowSchedule, r->sortWindow);
+			st = launch_frame(r->scene, r->dParams, r->fb, r->resX, r->resY, s, r->events, r->fused, r->shadowSchedule,
+			                  nullptr);
 			r->pendingTimes = true;
 		} else {
 			st = launch_frame(r->scene, r->dParams, r->fb, r->resX, r->resY, s, nullptr, r->fused,
-			                  r->concurrent ? &r->streams : nullptr);
+			                  r->shadowSchedule, &r->streams);
 		}
 		if (st) return st;
 	}

@@ -162,13 +162,19 @@ __global__ void __launch_bounds__(kWaveBlock, kWaveMinBlocks) primary_kernel(Dev
 	}
 }
 
+// Persistent any hit over one or two compacted shadow queues (A, then B when countB is given),
+// each result scattered to its (light, pixel) visibility slot.
 template <bool WIDE>
-__global__ void __launch_bounds__(kWaveBlock) any_queue_kernel(DeviceScene s, const phe_ray_in* __restrict__ rays,
-                                                               const uint32_t* __restrict__ slots,
-                                                               const uint32_t* __restrict__ count, uint8_t* __restrict__ inLight,
-                                                               uint32_t* __restrict__ work, uint32_t* __restrict__ status)
+__global__ void __launch_bounds__(kWaveBlock) any_queue_kernel(DeviceScene s, const phe_ray_in* __restrict__ raysA,
+                                                               const uint32_t* __restrict__ slotsA,
+                                                               const uint32_t* __restrict__ countA,
+                                                               const phe_ray_in* __restrict__ raysB,
+                                                               const uint32_t* __restrict__ slotsB,
+                                                               const uint32_t* __restrict__ countB,
+                                                               uint8_t* __restrict__ inLight, uint32_t* __restrict__ work,
+                                                               uint32_t* __restrict__ status)
 {
-	const uint32_t n = *count;
+	const uint32_t nA = *countA, n = nA + (countB ? *countB : 0u);
 	for (;;) {
 		uint32_t base = 0;
 		if (lane_id() == 0) base = atomicAdd(work, 32u);
@@ -176,11 +182,13 @@ __global__ void __launch_bounds__(kWaveBlock) any_queue_kernel(DeviceScene s, co
 		if (base >= n) break;
 		uint32_t i = base + lane_id();
 		if (i < n) {
-			RayState r = load_ray(rays, i);
+			const bool a = i < nA;
+			const uint32_t k = a ? i : i - nA;
+			RayState r = load_ray(a ? raysA : raysB, k);
 			HitRecord h = empty_hit(r);
 			uint32_t err = trace<true, WIDE>(s, r, h);
 			if (err) atomicOr(status, err);
-			inLight[__ldg(slots + i)] = h.slot == ~0u ? 1 : 0;
+			inLight[__ldg((a ? slotsA : slotsB) + k)] = h.slot == ~0u ? 1 : 0;
 		}
 		__syncwarp();
 	}
@@ -633,10 +641,11 @@ phe_status prepare_frame()
 }
 
 phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, const FrameBuffers& fb, uint32_t resX,
-                        uint32_t resY, cudaStream_t stream, cudaEvent_t* ev, bool fused, const FrameStreams* streams)
+                        uint32_t resY, cudaStream_t stream, cudaEvent_t* ev, bool fused, int schedule,
+                        const FrameStreams* streams)
 {
 	// Timed frames keep one stream so that the per-kernel events measure one kernel each.
-	const bool concurrent = streams && streams->side && !ev;
+	const bool beside = schedule == PHE_SHADOWS_BESIDE_BOUNCE && streams && streams->side && !ev;
 	phe_status st;
 	int g[kGridCount];
 	for (int k = 0; k < kGridCount; k++)
@@ -658,29 +667,41 @@ phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, c
 		const int gPrimary = g[wide ? kGridPrimaryWide : kGridPrimary];
 		const int gAny = g[wide ? kGridAnyQueueWide : kGridAnyQueue];
 		const int gBounce = g[wide ? kGridBounceWide : kGridBounce];
+		const phe_ray_in* rays1 = fb.shadowRays + fb.capacityLP;
+		const uint32_t* slots1 = fb.shadowSlots + fb.capacityLP;
 		primary<<<gPrimary, kWaveBlock, 0, stream>>>(scene->dev, dParams, fb, scene->status);
 		mark();
-		cudaStream_t shadowStream = stream;
-		if (concurrent) {
-			PHE_CUDA_TRY(cudaEventRecord(streams->fork, stream), "fork frame");
-			PHE_CUDA_TRY(cudaStreamWaitEvent(streams->side, streams->fork, 0), "fork frame");
-			shadowStream = streams->side;
+		if (schedule != PHE_SHADOWS_MERGED) {
+			cudaStream_t shadowStream = stream;
+			if (beside) {
+				PHE_CUDA_TRY(cudaEventRecord(streams->fork, stream), "fork frame");
+				PHE_CUDA_TRY(cudaStreamWaitEvent(streams->side, streams->fork, 0), "fork frame");
+				shadowStream = streams->side;
+			}
+			anyQueue<<<gAny, kWaveBlock, 0, shadowStream>>>(scene->dev, fb.shadowRays, fb.shadowSlots,
+			                                                 fb.counters + kCtrShadow0, nullptr, nullptr, nullptr,
+			                                                 fb.inLight, fb.counters + kCtrWork2, scene->status);
+			if (beside) PHE_CUDA_TRY(cudaEventRecord(streams->join, shadowStream), "join frame");
+			mark();
 		}
-		anyQueue<<<gAny, kWaveBlock, 0, shadowStream>>>(scene->dev, fb.shadowRays, fb.shadowSlots,
-		                                                 fb.counters + kCtrShadow0, fb.inLight, fb.counters + kCtrWork2,
-		                                                 scene->status);
-		if (concurrent) PHE_CUDA_TRY(cudaEventRecord(streams->join, shadowStream), "join frame");
-		mark();
 		if (fb.sortWindow > 0) {
 			bin_bounce_kernel<<<binGrid, kBinBlock, 0, stream>>>(fb);
 			mark();
 		}
 		bounce<<<gBounce, kWaveBlock, 0, stream>>>(scene->dev, dParams, fb, scene->status);
 		mark();
-		anyQueue<<<gAny, kWaveBlock, 0, stream>>>(scene->dev, fb.shadowRays + fb.capacityLP, fb.shadowSlots + fb.capacityLP,
-		                                           fb.counters + kCtrShadow1, fb.inLight, fb.counters + kCtrWork3,
-		                                           scene->status);
+		if (schedule == PHE_SHADOWS_MERGED) {
+			// bounce shadows first: their incoherent rays start early and the primary ones fill the tail
+			anyQueue<<<gAny, kWaveBlock, 0, stream>>>(scene->dev, rays1, slots1, fb.counters + kCtrShadow1,
+			                                           fb.shadowRays, fb.shadowSlots, fb.counters + kCtrShadow0,
+			                                           fb.inLight, fb.counters + kCtrWork3, scene->status);
+		} else {
+			anyQueue<<<gAny, kWaveBlock, 0, stream>>>(scene->dev, rays1, slots1, fb.counters + kCtrShadow1, nullptr,
+			                                           nullptr, nullptr, fb.inLight, fb.counters + kCtrWork3,
+			                                           scene->status);
+		}
 		mark();
+		if (beside) PHE_CUDA_TRY(cudaStreamWaitEvent(stream, streams->join, 0), "join frame");
 	} else {
 		primary_trace_kernel<<<g[kGridPrimaryTrace], kWaveBlock, 0, stream>>>(scene->dev, dParams, fb, scene->status);
 		mark();
@@ -706,7 +727,6 @@ phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, c
 		                                                                 scene->status);
 		mark();
 	}
-	if (concurrent && fused) PHE_CUDA_TRY(cudaStreamWaitEvent(stream, streams->join, 0), "join frame");
 	resolve_taa_kernel<<<grid, block, 0, stream>>>(dParams, fb);
 	mark();
 	PHE_CUDA_TRY(cudaGetLastError(), "frame kernel launch");

@@ -67,21 +67,25 @@ phe_status renderer_reserve(phe_renderer* r, uint64_t pixels, uint32_t lights);
 phe_status prepare_frame();
 // Kernels of one frame: primary trace, primary shade, primary any-hit, bounce binning, bounce trace,
 // bounce shade, bounce any-hit, resolve + TAA (kFrameKernels); the fused pipeline has six (primary
-// and bounce trace+shade fused). The binning kernel is launched only when sortWindow > 0, so the
-// frame has one kernel less without binning.
+// and bounce trace+shade fused), five with the merged shadow schedule. The binning kernel is launched
+// only when sortWindow > 0, so the frame has one kernel less without binning.
 constexpr int kFrameKernels = 8;
 constexpr int kFusedFrameKernels = 6;
+inline int frame_kernels(bool fused, int schedule, int sortWindow)
+{
+	int k = fused ? (schedule == PHE_SHADOWS_MERGED ? kFusedFrameKernels - 1 : kFusedFrameKernels) : kFrameKernels;
+	return sortWindow > 0 ? k : k - 1;
+}
 // `events` (optional, kernels + 1 entries) are recorded on `stream` around each kernel. `fused`
-// selects the pipeline with traversal and shading in one kernel.
-// `side` (optional, with `fork`/`join` events) runs the primary shadow pass concurrently with the bounce
-// pass: both only need the primary pass's queues, and the second persistent kernel fills the first one's
-// tail. In a captured graph this becomes two parallel branches.
+// selects the pipeline with traversal and shading in one kernel; `schedule` (PHE_SHADOWS_*) the
+// placement of its shadow passes. BESIDE_BOUNCE needs `streams` (a second stream and fork/join
+// events) and runs in order while `events` are recorded.
 struct FrameStreams {
 	cudaStream_t side = nullptr;
 	cudaEvent_t fork = nullptr, join = nullptr;
 };
 phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, const FrameBuffers& fb, uint32_t resX,
-                        uint32_t resY, cudaStream_t stream, cudaEvent_t* events = nullptr, bool fused = false,
-                        const FrameStreams* streams = nullptr);
+                        uint32_t resY, cudaStream_t stream, cudaEvent_t* events, bool fused, int schedule,
+                        const FrameStreams* streams);
 
 } // namespace phe_gb300

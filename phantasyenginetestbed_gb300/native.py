@@ -166,7 +166,7 @@ SIGNATURES: dict[str, tuple] = {
     "phe_renderer_frame_param_bytes": (_U32, []),
     "phe_renderer_kernel_times": (_I32, [_VP, C.POINTER(C.c_double), C.POINTER(_U32), C.POINTER(_U32)]),
     "phe_renderer_set_pipeline": (_I32, [_VP, _I32, _I32, _I32]),
-    "phe_renderer_set_concurrent": (_I32, [_VP, _I32]),
+    "phe_renderer_set_shadow_schedule": (_I32, [_VP, _I32]),
     "phe_renderer_read_async": (_I32, [_VP, _I32, _VP, _VP]),
     "phe_renderer_read_wait": (_I32, [_VP]),
     "phe_batch_default_params": (None, [C.POINTER(BatchParams)]),

@@ -32,6 +32,9 @@ def _stream(stream):
     return stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
 
 
+SHADOWS_IN_ORDER, SHADOWS_BESIDE_BOUNCE, SHADOWS_MERGED = 0, 1, 2
+
+
 class CudaTracerRenderer:
     def __init__(self, use_graph: bool = False):
         h = C.c_void_p()
@@ -127,9 +130,9 @@ class CudaTracerRenderer:
         check(lib().phe_renderer_set_pipeline(self.handle, 1 if fused else 0, refill, sort_window),
               "phe_renderer_set_pipeline")
 
-    def set_concurrent(self, concurrent: bool = True) -> None:
-        """Run the primary shadow pass beside the bounce pass on a second stream (same results)."""
-        check(lib().phe_renderer_set_concurrent(self.handle, 1 if concurrent else 0), "phe_renderer_set_concurrent")
+    def set_shadow_schedule(self, schedule: int = 2) -> None:
+        """SHADOWS_IN_ORDER, SHADOWS_BESIDE_BOUNCE or SHADOWS_MERGED (default); same results."""
+        check(lib().phe_renderer_set_shadow_schedule(self.handle, int(schedule)), "phe_renderer_set_shadow_schedule")
 
     def close(self) -> None:
         if getattr(self, "handle", None):

@@ -62,23 +62,35 @@ def test_frame_matches_oracle_small(graph, fused, refill, window):
 
 
 @pytest.mark.parametrize("graph", [False, True])
-def test_concurrent_shadow_pass_gives_the_serial_frame(graph):
-    """The primary shadow pass beside the bounce pass (second stream / parallel graph branch) writes the
-    same bytes as the in-order pipeline, frame after frame (TAA history included)."""
+def test_shadow_schedules_give_the_same_frame(graph):
+    """Primary shadows in order, beside the bounce pass (second stream / parallel graph branch) or merged
+    with the bounce shadows into one pass: the same bytes frame after frame (TAA history included), and
+    per-kernel timing reports one kernel per launch of each schedule."""
     res = (256, 160)
     s, b, datas, scene, cam, cam_pos, lights, r = _setup("c2_256_2000", res, [(0.5, 0.5, 2.0), (0.9, 0.2, 1.5)], graph)
     out = {}
-    for conc in (False, True):
-        r.set_concurrent(conc)
+    for sched in (0, 1, 2):
+        r.set_shadow_schedule(sched)
         r.set_seed(77, 0)
         r.resetTAA()
         for f in range(3):
             r.set_camera_def(cam_struct(cam), cam_pos, P.halton_jitter(f))
             r.render(lights)
-        out[conc] = (r.read(READ_RAW), r.read(READ_HISTORY), r.ray_counts())
-    assert np.array_equal(out[False][0], out[True][0])
-    assert np.array_equal(out[False][1], out[True][1])
-    assert np.array_equal(out[False][2], out[True][2])
+        out[sched] = (r.read(READ_RAW), r.read(READ_HISTORY), r.ray_counts())
+    for sched in (1, 2):
+        for a, b_ in zip(out[0], out[sched]):
+            assert np.array_equal(a, b_), sched
+    r.set_graph(False)
+    for sched, kernels in ((0, 5), (1, 5), (2, 4)):
+        r.set_shadow_schedule(sched)
+        r.set_kernel_timing(True)
+        r.render(lights)
+        r.render(lights)
+        ms, frames = r.kernel_times()
+        assert len(ms) == kernels and frames == 2 and np.all(ms > 0), (sched, ms, frames)
+        r.set_kernel_timing(False)
+    with pytest.raises(P.PheError):
+        r.set_shadow_schedule(3)
 
 
 @pytest.mark.parametrize("graph", [False, True])
