@@ -2,18 +2,18 @@
 // cuda_ray_tracer/CudaTracerRenderer.cpp:612-728) with the raster G-buffer replaced by ray-cast
 // primary hits, followed by the TAA resolve of resources/shaders/taa.frag:25-71.
 //
-// One frame is five kernels on one stream (the reference issues ~10 launches, each followed by
-// cudaDeviceSynchronize):
+// One frame is four kernels on one stream by default (the reference issues ~10 launches, each
+// followed by cudaDeviceSynchronize):
 //   1. primary_kernel     persistent: camera ray -> closest hit -> shading of every light -> append
 //                         the shadow rays that matter and one bounce ray per hit to compacted queues
 //                         (warp-aggregated atomics; the reference casts dummy rays instead,
 //                         MaterialKernel.cu:41-47,105-109)
-//   2. any_queue_kernel   persistent any hit over the primary shadow queue, scattered to the
-//                         (light, pixel) visibility slots
-//   3. bounce_kernel      persistent: bounce closest hit -> shading (throughput as mask) -> append
+//   2. bounce_kernel      persistent: bounce closest hit -> shading (throughput as mask) -> append
 //                         shadow rays
-//   4. any_queue_kernel   over the bounce shadow queue
-//   5. resolve_taa_kernel sum of lit contributions (primary lights, then bounce lights, in light
+//   3. any_queue_kernel   persistent any hit over both shadow queues (bounce shadows first), scattered
+//                         to the (light, pixel) visibility slots; the other shadow schedules run it
+//                         once per queue (PHE_SHADOWS_IN_ORDER, PHE_SHADOWS_BESIDE_BOUNCE)
+//   4. resolve_taa_kernel sum of lit contributions (primary lights, then bounce lights, in light
 //                         order: shadowLogicKernel, MaterialKernel.cu:361-388) and the TAA blend
 // Queue counts stay on the device; persistent kernels read them when they start, so a frame needs
 // no host synchronisation and can be captured in a CUDA graph.
