@@ -332,8 +332,8 @@ phe_status phe_renderer_reset_taa(phe_renderer* renderer, void* stream);
 phe_status phe_renderer_render(phe_renderer* renderer, const phe_sphere_light* lights, uint32_t numLights, void* stream);
 phe_status phe_renderer_result(const phe_renderer* renderer, phe_render_result* out);
 /* Copies one result buffer to host memory (0 = color, 1 = history, 2 = rawColor: 16 bytes per pixel;
- * 3 = roughness: 4 bytes per pixel). Synchronises `stream`. The headless stand-in for reading the
- * GL result texture. */
+ * 3 = roughness: 4 bytes per pixel; 4 = TAA velocity: 2 floats per pixel, in uv units). Synchronises
+ * `stream`. The headless stand-in for reading the GL result texture. */
 phe_status phe_renderer_read(const phe_renderer* renderer, int which, void* hostDst, void* stream);
 /* Asynchronous read-back for frame pipelines: snapshots the buffer into one of two device staging
  * slots on `stream` (so the next frames may overwrite it) and copies the snapshot to `hostDst` on the

@@ -553,6 +553,32 @@ static int cast1(frame_job* j, const or_ray* r, or_hit* h, int stage)
 	return rc;
 }
 
+/* uv of the camera ray through d (a point minus the camera origin, or a direction); 0 behind the camera */
+static int project_uv(const or_camera* c, v3 d, float* u, float* v)
+{
+	v3 dir = ld3(c->dir), dX = ld3(c->dX), dY = ld3(c->dY);
+	float z = dot(d, dir);
+	if (!(z > 0.0f)) return 0;
+	float cx = dot(d, dX) / (dot(dX, dX) * z);
+	float cy = dot(d, dY) / (dot(dY, dY) * z);
+	*u = (cx + 1.0f) * 0.5f;
+	*v = (cy + 1.0f) * 0.5f;
+	return 1;
+}
+
+static void pixel_velocity(const or_frame_params* fp, int hit, v3 pos, v3 dir, float* out)
+{
+	float u0, v0, u1, v1;
+	v3 d0 = hit ? sub(pos, ld3(fp->cam.origin)) : dir, d1 = hit ? sub(pos, ld3(fp->prevCam.origin)) : dir;
+	if (project_uv(&fp->cam, d0, &u0, &v0) && project_uv(&fp->prevCam, d1, &u1, &v1)) {
+		out[0] = u0 - u1;
+		out[1] = v0 - v1;
+	} else {
+		out[0] = 2.0f;
+		out[1] = 2.0f;
+	}
+}
+
 static void frame_pixel(frame_job* j, uint32_t x, uint32_t y)
 {
 	const or_frame_params* fp = j->fp;
@@ -570,9 +596,11 @@ static void frame_pixel(frame_job* j, uint32_t x, uint32_t y)
 	or_hit ph;
 	if (j->primaryHits) ph = j->primaryHits[pid];
 	else if (cast1(j, &pr, &ph, 0)) atomic_fetch_add(&j->overflows, 1);
+	if (fp->velocity && ph.tri == ~0u) pixel_velocity(fp, 0, mk(0.0f, 0.0f, 0.0f), ld3(pr.d), &fp->velocity[2 * pid]);
 	if (ph.tri == ~0u) goto done;
 	{
 		hit_info hi = interpret(j->datas, fp, j->srgb, &pr, &ph);
+		if (fp->velocity) pixel_velocity(fp, 1, hi.pos, ld3(pr.d), &fp->velocity[2 * pid]);
 		if (j->roughnessOut) j->roughnessOut[pid] = hi.surf.roughness;
 		or_pcg rng;
 		oracle_pixel_stream(&rng, fp->seed, fp->frame, pid, 0);

@@ -117,6 +117,11 @@ typedef struct {
 	uint64_t seed; uint32_t frame;
 	const or_texture* textures; uint32_t numTextures;
 	uint32_t rowBegin, rowEnd;  /* rows rendered: [rowBegin, rowEnd), rowEnd = 0 meaning resY */
+	/* Camera motion (velocity_gen.frag with a ray-cast surface): when `velocity` is set, it receives
+	 * per pixel (row-major float2) the uv of the primary surface point (or of the ray direction on a
+	 * miss) in `cam` minus its uv in `prevCam`, both without jitter; (2, 2) behind either camera. */
+	or_camera prevCam;
+	float* velocity;
 } or_frame_params;
 /* `rayCounts` (optional, 4): rays cast per stage (primary, primary shadow, bounce, bounce shadow);
  * `workSums` (optional, 8): castDebugRay's nodesVisited and triangleIntersectionTests summed per stage. */

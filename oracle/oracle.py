@@ -34,7 +34,7 @@ class FrameParams(C.Structure):
                 ("camPos", C.c_float * 3), ("lights", C.c_void_p), ("numLights", C.c_uint32),
                 ("materials", C.c_void_p), ("seed", C.c_uint64), ("frame", C.c_uint32),
                 ("textures", C.c_void_p), ("numTextures", C.c_uint32), ("rowBegin", C.c_uint32),
-                ("rowEnd", C.c_uint32)]
+                ("rowEnd", C.c_uint32), ("prevCam", C.c_float * 12), ("velocity", C.c_void_p)]
 
 
 class Texture(C.Structure):
@@ -217,11 +217,13 @@ def sincos_2pi(r):
 
 
 def render_frame(nodes, verts, slot_datas, materials, lights, cam12, res, jitter, cam_pos, seed, frame,
-                 primary_hits=None, nthreads=None, work=None, textures=(), rows=None):
+                 primary_hits=None, nthreads=None, work=None, textures=(), rows=None, prev_cam=None,
+                 velocity_out=None):
     """Oracle frame: (color (H, W, 4), roughness (H, W), ray counts per stage). `work` (optional
     uint64 array of 8) receives nodesVisited / triangle tests summed per stage; `textures` are
     (H, W, C) uint8 images indexed by the materials' texture indices; `rows` = (begin, end) renders
-    only those rows (the rest of the image is left unset, the counts cover those rows)."""
+    only those rows (the rest of the image is left unset, the counts cover those rows); `velocity_out`
+    ((H, W, 2) float32) receives the TAA velocity against the previous camera `prev_cam`."""
     fp = FrameParams()
     fp.resX, fp.resY = res
     fp.cam[:] = [float(x) for x in cam12]
@@ -238,6 +240,10 @@ def render_frame(nodes, verts, slot_datas, materials, lights, cam12, res, jitter
     fp.numTextures = len(textures)
     if rows is not None:
         fp.rowBegin, fp.rowEnd = int(rows[0]), int(rows[1])
+    if velocity_out is not None:
+        assert velocity_out.dtype == np.float32 and velocity_out.shape == (res[1], res[0], 2)
+        fp.prevCam[:] = [float(x) for x in (cam12 if prev_cam is None else prev_cam)]
+        fp.velocity = velocity_out.ctypes.data
     color = np.empty((res[1], res[0], 4), np.float32)
     rough = np.empty((res[1], res[0]), np.float32)
     counts = np.zeros(4, np.uint64)

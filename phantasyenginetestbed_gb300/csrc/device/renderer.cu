@@ -48,6 +48,10 @@ struct phe_renderer {
 	FrameStreams streams;                  // second stream for PHE_SHADOWS_BESIDE_BOUNCE
 	int shadowSchedule = PHE_SHADOWS_MERGED;
 	// Asynchronous read-back: two device staging slots copied to the host on copyStream.
+	// Camera motion (TAA velocity): the last rendered camera and which velocity sides are all zero.
+	phe_camera_def prevCam{};
+	bool hasPrevCam = false;
+	bool velocityZero[2] = {true, true};
 	cudaStream_t copyStream = nullptr;
 	void* staging[2] = {nullptr, nullptr};
 	size_t stagingBytes = 0;
@@ -73,6 +77,10 @@ static phe_status allocate(phe_renderer* r, uint32_t resX, uint32_t resY, uint32
 {
 	const size_t P = (size_t)resX * resY;
 	const size_t L = numLights ? numLights : 1;
+	if (resX != r->resX || resY != r->resY) {   // velocities of another resolution do not carry over
+		r->hasPrevCam = false;
+		r->velocityZero[0] = r->velocityZero[1] = true;
+	}
 	if (r->allocation && P <= r->capacityP && L <= r->capacityL) {
 		// Keep the buffers: every stride is computed from the current resolution at launch time. A
 		// captured graph holds launch shapes for the old resolution, so it is rebuilt.
@@ -105,6 +113,8 @@ static phe_status allocate(phe_renderer* r, uint32_t resX, uint32_t resY, uint32
 		P * sizeof(phe_ray_hit),      // bounceHits
 		4 * sizeof(unsigned long long), // rayTotals
 		P * sizeof(uint32_t),         // bouncePerm
+		P * sizeof(float2),           // velocity[0]
+		P * sizeof(float2),           // velocity[1]
 	};
 	size_t total = 0;
 	for (size_t s : sizes) total += align256(s);
@@ -131,6 +141,8 @@ static phe_status allocate(phe_renderer* r, uint32_t resX, uint32_t resY, uint32
 	fb.bounceHits = (phe_ray_hit*)take(14);
 	fb.rayTotals = (unsigned long long*)take(15);
 	fb.bouncePerm = (uint32_t*)take(16);
+	fb.velocity[0] = (float2*)take(17);
+	fb.velocity[1] = (float2*)take(18);
 	fb.sortWindow = r->sortWindow;
 	fb.capacityLP = (uint32_t)LP;
 	fb.refill = r->refill;
@@ -361,6 +373,8 @@ extern "C" phe_status phe_renderer_reset_taa(phe_renderer* r, void* stream)
 	size_t P = (size_t)r->resX * r->resY;
 	PHE_CUDA_TRY(cudaMemsetAsync(r->fb.history[0], 0, P * sizeof(float4), (cudaStream_t)stream), "reset TAA");
 	PHE_CUDA_TRY(cudaMemsetAsync(r->fb.history[1], 0, P * sizeof(float4), (cudaStream_t)stream), "reset TAA");
+	r->hasPrevCam = false;
+	r->velocityZero[0] = r->velocityZero[1] = true;
 	return PHE_OK;
 }
 
@@ -403,6 +417,13 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 	r->paramSlot = (slot + 1) % kParamSlots;
 	PHE_CUDA_TRY(cudaEventSynchronize(r->paramEvents[slot]), "wait for a free parameter slot");
 	FrameParamsDev& fp = r->hParams[slot];
+	// Camera motion: this frame writes the velocity on the side of its output history, the previous
+	// frame's velocity is on the other side; a camera equal to the previous one has velocity 0.
+	const uint32_t outSide = r->parity ^ 1u, inSide = r->parity;
+	const bool moving = r->hasPrevCam && std::memcmp(&r->prevCam, &r->cam, sizeof(phe_camera_def)) != 0;
+	fp.prevCam = r->hasPrevCam ? r->prevCam : r->cam;
+	fp.velocity = moving ? r->fb.velocity[outSide] : nullptr;
+	fp.prevVelocity = r->velocityZero[inSide] ? nullptr : r->fb.velocity[inSide];
 	fp.cam = r->cam;
 	fp.jitter[0] = r->jitter[0];
 	fp.jitter[1] = r->jitter[1];
@@ -460,6 +481,9 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 		}
 		if (st) return st;
 	}
+	r->velocityZero[outSide] = !moving;
+	r->prevCam = r->cam;
+	r->hasPrevCam = true;
 	r->frame++;
 	r->parity ^= 1u;
 	return PHE_OK;
@@ -499,7 +523,8 @@ static phe_status read_source(const phe_renderer* r, int which, const void** src
 	case 1: *src = r->fb.history[r->parity]; break;
 	case 2: *src = r->fb.rawColor; break;
 	case 3: *src = r->fb.roughness; *bytes = P * sizeof(float); break;
-	default: return fail(PHE_ERR_INVALID_ARGUMENT, "renderer read: which must be 0..3");
+	case 4: *src = r->velocityZero[r->parity] ? nullptr : r->fb.velocity[r->parity]; *bytes = P * sizeof(float2); break;
+	default: return fail(PHE_ERR_INVALID_ARGUMENT, "renderer read: which must be 0..4");
 	}
 	return PHE_OK;
 }
@@ -511,6 +536,11 @@ extern "C" phe_status phe_renderer_read(const phe_renderer* r, int which, void* 
 	size_t bytes = 0;
 	phe_status st = read_source(r, which, &src, &bytes);
 	if (st) return st;
+	if (!src) {   // a velocity that is 0 everywhere is not stored
+		PHE_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream), "read result");
+		std::memset(hostDst, 0, bytes);
+		return PHE_OK;
+	}
 	PHE_CUDA_TRY(cudaMemcpyAsync(hostDst, src, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)stream), "read result");
 	PHE_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream), "read result");
 	return PHE_OK;
@@ -544,7 +574,8 @@ extern "C" phe_status phe_renderer_read_async(phe_renderer* r, int which, void* 
 	const uint32_t k = r->readSlot;
 	r->readSlot ^= 1u;
 	if (r->readPending[k]) PHE_CUDA_TRY(cudaStreamWaitEvent(s, r->doneEvents[k], 0), "wait for staging slot");
-	PHE_CUDA_TRY(cudaMemcpyAsync(r->staging[k], src, bytes, cudaMemcpyDeviceToDevice, s), "snapshot result");
+	if (src) PHE_CUDA_TRY(cudaMemcpyAsync(r->staging[k], src, bytes, cudaMemcpyDeviceToDevice, s), "snapshot result");
+	else PHE_CUDA_TRY(cudaMemsetAsync(r->staging[k], 0, bytes, s), "snapshot zero velocity");
 	PHE_CUDA_TRY(cudaEventRecord(r->snapEvents[k], s), "record snapshot");
 	PHE_CUDA_TRY(cudaStreamWaitEvent(r->copyStream, r->snapEvents[k], 0), "order read-back");
 	PHE_CUDA_TRY(cudaMemcpyAsync(hostDst, r->staging[k], bytes, cudaMemcpyDeviceToHost, r->copyStream), "read result");

@@ -88,6 +88,37 @@ __device__ __forceinline__ void shade_all_lights(const FrameParamsDev& fp, const
 	}
 }
 
+// Image position (uv in [0, 1]^2, the ray-generation convention of genPrimaryRaysKernel) of the camera
+// ray through `d` (a point minus the camera origin, or a direction for a point at infinity); false
+// when it lies behind the camera.
+__device__ __forceinline__ bool project_uv(const phe_camera_def& c, f3 d, float& u, float& v)
+{
+	f3 dir = mk3(c.dir[0], c.dir[1], c.dir[2]);
+	f3 dX = mk3(c.dX[0], c.dX[1], c.dX[2]);
+	f3 dY = mk3(c.dY[0], c.dY[1], c.dY[2]);
+	float z = dot3(d, dir);
+	if (!(z > 0.0f)) return false;
+	float cx = __fdiv_rn(dot3(d, dX), __fmul_rn(dot3(dX, dX), z));
+	float cy = __fdiv_rn(dot3(d, dY), __fmul_rn(dot3(dY, dY), z));
+	u = __fmul_rn(__fadd_rn(cx, 1.0f), 0.5f);
+	v = __fmul_rn(__fadd_rn(cy, 1.0f), 0.5f);
+	return true;
+}
+
+// Velocity of the surface seen through a pixel (velocity_gen.frag without dynamic objects): its uv in
+// this frame's camera minus its uv in the previous frame's camera, both without jitter. A point behind
+// either camera gets (2, 2), which sends the TAA history lookup off screen (current colour only).
+__device__ __forceinline__ float2 pixel_velocity(const FrameParamsDev& fp, bool hit, f3 pos, f3 dir)
+{
+	f3 o = mk3(fp.cam.origin[0], fp.cam.origin[1], fp.cam.origin[2]);
+	f3 po = mk3(fp.prevCam.origin[0], fp.prevCam.origin[1], fp.prevCam.origin[2]);
+	float u0, v0, u1, v1;
+	if (project_uv(fp.cam, hit ? sub3(pos, o) : dir, u0, v0) &&
+	    project_uv(fp.prevCam, hit ? sub3(pos, po) : dir, u1, v1))
+		return make_float2(__fsub_rn(u0, u1), __fsub_rn(v0, v1));
+	return make_float2(2.0f, 2.0f);
+}
+
 template <bool WIDE>
 __global__ void __launch_bounds__(kWaveBlock, kWaveMinBlocks) primary_kernel(DeviceScene s, const FrameParamsDev* __restrict__ fpp,
                                                              FrameBuffers fb, uint32_t* __restrict__ status)
@@ -139,6 +170,7 @@ __global__ void __launch_bounds__(kWaveBlock, kWaveMinBlocks) primary_kernel(Dev
 			hi.alpha = hi.roughness = hi.metallic = 0.0f;
 		}
 		if (active) fb.roughness[pid] = hit ? hi.roughness : 0.0f;
+		if (active && fp.velocity) fp.velocity[pid] = pixel_velocity(fp, hit, hi.pos, r.d);
 		shade_all_lights(fp, fb, 0, hit, hi, mk3(1.0f, 1.0f, 1.0f), toCamera, rng, pid);
 		// Bounce ray (one per hit) into the bounce queue.
 		float btMin = 0.001f;
@@ -426,6 +458,9 @@ __global__ void __launch_bounds__(kWaveBlock) primary_shade_kernel(DeviceScene s
 			hi.alpha = hi.roughness = hi.metallic = 0.0f;
 		}
 		if (active) fb.roughness[pid] = hit ? hi.roughness : 0.0f;
+		if (active && fp.velocity)
+			fp.velocity[pid] = pixel_velocity(fp, hit, hi.pos,
+			                                  hit ? hi.pos : primary_dir(fp.cam, x, y, W, fp.resY, fp.jitter[0], fp.jitter[1]));
 		shade_all_lights(fp, fb, 0, hit, hi, mk3(1.0f, 1.0f, 1.0f), toCamera, rng, pid);
 		float btMin = 0.001f;
 		f3 thr = mk3(0.0f, 0.0f, 0.0f), bdir = mk3(0.0f, 0.0f, 0.0f);
@@ -555,9 +590,27 @@ __global__ void resolve_taa_kernel(const FrameParamsDev* __restrict__ fpp, Frame
 		atomicAdd(&fb.rayTotals[2], (unsigned long long)fb.counters[kCtrBounce]);
 		atomicAdd(&fb.rayTotals[3], (unsigned long long)fb.counters[kCtrShadow1]);
 	}
-	// Every load this pixel needs is issued before the first store (the stores could alias them for
-	// the compiler). With zero velocity the history texel is the pixel itself and both velocity
-	// lengths are 0, so velocityDistrust = 0 and trust = clamp(1 - roughnessDistrust * 0).
+	if (fp.velocity || fp.prevVelocity) {   // camera motion: the full TAA with reprojected history
+		f3 acc = mk3(0.0f, 0.0f, 0.0f);
+		for (uint32_t k = 0; k < 2 * L; k++) {
+			size_t slot = (size_t)k * P + pid;
+			if (fb.inLight[slot]) {
+				float4 c = fb.contrib[slot];
+				acc = add3(acc, mk3(c.x, c.y, c.z));
+			}
+		}
+		float4 cur = make_float4(acc.x, acc.y, acc.z, 1.0f);
+		float4 oc, oh;
+		taa_pixel(x, y, fp.resX, fp.resY, cur, fb.history[fp.parity], fp.velocity, fp.prevVelocity, fb.roughness[pid],
+		          oc, oh);
+		fb.rawColor[pid] = cur;
+		fb.color[pid] = oc;
+		fb.history[fp.parity ^ 1u][pid] = oh;
+		return;
+	}
+	// Still camera. Every load this pixel needs is issued before the first store (the stores could
+	// alias them for the compiler). With zero velocity the history texel is the pixel itself and both
+	// velocity lengths are 0, so velocityDistrust = 0 and trust = clamp(1 - roughnessDistrust * 0).
 	const float4 h = __ldg(fb.history[fp.parity] + pid);
 	const float rough = __ldg(fb.roughness + pid);
 	uint8_t lit[2 * kMaxLights];

@@ -34,6 +34,12 @@ struct FrameParamsDev {
 	uint32_t frame, parity;  // frame index (random streams) and history ping-pong side
 	uint64_t seed;
 	phe_sphere_light lights[kMaxLights];
+	// Camera motion for TAA (velocity_gen.frag): the previous frame's camera (no jitter), this frame's
+	// velocity output (null while the camera stands still: velocity 0 everywhere) and the previous
+	// frame's velocity (null when it was 0 everywhere).
+	phe_camera_def prevCam;
+	float2* velocity;
+	const float2* prevVelocity;
 };
 
 struct FrameBuffers {
@@ -47,6 +53,7 @@ struct FrameBuffers {
 	float* roughness;         // [P] roughness at the primary hit (0 on a miss), read by TAA
 	float4* rawColor;         // [P] resolved colour before TAA
 	float4* history[2];       // [P] TAA history ping-pong (rgb + effective sample count)
+	float2* velocity[2];      // [P] uv velocity ping-pong (same side as the history)
 	float4* color;            // [P] TAA output
 	uint32_t* counters;       // [kNumCounters]
 	uint32_t capacityLP;      // L * P

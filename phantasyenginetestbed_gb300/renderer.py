@@ -14,7 +14,7 @@ import numpy as np
 from . import native as _n
 from .native import LIGHT_DTYPE, check, lib, ptr
 
-READ_COLOR, READ_HISTORY, READ_RAW, READ_ROUGHNESS = 0, 1, 2, 3
+READ_COLOR, READ_HISTORY, READ_RAW, READ_ROUGHNESS, READ_VELOCITY = 0, 1, 2, 3, 4
 
 
 @dataclass
@@ -94,14 +94,15 @@ class CudaTracerRenderer:
     def read(self, which: int = READ_COLOR, out: np.ndarray | None = None, stream=None) -> np.ndarray:
         W, H = self.res
         if out is None:
-            out = np.empty((H, W) if which == READ_ROUGHNESS else (H, W, 4), np.float32)
+            out = np.empty((H, W) if which == READ_ROUGHNESS else (H, W, 2) if which == READ_VELOCITY else (H, W, 4),
+                           np.float32)
         check(lib().phe_renderer_read(self.handle, which, ptr(out), _stream(stream)), "phe_renderer_read")
         return out
 
     def read_async(self, out: np.ndarray, which: int = READ_COLOR, stream=None) -> None:
         """Queue a read-back into `out` (pinned for overlap); the image is there after read_wait()."""
         W, H = self.res
-        need = W * H * (4 if which == READ_ROUGHNESS else 16)
+        need = W * H * (4 if which == READ_ROUGHNESS else 8 if which == READ_VELOCITY else 16)
         if out.nbytes < need or not out.flags.c_contiguous:
             raise ValueError(f"read_async: need a contiguous buffer of {need} bytes")
         check(lib().phe_renderer_read_async(self.handle, which, ptr(out), _stream(stream)), "phe_renderer_read_async")

@@ -8,7 +8,8 @@ import numpy as np
 import pytest
 
 import phantasyenginetestbed_gb300 as P
-from phantasyenginetestbed_gb300.renderer import READ_COLOR, READ_HISTORY, READ_RAW, READ_ROUGHNESS, CudaTracerRenderer, make_lights, taa_resolve
+from phantasyenginetestbed_gb300.renderer import (READ_COLOR, READ_HISTORY, READ_RAW, READ_ROUGHNESS, READ_VELOCITY,
+                                                   CudaTracerRenderer, make_lights, taa_resolve)
 from oracle import oracle as O
 from tests.helpers import C1_CAM, built_scene, cam_struct, device_empty, from_device, to_device
 
@@ -163,6 +164,43 @@ def test_scaling_pass_matches_oracle(src, dst, viewport):
     rgba = from_device(d_rgba, np.uint8).reshape(dst[1], dst[0], 4)
     assert np.array_equal(rgba[..., :3], np.rint(np.clip(ref[..., :3], 0, 1) * 255).astype(np.uint8))
     assert np.all(rgba[..., 3] == 255)
+
+
+@pytest.mark.parametrize("graph", [False, True])
+def test_moving_camera_velocity_and_taa_match_oracle(graph):
+    """Camera motion: still, moving, rotating, then still again (the previous velocity still weighs in)
+    and still twice (the direct path). Per frame the velocity is bit-identical to the oracle's and the
+    raw frame, TAA colour and history agree with the oracle's TAA chain."""
+    res = (256, 160)
+    s, b, datas, scene, cam, cam_pos, lights, r = _setup("c2_256_2000", res, [(0.5, 0.5, 2.0)], graph)
+    k = s.scale
+    d0 = np.array(C1_CAM["dir"], np.float64)
+    d1 = d0 + np.array([0.03, 0.0, 0.01])
+    p0 = np.array(cam_pos, np.float64)
+    path = [(p0, d0), (p0, d0), (p0 + [0.004 * k, 0.001 * k, 0.0], d0), (p0 + [0.008 * k, 0.0, 0.002 * k], d1),
+            (p0 + [0.008 * k, 0.0, 0.002 * k], d1), (p0 + [0.008 * k, 0.0, 0.002 * k], d1)]
+    r.set_seed(5, 0)
+    r.resetTAA()
+    hist = np.zeros((res[1], res[0], 4), np.float32)
+    prev_cam, prev_vel = None, np.zeros((res[1], res[0], 2), np.float32)
+    for f, (pos, d) in enumerate(path):
+        up = np.cross(np.cross(d, np.array(C1_CAM["up"])), d)   # orthogonal to d, as generateCameraDef needs
+        up = -up if up[2] < 0 else up
+        cam_f = O.camera_def(pos, d, up, math.radians(60), res)
+        jit = P.halton_jitter(f)
+        r.set_camera_def(cam_struct(cam_f), pos, jit)
+        r.render(lights)
+        vel = np.zeros((res[1], res[0], 2), np.float32)
+        ref, rough, _ = O.render_frame(b.nodes, b.verts, datas, s.materials, lights, cam_f, res, jit, pos, 5, f,
+                                       prev_cam=cam_f if prev_cam is None else prev_cam, velocity_out=vel)
+        _compare(r.read(READ_RAW), ref, f"raw frame {f}")
+        got_vel = r.read(READ_VELOCITY)
+        assert np.array_equal(got_vel, vel), f
+        assert (np.abs(vel).max() > 0) == (f in (2, 3)), f
+        out_c, hist = O.taa(ref, hist, rough, vel, prev_vel)
+        _compare(r.read(READ_COLOR), out_c, f"TAA colour {f}")
+        _compare(r.read(READ_HISTORY), hist, f"TAA history {f}")
+        prev_cam, prev_vel = cam_f, vel
 
 
 def test_frame_full_resolution_and_taa_sequence():

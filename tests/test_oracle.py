@@ -223,3 +223,35 @@ def test_oracle_scaling_pass_reproduces_linear_images():
     out = O.scale(img, (64, 40), viewport=(32, 20))
     assert out[..., 0].max() <= img[:21, :33, 0].max() + 1e-6
     assert out[..., 0].max() > img[:20, :32, 0].max() - 0.02
+
+
+def test_oracle_velocity_for_camera_motion():
+    """TAA velocity restatement: 0 everywhere for an unchanged camera; a sideways camera move gives
+    surface points a velocity against the move (larger for nearer points) and leaves directions at
+    infinity (misses) still."""
+    s = P.generate_scene(24, 20, True, 7)
+    b = P.build_sbvh(s.tri_verts)
+    slot_datas = b.slot_datas(s.datas)
+    k = s.scale
+    res = (64, 48)
+    from phantasyenginetestbed_gb300.renderer import make_lights
+    lights = make_lights(np.array([(0.5, 0.5, 2.0)], np.float32) * np.float32(k), range_=1000.0 * k)
+    # look slightly above the horizon so that some pixels miss
+    up = np.array([0.0, 0.2, 0.98]); d = np.array([0.0, 0.98, -0.2])
+    pos0 = np.array([0.5 * k, -0.3 * k, 0.3 * k])
+    cam0 = O.camera_def(pos0, d, up, math.radians(60), res)
+    vel = np.full((res[1], res[0], 2), np.nan, np.float32)
+    O.render_frame(b.nodes, b.verts, slot_datas, s.materials, lights, cam0, res, (0.1, -0.2), pos0, 3, 0,
+                   prev_cam=cam0, velocity_out=vel)
+    assert np.all(vel == 0.0)
+    right = cam0[6:9] / np.linalg.norm(cam0[6:9])
+    pos1 = pos0 + 0.02 * k * right
+    cam1 = O.camera_def(pos1, d, up, math.radians(60), res)
+    O.render_frame(b.nodes, b.verts, slot_datas, s.materials, lights, cam1, res, (0.0, 0.0), pos1, 3, 1,
+                   prev_cam=cam0, velocity_out=vel)
+    rays = O.gen_primary(cam1, res)   # row-major ray order, no jitter (as the frame above)
+    h = O.cast_rays(b.nodes, b.verts, rays)
+    hits = (h["triangleIndex"] != 0xFFFFFFFF).reshape(res[1], res[0])
+    assert hits.any() and (~hits).any()
+    assert np.all(vel[..., 0][hits] < 0) and np.all(vel[..., 1][hits] == 0.0)   # a move along the image x axis
+    assert np.all(vel[~hits] == 0.0)
