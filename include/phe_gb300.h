@@ -308,6 +308,10 @@ typedef struct phe_render_result {
 	const float* history;    /* device, float4 per pixel: TAA history, alpha = sample count */
 	const float* rawColor;   /* device, float4 per pixel: resolved frame before TAA */
 	const float* roughness;  /* device, float per pixel: roughness at the primary hit (materialTexture) */
+	const float* velocity;   /* device, float2 per pixel: TAA uv velocity of the last frame, NULL when the
+	                          * camera stood still (0 everywhere). The reference's velocityTexture holds
+	                          * object world velocity, 0 for the static scene; this is what its
+	                          * velocity_gen.frag derives from it and the depth buffer. */
 } phe_render_result;
 phe_status phe_renderer_create(phe_renderer** out);
 phe_status phe_renderer_destroy(phe_renderer* renderer);

@@ -498,6 +498,7 @@ extern "C" phe_status phe_renderer_result(const phe_renderer* r, phe_render_resu
 	out->history = (const float*)r->fb.history[r->parity];   // written by the last frame
 	out->rawColor = (const float*)r->fb.rawColor;
 	out->roughness = r->fb.roughness;
+	out->velocity = r->velocityZero[r->parity] ? nullptr : (const float*)r->fb.velocity[r->parity];
 	return PHE_OK;
 }
 

@@ -69,7 +69,7 @@ class SbvhParams(C.Structure):
 
 class RenderResult(C.Structure):
     _fields_ = [("resX", C.c_uint32), ("resY", C.c_uint32), ("color", C.c_void_p), ("history", C.c_void_p),
-                ("rawColor", C.c_void_p), ("roughness", C.c_void_p)]
+                ("rawColor", C.c_void_p), ("roughness", C.c_void_p), ("velocity", C.c_void_p)]
 
 
 class BatchItem(C.Structure):

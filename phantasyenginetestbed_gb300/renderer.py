@@ -24,6 +24,7 @@ class RenderResult:
     history: int
     raw_color: int
     roughness: int
+    velocity: int | None = None   # device float2 per pixel, None while the camera stands still
 
 
 def _stream(stream):
@@ -89,7 +90,7 @@ class CudaTracerRenderer:
               "phe_renderer_render")
         r = _n.RenderResult()
         check(lib().phe_renderer_result(self.handle, C.byref(r)), "phe_renderer_result")
-        return RenderResult((r.resX, r.resY), r.color, r.history, r.rawColor, r.roughness)
+        return RenderResult((r.resX, r.resY), r.color, r.history, r.rawColor, r.roughness, r.velocity)
 
     def read(self, which: int = READ_COLOR, out: np.ndarray | None = None, stream=None) -> np.ndarray:
         W, H = self.res
