@@ -34,6 +34,7 @@ typedef int phe_status;
 #define PHE_ERR_TOO_LARGE 8          /* size beyond a documented maximum */
 #define PHE_ERR_NOT_READY 9          /* result not available yet (poll again) */
 #define PHE_ERR_NO_DEVICE 10         /* no CUDA device is visible */
+#define PHE_ERR_CANCELLED 11         /* the request was cancelled before it was admitted */
 
 /* ---------------------------------------------------------------------------------------------
  * Layouts (byte-identical to the reference)
@@ -463,6 +464,10 @@ phe_status phe_server_wait(phe_server* server, uint64_t requestId, phe_request_s
 phe_status phe_server_drain(phe_server* server);
 /* Forgets a completed request. */
 phe_status phe_server_release(phe_server* server, uint64_t requestId);
+/* Cancels a request that has not been admitted yet: it completes at once with status
+ * PHE_ERR_CANCELLED and its output buffer is never written. An admitted request cannot be cancelled
+ * (its work is on the GPU): PHE_ERR_NOT_READY, and it completes normally. */
+phe_status phe_server_cancel(phe_server* server, uint64_t requestId);
 phe_status phe_server_get_stats(phe_server* server, phe_server_stats* stats);
 phe_status phe_server_destroy(phe_server* server);
 

@@ -563,6 +563,27 @@ extern "C" phe_status phe_server_release(phe_server* s, uint64_t id)
 	return PHE_OK;
 }
 
+extern "C" phe_status phe_server_cancel(phe_server* s, uint64_t id)
+{
+	if (!s) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_server_cancel: null server");
+	std::lock_guard<std::mutex> lock(s->m);
+	auto it = s->all.find(id);
+	if (it == s->all.end()) return fail(PHE_ERR_NOT_FOUND, "phe_server_cancel: unknown request");
+	Request* r = it->second;
+	if (r->state == kDone) return r->status == PHE_ERR_CANCELLED ? PHE_OK : fail(PHE_ERR_NOT_READY, "phe_server_cancel: request already completed");
+	auto p = std::find(s->pending.begin(), s->pending.end(), r);
+	if (r->state != kPending || p == s->pending.end())
+		return fail(PHE_ERR_NOT_READY, "phe_server_cancel: request already admitted");
+	s->pending.erase(p);
+	r->status = PHE_ERR_CANCELLED;
+	r->error = "cancelled before admission";
+	r->tDone = now_ms(s->t0);
+	r->state = kDone;
+	s->cvDone.notify_all();
+	s->cvWork.notify_one();
+	return PHE_OK;
+}
+
 extern "C" phe_status phe_server_get_stats(phe_server* s, phe_server_stats* out)
 {
 	if (!s || !out) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_server_get_stats: null argument");

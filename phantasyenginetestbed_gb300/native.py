@@ -23,6 +23,7 @@ PHE_ERR_TIMEOUT = 6
 PHE_ERR_NOT_FOUND = 7
 PHE_ERR_TOO_LARGE = 8
 PHE_ERR_NOT_READY = 9
+PHE_ERR_CANCELLED = 11
 PHE_ERR_NO_DEVICE = 10
 
 PTR_HOST = 0
@@ -189,6 +190,7 @@ SIGNATURES: dict[str, tuple] = {
     "phe_server_wait": (_I32, [_VP, C.c_uint64, C.POINTER(RequestStats)]),
     "phe_server_drain": (_I32, [_VP]),
     "phe_server_release": (_I32, [_VP, C.c_uint64]),
+    "phe_server_cancel": (_I32, [_VP, C.c_uint64]),
     "phe_server_get_stats": (_I32, [_VP, C.POINTER(ServerStats)]),
     "phe_server_destroy": (_I32, [_VP]),
     "phe_postprocess": (_I32, [_U32, _U32, _VP, _F, _VP, _VP, _VP]),

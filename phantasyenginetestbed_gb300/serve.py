@@ -98,6 +98,14 @@ class Server:
         check(lib().phe_server_release(self.handle, rid), "phe_server_release")
         self._keep.pop(rid, None)
 
+    def cancel(self, rid: int) -> bool:
+        """Cancels a request not yet admitted (True); False when it is already admitted or done."""
+        s = lib().phe_server_cancel(self.handle, rid)
+        if s == _n.PHE_ERR_NOT_READY:
+            return False
+        check(s, "phe_server_cancel")
+        return True
+
     def stats(self):
         st = _n.ServerStats()
         check(lib().phe_server_get_stats(self.handle, C.byref(st)), "phe_server_get_stats")

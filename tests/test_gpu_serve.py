@@ -145,3 +145,60 @@ def test_budget_admission_and_serial_baseline(scenes):
         serial.wait(serial.submit_rays(ids[0], rays, out2))
         assert np.array_equal(out2, out)
     serial.close()
+
+
+def test_cancel_and_malformed_requests(scenes):
+    """Host-side fault injection: a queued request is cancelled (its output is never written), an
+    admitted one is not; unknown scene ids and empty queries are refused at submit; rays with NaN
+    components or tMin > tMax go through the server and give the results of a direct cast."""
+    import torch
+    s, b, scene = scenes[1]
+    server = Server(serial=True, render_slots=1)
+    sid = server.add_scene(scene)
+    k = s.scale
+    res = (1920, 1080)
+    cam_pos = (0.5 * k, -0.3 * k, 0.6 * k)
+    cam = O.camera_def(cam_pos, C1_CAM["dir"], C1_CAM["up"], math.radians(60), res)
+    lights = make_lights(np.array([[0.5, 0.5, 2.0]], np.float32) * np.float32(k), range_=1000.0 * k)
+    big = pinned((res[1], res[0], 4), np.float32)
+    first = server.submit_render(sid, res, 16, cam_struct(cam), cam_pos, lights, 1, big)   # keeps the server busy
+    rays = random_rays(5000, [0, 0, 0.02], [k, k, 0.4 * k], 91)
+    rays["dir"][::7, 1] = np.nan
+    rays["origin"][3::11, 0] = np.nan
+    rays["tMin"][5::13] = rays["tMax"][5::13] = 0.25 * k          # empty interval
+    rays["tMin"][6::13] = np.float32(0.5 * k)
+    rays["tMax"][6::13] = np.float32(0.1 * k)                      # tMin > tMax
+    h_rays = pinned(len(rays), P.RAY_IN_DTYPE)
+    h_rays[:] = rays
+    outs = []
+    ids = []
+    for _ in range(3):
+        out = pinned(len(rays) * 16, np.uint8)
+        out[:] = 0xAB
+        outs.append(out)
+        ids.append(server.submit_rays(sid, h_rays, out, REQ_CLOSEST))
+    assert server.cancel(ids[2]) is True                           # still queued behind the render
+    assert server.cancel(ids[2]) is True                           # cancelling twice is harmless
+    with pytest.raises(P.PheError) as e:
+        server.wait(ids[2])
+    assert e.value.status == 11
+    server.wait(first)
+    server.wait(ids[0])
+    server.wait(ids[1])
+    assert server.cancel(ids[0]) is False                          # completed: nothing to cancel
+    assert np.all(outs[2] == 0xAB)
+    d_rays = torch.from_numpy(rays.view(np.uint8)).cuda()
+    d_hits = torch.empty(len(rays) * 16, dtype=torch.uint8, device="cuda")
+    P.cast_closest(scene, d_rays, d_hits, len(rays))
+    torch.cuda.synchronize()
+    want = d_hits.cpu().numpy()
+    assert np.array_equal(outs[0], want) and np.array_equal(outs[1], want)
+    hits = want.view(P.RAY_HIT_DTYPE)
+    assert np.all(hits["triangleIndex"][5::13] == 0xFFFFFFFF) and np.all(hits["triangleIndex"][6::13] == 0xFFFFFFFF)
+    with pytest.raises(P.PheError) as e:
+        server.submit_rays(sid + 5, h_rays, outs[2], REQ_CLOSEST)
+    assert e.value.status == 7
+    with pytest.raises(P.PheError) as e:
+        server.submit_rays(sid, h_rays[:0], outs[2], REQ_CLOSEST)
+    assert e.value.status == 1
+    server.close()
