@@ -28,6 +28,11 @@ NVCC_FLAGS = ARCH + [
 CXX_FLAGS = ["-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-std=c++17", f"-I{ROOT / 'include'}"]
 
 
+def _cuda_include() -> str:
+    """The toolkit's include directory (host files use its header-only NVTX)."""
+    return str(Path(_nvcc()).resolve().parent.parent / "include")
+
+
 def _nvcc() -> str:
     for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
         if cand and Path(cand).exists():
@@ -67,7 +72,8 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     for src in cpp:
         obj = BUILD / (src.stem + ".cpp.o")
         objs.append(obj)
-        jobs.append(([cxx, *CXX_FLAGS, "-c", str(src), "-o", str(obj)], BUILD / (src.stem + ".cpp.log")))
+        jobs.append(([cxx, *CXX_FLAGS, f"-I{_cuda_include()}", "-c", str(src), "-o", str(obj)],
+                     BUILD / (src.stem + ".cpp.log")))
     with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
         list(ex.map(lambda j: _compile(*j), jobs))
     tmp = LIB.with_suffix(".so.tmp")

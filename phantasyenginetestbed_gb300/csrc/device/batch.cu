@@ -286,6 +286,7 @@ static phe_status batch_enqueue(phe_batch* b, cudaStream_t stream)
 extern "C" phe_status phe_batch_launch(phe_batch* b, void* stream)
 {
 	if (!b) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_batch_launch: null batch");
+	NvtxRange range("phe_batch_launch");
 	cudaStream_t s = (cudaStream_t)stream;
 	if (!b->params.useGraph) return batch_enqueue(b, s);
 	if (!b->graph) {

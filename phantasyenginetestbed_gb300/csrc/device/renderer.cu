@@ -400,6 +400,7 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 	if (!r->scene) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_render: no static scene");
 	if (!r->resX) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_render: no target resolution");
 	if (!r->cameraSet) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_render: no camera");
+	NvtxRange range("phe_renderer_render");
 	if (!r->scene->dev.materials)
 		return fail(PHE_ERR_INVALID_SCENE, "phe_renderer_render: the scene has no materials");
 	if (numLights > kMaxLights) return fail(PHE_ERR_TOO_LARGE, "at most %u lights", kMaxLights);

@@ -234,6 +234,7 @@ extern "C" phe_status phe_scene_create(const phe_bvh_node* nodes, uint32_t numNo
                                        uint32_t numMaterials, int where, phe_scene** out)
 {
 	if (!out) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_scene_create: out is null");
+	NvtxRange range("phe_scene_create");
 	*out = nullptr;
 	if (!nodes || !verts || numNodes == 0 || numSlots == 0)
 		return fail(PHE_ERR_INVALID_ARGUMENT, "phe_scene_create: empty scene");

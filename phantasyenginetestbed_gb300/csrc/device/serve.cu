@@ -163,6 +163,7 @@ phe_status admit_query(phe_server* s, Request* r)
 // Launches one wave over every admitted query (called with the lock held).
 phe_status launch_wave(phe_server* s, Wave& w)
 {
+	NvtxRange range("phe_server wave");
 	uint32_t n = (uint32_t)std::min<size_t>(s->admitted.size(), kMaxWaveItems);
 	uint32_t base = 0;
 	for (uint32_t i = 0; i < n; i++) {

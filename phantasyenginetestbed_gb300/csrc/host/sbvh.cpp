@@ -540,6 +540,7 @@ extern "C" phe_status phe_sbvh_build(const float* triVerts, uint32_t numTris, co
 {
 	if (!triVerts || !out) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_sbvh_build: null argument");
 	if (numTris == 0) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_sbvh_build: no triangles");
+	NvtxRange range("phe_sbvh_build");
 	*out = nullptr;
 	Builder b;
 	b.verts = triVerts;
