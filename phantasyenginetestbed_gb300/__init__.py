@@ -177,6 +177,13 @@ class Scene:
         check(lib().phe_scene_get_layout(self.handle, C.byref(lay), C.byref(avail)), "phe_scene_get_layout")
         return int(lay.value), bool(avail.value)
 
+    def status(self) -> int:
+        """Error bits raised by kernels on this scene so far (1 = traversal stack overflow, 2 = index
+        outside its array, which only the checked build tests); 0 when every traversal was sound."""
+        bits = C.c_uint32()
+        check(lib().phe_scene_status(self.handle, C.byref(bits)), "phe_scene_status")
+        return int(bits.value)
+
     def device_bytes(self) -> int:
         b = C.c_uint64()
         check(lib().phe_scene_device_bytes(self.handle, C.byref(b)), "phe_scene_device_bytes")

@@ -19,6 +19,7 @@ ROOT = PKG.parent
 CSRC = PKG / "csrc"
 BUILD = PKG / "_build"
 LIB = PKG / "libphe_gb300.so"
+CHECKED_LIB = PKG / "libphe_gb300_checked.so"
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + [
@@ -53,37 +54,42 @@ def _compile(cmd: list[str], log: Path) -> None:
         raise RuntimeError(f"compile failed: {' '.join(cmd)}\n{res.stdout}\n{res.stderr}")
 
 
-def build(force: bool = False, verbose: bool = False) -> Path:
-    """Builds libphe_gb300.so next to this file and returns its path."""
+def build(force: bool = False, verbose: bool = False, checked: bool = False) -> Path:
+    """Builds libphe_gb300.so next to this file and returns its path. `checked` builds
+    libphe_gb300_checked.so instead: the same sources with PHE_DEVICE_CHECKS=1 (device-side index
+    checks in every traversal that set an error bit instead of reading out of bounds)."""
     nvcc = _nvcc()
     cu, cpp = sources()
+    lib = CHECKED_LIB if checked else LIB
+    build_dir = BUILD / "checked" if checked else BUILD
+    defs = ["-DPHE_DEVICE_CHECKS=1"] if checked else []
     headers = list(CSRC.rglob("*.cuh")) + list(CSRC.rglob("*.hpp")) + list((ROOT / "include").glob("*.h"))
     newest_dep = max(p.stat().st_mtime for p in cu + cpp + headers + [Path(__file__)])
-    if LIB.exists() and not force and LIB.stat().st_mtime >= newest_dep:
-        return LIB
-    BUILD.mkdir(exist_ok=True)
+    if lib.exists() and not force and lib.stat().st_mtime >= newest_dep:
+        return lib
+    build_dir.mkdir(parents=True, exist_ok=True)
     jobs = []
     objs = []
     for src in cu:
-        obj = BUILD / (src.stem + ".cu.o")
+        obj = build_dir / (src.stem + ".cu.o")
         objs.append(obj)
-        jobs.append(([nvcc, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)], BUILD / (src.stem + ".cu.log")))
+        jobs.append(([nvcc, *NVCC_FLAGS, *defs, "-c", str(src), "-o", str(obj)], build_dir / (src.stem + ".cu.log")))
     cxx = os.environ.get("CXX", "g++")
     for src in cpp:
-        obj = BUILD / (src.stem + ".cpp.o")
+        obj = build_dir / (src.stem + ".cpp.o")
         objs.append(obj)
-        jobs.append(([cxx, *CXX_FLAGS, f"-I{_cuda_include()}", "-c", str(src), "-o", str(obj)],
-                     BUILD / (src.stem + ".cpp.log")))
+        jobs.append(([cxx, *CXX_FLAGS, *defs, f"-I{_cuda_include()}", "-c", str(src), "-o", str(obj)],
+                     build_dir / (src.stem + ".cpp.log")))
     with ThreadPoolExecutor(max_workers=min(16, os.cpu_count() or 4)) as ex:
         list(ex.map(lambda j: _compile(*j), jobs))
-    tmp = LIB.with_suffix(".so.tmp")
-    _compile([nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lpthread"], BUILD / "link.log")
-    os.replace(tmp, LIB)
+    tmp = lib.with_suffix(".so.tmp")
+    _compile([nvcc, *ARCH, "-shared", "-o", str(tmp), *map(str, objs), "-lpthread"], build_dir / "link.log")
+    os.replace(tmp, lib)
     if verbose:
-        for log in sorted(BUILD.glob("*.cu.log")):
+        for log in sorted(build_dir.glob("*.cu.log")):
             sys.stdout.write(log.read_text())
-    return LIB
+    return lib
 
 
 if __name__ == "__main__":
-    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build(force="--force" in sys.argv, verbose="-v" in sys.argv, checked="--checked" in sys.argv))

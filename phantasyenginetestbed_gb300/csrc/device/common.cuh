@@ -64,6 +64,20 @@ constexpr int32_t kSentinel = 0x7FFFFFFF;
 
 // Error bits written to the per-launch status word.
 constexpr uint32_t kErrStackOverflow = 1u;
+constexpr uint32_t kErrBadIndex = 2u;   // checked build: a node or slot index outside its array
+
+// The checked build (-DPHE_DEVICE_CHECKS=1, libphe_gb300_checked.so) tests every node and slot index a
+// traversal is about to read against the array sizes; an index outside sets kErrBadIndex and ends that
+// ray (no trap, no out-of-bounds access). The normal build relies on the host validation of the tree
+// done at upload, and these tests compile away.
+#ifndef PHE_DEVICE_CHECKS
+#define PHE_DEVICE_CHECKS 0
+#endif
+constexpr bool kDeviceChecks = PHE_DEVICE_CHECKS != 0;
+struct TraversalBounds {
+	uint32_t numNodes;   // nodes of the layout being traversed (binary or 4-wide)
+	uint32_t numSlots;
+};
 
 struct f3 { float x, y, z; };
 

@@ -67,7 +67,7 @@ struct HitRecord {
 // Returns the error bits (0, or kErrStackOverflow when the stack would overflow).
 template <bool SAFE, bool ANY>
 __device__ __forceinline__ uint32_t traverse(const float4* __restrict__ nodes, const float4* __restrict__ tris,
-                                             const RayState& r, HitRecord& hit)
+                                             const TraversalBounds& bd, const RayState& r, HitRecord& hit)
 {
 	int32_t stack[kStackSize];
 	int sp = 0;
@@ -78,6 +78,12 @@ __device__ __forceinline__ uint32_t traverse(const float4* __restrict__ nodes, c
 
 	while (nodeAddr != kSentinel) {
 		while (nodeAddr >= 0 && nodeAddr != kSentinel) {
+			if (kDeviceChecks && (uint32_t)nodeAddr >= bd.numNodes) {
+				err |= kErrBadIndex;
+				nodeAddr = kSentinel;
+				leafAddr = 0;
+				break;
+			}
 			const float4* np = nodes + 4 * (size_t)nodeAddr;
 			float4 b0 = __ldg(np), b1 = __ldg(np + 1), b2 = __ldg(np + 2);
 			int4 ix = __ldg(reinterpret_cast<const int4*>(np + 3));
@@ -113,6 +119,12 @@ __device__ __forceinline__ uint32_t traverse(const float4* __restrict__ nodes, c
 		while (leafAddr < 0) {
 			int32_t slot = ~leafAddr;
 			for (;;) {
+				if (kDeviceChecks && (uint32_t)slot >= bd.numSlots) {
+					err |= kErrBadIndex;
+					nodeAddr = kSentinel;
+					leafAddr = 0;
+					break;
+				}
 				const float4* tp = tris + 3 * (size_t)slot;
 				float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
 				float t, u, v;
@@ -130,7 +142,7 @@ __device__ __forceinline__ uint32_t traverse(const float4* __restrict__ nodes, c
 				if (a.w < 0.0f) break;
 				slot++;
 			}
-			if (ANY && nodeAddr == kSentinel && leafAddr == 0) break;
+			if ((ANY || kDeviceChecks) && nodeAddr == kSentinel && leafAddr == 0) break;
 			leafAddr = nodeAddr;
 			if (nodeAddr < 0) nodeAddr = stack[sp--];
 		}
@@ -169,7 +181,7 @@ __device__ __forceinline__ void cswap(float& ka, int32_t& pa, float& kb, int32_t
 // only if the skipped binary test would pass too: the set of reachable leaves is the binary one.
 template <bool ANY>
 __device__ __forceinline__ uint32_t traverse4(const float4* __restrict__ nodes4, const float4* __restrict__ tris,
-                                              const RayState& r, HitRecord& hit)
+                                              const TraversalBounds& bd, const RayState& r, HitRecord& hit)
 {
 	int32_t stack[kStackSize4];
 	int sp = 0;
@@ -181,6 +193,12 @@ __device__ __forceinline__ uint32_t traverse4(const float4* __restrict__ nodes4,
 
 	while (nodeAddr != kSentinel) {
 		while (nodeAddr >= 0 && nodeAddr != kSentinel) {
+			if (kDeviceChecks && (uint32_t)nodeAddr >= bd.numNodes) {
+				err |= kErrBadIndex;
+				nodeAddr = kSentinel;
+				leafAddr = 0;
+				break;
+			}
 			const float4* np = nodes4 + 8 * (size_t)nodeAddr;
 			float4 lx = __ldg(np), ly = __ldg(np + 1), lz = __ldg(np + 2);
 			float4 hx = __ldg(np + 3), hy = __ldg(np + 4), hz = __ldg(np + 5);
@@ -232,6 +250,12 @@ __device__ __forceinline__ uint32_t traverse4(const float4* __restrict__ nodes4,
 		while (leafAddr < 0) {
 			int32_t slot = ~leafAddr;
 			for (;;) {
+				if (kDeviceChecks && (uint32_t)slot >= bd.numSlots) {
+					err |= kErrBadIndex;
+					nodeAddr = kSentinel;
+					leafAddr = 0;
+					break;
+				}
 				const float4* tp = tris + 3 * (size_t)slot;
 				float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
 				float t, u, v;
@@ -249,7 +273,7 @@ __device__ __forceinline__ uint32_t traverse4(const float4* __restrict__ nodes4,
 				if (a.w < 0.0f) break;
 				slot++;
 			}
-			if (ANY && nodeAddr == kSentinel && leafAddr == 0) break;
+			if ((ANY || kDeviceChecks) && nodeAddr == kSentinel && leafAddr == 0) break;
 			leafAddr = nodeAddr;
 			if (nodeAddr < 0) nodeAddr = stack[sp--];
 		}
@@ -265,11 +289,11 @@ __device__ __forceinline__ uint32_t trace(const DeviceScene& s, const RayState& 
 {
 	if (r.safe) {
 		if constexpr (WIDE) {
-			if (s.nodes4) return traverse4<ANY>(s.nodes4, s.tris, r, hit);
+			if (s.nodes4) return traverse4<ANY>(s.nodes4, s.tris, TraversalBounds{s.numNodes4, s.numSlots}, r, hit);
 		}
-		return traverse<true, ANY>(s.nodes, s.tris, r, hit);
+		return traverse<true, ANY>(s.nodes, s.tris, TraversalBounds{s.numNodes, s.numSlots}, r, hit);
 	}
-	return traverse<false, ANY>(s.nodes, s.tris, r, hit);
+	return traverse<false, ANY>(s.nodes, s.tris, TraversalBounds{s.numNodes, s.numSlots}, r, hit);
 }
 
 __device__ __forceinline__ void store_hit(phe_ray_hit* __restrict__ hits, uint32_t i, const RayState& r, const HitRecord& h)
@@ -297,10 +321,17 @@ namespace phe_gb300 {
 // ------------------------------------------------------------------------------------------------
 template <bool ANY, bool SAFE>
 __device__ __forceinline__ void trace_step(const float4* __restrict__ nodes, const float4* __restrict__ tris,
-                                           const RayState& r, HitRecord& hit, int32_t* stack, int& sp,
-                                           int32_t& nodeAddr, int32_t& leafAddr, uint32_t& err)
+                                           const TraversalBounds& bd, const RayState& r, HitRecord& hit,
+                                           int32_t* stack, int& sp, int32_t& nodeAddr, int32_t& leafAddr,
+                                           uint32_t& err)
 {
 	while (nodeAddr >= 0 && nodeAddr != kSentinel) {
+		if (kDeviceChecks && (uint32_t)nodeAddr >= bd.numNodes) {
+			err |= kErrBadIndex;
+			nodeAddr = kSentinel;
+			leafAddr = 0;
+			return;
+		}
 		const float4* np = nodes + 4 * (size_t)nodeAddr;
 		float4 b0 = __ldg(np), b1 = __ldg(np + 1), b2 = __ldg(np + 2);
 		int4 ix = __ldg(reinterpret_cast<const int4*>(np + 3));
@@ -335,6 +366,12 @@ __device__ __forceinline__ void trace_step(const float4* __restrict__ nodes, con
 	while (leafAddr < 0) {
 		int32_t slot = ~leafAddr;
 		for (;;) {
+			if (kDeviceChecks && (uint32_t)slot >= bd.numSlots) {
+				err |= kErrBadIndex;
+				nodeAddr = kSentinel;
+				leafAddr = 0;
+				return;
+			}
 			const float4* tp = tris + 3 * (size_t)slot;
 			float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
 			float t, u, v;
@@ -359,7 +396,8 @@ __device__ __forceinline__ void trace_step(const float4* __restrict__ nodes, con
 
 template <bool ANY, class Source, class Sink>
 __device__ __forceinline__ uint32_t persistent_trace(const float4* __restrict__ nodes, const float4* __restrict__ tris,
-                                                     const Source& src, const Sink& sink, uint32_t n,
+                                                     const TraversalBounds& bd, const Source& src, const Sink& sink,
+                                                     uint32_t n,
                                                      uint32_t* __restrict__ counter, int refill)
 {
 	const uint32_t lane = threadIdx.x & 31u;
@@ -402,12 +440,12 @@ __device__ __forceinline__ uint32_t persistent_trace(const float4* __restrict__ 
 		if (hasRay) {
 			if (r.safe) {
 				while (nodeAddr != kSentinel) {
-					trace_step<ANY, true>(nodes, tris, r, h, stack, sp, nodeAddr, leafAddr, err);
+					trace_step<ANY, true>(nodes, tris, bd, r, h, stack, sp, nodeAddr, leafAddr, err);
 					if (__popc(__activemask()) < refill) break;
 				}
 			} else {
 				while (nodeAddr != kSentinel) {
-					trace_step<ANY, false>(nodes, tris, r, h, stack, sp, nodeAddr, leafAddr, err);
+					trace_step<ANY, false>(nodes, tris, bd, r, h, stack, sp, nodeAddr, leafAddr, err);
 					if (__popc(__activemask()) < refill) break;
 				}
 			}

@@ -402,7 +402,7 @@ struct VisibilitySink {
 __global__ void __launch_bounds__(kWaveBlock) primary_trace_kernel(DeviceScene s, const FrameParamsDev* __restrict__ fpp,
                                                                    FrameBuffers fb, uint32_t* __restrict__ status)
 {
-	uint32_t err = persistent_trace<false>(s.nodes, s.tris, CameraSource{fpp}, HitSink{fb.primaryHits}, fpp->numPixels,
+	uint32_t err = persistent_trace<false>(s.nodes, s.tris, TraversalBounds{s.numNodes, s.numSlots}, CameraSource{fpp}, HitSink{fb.primaryHits}, fpp->numPixels,
 	                                       fb.counters + kCtrWork0, fb.refill);
 	if (err) atomicOr(status, err);
 }
@@ -413,14 +413,14 @@ __global__ void __launch_bounds__(kWaveBlock) any_refill_kernel(DeviceScene s, c
                                                                 uint8_t* __restrict__ inLight, uint32_t* __restrict__ work,
                                                                 int refill, uint32_t* __restrict__ status)
 {
-	uint32_t err = persistent_trace<true>(s.nodes, s.tris, ArraySource{rays, nullptr}, VisibilitySink{inLight, slots}, *count,
+	uint32_t err = persistent_trace<true>(s.nodes, s.tris, TraversalBounds{s.numNodes, s.numSlots}, ArraySource{rays, nullptr}, VisibilitySink{inLight, slots}, *count,
 	                                      work, refill);
 	if (err) atomicOr(status, err);
 }
 
 __global__ void __launch_bounds__(kWaveBlock) bounce_trace_kernel(DeviceScene s, FrameBuffers fb, uint32_t* __restrict__ status)
 {
-	uint32_t err = persistent_trace<false>(s.nodes, s.tris, ArraySource{fb.bounceRays, fb.sortWindow > 0 ? fb.bouncePerm : nullptr},
+	uint32_t err = persistent_trace<false>(s.nodes, s.tris, TraversalBounds{s.numNodes, s.numSlots}, ArraySource{fb.bounceRays, fb.sortWindow > 0 ? fb.bouncePerm : nullptr},
 	                                       HitSink{fb.bounceHits},
 	                                       fb.counters[kCtrBounce], fb.counters + kCtrWork1, fb.refill);
 	if (err) atomicOr(status, err);

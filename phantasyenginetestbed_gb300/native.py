@@ -6,11 +6,15 @@ loudly when the library has not been built (``python -m phantasyenginetestbed_gb
 from __future__ import annotations
 
 import ctypes as C
+import os
 from pathlib import Path
 
 import numpy as np
 
-LIB_PATH = Path(__file__).resolve().parent / "libphe_gb300.so"
+# PHE_GB300_CHECKED=1 selects the checked build (device-side index checks, libphe_gb300_checked.so,
+# built with `python -m phantasyenginetestbed_gb300.build --checked`).
+CHECKED = os.environ.get("PHE_GB300_CHECKED") == "1"
+LIB_PATH = Path(__file__).resolve().parent / ("libphe_gb300_checked.so" if CHECKED else "libphe_gb300.so")
 
 # Status codes (include/phe_gb300.h).
 PHE_OK = 0
@@ -206,7 +210,8 @@ def lib() -> C.CDLL:
     global _lib
     if _lib is None:
         if not LIB_PATH.exists():
-            raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -m phantasyenginetestbed_gb300.build`")
+            raise RuntimeError(f"{LIB_PATH} is missing: build it with `python -m phantasyenginetestbed_gb300.build"
+                               f"{' --checked' if CHECKED else ''}`")
         L = C.CDLL(str(LIB_PATH))
         for name, (res, args) in SIGNATURES.items():
             fn = getattr(L, name)

@@ -135,6 +135,7 @@ def test_closest_and_any_full_size_vs_oracle(name):
     orc_any = O.any_rays(b.nodes, b.verts, sh)
     assert np.array_equal(gpu_any, orc_any)
     assert 0.05 < orc_any.mean() < 0.999
+    assert scene.status() == 0          # no stack overflow; in the checked build, no index out of range
 
 
 def test_edge_cases():
