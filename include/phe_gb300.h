@@ -157,7 +157,10 @@ phe_status phe_bvh_validate(const phe_bvh_node* nodes, uint32_t numNodes, uint32
 
 /* BVH cache file (testbed_application/Main.cpp:105-154): three headerless raw arrays
  * <base>_nodes.bin, <base>_verts.bin, <base>_datas.bin. Read sizes come from the file sizes;
- * datas must have as many entries as verts (the reference's only check, Main.cpp:131-133). */
+ * datas must have as many entries as verts (the reference's only check, Main.cpp:131-133). Writes
+ * also put <base>_header.bin beside them (magic, version, record sizes, counts, a 64-bit checksum of
+ * each array); a read verifies it when it exists (PHE_ERR_INVALID_SCENE on a mismatch) and reads
+ * caches without one, as the reference writes them, unchecked. */
 phe_status phe_bvh_cache_write(const char* basePath, const phe_bvh_node* nodes, uint32_t numNodes,
                                const phe_triangle_vertices* verts, const phe_triangle_data* datas, uint32_t numSlots);
 phe_status phe_bvh_cache_sizes(const char* basePath, uint32_t* numNodes, uint32_t* numSlots);

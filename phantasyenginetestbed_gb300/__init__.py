@@ -25,7 +25,7 @@ from .native import (LIGHT_DTYPE, MATERIAL_DTYPE, NODE_DTYPE, RAY_HIT_DTYPE, RAY
 
 __all__ = [
     "CameraDef", "PheError", "Scene", "HostBVH", "SceneArrays", "generate_scene", "build_sbvh", "camera_def",
-    "halton_jitter", "cast_closest", "cast_closest_plain", "cast_any", "gen_primary_rays", "STANDARD_SCENES",
+    "halton_jitter", "write_bvh_cache", "read_bvh_cache", "cast_closest", "cast_closest_plain", "cast_any", "gen_primary_rays", "STANDARD_SCENES",
     "NODE_DTYPE", "TRI_VERTS_DTYPE", "TRI_DATA_DTYPE", "RAY_IN_DTYPE", "RAY_HIT_DTYPE", "MATERIAL_DTYPE", "LIGHT_DTYPE",
 ]
 
@@ -100,6 +100,26 @@ def build_sbvh(tri_verts: np.ndarray, threads: int = 0, split_alpha: float = 1e-
     finally:
         lib().phe_host_bvh_free(h)
     return HostBVH(nodes, verts, s2t, int(md.value))
+
+
+def write_bvh_cache(base: str, bvh: HostBVH, slot_datas: np.ndarray) -> None:
+    """The reference's three-file BVH cache (Main.cpp:105-154) plus a checksummed header file."""
+    datas = np.ascontiguousarray(slot_datas)
+    assert datas.dtype == TRI_DATA_DTYPE and len(datas) == len(bvh.verts)
+    check(lib().phe_bvh_cache_write(str(base).encode(), ptr(bvh.nodes), len(bvh.nodes), ptr(bvh.verts), ptr(datas),
+                                    len(bvh.verts)), "phe_bvh_cache_write")
+
+
+def read_bvh_cache(base: str):
+    """(nodes, slot vertices, slot datas) of a cache; verified against its header when it has one."""
+    nn, ns = C.c_uint32(), C.c_uint32()
+    b = str(base).encode()
+    check(lib().phe_bvh_cache_sizes(b, C.byref(nn), C.byref(ns)), "phe_bvh_cache_sizes")
+    nodes = np.empty(nn.value, NODE_DTYPE)
+    verts = np.empty(ns.value, TRI_VERTS_DTYPE)
+    datas = np.empty(ns.value, TRI_DATA_DTYPE)
+    check(lib().phe_bvh_cache_read(b, ptr(nodes), nn.value, ptr(verts), ptr(datas), ns.value), "phe_bvh_cache_read")
+    return nodes, verts, datas
 
 
 def validate_bvh(nodes: np.ndarray, num_slots: int) -> int:

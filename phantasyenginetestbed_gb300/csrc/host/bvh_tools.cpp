@@ -62,7 +62,10 @@ extern "C" phe_status phe_bvh_validate(const phe_bvh_node* nodes, uint32_t numNo
 }
 
 // ------------------------------------------------------------------------------------------------
-// BVH cache (testbed_application/Main.cpp:105-154): three raw dumps, no header.
+// BVH cache (testbed_application/Main.cpp:105-154): three raw dumps, no header, so that caches move
+// between the reference and this library unchanged. Beside them this library writes
+// <base>_header.bin: magic, version, record sizes, counts and a 64-bit checksum of each dump. A
+// cache read verifies it when present (a reference-written cache has none and is read as is).
 
 static std::string cachePath(const char* base, const char* suffix) { return std::string(base) + suffix; }
 
@@ -98,6 +101,36 @@ static phe_status readFile(const std::string& path, void* data, size_t bytes)
 	return PHE_OK;
 }
 
+namespace {
+
+struct CacheHeader {
+	char magic[8];          // "PHEBVHC\0"
+	uint32_t version;       // 1
+	uint32_t nodeBytes, vertBytes, dataBytes;   // record sizes: 64, 48, 64
+	uint32_t numNodes, numSlots;
+	uint64_t sumNodes, sumVerts, sumDatas;      // checksum64 of each dump
+};
+static_assert(sizeof(CacheHeader) == 56, "cache header is 56 bytes");
+constexpr char kCacheMagic[8] = {'P', 'H', 'E', 'B', 'V', 'H', 'C', 0};
+
+// FNV-1a over little-endian 64-bit words (then the tail bytes), the word count mixed in at the end.
+uint64_t checksum64(const void* data, size_t bytes)
+{
+	const uint64_t prime = 0x100000001b3ull;
+	uint64_t h = 0xcbf29ce484222325ull;
+	const unsigned char* p = static_cast<const unsigned char*>(data);
+	size_t words = bytes / 8;
+	for (size_t i = 0; i < words; i++) {
+		uint64_t w = 0;
+		for (int k = 7; k >= 0; k--) w = (w << 8) | p[8 * i + (size_t)k];
+		h = (h ^ w) * prime;
+	}
+	for (size_t i = words * 8; i < bytes; i++) h = (h ^ p[i]) * prime;
+	return (h ^ (uint64_t)bytes) * prime;
+}
+
+} // namespace
+
 extern "C" phe_status phe_bvh_cache_write(const char* base, const phe_bvh_node* nodes, uint32_t numNodes,
                                           const phe_triangle_vertices* verts, const phe_triangle_data* datas,
                                           uint32_t numSlots)
@@ -107,7 +140,20 @@ extern "C" phe_status phe_bvh_cache_write(const char* base, const phe_bvh_node* 
 	if (s) return s;
 	s = writeFile(cachePath(base, "_verts.bin"), verts, sizeof(phe_triangle_vertices) * (size_t)numSlots);
 	if (s) return s;
-	return writeFile(cachePath(base, "_datas.bin"), datas, sizeof(phe_triangle_data) * (size_t)numSlots);
+	s = writeFile(cachePath(base, "_datas.bin"), datas, sizeof(phe_triangle_data) * (size_t)numSlots);
+	if (s) return s;
+	CacheHeader h{};
+	std::memcpy(h.magic, kCacheMagic, sizeof(h.magic));
+	h.version = 1;
+	h.nodeBytes = sizeof(phe_bvh_node);
+	h.vertBytes = sizeof(phe_triangle_vertices);
+	h.dataBytes = sizeof(phe_triangle_data);
+	h.numNodes = numNodes;
+	h.numSlots = numSlots;
+	h.sumNodes = checksum64(nodes, sizeof(phe_bvh_node) * (size_t)numNodes);
+	h.sumVerts = checksum64(verts, sizeof(phe_triangle_vertices) * (size_t)numSlots);
+	h.sumDatas = checksum64(datas, sizeof(phe_triangle_data) * (size_t)numSlots);
+	return writeFile(cachePath(base, "_header.bin"), &h, sizeof(h));
 }
 
 extern "C" phe_status phe_bvh_cache_sizes(const char* base, uint32_t* numNodes, uint32_t* numSlots)
@@ -138,7 +184,27 @@ extern "C" phe_status phe_bvh_cache_read(const char* base, phe_bvh_node* nodes, 
 		            nn, nsl, numNodes, numSlots);
 	if ((s = readFile(cachePath(base, "_nodes.bin"), nodes, sizeof(phe_bvh_node) * (size_t)nn))) return s;
 	if ((s = readFile(cachePath(base, "_verts.bin"), verts, sizeof(phe_triangle_vertices) * (size_t)nsl))) return s;
-	return readFile(cachePath(base, "_datas.bin"), datas, sizeof(phe_triangle_data) * (size_t)nsl);
+	if ((s = readFile(cachePath(base, "_datas.bin"), datas, sizeof(phe_triangle_data) * (size_t)nsl))) return s;
+	uint64_t hs = 0;
+	if (fileSize(cachePath(base, "_header.bin"), &hs) != PHE_OK) {
+		clear_error();
+		return PHE_OK;   // no header: a cache written by the reference
+	}
+	CacheHeader h{};
+	if (hs != sizeof(h) || (s = readFile(cachePath(base, "_header.bin"), &h, sizeof(h))))
+		return fail(PHE_ERR_INVALID_SCENE, "BVH cache %s: unreadable header", base);
+	if (std::memcmp(h.magic, kCacheMagic, sizeof(h.magic)) != 0 || h.version != 1 ||
+	    h.nodeBytes != sizeof(phe_bvh_node) || h.vertBytes != sizeof(phe_triangle_vertices) ||
+	    h.dataBytes != sizeof(phe_triangle_data))
+		return fail(PHE_ERR_INVALID_SCENE, "BVH cache %s: unknown header format", base);
+	if (h.numNodes != nn || h.numSlots != nsl)
+		return fail(PHE_ERR_INVALID_SCENE, "BVH cache %s: header counts %u / %u, files hold %u / %u", base, h.numNodes,
+		            h.numSlots, nn, nsl);
+	if (h.sumNodes != checksum64(nodes, sizeof(phe_bvh_node) * (size_t)nn) ||
+	    h.sumVerts != checksum64(verts, sizeof(phe_triangle_vertices) * (size_t)nsl) ||
+	    h.sumDatas != checksum64(datas, sizeof(phe_triangle_data) * (size_t)nsl))
+		return fail(PHE_ERR_INVALID_SCENE, "BVH cache %s: checksum mismatch (a file changed after it was written)", base);
+	return PHE_OK;
 }
 
 // ------------------------------------------------------------------------------------------------

@@ -168,6 +168,31 @@ def test_bvh_cache_round_trip(tmp_path):
     d2 = np.empty(ns.value, P.TRI_DATA_DTYPE)
     native.check(L.phe_bvh_cache_read(base, native.ptr(n2), nn.value, native.ptr(v2), native.ptr(d2), ns.value), "read")
     assert n2.tobytes() == b.nodes.tobytes() and v2.tobytes() == b.verts.tobytes() and d2.tobytes() == datas.tobytes()
+    assert (tmp_path / "scene_header.bin").stat().st_size == 56
+
+    def read():
+        native.check(L.phe_bvh_cache_read(base, native.ptr(n2), nn.value, native.ptr(v2), native.ptr(d2), ns.value),
+                     "read")
+
+    # one flipped bit in an array is caught by the header's checksum ...
+    raw = bytearray((tmp_path / "scene_verts.bin").read_bytes())
+    raw[len(raw) // 2] ^= 0x10
+    (tmp_path / "scene_verts.bin").write_bytes(bytes(raw))
+    with pytest.raises(P.PheError) as e:
+        read()
+    assert e.value.status == 2 and "checksum" in str(e.value)
+    # ... and a cache without the header (as the reference writes them) is read unchecked
+    (tmp_path / "scene_header.bin").unlink()
+    read()
+    assert v2.tobytes() == bytes(raw)
+    # a header of other counts is refused
+    native.check(L.phe_bvh_cache_write(base, native.ptr(b.nodes), len(b.nodes), native.ptr(b.verts),
+                                       native.ptr(datas), len(b.verts)), "write")
+    hdr = bytearray((tmp_path / "scene_header.bin").read_bytes())
+    hdr[24] ^= 1                      # numNodes
+    (tmp_path / "scene_header.bin").write_bytes(bytes(hdr))
+    with pytest.raises(P.PheError):
+        read()
     # the reference's only check: vertex and data counts agree
     (tmp_path / "scene_datas.bin").write_bytes(d2[:-1].tobytes())
     with pytest.raises(P.PheError):
@@ -195,3 +220,14 @@ def test_persistent_launch_size_limit_is_checked_before_any_device_work():
     assert L.phe_cast_closest(fake, fake, fake, 0xFC000001, None) == 8
     assert L.phe_cast_any(fake, fake, fake, 0xFFFFFFFF, None, None) == 8
     assert "rays per launch" in L.phe_last_error().decode()
+
+
+def test_bvh_cache_python_wrappers(tmp_path):
+    s = P.generate_scene(8, 3, True, 5)
+    b = P.build_sbvh(s.tri_verts)
+    datas = b.slot_datas(s.datas)
+    P.write_bvh_cache(tmp_path / "c", b, datas)
+    nodes, verts, d2 = P.read_bvh_cache(tmp_path / "c")
+    assert nodes.tobytes() == b.nodes.tobytes() and verts.tobytes() == b.verts.tobytes()
+    assert d2.tobytes() == datas.tobytes()
+    assert P.validate_bvh(nodes, len(verts)) == b.max_depth
