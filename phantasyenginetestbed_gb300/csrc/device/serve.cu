@@ -427,7 +427,7 @@ extern "C" phe_status phe_server_create(const phe_server_config* cfg, phe_server
 		if ((ps = renderer_reserve(sl.renderer, c.maxRenderPixels, std::max<uint32_t>(1, c.maxLights)))) break;
 	}
 	if (e == cudaSuccess && !ps) {
-		// Keep freed request memory in the stream-ordered pool instead of returning it to the driver.
+		// Keep freed request memory in the stream-ordered pool instead of returning it to the CUDA driver.
 		cudaMemPool_t pool;
 		if (cudaDeviceGetDefaultMemPool(&pool, s->device) == cudaSuccess) {
 			uint64_t keep = UINT64_MAX;
