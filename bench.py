@@ -375,10 +375,17 @@ def run_ours(args, world, rank, local):
         peak_src = "measured"
     else:
         peak, peak_src = 6800.0, "fallback"
-    traffic = None
+    traffic, issue = None, None
     tpath = ROOT / "profiles" / "ncu_traffic.json"
     if tpath.exists():
-        traffic = json.loads(tpath.read_text()).get(dominant)
+        nc = json.loads(tpath.read_text())
+        traffic = nc.get(dominant)
+        if f"{dominant}_inst_per_cycle" in nc:
+            # the limit that binds (the scene is L2-resident): issue, from the committed ncu capture
+            issue = {"inst_per_cycle": nc[f"{dominant}_inst_per_cycle"], "of": 4,
+                     "frac": round(nc[f"{dominant}_inst_per_cycle"] / 4, 3),
+                     "simd_efficiency": nc.get(f"{dominant}_simd_efficiency"),
+                     "dram_frac": nc.get(f"{dominant}_dram_throughput"), "source": "profiles/bounce_kernel_1080p_ncu.md"}
     dom = per_kernel[dominant]
     achieved = dom.get("GB_s")
     lat = sorted(per)
@@ -406,9 +413,11 @@ def run_ours(args, world, rank, local):
         "passes": per_kernel,
         "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": round(achieved / peak, 4) if achieved else None, "traffic": traffic,
-                     "peak_source": peak_src,
+                     "peak_source": peak_src, "issue": issue,
                      "note": "algorithmic bytes = ray I/O + 64 B x nodes + 48 B x triangle tests per ray (oracle "
-                             "castDebugRay means, profiles/work_per_ray.json); most of it is served from L1/L2"},
+                             "castDebugRay means, profiles/work_per_ray.json); the scene is L2-resident, so most of "
+                             "it is served from L1/L2 (traffic = DRAM bytes per launch) and frac is an effective "
+                             "bandwidth; the binding limit is instruction issue (see issue)"},
         "clocks": clocks.summary(),
         "e2e": {"value": round(e2e_value, 2), "unit": "Mrays/s",
                 "h2d_bytes_per_step": int(native.lib().phe_renderer_frame_param_bytes()),
