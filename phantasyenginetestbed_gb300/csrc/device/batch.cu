@@ -79,7 +79,8 @@ static phe_status launch_batch_kernel(const BatchTableDev& t, bool wide, int blo
 {
 	auto kernel = wide ? batch_kernel<BLOCK, true> : batch_kernel<BLOCK, false>;
 	int maxB = 0;
-	PHE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxB, kernel, BLOCK, 0), "occupancy");
+	PHE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxB, kernel, BLOCK, stack_smem_bytes(BLOCK)),
+	             "occupancy");
 	if (occupancyOut) {
 		*occupancyOut = maxB;
 		return PHE_OK;
@@ -89,7 +90,7 @@ static phe_status launch_batch_kernel(const BatchTableDev& t, bool wide, int blo
 	uint32_t grid = (uint32_t)(b * numSMs);
 	uint32_t need = (t.totalPadded + BLOCK - 1) / BLOCK;
 	if (grid > need) grid = need > 0 ? need : 1;
-	kernel<<<grid, BLOCK, 0, stream>>>(t, counter, status);
+	kernel<<<grid, BLOCK, stack_smem_bytes(BLOCK), stream>>>(t, counter, status);
 	PHE_CUDA_TRY(cudaGetLastError(), "batch_kernel launch");
 	return PHE_OK;
 }
@@ -535,12 +536,13 @@ extern "C" phe_status phe_batch_cast_noalloc(const phe_scene* const* scenes, uin
 	PHE_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
 	PHE_CUDA_TRY(cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, dev), "SM count");
 	auto kernel = wide ? batch_kernel<128, true> : batch_kernel<128, false>;
-	PHE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kernel, 128, 0), "occupancy");
+	PHE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kernel, 128, stack_smem_bytes(128)),
+	             "occupancy");
 	uint32_t grid = (uint32_t)(perSM > 0 ? perSM : 1) * (uint32_t)numSMs;
 	uint32_t need = (base + 127u) / 128u;
 	if (grid > need) grid = need;
 	BatchTableDev t{dItems, dScenes, numItems, base};
-	kernel<<<grid, 128, 0, s>>>(t, dCounter, dStatus);
+	kernel<<<grid, 128, stack_smem_bytes(128), s>>>(t, dCounter, dStatus);
 	PHE_CUDA_TRY(cudaGetLastError(), "batch_kernel launch (no-alloc)");
 	return PHE_OK;
 }

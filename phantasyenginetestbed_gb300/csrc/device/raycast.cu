@@ -93,7 +93,8 @@ static phe_status persistent_grid(int which, const void* kernel, int* grid)
 	if (st) return st;
 	if (g_persistentBlocksPerSM[which] == 0) {
 		int b = 0;
-		PHE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, kPersistentBlock, 0), "occupancy");
+		PHE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, kPersistentBlock,
+		                                                           stack_smem_bytes(kPersistentBlock)), "occupancy");
 		g_persistentBlocksPerSM[which] = b > 0 ? b : 1;
 	}
 	*grid = g_persistentBlocksPerSM[which] * d->numSMs;
@@ -121,7 +122,8 @@ extern "C" phe_status phe_cast_closest_plain(const phe_scene* scene, const phe_r
 	if (n == 0) return PHE_OK;
 	uint32_t grid = (n + kPlainBlock - 1) / kPlainBlock;
 	auto kernel = scene->dev.nodes4 ? closest_plain_kernel<true> : closest_plain_kernel<false>;
-	kernel<<<grid, kPlainBlock, 0, (cudaStream_t)stream>>>(scene->dev, rays, hits, n, scene->status);
+	kernel<<<grid, kPlainBlock, stack_smem_bytes(kPlainBlock), (cudaStream_t)stream>>>(scene->dev, rays, hits, n,
+	                                                                                   scene->status);
 	PHE_CUDA_TRY(cudaGetLastError(), "closest_plain_kernel launch");
 	return PHE_OK;
 }
@@ -142,7 +144,9 @@ extern "C" phe_status phe_cast_closest(const phe_scene* scene, const phe_ray_in*
 	if ((uint32_t)grid > maxGrid) grid = (int)maxGrid;
 	uint32_t* counter = nullptr;
 	if ((st = acquire_counter((cudaStream_t)stream, &counter))) return st;
-	kernel<<<grid, kPersistentBlock, 0, (cudaStream_t)stream>>>(scene->dev, rays, hits, n, counter, scene->status);
+	kernel<<<grid, kPersistentBlock, stack_smem_bytes(kPersistentBlock), (cudaStream_t)stream>>>(scene->dev, rays, hits,
+	                                                                                             n, counter,
+	                                                                                             scene->status);
 	PHE_CUDA_TRY(cudaGetLastError(), "closest_persistent_kernel launch");
 	return PHE_OK;
 }
@@ -162,7 +166,9 @@ extern "C" phe_status phe_cast_any(const phe_scene* scene, const phe_ray_in* ray
 	if ((uint32_t)grid > maxGrid) grid = (int)maxGrid;
 	uint32_t* counter = nullptr;
 	if ((st = acquire_counter((cudaStream_t)stream, &counter))) return st;
-	kernel<<<grid, kPersistentBlock, 0, (cudaStream_t)stream>>>(scene->dev, rays, inLight, scatter, n, counter,
+	kernel<<<grid, kPersistentBlock, stack_smem_bytes(kPersistentBlock), (cudaStream_t)stream>>>(scene->dev, rays,
+	                                                                                             inLight, scatter, n,
+	                                                                                             counter,
 	                                                        scene->status);
 	PHE_CUDA_TRY(cudaGetLastError(), "any_persistent_kernel launch");
 	return PHE_OK;

@@ -63,15 +63,44 @@ struct HitRecord {
 	float t, u, v;
 };
 
+// Traversal stack of one thread. The first kSmemStack entries live in shared memory, one column per
+// thread with a stride of the block size, so the 32 lanes of a warp always touch 32 different banks
+// whatever their stack depths; deeper entries spill to a per-thread local array. Kernels that
+// traverse use 1-D blocks and are launched with stack_smem_bytes(blockDim.x) of dynamic shared
+// memory. kSmemStack = 0 keeps the whole stack in local memory (no shared memory).
+#ifndef PHE_SMEM_STACK
+#define PHE_SMEM_STACK 0
+#endif
+constexpr int kSmemStack = PHE_SMEM_STACK;
+static_assert(kSmemStack >= 0 && kSmemStack <= kStackSize, "shared stack depth");
+extern __shared__ int32_t g_stackSmem[];
+inline size_t stack_smem_bytes(int block) { return (size_t)kSmemStack * sizeof(int32_t) * (size_t)block; }
+
+struct TraversalStack {
+	int32_t* col;
+	uint32_t stride;
+	int32_t spill[kStackSize - kSmemStack > 0 ? kStackSize - kSmemStack : 1];
+	__device__ __forceinline__ TraversalStack() : col(g_stackSmem + threadIdx.x), stride(blockDim.x) {}
+	__device__ __forceinline__ void set(int i, int32_t v)
+	{
+		if (kSmemStack > 0 && i < kSmemStack) col[(uint32_t)i * stride] = v;
+		else spill[i - kSmemStack] = v;
+	}
+	__device__ __forceinline__ int32_t get(int i) const
+	{
+		return (kSmemStack > 0 && i < kSmemStack) ? col[(uint32_t)i * stride] : spill[i - kSmemStack];
+	}
+};
+
 // Traverses the scene for one ray. ANY = true stops at the first triangle with tMin <= t < tMax.
 // Returns the error bits (0, or kErrStackOverflow when the stack would overflow).
 template <bool SAFE, bool ANY>
 __device__ __forceinline__ uint32_t traverse(const float4* __restrict__ nodes, const float4* __restrict__ tris,
                                              const TraversalBounds& bd, const RayState& r, HitRecord& hit)
 {
-	int32_t stack[kStackSize];
+	TraversalStack stack;
 	int sp = 0;
-	stack[0] = kSentinel;
+	stack.set(0, kSentinel);
 	int32_t nodeAddr = 0;
 	int32_t leafAddr = 0;
 	uint32_t err = 0;
@@ -91,7 +120,7 @@ __device__ __forceinline__ uint32_t traverse(const float4* __restrict__ nodes, c
 			bool v0 = visit_box<SAFE>(r, b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, hit.t, tIn0);
 			bool v1 = visit_box<SAFE>(r, b1.z, b1.w, b2.x, b2.y, b2.z, b2.w, hit.t, tIn1);
 			if (!v0 && !v1) {
-				nodeAddr = stack[sp--];
+				nodeAddr = stack.get(sp--);
 			} else {
 				nodeAddr = v0 ? ix.x : ix.y;
 				if (v0 && v1) {
@@ -106,12 +135,12 @@ __device__ __forceinline__ uint32_t traverse(const float4* __restrict__ nodes, c
 						leafAddr = 0;
 						break;
 					}
-					stack[++sp] = other;
+					stack.set(++sp, other);
 				}
 			}
 			if (nodeAddr < 0 && leafAddr >= 0) {
 				leafAddr = nodeAddr;
-				nodeAddr = stack[sp--];
+				nodeAddr = stack.get(sp--);
 			}
 			if (!__any_sync(__activemask(), leafAddr >= 0)) break;
 		}
@@ -144,7 +173,7 @@ __device__ __forceinline__ uint32_t traverse(const float4* __restrict__ nodes, c
 			}
 			if ((ANY || kDeviceChecks) && nodeAddr == kSentinel && leafAddr == 0) break;
 			leafAddr = nodeAddr;
-			if (nodeAddr < 0) nodeAddr = stack[sp--];
+			if (nodeAddr < 0) nodeAddr = stack.get(sp--);
 		}
 	}
 	return err;
@@ -322,7 +351,7 @@ namespace phe_gb300 {
 template <bool ANY, bool SAFE>
 __device__ __forceinline__ void trace_step(const float4* __restrict__ nodes, const float4* __restrict__ tris,
                                            const TraversalBounds& bd, const RayState& r, HitRecord& hit,
-                                           int32_t* stack, int& sp, int32_t& nodeAddr, int32_t& leafAddr,
+                                           TraversalStack& stack, int& sp, int32_t& nodeAddr, int32_t& leafAddr,
                                            uint32_t& err)
 {
 	while (nodeAddr >= 0 && nodeAddr != kSentinel) {
@@ -339,7 +368,7 @@ __device__ __forceinline__ void trace_step(const float4* __restrict__ nodes, con
 		bool v0 = visit_box<SAFE>(r, b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, hit.t, tIn0);
 		bool v1 = visit_box<SAFE>(r, b1.z, b1.w, b2.x, b2.y, b2.z, b2.w, hit.t, tIn1);
 		if (!v0 && !v1) {
-			nodeAddr = stack[sp--];
+			nodeAddr = stack.get(sp--);
 		} else {
 			nodeAddr = v0 ? ix.x : ix.y;
 			if (v0 && v1) {
@@ -354,12 +383,12 @@ __device__ __forceinline__ void trace_step(const float4* __restrict__ nodes, con
 					leafAddr = 0;
 					return;
 				}
-				stack[++sp] = other;
+				stack.set(++sp, other);
 			}
 		}
 		if (nodeAddr < 0 && leafAddr >= 0) {
 			leafAddr = nodeAddr;
-			nodeAddr = stack[sp--];
+			nodeAddr = stack.get(sp--);
 		}
 		if (!__any_sync(__activemask(), leafAddr >= 0)) break;
 	}
@@ -390,7 +419,7 @@ __device__ __forceinline__ void trace_step(const float4* __restrict__ nodes, con
 			slot++;
 		}
 		leafAddr = nodeAddr;
-		if (nodeAddr < 0) nodeAddr = stack[sp--];
+		if (nodeAddr < 0) nodeAddr = stack.get(sp--);
 	}
 }
 
@@ -402,7 +431,7 @@ __device__ __forceinline__ uint32_t persistent_trace(const float4* __restrict__ 
 {
 	const uint32_t lane = threadIdx.x & 31u;
 	const uint32_t below = (1u << lane) - 1u;
-	int32_t stack[kStackSize];
+	TraversalStack stack;
 	int sp = 0;
 	int32_t nodeAddr = kSentinel, leafAddr = 0;
 	RayState r;
@@ -427,7 +456,7 @@ __device__ __forceinline__ uint32_t persistent_trace(const float4* __restrict__ 
 					r = src.load(rayIdx);
 					h = empty_hit(r);
 					sp = 0;
-					stack[0] = kSentinel;
+					stack.set(0, kSentinel);
 					nodeAddr = 0;
 					leafAddr = 0;
 					hasRay = true;

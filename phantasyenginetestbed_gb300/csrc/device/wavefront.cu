@@ -36,6 +36,7 @@ constexpr int kWaveBlock = 128;
 // measured on GB300 at 1080p: 8 blocks 0.893 ms per frame, 9 0.926, 10 0.915, 12 0.959, uncapped
 // (88-92 registers) 0.970.
 constexpr int kWaveMinBlocks = 8;
+const size_t kStackSmem = stack_smem_bytes(kWaveBlock);   // dynamic shared memory of the traversal kernels
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
 
@@ -676,7 +677,9 @@ static phe_status wave_grid(int which, int* grid)
 	if (st) return st;
 	if (g_waveBlocksPerSM[which] == 0) {
 		int b = 0;
-		PHE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, wave_kernel(which), kWaveBlock, 0), "occupancy");
+		const bool traverses = which != kGridPrimaryShade && which != kGridBounceShade;
+		PHE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, wave_kernel(which), kWaveBlock,
+		                                                           traverses ? kStackSmem : 0), "occupancy");
 		g_waveBlocksPerSM[which] = b > 0 ? b : 1;
 	}
 	*grid = g_waveBlocksPerSM[which] * d->numSMs;
@@ -722,7 +725,7 @@ phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, c
 		const int gBounce = g[wide ? kGridBounceWide : kGridBounce];
 		const phe_ray_in* rays1 = fb.shadowRays + fb.capacityLP;
 		const uint32_t* slots1 = fb.shadowSlots + fb.capacityLP;
-		primary<<<gPrimary, kWaveBlock, 0, stream>>>(scene->dev, dParams, fb, scene->status);
+		primary<<<gPrimary, kWaveBlock, kStackSmem, stream>>>(scene->dev, dParams, fb, scene->status);
 		mark();
 		if (schedule != PHE_SHADOWS_MERGED) {
 			cudaStream_t shadowStream = stream;
@@ -731,7 +734,7 @@ phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, c
 				PHE_CUDA_TRY(cudaStreamWaitEvent(streams->side, streams->fork, 0), "fork frame");
 				shadowStream = streams->side;
 			}
-			anyQueue<<<gAny, kWaveBlock, 0, shadowStream>>>(scene->dev, fb.shadowRays, fb.shadowSlots,
+			anyQueue<<<gAny, kWaveBlock, kStackSmem, shadowStream>>>(scene->dev, fb.shadowRays, fb.shadowSlots,
 			                                                 fb.counters + kCtrShadow0, nullptr, nullptr, nullptr,
 			                                                 fb.inLight, fb.counters + kCtrWork2, scene->status);
 			if (beside) PHE_CUDA_TRY(cudaEventRecord(streams->join, shadowStream), "join frame");
@@ -741,26 +744,26 @@ phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, c
 			bin_bounce_kernel<<<binGrid, kBinBlock, 0, stream>>>(fb);
 			mark();
 		}
-		bounce<<<gBounce, kWaveBlock, 0, stream>>>(scene->dev, dParams, fb, scene->status);
+		bounce<<<gBounce, kWaveBlock, kStackSmem, stream>>>(scene->dev, dParams, fb, scene->status);
 		mark();
 		if (schedule == PHE_SHADOWS_MERGED) {
 			// bounce shadows first: their incoherent rays start early and the primary ones fill the tail
-			anyQueue<<<gAny, kWaveBlock, 0, stream>>>(scene->dev, rays1, slots1, fb.counters + kCtrShadow1,
+			anyQueue<<<gAny, kWaveBlock, kStackSmem, stream>>>(scene->dev, rays1, slots1, fb.counters + kCtrShadow1,
 			                                           fb.shadowRays, fb.shadowSlots, fb.counters + kCtrShadow0,
 			                                           fb.inLight, fb.counters + kCtrWork3, scene->status);
 		} else {
-			anyQueue<<<gAny, kWaveBlock, 0, stream>>>(scene->dev, rays1, slots1, fb.counters + kCtrShadow1, nullptr,
+			anyQueue<<<gAny, kWaveBlock, kStackSmem, stream>>>(scene->dev, rays1, slots1, fb.counters + kCtrShadow1, nullptr,
 			                                           nullptr, nullptr, fb.inLight, fb.counters + kCtrWork3,
 			                                           scene->status);
 		}
 		mark();
 		if (beside) PHE_CUDA_TRY(cudaStreamWaitEvent(stream, streams->join, 0), "join frame");
 	} else {
-		primary_trace_kernel<<<g[kGridPrimaryTrace], kWaveBlock, 0, stream>>>(scene->dev, dParams, fb, scene->status);
+		primary_trace_kernel<<<g[kGridPrimaryTrace], kWaveBlock, kStackSmem, stream>>>(scene->dev, dParams, fb, scene->status);
 		mark();
 		primary_shade_kernel<<<g[kGridPrimaryShade], kWaveBlock, 0, stream>>>(scene->dev, dParams, fb);
 		mark();
-		any_refill_kernel<<<g[kGridAnyRefill], kWaveBlock, 0, stream>>>(scene->dev, fb.shadowRays, fb.shadowSlots,
+		any_refill_kernel<<<g[kGridAnyRefill], kWaveBlock, kStackSmem, stream>>>(scene->dev, fb.shadowRays, fb.shadowSlots,
 		                                                                 fb.counters + kCtrShadow0, fb.inLight,
 		                                                                 fb.counters + kCtrWork2, fb.refill,
 		                                                                 scene->status);
@@ -769,11 +772,11 @@ phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, c
 			bin_bounce_kernel<<<binGrid, kBinBlock, 0, stream>>>(fb);
 			mark();
 		}
-		bounce_trace_kernel<<<g[kGridBounceTrace], kWaveBlock, 0, stream>>>(scene->dev, fb, scene->status);
+		bounce_trace_kernel<<<g[kGridBounceTrace], kWaveBlock, kStackSmem, stream>>>(scene->dev, fb, scene->status);
 		mark();
 		bounce_shade_kernel<<<g[kGridBounceShade], kWaveBlock, 0, stream>>>(scene->dev, dParams, fb);
 		mark();
-		any_refill_kernel<<<g[kGridAnyRefill], kWaveBlock, 0, stream>>>(scene->dev, fb.shadowRays + fb.capacityLP,
+		any_refill_kernel<<<g[kGridAnyRefill], kWaveBlock, kStackSmem, stream>>>(scene->dev, fb.shadowRays + fb.capacityLP,
 		                                                                 fb.shadowSlots + fb.capacityLP,
 		                                                                 fb.counters + kCtrShadow1, fb.inLight,
 		                                                                 fb.counters + kCtrWork3, fb.refill,
