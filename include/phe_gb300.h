@@ -266,6 +266,11 @@ typedef struct phe_batch_params {
 	int32_t order;           /* PHE_BATCH_ORDER_* */
 	int32_t useGraph;        /* 1 = replay from a CUDA graph captured on first launch */
 	int32_t layout;          /* PHE_LAYOUT_* for every scene of the batch (wide only where available) */
+	int32_t stackShared;     /* traversal-stack entries kept in shared memory: 0 or 16 (the rest: local) */
+	int32_t sortWindow;      /* ray-sort granularity: 0 = rays in the given order, else 256..4096 (a
+	                          * multiple of 256): within windows of that many rays of a batch, rays are
+	                          * traced grouped by direction octant (stable); results land at the rays'
+	                          * own indices either way */
 	int32_t pad;
 } phe_batch_params;
 typedef struct phe_batch_tuning_row { phe_batch_params params; float ms; } phe_batch_tuning_row;
@@ -279,7 +284,8 @@ phe_status phe_batch_set_params(phe_batch* batch, const phe_batch_params* params
 /* One persistent launch over every item, asynchronous on `stream`. */
 phe_status phe_batch_launch(phe_batch* batch, void* stream);
 phe_status phe_batch_info(const phe_batch* batch, uint64_t* totalRays, uint32_t* paddedRays);
-/* Times every candidate (block size x batch order x occupancy x node layout) `repeats` times on this batch with
+/* Times every candidate (block size x batch order x occupancy x node layout x shared stack depth x ray-sort
+ * granularity) `repeats` times on this batch with
  * CUDA events on `stream`, sets the fastest on the batch and returns it; `rows` (optional) receives
  * every candidate's time. Synchronous. */
 phe_status phe_batch_autotune(phe_batch* batch, int repeats, void* stream, phe_batch_params* best, float* bestMs,

@@ -20,12 +20,13 @@ def _stream(stream):
 
 
 class Batch:
-    def __init__(self, scenes, items, block_size=128, blocks_per_sm=0, order=ORDER_GIVEN, use_graph=True, layout=0):
+    def __init__(self, scenes, items, block_size=128, blocks_per_sm=0, order=ORDER_GIVEN, use_graph=True, layout=0,
+                 stack_shared=0, sort_window=0):
         """scenes: list of Scene; items: list of (scene index, kind, count, device rays, device out)."""
         self.scenes = list(scenes)
         arr = (C.c_void_p * len(scenes))(*[s.handle.value for s in scenes])
         self._items = self._table(items)
-        p = _n.BatchParams(block_size, blocks_per_sm, order, 1 if use_graph else 0, layout, 0)
+        p = _n.BatchParams(block_size, blocks_per_sm, order, 1 if use_graph else 0, layout, stack_shared, sort_window, 0)
         h = C.c_void_p()
         check(lib().phe_batch_create(arr, len(scenes), self._items, len(items), C.byref(p), C.byref(h)), "phe_batch_create")
         self.handle = h
@@ -41,8 +42,11 @@ class Batch:
         self._items = self._table(items)
         check(lib().phe_batch_update(self.handle, self._items, len(items)), "phe_batch_update")
 
-    def set_params(self, block_size=128, blocks_per_sm=0, order=ORDER_GIVEN, use_graph=True, layout=0) -> None:
-        p = _n.BatchParams(block_size, blocks_per_sm, order, 1 if use_graph else 0, layout, 0)
+    def set_params(self, block_size=128, blocks_per_sm=0, order=ORDER_GIVEN, use_graph=True, layout=0, stack_shared=0,
+                   sort_window=0) -> None:
+        """stack_shared: traversal-stack entries in shared memory (0 or 16); sort_window: 0, or rays traced
+        grouped by direction octant within windows of that many rays (a multiple of 256 up to 4096)."""
+        p = _n.BatchParams(block_size, blocks_per_sm, order, 1 if use_graph else 0, layout, stack_shared, sort_window, 0)
         check(lib().phe_batch_set_params(self.handle, C.byref(p)), "phe_batch_set_params")
 
     def launch(self, stream=None) -> None:
@@ -57,13 +61,15 @@ class Batch:
         """Returns (best params dict, best ms, all candidate rows)."""
         best = _n.BatchParams()
         ms = C.c_float()
-        rows = (_n.BatchTuningRow * 64)()
+        cap = 512
+        rows = (_n.BatchTuningRow * cap)()
         n = C.c_uint32()
-        check(lib().phe_batch_autotune(self.handle, repeats, _stream(stream), C.byref(best), C.byref(ms), rows, 64,
+        check(lib().phe_batch_autotune(self.handle, repeats, _stream(stream), C.byref(best), C.byref(ms), rows, cap,
                                        C.byref(n)), "phe_batch_autotune")
         as_dict = lambda p: {"blockSize": p.blockSize, "blocksPerSM": p.blocksPerSM, "order": p.order,
-                             "useGraph": p.useGraph, "layout": p.layout}
-        table = [dict(as_dict(rows[i].params), ms=rows[i].ms) for i in range(min(n.value, 64))]
+                             "useGraph": p.useGraph, "layout": p.layout, "stackShared": p.stackShared,
+                             "sortWindow": p.sortWindow}
+        table = [dict(as_dict(rows[i].params), ms=rows[i].ms) for i in range(min(n.value, cap))]
         return as_dict(best), float(ms.value), table
 
     def close(self) -> None:

@@ -18,6 +18,7 @@
 #include <vector>
 
 #include "batch.cuh"
+#include "octant_sort.cuh"
 #include "runtime.cuh"
 #include "traverse.cuh"
 
@@ -28,7 +29,11 @@ struct BatchTableDev {
 	const DeviceScene* scenes;
 	uint32_t numItems;
 	uint32_t totalPadded;
+	const uint32_t* perm;   // ray-sort permutation: global index -> item-local ray index (null: identity)
 };
+
+// Shared-memory depth of the traversal stack the autotuner may pick besides 0.
+constexpr int kBatchStackShared = 16;
 
 __device__ __forceinline__ uint32_t find_item(const BatchItemDev* __restrict__ items, uint32_t n, uint32_t g)
 {
@@ -41,7 +46,7 @@ __device__ __forceinline__ uint32_t find_item(const BatchItemDev* __restrict__ i
 	return lo;
 }
 
-template <int BLOCK, bool WIDE>
+template <int BLOCK, bool WIDE, int SN>
 __global__ void __launch_bounds__(BLOCK) batch_kernel(BatchTableDev t, uint32_t* __restrict__ counter,
                                                       uint32_t* __restrict__ status)
 {
@@ -55,15 +60,16 @@ __global__ void __launch_bounds__(BLOCK) batch_kernel(BatchTableDev t, uint32_t*
 		const BatchItemDev item = t.items[it];
 		uint32_t i = g - item.base + lane;
 		if (i < item.count) {
+			if (t.perm) i = __ldg(t.perm + g + lane);   // the ray traced at this slot after sorting
 			const DeviceScene s = t.scenes[item.scene];
 			RayState r = load_ray(item.rays, i);
 			HitRecord h = empty_hit(r);
 			uint32_t err;
 			if (item.kind == 0) {
-				err = trace<false, WIDE>(s, r, h);
+				err = trace<false, WIDE, SN>(s, r, h);
 				store_hit((phe_ray_hit*)item.out, i, r, h);
 			} else {
-				err = trace<true, WIDE>(s, r, h);
+				err = trace<true, WIDE, SN>(s, r, h);
 				((uint8_t*)item.out)[i] = h.slot == ~0u ? 1 : 0;
 			}
 			if (err) atomicOr(status, err);
@@ -72,15 +78,18 @@ __global__ void __launch_bounds__(BLOCK) batch_kernel(BatchTableDev t, uint32_t*
 	}
 }
 
-// `wide` selects the instantiation with the 4-wide traversal (for scene tables holding 4-wide scenes).
+// `wide` selects the instantiation with the 4-wide traversal (for scene tables holding 4-wide scenes),
+// `stackShared` (0 or kBatchStackShared) the one keeping that many stack entries in shared memory.
 template <int BLOCK>
-static phe_status launch_batch_kernel(const BatchTableDev& t, bool wide, int blocksPerSM, int numSMs, uint32_t* counter,
-                                      uint32_t* status, cudaStream_t stream, int* occupancyOut)
+static phe_status launch_batch_kernel(const BatchTableDev& t, bool wide, int stackShared, int blocksPerSM, int numSMs,
+                                      uint32_t* counter, uint32_t* status, cudaStream_t stream, int* occupancyOut)
 {
-	auto kernel = wide ? batch_kernel<BLOCK, true> : batch_kernel<BLOCK, false>;
+	const bool sh = stackShared > 0;
+	auto kernel = wide ? (sh ? batch_kernel<BLOCK, true, kBatchStackShared> : batch_kernel<BLOCK, true, 0>)
+	                   : (sh ? batch_kernel<BLOCK, false, kBatchStackShared> : batch_kernel<BLOCK, false, 0>);
+	const size_t smem = stack_smem_bytes(BLOCK, sh ? kBatchStackShared : 0);
 	int maxB = 0;
-	PHE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxB, kernel, BLOCK, stack_smem_bytes(BLOCK)),
-	             "occupancy");
+	PHE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&maxB, kernel, BLOCK, smem), "occupancy");
 	if (occupancyOut) {
 		*occupancyOut = maxB;
 		return PHE_OK;
@@ -90,9 +99,41 @@ static phe_status launch_batch_kernel(const BatchTableDev& t, bool wide, int blo
 	uint32_t grid = (uint32_t)(b * numSMs);
 	uint32_t need = (t.totalPadded + BLOCK - 1) / BLOCK;
 	if (grid > need) grid = need > 0 ? need : 1;
-	kernel<<<grid, BLOCK, stack_smem_bytes(BLOCK), stream>>>(t, counter, status);
+	kernel<<<grid, BLOCK, smem, stream>>>(t, counter, status);
 	PHE_CUDA_TRY(cudaGetLastError(), "batch_kernel launch");
 	return PHE_OK;
+}
+
+// Ray-sort granularity: one block per window of W consecutive rays of one item (the item of window w
+// is the last one whose first window is <= w) sorts the window by direction octant (stable) and writes
+// perm[item.base + w0 + position] = item-local index of the ray traced there.
+__global__ void __launch_bounds__(kOctantBlock) batch_sort_kernel(BatchTableDev t, const uint32_t* __restrict__ windowStart,
+                                                                 uint32_t numWindows, int W, uint32_t* __restrict__ perm)
+{
+	__shared__ uint32_t cnt[8][kOctantBlock];
+	__shared__ uint32_t bucketBase[8];
+	const int per = W / kOctantBlock;
+	const int tid = threadIdx.x;
+	for (uint32_t w = blockIdx.x; w < numWindows; w += gridDim.x) {
+		uint32_t lo = 0, hi = t.numItems;
+		while (hi - lo > 1) {
+			uint32_t mid = (lo + hi) >> 1;
+			if (__ldg(windowStart + mid) <= w) lo = mid;
+			else hi = mid;
+		}
+		const BatchItemDev item = t.items[lo];
+		const uint32_t w0 = (w - __ldg(windowStart + lo)) * (uint32_t)W;
+		const uint32_t n = min((uint32_t)W, item.count - w0);
+		uint8_t keys[kMaxOctantWindow / kOctantBlock];
+		for (int k = 0; k < per; k++) {
+			uint32_t j = (uint32_t)(tid * per + k);
+			keys[k] = j < n ? octant_key(__ldg(reinterpret_cast<const float4*>(item.rays + w0 + j) + 1)) : (uint8_t)0xFF;
+		}
+		uint32_t rank[8];
+		octant_ranks(keys, per, cnt, bucketBase, rank);
+		for (int k = 0; k < per; k++)
+			if (keys[k] != 0xFF) perm[item.base + w0 + rank[keys[k]]++] = w0 + (uint32_t)(tid * per + k);
+	}
 }
 
 phe_status launch_batch_table(const BatchItemDev* items, uint32_t numItems, uint32_t totalPadded,
@@ -103,11 +144,11 @@ phe_status launch_batch_table(const BatchItemDev* items, uint32_t numItems, uint
 	phe_status st = device_info(&d);
 	if (st) return st;
 	if (totalPadded == 0) return PHE_OK;
-	BatchTableDev t{items, scenes, numItems, totalPadded};
+	BatchTableDev t{items, scenes, numItems, totalPadded, nullptr};
 	switch (blockSize) {
-	case 64: return launch_batch_kernel<64>(t, wide, blocksPerSM, d->numSMs, counter, status, stream, nullptr);
-	case 256: return launch_batch_kernel<256>(t, wide, blocksPerSM, d->numSMs, counter, status, stream, nullptr);
-	default: return launch_batch_kernel<128>(t, wide, blocksPerSM, d->numSMs, counter, status, stream, nullptr);
+	case 64: return launch_batch_kernel<64>(t, wide, 0, blocksPerSM, d->numSMs, counter, status, stream, nullptr);
+	case 256: return launch_batch_kernel<256>(t, wide, 0, blocksPerSM, d->numSMs, counter, status, stream, nullptr);
+	default: return launch_batch_kernel<128>(t, wide, 0, blocksPerSM, d->numSMs, counter, status, stream, nullptr);
 	}
 }
 
@@ -129,6 +170,11 @@ struct phe_batch {
 	uint32_t totalPadded = 0;
 	uint64_t totalRays = 0;
 	cudaGraphExec_t graph = nullptr;
+	// Ray sorting (params.sortWindow > 0): window table of the item order and the permutation.
+	uint32_t* dPerm = nullptr;             // [totalPadded]
+	uint32_t* dWindowStart = nullptr;      // [items + 1]
+	uint32_t numWindows = 0;
+	size_t permCapacity = 0, windowCapacity = 0;
 };
 
 static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -142,6 +188,23 @@ extern "C" void phe_batch_default_params(phe_batch_params* p)
 	p->order = PHE_BATCH_ORDER_GIVEN;
 	p->useGraph = 1;
 	p->layout = PHE_LAYOUT_BINARY;
+	p->stackShared = 0;
+	p->sortWindow = 0;
+}
+
+static phe_status check_params(const phe_batch_params* p)
+{
+	if (p->blockSize != 64 && p->blockSize != 128 && p->blockSize != 256)
+		return fail(PHE_ERR_INVALID_ARGUMENT, "batch block size must be 64, 128 or 256");
+	if (p->stackShared != 0 && p->stackShared != kBatchStackShared)
+		return fail(PHE_ERR_INVALID_ARGUMENT, "batch stackShared must be 0 or %d", kBatchStackShared);
+	if (p->sortWindow != 0 && (p->sortWindow < kOctantBlock || p->sortWindow > kMaxOctantWindow ||
+	                           p->sortWindow % kOctantBlock))
+		return fail(PHE_ERR_INVALID_ARGUMENT, "batch sortWindow must be 0 or a multiple of %d up to %d", kOctantBlock,
+		            kMaxOctantWindow);
+	if (p->layout != PHE_LAYOUT_BINARY && p->layout != PHE_LAYOUT_WIDE4)
+		return fail(PHE_ERR_INVALID_ARGUMENT, "batch layout must be PHE_LAYOUT_BINARY or PHE_LAYOUT_WIDE4");
+	return PHE_OK;
 }
 
 static phe_status upload_table(phe_batch* b)
@@ -187,6 +250,35 @@ static phe_status upload_table(phe_batch* b)
 	if (!st.empty())
 		PHE_CUDA_TRY(cudaMemcpy(b->dScenes, st.data(), st.size() * sizeof(DeviceScene), cudaMemcpyHostToDevice),
 		             "upload scene table");
+	b->numWindows = 0;
+	if (b->params.sortWindow > 0) {
+		const uint32_t W = (uint32_t)b->params.sortWindow;
+		std::vector<uint32_t> ws(n + 1);
+		uint32_t acc = 0;
+		for (size_t k = 0; k < n; k++) {
+			ws[k] = acc;
+			acc += (dev[k].count + W - 1) / W;
+		}
+		ws[n] = acc;
+		b->numWindows = acc;
+		if (b->permCapacity < b->totalPadded || !b->dPerm) {
+			if (b->dPerm) cudaFree(b->dPerm);
+			b->dPerm = nullptr;
+			b->permCapacity = 0;
+			PHE_CUDA_TRY(cudaMalloc(&b->dPerm, std::max<size_t>(1, b->totalPadded) * sizeof(uint32_t)),
+			             "cudaMalloc(batch ray permutation)");
+			b->permCapacity = std::max<size_t>(1, b->totalPadded);
+		}
+		if (b->windowCapacity < n + 1 || !b->dWindowStart) {
+			if (b->dWindowStart) cudaFree(b->dWindowStart);
+			b->dWindowStart = nullptr;
+			b->windowCapacity = 0;
+			PHE_CUDA_TRY(cudaMalloc(&b->dWindowStart, (n + 1) * sizeof(uint32_t)), "cudaMalloc(batch sort windows)");
+			b->windowCapacity = n + 1;
+		}
+		PHE_CUDA_TRY(cudaMemcpy(b->dWindowStart, ws.data(), (n + 1) * sizeof(uint32_t), cudaMemcpyHostToDevice),
+		             "upload batch sort windows");
+	}
 	if (b->graph) {
 		cudaGraphExecDestroy(b->graph);
 		b->graph = nullptr;
@@ -218,6 +310,7 @@ extern "C" phe_status phe_batch_create(const phe_scene* const* scenes, uint32_t 
 		if (!scenes[i]) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_batch_create: scene %u is null", i);
 	phe_status st = check_items(items, numItems, numScenes);
 	if (st) return st;
+	if (params && (st = check_params(params))) return st;
 	DeviceInfo* d = nullptr;
 	if ((st = device_info(&d))) return st;
 	phe_batch* b = new phe_batch();
@@ -272,14 +365,22 @@ static phe_status batch_enqueue(phe_batch* b, cudaStream_t stream)
 	DeviceInfo* d = nullptr;
 	phe_status st = device_info(&d);
 	if (st) return st;
-	BatchTableDev t{b->dItems, b->dScenes, (uint32_t)b->items.size(), b->totalPadded};
+	const bool sorted = b->params.sortWindow > 0 && b->numWindows > 0;
+	BatchTableDev t{b->dItems, b->dScenes, (uint32_t)b->items.size(), b->totalPadded, sorted ? b->dPerm : nullptr};
 	PHE_CUDA_TRY(cudaMemsetAsync(b->dCounter, 0, sizeof(uint32_t), stream), "clear batch counter");
 	if (b->totalPadded == 0) return PHE_OK;
+	if (sorted) {
+		uint32_t grid = std::min<uint32_t>(b->numWindows, (uint32_t)d->numSMs * 8u);
+		batch_sort_kernel<<<grid, kOctantBlock, 0, stream>>>(t, b->dWindowStart, b->numWindows, b->params.sortWindow,
+		                                                    b->dPerm);
+		PHE_CUDA_TRY(cudaGetLastError(), "batch_sort_kernel launch");
+	}
 	const bool wide = b->params.layout == PHE_LAYOUT_WIDE4;
+	const int sh = b->params.stackShared;
 	switch (b->params.blockSize) {
-	case 64: return launch_batch_kernel<64>(t, wide, b->params.blocksPerSM, d->numSMs, b->dCounter, b->dStatus, stream, nullptr);
-	case 256: return launch_batch_kernel<256>(t, wide, b->params.blocksPerSM, d->numSMs, b->dCounter, b->dStatus, stream, nullptr);
-	case 128: return launch_batch_kernel<128>(t, wide, b->params.blocksPerSM, d->numSMs, b->dCounter, b->dStatus, stream, nullptr);
+	case 64: return launch_batch_kernel<64>(t, wide, sh, b->params.blocksPerSM, d->numSMs, b->dCounter, b->dStatus, stream, nullptr);
+	case 256: return launch_batch_kernel<256>(t, wide, sh, b->params.blocksPerSM, d->numSMs, b->dCounter, b->dStatus, stream, nullptr);
+	case 128: return launch_batch_kernel<128>(t, wide, sh, b->params.blocksPerSM, d->numSMs, b->dCounter, b->dStatus, stream, nullptr);
 	default: return fail(PHE_ERR_INVALID_ARGUMENT, "batch block size must be 64, 128 or 256");
 	}
 }
@@ -295,10 +396,11 @@ extern "C" phe_status phe_batch_launch(phe_batch* b, void* stream)
 		int occ = 0;
 		BatchTableDev t{};
 		const bool wide = b->params.layout == PHE_LAYOUT_WIDE4;
+		const int sh = b->params.stackShared;
 		switch (b->params.blockSize) {
-		case 64: launch_batch_kernel<64>(t, wide, 0, 1, nullptr, nullptr, nullptr, &occ); break;
-		case 256: launch_batch_kernel<256>(t, wide, 0, 1, nullptr, nullptr, nullptr, &occ); break;
-		default: launch_batch_kernel<128>(t, wide, 0, 1, nullptr, nullptr, nullptr, &occ); break;
+		case 64: launch_batch_kernel<64>(t, wide, sh, 0, 1, nullptr, nullptr, nullptr, &occ); break;
+		case 256: launch_batch_kernel<256>(t, wide, sh, 0, 1, nullptr, nullptr, nullptr, &occ); break;
+		default: launch_batch_kernel<128>(t, wide, sh, 0, 1, nullptr, nullptr, nullptr, &occ); break;
 		}
 		cudaStream_t cap = nullptr;
 		PHE_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), "create capture stream");
@@ -323,8 +425,8 @@ extern "C" phe_status phe_batch_launch(phe_batch* b, void* stream)
 extern "C" phe_status phe_batch_set_params(phe_batch* b, const phe_batch_params* params)
 {
 	if (!b || !params) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_batch_set_params: null argument");
-	if (params->blockSize != 64 && params->blockSize != 128 && params->blockSize != 256)
-		return fail(PHE_ERR_INVALID_ARGUMENT, "batch block size must be 64, 128 or 256");
+	phe_status st = check_params(params);
+	if (st) return st;
 	b->params = *params;
 	return upload_table(b);
 }
@@ -341,6 +443,8 @@ extern "C" phe_status phe_batch_destroy(phe_batch* b)
 {
 	if (!b) return PHE_OK;
 	if (b->graph) cudaGraphExecDestroy(b->graph);
+	if (b->dPerm) cudaFree(b->dPerm);
+	if (b->dWindowStart) cudaFree(b->dWindowStart);
 	cudaFree(b->allocation);
 	delete b;
 	return PHE_OK;
@@ -364,6 +468,8 @@ extern "C" phe_status phe_batch_autotune(phe_batch* b, int repeats, void* stream
 	const int orders[] = {PHE_BATCH_ORDER_GIVEN, PHE_BATCH_ORDER_LARGEST_FIRST};
 	const int occFrac[] = {4, 3, 2};  // quarters of the occupancy limit: 4/4, 3/4, 2/4
 	const int layouts[] = {PHE_LAYOUT_BINARY, PHE_LAYOUT_WIDE4};
+	const int stacks[] = {0, kBatchStackShared};
+	const int sorts[] = {0, 1024, 4096};
 	cudaEvent_t e0, e1;
 	PHE_CUDA_TRY(cudaEventCreate(&e0), "cudaEventCreate");
 	PHE_CUDA_TRY(cudaEventCreate(&e1), "cudaEventCreate");
@@ -374,18 +480,22 @@ extern "C" phe_status phe_batch_autotune(phe_batch* b, int repeats, void* stream
 	for (int bs : blocks) {
 		int occ = 0;
 		BatchTableDev t{};
-		if (bs == 64) launch_batch_kernel<64>(t, false, 0, 1, nullptr, nullptr, nullptr, &occ);
-		else if (bs == 128) launch_batch_kernel<128>(t, false, 0, 1, nullptr, nullptr, nullptr, &occ);
-		else launch_batch_kernel<256>(t, false, 0, 1, nullptr, nullptr, nullptr, &occ);
+		if (bs == 64) launch_batch_kernel<64>(t, false, 0, 0, 1, nullptr, nullptr, nullptr, &occ);
+		else if (bs == 128) launch_batch_kernel<128>(t, false, 0, 0, 1, nullptr, nullptr, nullptr, &occ);
+		else launch_batch_kernel<256>(t, false, 0, 0, 1, nullptr, nullptr, nullptr, &occ);
 		for (int ord : orders)
 			for (int q : occFrac)
-				for (int lay : layouts) {
+				for (int lay : layouts)
+				for (int sh : stacks)
+				for (int sw : sorts) {
 				phe_batch_params p = saved;
 				p.blockSize = bs;
 				p.order = ord;
 				p.blocksPerSM = std::max(1, occ * q / 4);
 				p.useGraph = 0;
 				p.layout = lay;
+				p.stackShared = sh;
+				p.sortWindow = sw;
 				b->params = p;
 				if ((st = upload_table(b))) goto done;
 				if ((st = batch_enqueue(b, s))) goto done;  // warm-up
@@ -535,14 +645,13 @@ extern "C" phe_status phe_batch_cast_noalloc(const phe_scene* const* scenes, uin
 	int dev = 0, numSMs = 0, perSM = 0;
 	PHE_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
 	PHE_CUDA_TRY(cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, dev), "SM count");
-	auto kernel = wide ? batch_kernel<128, true> : batch_kernel<128, false>;
-	PHE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kernel, 128, stack_smem_bytes(128)),
-	             "occupancy");
+	auto kernel = wide ? batch_kernel<128, true, 0> : batch_kernel<128, false, 0>;
+	PHE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kernel, 128, 0), "occupancy");
 	uint32_t grid = (uint32_t)(perSM > 0 ? perSM : 1) * (uint32_t)numSMs;
 	uint32_t need = (base + 127u) / 128u;
 	if (grid > need) grid = need;
-	BatchTableDev t{dItems, dScenes, numItems, base};
-	kernel<<<grid, 128, stack_smem_bytes(128), s>>>(t, dCounter, dStatus);
+	BatchTableDev t{dItems, dScenes, numItems, base, nullptr};
+	kernel<<<grid, 128, 0, s>>>(t, dCounter, dStatus);
 	PHE_CUDA_TRY(cudaGetLastError(), "batch_kernel launch (no-alloc)");
 	return PHE_OK;
 }

@@ -74,31 +74,38 @@ struct HitRecord {
 constexpr int kSmemStack = PHE_SMEM_STACK;
 static_assert(kSmemStack >= 0 && kSmemStack <= kStackSize, "shared stack depth");
 extern __shared__ int32_t g_stackSmem[];
-inline size_t stack_smem_bytes(int block) { return (size_t)kSmemStack * sizeof(int32_t) * (size_t)block; }
+inline size_t stack_smem_bytes(int block, int entries = kSmemStack)
+{
+	return (size_t)entries * sizeof(int32_t) * (size_t)block;
+}
 
-struct TraversalStack {
+// SN: stack entries kept in shared memory (the batch autotuner instantiates other depths).
+template <int SN>
+struct TraversalStackT {
+	static_assert(SN >= 0 && SN <= kStackSize, "shared stack depth");
 	int32_t* col;
 	uint32_t stride;
-	int32_t spill[kStackSize - kSmemStack > 0 ? kStackSize - kSmemStack : 1];
-	__device__ __forceinline__ TraversalStack() : col(g_stackSmem + threadIdx.x), stride(blockDim.x) {}
+	int32_t spill[kStackSize - SN > 0 ? kStackSize - SN : 1];
+	__device__ __forceinline__ TraversalStackT() : col(g_stackSmem + threadIdx.x), stride(blockDim.x) {}
 	__device__ __forceinline__ void set(int i, int32_t v)
 	{
-		if (kSmemStack > 0 && i < kSmemStack) col[(uint32_t)i * stride] = v;
-		else spill[i - kSmemStack] = v;
+		if (SN > 0 && i < SN) col[(uint32_t)i * stride] = v;
+		else spill[i - SN] = v;
 	}
 	__device__ __forceinline__ int32_t get(int i) const
 	{
-		return (kSmemStack > 0 && i < kSmemStack) ? col[(uint32_t)i * stride] : spill[i - kSmemStack];
+		return (SN > 0 && i < SN) ? col[(uint32_t)i * stride] : spill[i - SN];
 	}
 };
+using TraversalStack = TraversalStackT<kSmemStack>;
 
 // Traverses the scene for one ray. ANY = true stops at the first triangle with tMin <= t < tMax.
 // Returns the error bits (0, or kErrStackOverflow when the stack would overflow).
-template <bool SAFE, bool ANY>
+template <bool SAFE, bool ANY, int SN = kSmemStack>
 __device__ __forceinline__ uint32_t traverse(const float4* __restrict__ nodes, const float4* __restrict__ tris,
                                              const TraversalBounds& bd, const RayState& r, HitRecord& hit)
 {
-	TraversalStack stack;
+	TraversalStackT<SN> stack;
 	int sp = 0;
 	stack.set(0, kSentinel);
 	int32_t nodeAddr = 0;
@@ -313,16 +320,16 @@ __device__ __forceinline__ uint32_t traverse4(const float4* __restrict__ nodes4,
 // WIDE = false compiles the binary traversal only; kernels are instantiated for both layouts and
 // the host launches the WIDE one only for scenes whose 4-wide layout is selected, so binary
 // launches carry neither the 4-wide code nor its larger stack.
-template <bool ANY, bool WIDE = false>
+template <bool ANY, bool WIDE = false, int SN = kSmemStack>
 __device__ __forceinline__ uint32_t trace(const DeviceScene& s, const RayState& r, HitRecord& hit)
 {
 	if (r.safe) {
 		if constexpr (WIDE) {
 			if (s.nodes4) return traverse4<ANY>(s.nodes4, s.tris, TraversalBounds{s.numNodes4, s.numSlots}, r, hit);
 		}
-		return traverse<true, ANY>(s.nodes, s.tris, TraversalBounds{s.numNodes, s.numSlots}, r, hit);
+		return traverse<true, ANY, SN>(s.nodes, s.tris, TraversalBounds{s.numNodes, s.numSlots}, r, hit);
 	}
-	return traverse<false, ANY>(s.nodes, s.tris, TraversalBounds{s.numNodes, s.numSlots}, r, hit);
+	return traverse<false, ANY, SN>(s.nodes, s.tris, TraversalBounds{s.numNodes, s.numSlots}, r, hit);
 }
 
 __device__ __forceinline__ void store_hit(phe_ray_hit* __restrict__ hits, uint32_t i, const RayState& r, const HitRecord& h)

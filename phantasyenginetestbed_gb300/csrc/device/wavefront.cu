@@ -23,6 +23,7 @@
 
 #include "raygen.cuh"
 #include "runtime.cuh"
+#include "octant_sort.cuh"
 #include "sampling.cuh"
 #include "shading.cuh"
 #include "traverse.cuh"
@@ -227,71 +228,32 @@ __global__ void __launch_bounds__(kWaveBlock) any_queue_kernel(DeviceScene s, co
 	}
 }
 
-// Bins the bounce queue by direction octant (sign bits of dir.xyz) inside windows of fb.sortWindow
-// consecutive entries: a deterministic counting sort per window, so warps of the bounce pass trace
-// rays of one octant from one neighbourhood of the image. Writes fb.bouncePerm.
-constexpr int kBinBlock = 256;
-constexpr int kMaxSortWindow = 4096;
+// Bins the bounce queue by direction octant inside windows of fb.sortWindow consecutive entries (a
+// stable counting sort per window, octant_sort.cuh), so warps of the bounce pass trace rays of one
+// octant from one neighbourhood of the image. Writes fb.bouncePerm.
+constexpr int kBinBlock = kOctantBlock;
 
 __global__ void __launch_bounds__(kBinBlock) bin_bounce_kernel(FrameBuffers fb)
 {
 	const int W = fb.sortWindow;
 	if (W <= 0) return;
 	const uint32_t n = fb.counters[kCtrBounce];
-	const int per = W / kBinBlock;   // entries per thread (W is a multiple of kBinBlock, <= kMaxSortWindow)
+	const int per = W / kBinBlock;   // entries per thread (W is a multiple of kBinBlock, <= kMaxOctantWindow)
 	__shared__ uint32_t cnt[8][kBinBlock];
 	__shared__ uint32_t bucketBase[8];
 	const int t = threadIdx.x;
 	for (uint32_t w0 = blockIdx.x * (uint32_t)W; w0 < n; w0 += gridDim.x * (uint32_t)W) {
-		uint32_t c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-		uint8_t keys[kMaxSortWindow / kBinBlock];
+		uint8_t keys[kMaxOctantWindow / kBinBlock];
 		for (int k = 0; k < per; k++) {
 			uint32_t i = w0 + (uint32_t)(t * per + k);
-			uint8_t key = 0xFF;
-			if (i < n) {
-				float4 d = reinterpret_cast<const float4*>(fb.bounceRays + i)[1];
-				key = (uint8_t)((d.x < 0.0f ? 1 : 0) | (d.y < 0.0f ? 2 : 0) | (d.z < 0.0f ? 4 : 0));
-				c[key]++;
-			}
-			keys[k] = key;
+			keys[k] = i < n ? octant_key(reinterpret_cast<const float4*>(fb.bounceRays + i)[1]) : (uint8_t)0xFF;
 		}
-		for (int b = 0; b < 8; b++) cnt[b][t] = c[b];
-		__syncthreads();
-		// Exclusive scan of each bucket's per-thread counts: warp b scans bucket b (8 warps).
-		const int warp = t >> 5, lane = t & 31;
-		if (warp < 8) {
-			uint32_t local[kBinBlock / 32];
-			uint32_t sum = 0;
-			for (int j = 0; j < kBinBlock / 32; j++) {
-				local[j] = sum;
-				sum += cnt[warp][lane * (kBinBlock / 32) + j];
-			}
-			uint32_t incl = sum;
-			for (int o = 1; o < 32; o <<= 1) {
-				uint32_t v = __shfl_up_sync(0xFFFFFFFFu, incl, o);
-				if (lane >= o) incl += v;
-			}
-			uint32_t excl = incl - sum;
-			for (int j = 0; j < kBinBlock / 32; j++) cnt[warp][lane * (kBinBlock / 32) + j] = excl + local[j];
-			if (lane == 31) bucketBase[warp] = incl;   // bucket total for now
-		}
-		__syncthreads();
-		if (t == 0) {
-			uint32_t acc = 0;
-			for (int b = 0; b < 8; b++) {
-				uint32_t tot = bucketBase[b];
-				bucketBase[b] = acc;
-				acc += tot;
-			}
-		}
-		__syncthreads();
 		uint32_t rank[8];
-		for (int b = 0; b < 8; b++) rank[b] = bucketBase[b] + cnt[b][t];
+		octant_ranks(keys, per, cnt, bucketBase, rank);
 		for (int k = 0; k < per; k++) {
 			uint8_t key = keys[k];
 			if (key != 0xFF) fb.bouncePerm[w0 + rank[key]++] = w0 + (uint32_t)(t * per + k);
 		}
-		__syncthreads();
 	}
 }
 

@@ -84,7 +84,7 @@ class BatchItem(C.Structure):
 
 class BatchParams(C.Structure):
     _fields_ = [("blockSize", C.c_int32), ("blocksPerSM", C.c_int32), ("order", C.c_int32), ("useGraph", C.c_int32),
-                ("layout", C.c_int32), ("pad", C.c_int32)]
+                ("layout", C.c_int32), ("stackShared", C.c_int32), ("sortWindow", C.c_int32), ("pad", C.c_int32)]
 
 
 class BatchTuningRow(C.Structure):

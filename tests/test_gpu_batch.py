@@ -86,14 +86,45 @@ def test_autotuner_picks_a_valid_configuration():
     items, host = _mix(scenes, [50000, 2000, 300, 10000, 64, 100000], 4)
     batch = Batch([x[2] for x in scenes], items)
     best, ms, table = batch.autotune(repeats=2)
-    assert len(table) == 36 and ms > 0
+    assert len(table) == 216 and ms > 0
     assert {r["layout"] for r in table} == {0, 1}
+    assert {r["stackShared"] for r in table} == {0, 16} and {r["sortWindow"] for r in table} == {0, 1024, 4096}
     assert best["blockSize"] in (64, 128, 256)
     assert ms == min(r["ms"] for r in table)
     for it in items:
         it[4].zero_()
     batch.launch()
     _check(scenes, items, host)
+
+
+def test_sorted_and_shared_stack_launches_give_the_same_bytes():
+    """Ray-sort granularity and the shared-memory stack depth change the order of work only: every
+    window size (including windows larger than a batch and ragged last windows) and both stack depths
+    write the same bytes as the plain launch, for closest and any hit."""
+    import torch
+    scenes = _scenes()
+    sizes = [1, 31, 255, 256, 257, 1000, 4096, 5000, 20000, 0, 3, 777]
+    items, host = _mix(scenes, sizes, 8)
+    batch = Batch([x[2] for x in scenes], items, use_graph=False)
+    batch.launch()
+    torch.cuda.synchronize()
+    want = [from_device(it[4], np.uint8).copy() for it in items]
+    _check(scenes, items, host)
+    for sw, sh, graph in ((256, 0, False), (1024, 16, False), (4096, 0, True), (0, 16, True), (2048, 16, True)):
+        for it in items:
+            it[4].fill_(0xCD)
+        batch.set_params(block_size=64 if sh else 256, use_graph=graph, stack_shared=sh, sort_window=sw)
+        batch.launch()
+        batch.launch()
+        torch.cuda.synchronize()
+        for w, it in zip(want, items):
+            assert np.array_equal(w, from_device(it[4], np.uint8)), (sw, sh)
+    for s_ in scenes:
+        assert s_[2].status() == 0
+    with pytest.raises(P.PheError):
+        batch.set_params(sort_window=100)
+    with pytest.raises(P.PheError):
+        batch.set_params(stack_shared=8)
 
 
 def test_batch_rejects_bad_items():
