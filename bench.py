@@ -565,7 +565,7 @@ def run_batch(args):
     best, best_ms, table = batch.autotune(repeats=3)
     save_tuning(ROOT / "profiles" / "batch_autotune.json", best, best_ms, table)
     batch.set_params(block_size=best["blockSize"], blocks_per_sm=best["blocksPerSM"], order=best["order"], use_graph=True,
-                     layout=best["layout"])
+                     layout=best["layout"], stack_shared=best["stackShared"], sort_window=best["sortWindow"])
     for _ in range(args.warmup):
         batch.launch(stream)
     t_batched = _timed(lambda: batch.launch(stream), args.steps, stream, flush)
