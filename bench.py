@@ -563,7 +563,9 @@ def run_batch(args):
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
     batch = Batch(scenes, items, use_graph=False)
     best, best_ms, table = batch.autotune(repeats=3)
-    save_tuning(ROOT / "profiles" / "batch_autotune.json", best, best_ms, table)
+    save_tuning(ROOT / "profiles" / "batch_autotune.json", best, best_ms, table,
+                command=f"python bench.py --workload batch --steps {args.steps} --warmup {args.warmup} "
+                        "(phe_batch_autotune, repeats=3, cold L2)")
     batch.set_params(block_size=best["blockSize"], blocks_per_sm=best["blocksPerSM"], order=best["order"], use_graph=True,
                      layout=best["layout"], stack_shared=best["stackShared"], sort_window=best["sortWindow"])
     for _ in range(args.warmup):

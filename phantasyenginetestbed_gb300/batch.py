@@ -84,6 +84,18 @@ class Batch:
             pass
 
 
-def save_tuning(path, best, ms, table) -> None:
+def save_tuning(path, best, ms, table, command="") -> None:
+    """A short record of an autotune: the winner, the best time for each value of each parameter, the ten
+    fastest candidates and the slowest."""
+    rows = sorted(table, key=lambda r: r["ms"])
+    per = {}
+    for key in ("blockSize", "order", "layout", "stackShared", "sortWindow"):
+        best_of = {}
+        for r in rows:
+            best_of[str(r[key])] = min(best_of.get(str(r[key]), 1e30), r["ms"])
+        per[key] = {k: round(v, 4) for k, v in best_of.items()}
+    out = {"command": command, "candidates": len(rows), "best": best, "best_ms": round(ms, 4),
+           "best_ms_per_value": per, "top10": [dict(r, ms=round(r["ms"], 4)) for r in rows[:10]],
+           "slowest": dict(rows[-1], ms=round(rows[-1]["ms"], 4)) if rows else None}
     with open(path, "w") as f:
-        json.dump({"best": best, "best_ms": ms, "candidates": table}, f, indent=1)
+        json.dump(out, f, indent=1)
