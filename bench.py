@@ -464,6 +464,12 @@ def _surface_rays(s, n, rng, tmax=3.4028235e38):
     return rays
 
 
+def _percentiles(times_ms):
+    """p50 / p99 of per-step times (ms): the time for the whole 64-batch mix to complete."""
+    t = sorted(times_ms)
+    return {"p50": round(t[len(t) // 2], 4), "p99": round(t[min(len(t) - 1, int(0.99 * len(t)))], 4)}
+
+
 def _timed(fn, steps, stream, flush=None):
     import torch
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
@@ -598,9 +604,12 @@ def run_batch(args):
     ms_sync = statistics.median(walls)
     line = {"workload": "batch", "metric": METRIC, "unit": "Mrays/s", "batches": 64, "rays": total,
             "scenes": {n: int(len(b.verts)) for n, (_, b, _) in zip(names, built)},
-            "batched_graph": {"ms": round(mb, 4), "Mrays_s": round(total / mb / 1e3, 1), "params": best},
-            "plain_64_launches": {"ms": round(mp, 4), "Mrays_s": round(total / mp / 1e3, 1)},
-            "plain_64_launches_synchronised": {"ms": round(ms_sync, 4), "Mrays_s": round(total / ms_sync / 1e3, 1)},
+            "batched_graph": {"ms": round(mb, 4), "Mrays_s": round(total / mb / 1e3, 1), "params": best,
+                              "latency_ms": _percentiles(t_batched)},
+            "plain_64_launches": {"ms": round(mp, 4), "Mrays_s": round(total / mp / 1e3, 1),
+                                  "latency_ms": _percentiles(t_plain)},
+            "plain_64_launches_synchronised": {"ms": round(ms_sync, 4), "Mrays_s": round(total / ms_sync / 1e3, 1),
+                                               "latency_ms": _percentiles(walls)},
             "speedup_vs_plain": round(mp / mb, 3), "speedup_vs_synchronised": round(ms_sync / mb, 3),
             "autotune_candidates": len(table), "layouts_tried": sorted({r["layout"] for r in table}),
             "l2": "flushed before every timed step"}
