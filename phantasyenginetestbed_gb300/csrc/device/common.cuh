@@ -79,6 +79,27 @@ struct TraversalBounds {
 	uint32_t numSlots;
 };
 
+// Cache hints for data that is read or written once per launch (rays in, hits out, the frame's queues
+// and contributions): with kStreamHints they use the evict-first ("streaming") cache policy, so these
+// streams do not push scene nodes and triangles out of L2. Plain loads through the read-only path and
+// plain stores otherwise.
+#ifndef PHE_STREAM_HINTS
+#define PHE_STREAM_HINTS 0
+#endif
+constexpr bool kStreamHints = PHE_STREAM_HINTS != 0;
+template <class T>
+__device__ __forceinline__ T ld_stream(const T* p)
+{
+	if constexpr (kStreamHints) return __ldcs(p);
+	else return __ldg(p);
+}
+template <class T>
+__device__ __forceinline__ void st_stream(T* p, T v)
+{
+	if constexpr (kStreamHints) __stcs(p, v);
+	else *p = v;
+}
+
 struct f3 { float x, y, z; };
 
 __device__ __forceinline__ f3 mk3(float x, float y, float z) { return f3{x, y, z}; }

@@ -25,7 +25,7 @@ struct RayState {
 __device__ __forceinline__ RayState load_ray(const phe_ray_in* __restrict__ rays, uint32_t i)
 {
 	const float4* p = reinterpret_cast<const float4*>(rays + i);
-	float4 a = __ldg(p), b = __ldg(p + 1);
+	float4 a = ld_stream(p), b = ld_stream(p + 1);
 	RayState r;
 	r.o = mk3(a.x, a.y, a.z);
 	r.tMin = a.w;
@@ -337,7 +337,7 @@ __device__ __forceinline__ void store_hit(phe_ray_hit* __restrict__ hits, uint32
 	float4 o;
 	if (h.slot != ~0u) o = make_float4(__uint_as_float(h.slot), h.t, h.u, h.v);
 	else o = make_float4(__uint_as_float(~0u), r.tMax, 0.0f, 0.0f);
-	reinterpret_cast<float4*>(hits)[i] = o;
+	st_stream(reinterpret_cast<float4*>(hits) + i, o);
 }
 
 } // namespace phe_gb300

@@ -56,8 +56,8 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred, ui
 __device__ __forceinline__ void store_ray(phe_ray_in* rays, uint32_t i, f3 o, float tMin, f3 d, float tMax)
 {
 	float4* p = reinterpret_cast<float4*>(rays + i);
-	p[0] = make_float4(o.x, o.y, o.z, tMin);
-	p[1] = make_float4(d.x, d.y, d.z, tMax);
+	st_stream(p, make_float4(o.x, o.y, o.z, tMin));
+	st_stream(p + 1, make_float4(d.x, d.y, d.z, tMax));
 }
 
 // Shades one hit for every light and appends shadow rays. `stage` 0 = primary, 1 = bounce.
@@ -79,10 +79,10 @@ __device__ __forceinline__ void shade_all_lights(const FrameParamsDev& fp, const
 		uint32_t slot = (stage * L + l) * P + pid;
 		uint32_t q = warp_append(queueCount, valid && cast, 0xFFFFFFFFu);
 		if (valid) {
-			fb.contrib[slot] = make_float4(c.x, c.y, c.z, 0.0f);
+			st_stream(fb.contrib + slot, make_float4(c.x, c.y, c.z, 0.0f));
 			if (cast) {
 				store_ray(qRays, q, hi.pos, 0.001f, sdir, stmax);
-				qSlots[q] = slot;
+				st_stream(qSlots + q, slot);
 			} else {
 				fb.inLight[slot] = 1;   // the reference's dummy ray is never occluded
 			}
@@ -181,8 +181,8 @@ __global__ void __launch_bounds__(kWaveBlock, kWaveMinBlocks) primary_kernel(Dev
 		uint32_t q = warp_append(fb.counters + kCtrBounce, hit, 0xFFFFFFFFu);
 		if (hit) {
 			store_ray(fb.bounceRays, q, hi.pos, btMin, bdir, 3.402823466e+38f);
-			fb.bouncePixel[q] = pid;
-			fb.bounceThroughput[q] = make_float4(thr.x, thr.y, thr.z, 0.0f);
+			st_stream(fb.bouncePixel + q, pid);
+			st_stream(fb.bounceThroughput + q, make_float4(thr.x, thr.y, thr.z, 0.0f));
 		} else if (active) {
 			// no primary hit: nothing to add for this pixel in either stage
 			for (uint32_t l = 0; l < L; l++) {
@@ -222,7 +222,7 @@ __global__ void __launch_bounds__(kWaveBlock) any_queue_kernel(DeviceScene s, co
 			HitRecord h = empty_hit(r);
 			uint32_t err = trace<true, WIDE>(s, r, h);
 			if (err) atomicOr(status, err);
-			inLight[__ldg((a ? slotsA : slotsB) + k)] = h.slot == ~0u ? 1 : 0;
+			inLight[ld_stream((a ? slotsA : slotsB) + k)] = h.slot == ~0u ? 1 : 0;
 		}
 		__syncwarp();
 	}
@@ -280,8 +280,8 @@ __global__ void __launch_bounds__(kWaveBlock, kWaveMinBlocks) bounce_kernel(Devi
 		if (active) {
 			uint32_t j = fb.sortWindow > 0 ? fb.bouncePerm[i] : i;
 			r = load_ray(fb.bounceRays, j);
-			pid = fb.bouncePixel[j];
-			float4 t4 = fb.bounceThroughput[j];
+			pid = ld_stream(fb.bouncePixel + j);
+			float4 t4 = ld_stream(fb.bounceThroughput + j);
 			thr = mk3(t4.x, t4.y, t4.z);
 			h = empty_hit(r);
 			uint32_t err = trace<false, WIDE>(s, r, h);
@@ -431,8 +431,8 @@ __global__ void __launch_bounds__(kWaveBlock) primary_shade_kernel(DeviceScene s
 		uint32_t q = warp_append(fb.counters + kCtrBounce, hit, 0xFFFFFFFFu);
 		if (hit) {
 			store_ray(fb.bounceRays, q, hi.pos, btMin, bdir, 3.402823466e+38f);
-			fb.bouncePixel[q] = pid;
-			fb.bounceThroughput[q] = make_float4(thr.x, thr.y, thr.z, 0.0f);
+			st_stream(fb.bouncePixel + q, pid);
+			st_stream(fb.bounceThroughput + q, make_float4(thr.x, thr.y, thr.z, 0.0f));
 		} else if (active) {
 			for (uint32_t l = 0; l < L; l++) {
 				fb.contrib[(size_t)l * P + pid] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -458,8 +458,8 @@ __global__ void __launch_bounds__(kWaveBlock) bounce_shade_kernel(DeviceScene s,
 		float4 hv = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 		if (active) {
 			uint32_t j = fb.sortWindow > 0 ? fb.bouncePerm[i] : i;
-			pid = fb.bouncePixel[j];
-			float4 t4 = fb.bounceThroughput[j];
+			pid = ld_stream(fb.bouncePixel + j);
+			float4 t4 = ld_stream(fb.bounceThroughput + j);
 			thr = mk3(t4.x, t4.y, t4.z);
 			hv = reinterpret_cast<const float4*>(fb.bounceHits)[i];
 			slot = __float_as_uint(hv.x);
@@ -574,22 +574,22 @@ __global__ void resolve_taa_kernel(const FrameParamsDev* __restrict__ fpp, Frame
 	// Still camera. Every load this pixel needs is issued before the first store (the stores could
 	// alias them for the compiler). With zero velocity the history texel is the pixel itself and both
 	// velocity lengths are 0, so velocityDistrust = 0 and trust = clamp(1 - roughnessDistrust * 0).
-	const float4 h = __ldg(fb.history[fp.parity] + pid);
-	const float rough = __ldg(fb.roughness + pid);
+	const float4 h = ld_stream(fb.history[fp.parity] + pid);
+	const float rough = ld_stream(fb.roughness + pid);
 	uint8_t lit[2 * kMaxLights];
-	for (uint32_t k = 0; k < 2 * L; k++) lit[k] = __ldg(fb.inLight + (size_t)k * P + pid);
+	for (uint32_t k = 0; k < 2 * L; k++) lit[k] = ld_stream(fb.inLight + (size_t)k * P + pid);
 	f3 acc = mk3(0.0f, 0.0f, 0.0f);
 	for (uint32_t k = 0; k < 2 * L; k++)
 		if (lit[k]) {
-			float4 c = __ldg(fb.contrib + (size_t)k * P + pid);
+			float4 c = ld_stream(fb.contrib + (size_t)k * P + pid);
 			acc = add3(acc, mk3(c.x, c.y, c.z));
 		}
 	float4 cur = make_float4(acc.x, acc.y, acc.z, 1.0f);
 	float4 oc, oh;
 	taa_blend(cur, h, clampf(__fsub_rn(1.0f, __fmul_rn(glsl_mix(3.0f, 1.0f, rough), 0.0f)), 0.0f, 1.0f), oc, oh);
-	fb.rawColor[pid] = cur;
-	fb.color[pid] = oc;
-	fb.history[fp.parity ^ 1u][pid] = oh;
+	st_stream(fb.rawColor + pid, cur);
+	st_stream(fb.color + pid, oc);
+	st_stream(fb.history[fp.parity ^ 1u] + pid, oh);
 }
 
 __global__ void taa_kernel(uint32_t W, uint32_t H, const float4* __restrict__ cur, const float4* __restrict__ hist,
