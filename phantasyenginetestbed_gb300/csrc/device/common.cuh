@@ -84,7 +84,7 @@ struct TraversalBounds {
 // streams do not push scene nodes and triangles out of L2. Plain loads through the read-only path and
 // plain stores otherwise.
 #ifndef PHE_STREAM_HINTS
-#define PHE_STREAM_HINTS 0
+#define PHE_STREAM_HINTS 1
 #endif
 constexpr bool kStreamHints = PHE_STREAM_HINTS != 0;
 template <class T>
