@@ -55,7 +55,7 @@ def parse():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-graph", action="store_true")
     ap.add_argument("--pipeline", choices=["fused", "split"], default="fused",
-                    help="fused: traversal + shading in one kernel per bounce (5 kernels); split: 7 kernels")
+                    help="fused: traversal + shading in one kernel per bounce (4 kernels with merged shadows); split: 7 kernels")
     ap.add_argument("--refill", type=int, default=28, help="lane-refill threshold of the split pipeline")
     ap.add_argument("--sort-window", type=int, default=0, help="bin bounce rays by octant in windows of N (0 = off)")
     ap.add_argument("--shadows", choices=["merged", "beside", "in-order"], default="merged",
