@@ -202,3 +202,62 @@ def test_cancel_and_malformed_requests(scenes):
         server.submit_rays(sid, h_rays[:0], outs[2], REQ_CLOSEST)
     assert e.value.status == 1
     server.close()
+
+
+def test_concurrent_submitters_and_cancellers(scenes):
+    """Four host threads submit queries at once while a fifth cancels some of them: every request ends
+    exactly once, as done (bytes equal to a direct cast) or cancelled (output untouched)."""
+    import threading
+    import torch
+    s, b, scene = scenes[0]
+    server = Server(max_in_flight=4)
+    sid = server.add_scene(scene)
+    k = s.scale
+    rays = random_rays(3000, [0, 0, 0.02], [k, k, 0.4 * k], 77)
+    d_rays = torch.from_numpy(rays.view(np.uint8)).cuda()
+    d_hits = torch.empty(len(rays) * 16, dtype=torch.uint8, device="cuda")
+    P.cast_closest(scene, d_rays, d_hits, len(rays))
+    torch.cuda.synchronize()
+    want = d_hits.cpu().numpy()
+    h_rays = pinned(len(rays), P.RAY_IN_DTYPE)
+    h_rays[:] = rays
+    lock = threading.Lock()
+    subs = []
+
+    def submitter(t):
+        for i in range(12):
+            out = pinned(len(rays) * 16, np.uint8)
+            out[:] = 0x5A
+            rid = server.submit_rays(sid, h_rays, out, REQ_CLOSEST)
+            with lock:
+                subs.append((rid, out))
+
+    def canceller():
+        cancelled = 0
+        for _ in range(200):
+            with lock:
+                cand = [rid for rid, _ in subs[-4:]]
+            for rid in cand:
+                cancelled += server.cancel(rid)
+        return cancelled
+
+    threads = [threading.Thread(target=submitter, args=(t,)) for t in range(4)] + [threading.Thread(target=canceller)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    server.drain()
+    done = cancelled = 0
+    for rid, out in subs:
+        try:
+            server.wait(rid)
+            assert np.array_equal(out, want)
+            done += 1
+        except P.PheError as e:
+            assert e.status == 11 and np.all(out == 0x5A)
+            cancelled += 1
+        server.release(rid)
+    assert done + cancelled == 48 and done > 0
+    st = server.stats()
+    assert st["pending"] == 0 and st["in_flight"] == 0
+    server.close()

@@ -287,3 +287,41 @@ def test_postprocess_matches_oracle_and_writes_an_image(tmp_path):
     assert np.abs(rgba.astype(np.int32) - want).max() <= 1
     write_ppm(tmp_path / "frame.ppm", rgba)
     assert (tmp_path / "frame.ppm").stat().st_size == len(b"P6\n64 40\n255\n") + W * H * 3
+
+
+def test_renderer_lifecycle_lights_resolutions_and_resets():
+    """8 lights (the maximum), a resolution that shrinks (buffers reused) and grows again, TAA resets in
+    the middle, async read-backs across a resize: every frame equals the oracle's frame for its
+    parameters."""
+    import torch
+    s, b = built_scene("c1_64_100")
+    datas = b.slot_datas(s.datas)
+    scene = P.Scene(b.nodes, b.verts, datas, s.materials)
+    k = s.scale
+    pts = np.array([(0.5, 0.5, 2.0), (0.1, 0.9, 1.0), (0.9, 0.1, 1.5), (0.3, 0.3, 0.8), (0.7, 0.7, 1.2),
+                    (0.2, 0.6, 2.5), (0.8, 0.4, 0.9), (0.5, 0.1, 1.8)], np.float32) * np.float32(k)
+    lights8 = make_lights(pts, range_=1000.0 * k)
+    lights8["radius"][::2] = 0.02 * k          # area lights: random offsets on the light disc
+    r = CudaTracerRenderer(use_graph=True)
+    r.setStaticScene(scene)
+    cam_pos = (0.5 * k, -0.3 * k, 0.6 * k)
+    pinned = torch.empty((96, 128, 4), dtype=torch.float32, pin_memory=True).numpy()
+    for f, (res, nl, reset) in enumerate([((128, 96), 8, True), ((64, 48), 3, False), ((64, 48), 1, True),
+                                          ((128, 96), 8, False)]):
+        r.setTargetResolution(res)
+        cam = O.camera_def(cam_pos, C1_CAM["dir"], C1_CAM["up"], math.radians(60), res)
+        if reset:
+            r.resetTAA()
+        r.set_seed(40 + f, f)
+        jit = P.halton_jitter(f)
+        r.set_camera_def(cam_struct(cam), cam_pos, jit)
+        r.render(lights8[:nl])
+        raw = r.read(READ_RAW)
+        ref, rough, counts = O.render_frame(b.nodes, b.verts, datas, s.materials, lights8[:nl], cam, res, jit,
+                                            cam_pos, 40 + f, f)
+        _compare(raw, ref, f"frame {f}")
+        assert np.array_equal(r.ray_counts(), counts.astype(np.uint64))
+        out = pinned[: res[1], : res[0]].copy()
+        r.read_async(out)
+        r.read_wait()
+        assert np.array_equal(out, r.read(READ_COLOR))
