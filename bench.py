@@ -385,7 +385,9 @@ def run_ours(args, world, rank, local):
             issue = {"inst_per_cycle": nc[f"{dominant}_inst_per_cycle"], "of": 4,
                      "frac": round(nc[f"{dominant}_inst_per_cycle"] / 4, 3),
                      "simd_efficiency": nc.get(f"{dominant}_simd_efficiency"),
-                     "dram_frac": nc.get(f"{dominant}_dram_throughput"), "source": "profiles/bounce_kernel_1080p_ncu.md"}
+                     "dram_frac": nc.get(f"{dominant}_dram_throughput"),
+                     "l2_frac": nc.get(f"{dominant}_l2_throughput"), "l1_frac": nc.get(f"{dominant}_l1_throughput"),
+                     "l2_bytes": nc.get(f"{dominant}_l2_bytes"), "source": "profiles/bounce_kernel_1080p_ncu.md"}
     dom = per_kernel[dominant]
     achieved = dom.get("GB_s")
     lat = sorted(per)
