@@ -76,7 +76,7 @@ def test_large_scene_frame_band_and_incoherent_rays_match_the_oracle():
     ref, _, _ = O.render_frame(b.nodes, b.verts, datas, s.materials, lights, cam, res, jit, cam_pos, 9, 0, rows=band)
     d = np.abs(raw[band[0]:band[1]].astype(np.float64) - ref[band[0]:band[1]].astype(np.float64))
     assert (d > 1e-4).any(axis=-1).mean() <= 1e-4, d.max()
-    assert raw[band[0]:band[1], :, :3].max() > 0.01
+    assert raw[band[0]:band[1], :, :3].max() > 1e-3 and (raw[band[0]:band[1], :, :3] > 0).mean() > 0.2
     inc = random_rays(200_000, [0, 0, 0.02], [k, k, 0.3 * k], 321)
     d_rays = torch.from_numpy(inc.view(np.uint8)).cuda()
     d_hits = torch.empty(len(inc) * 16, dtype=torch.uint8, device="cuda")
