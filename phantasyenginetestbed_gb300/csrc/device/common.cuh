@@ -126,6 +126,14 @@ __device__ __forceinline__ float stdmax(float a, float b) { return (a < b) ? b :
 // ------------------------------------------------------------------------------------------------
 // Moller-Trumbore with the reference's absolute determinant epsilon (Intersection.hpp:24-67,
 // RayCastKernel.cu:96-131), on a slot stored as (p0, e1, e2). Returns true on a hit.
+//
+// Every quantity is computed with the reference's operations and rounding; only the control flow
+// differs. The reference returns early after the determinant, u and v tests; here all of u, v and t
+// are computed and the same three tests are combined into one predicate, so a rejected triangle gives
+// the same answer. In a warp the early returns saved little (the warp runs until its last lane
+// rejects), while the straight-line form has no branches and overlaps the reciprocal with the other
+// products. f = rn(1 / det) is taken as the correctly rounded reciprocal, the same value as the
+// correctly rounded quotient 1.0f / det.
 // ------------------------------------------------------------------------------------------------
 __device__ __forceinline__ bool intersect_tri(float4 a, float4 b, float4 c, f3 o, f3 d, float& t, float& u, float& v)
 {
@@ -133,18 +141,15 @@ __device__ __forceinline__ bool intersect_tri(float4 a, float4 b, float4 c, f3 o
 	f3 p0 = mk3(a.x, a.y, a.z), e1 = mk3(b.x, b.y, b.z), e2 = mk3(c.x, c.y, c.z);
 	f3 q = cross3(d, e2);
 	float det = dot3(e1, q);
-	if (-EPS < det && det < EPS) return false;
-	float f = __fdiv_rn(1.0f, det);
 	f3 s = sub3(o, p0);
-	float uu = __fmul_rn(f, dot3(s, q));
-	if (uu < 0.0f) return false;
 	f3 r = cross3(s, e1);
+	float f = __frcp_rn(det);
+	float uu = __fmul_rn(f, dot3(s, q));
 	float vv = __fmul_rn(f, dot3(d, r));
-	if (vv < 0.0f || __fadd_rn(uu, vv) > 1.0f) return false;
 	t = __fmul_rn(f, dot3(e2, r));
 	u = uu;
 	v = vv;
-	return true;
+	return !(-EPS < det && det < EPS) && !(uu < 0.0f) && !(vv < 0.0f || __fadd_rn(uu, vv) > 1.0f);
 }
 
 // ------------------------------------------------------------------------------------------------

@@ -82,10 +82,17 @@ ChildRef binary_child(const std::vector<float4>& dn, uint32_t node, int c)
 	return r;
 }
 
+// True when `inner` is a non-inverted box (lo <= hi on every axis) inside `outer`. Then, for a ray
+// with finite 1/dir, the rounded slab test gives inner an entry distance >= outer's and an exit
+// distance <= outer's on every axis ((b - o) rounds monotonically in b, and the sign of 1/dir picks
+// the same plane for both boxes), so inner passes the visit rule only if outer passes it too. An
+// inverted box (lo > hi) is tested by the reference's min/max slab code as the swapped interval,
+// which need not lie inside outer.
 bool contains(const float* outer, const float* inner)
 {
 	return inner[0] >= outer[0] && inner[1] >= outer[1] && inner[2] >= outer[2] && inner[3] <= outer[3] &&
-	       inner[4] <= outer[4] && inner[5] <= outer[5];
+	       inner[4] <= outer[4] && inner[5] <= outer[5] && inner[0] <= inner[3] && inner[1] <= inner[4] &&
+	       inner[2] <= inner[5];
 }
 
 // Collapses the binary tree (traversal layout `dn`) into 4-wide nodes: a binary node's inner children

@@ -255,3 +255,28 @@ def test_wide_layout_gives_the_binary_results():
     assert np.array_equal(_gpu_any(scene, rays), binary_any)
     orc = O.cast_rays(b.nodes, b.verts, rays)
     _check(O.compare_closest(_gpu_closest(scene, rays), orc, rays, b.slot_to_tri, b.verts), len(rays))
+
+
+def test_inverted_child_box_keeps_the_binary_layout():
+    """A child box stored with lo > hi on one axis is valid input (the reference's min/max slab test
+    treats it as the swapped interval) but breaks the box nesting the 4-wide collapse relies on: the
+    scene offers the binary layout only, refuses the 4-wide one, and its casts match the oracle."""
+    s, b = built_scene("c1_64_100")
+    nodes = b.nodes.copy()
+    root = nodes[0]
+    inner = [int(root["iData"][c]) for c in range(2) if root["iData"][2 + c] == 0]
+    assert inner, "root has no inner child"
+    child = inner[0]
+    box = nodes[child]["fData"]
+    box[0], box[3] = box[3], box[0]          # first child box of that node: swap lo.x and hi.x
+    assert box[0] > box[3]
+    scene = P.Scene(nodes, b.verts)
+    assert scene.layout() == (0, False)
+    with pytest.raises(P.PheError):
+        scene.set_layout(1)
+    k = s.scale
+    cam = O.camera_def((0.5 * k, -0.3 * k, 0.6 * k), C1_CAM["dir"], C1_CAM["up"], math.radians(60), (256, 256))
+    rays = np.concatenate([O.gen_primary(cam, (256, 256)), random_rays(20000, [0, 0, 0.02], [k, k, 0.3 * k], 4)])
+    orc = O.cast_rays(nodes, b.verts, rays)
+    _check(O.compare_closest(_gpu_closest(scene, rays), orc, rays, b.slot_to_tri, b.verts), len(rays))
+    assert np.array_equal(_gpu_any(scene, rays), O.any_rays(nodes, b.verts, rays))
