@@ -126,24 +126,21 @@ __device__ __forceinline__ uint32_t traverse(const float4* __restrict__ nodes, c
 			float tIn0, tIn1;
 			bool v0 = visit_box<SAFE>(r, b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, hit.t, tIn0);
 			bool v1 = visit_box<SAFE>(r, b1.z, b1.w, b2.x, b2.y, b2.z, b2.w, hit.t, tIn1);
-			if (!v0 && !v1) {
-				nodeAddr = stack.get(sp--);
-			} else {
-				nodeAddr = v0 ? ix.x : ix.y;
-				if (v0 && v1) {
-					int32_t other = ix.y;
-					if (!ANY && tIn1 < tIn0) {
-						other = ix.x;
-						nodeAddr = ix.y;
-					}
+			{
+				const bool both = v0 && v1;
+				const bool swp = !ANY && both && tIn1 < tIn0;
+				int32_t nearC = (v0 && !swp) ? ix.x : ix.y;
+				int32_t farC = swp ? ix.x : ix.y;
+				if (both) {
 					if (sp >= kStackSize - 1) {
 						err |= kErrStackOverflow;
 						nodeAddr = kSentinel;
 						leafAddr = 0;
 						break;
 					}
-					stack.set(++sp, other);
+					stack.set(++sp, farC);
 				}
+				nodeAddr = (v0 || v1) ? nearC : stack.get(sp--);
 			}
 			if (nodeAddr < 0 && leafAddr >= 0) {
 				leafAddr = nodeAddr;

@@ -35,8 +35,12 @@ constexpr int kWaveBlock = 128;
 // Resident blocks per SM asked of the compiler for the fused traversal + shading kernels: caps them
 // at 64 registers (32 warps per SM instead of 20-24). The spills this costs sit in the shading code;
 // measured on GB300 at 1080p: 8 blocks 0.893 ms per frame, 9 0.926, 10 0.915, 12 0.959, uncapped
-// (88-92 registers) 0.970.
+// (88-92 registers) 0.970. With the branch-free triangle test (fewer live values) the bounce kernel,
+// whose incoherent rays wait longest on node fetches, gains from more resident warps while the
+// primary kernel does not: bounce pass 0.369 ms at 10 blocks (48 registers) vs 0.376 at 8 and 0.377
+// at 12; primary 0.242 ms at 8 vs 0.245 at 9 or 10.
 constexpr int kWaveMinBlocks = 8;
+constexpr int kBounceMinBlocks = 10;
 const size_t kStackSmem = stack_smem_bytes(kWaveBlock);   // dynamic shared memory of the traversal kernels
 
 __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
@@ -258,7 +262,7 @@ __global__ void __launch_bounds__(kBinBlock) bin_bounce_kernel(FrameBuffers fb)
 }
 
 template <bool WIDE>
-__global__ void __launch_bounds__(kWaveBlock, kWaveMinBlocks) bounce_kernel(DeviceScene s, const FrameParamsDev* __restrict__ fpp,
+__global__ void __launch_bounds__(kWaveBlock, kBounceMinBlocks) bounce_kernel(DeviceScene s, const FrameParamsDev* __restrict__ fpp,
                                                             FrameBuffers fb, uint32_t* __restrict__ status)
 {
 	const FrameParamsDev& fp = *fpp;
