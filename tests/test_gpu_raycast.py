@@ -280,3 +280,46 @@ def test_inverted_child_box_keeps_the_binary_layout():
     orc = O.cast_rays(nodes, b.verts, rays)
     _check(O.compare_closest(_gpu_closest(scene, rays), orc, rays, b.slot_to_tri, b.verts), len(rays))
     assert np.array_equal(_gpu_any(scene, rays), O.any_rays(nodes, b.verts, rays))
+
+
+@pytest.mark.parametrize("a", [3.16e-3, 3.17e-3, 3.2e-3, 3.25e-3, 1.0e-2])
+def test_triangle_test_decision_boundaries(a):
+    """One small right triangle (legs a, so det = a^2 |d.z| for a ray along d) hit by rays whose
+    |det| falls on both sides of the reference's 1e-5 epsilon, aimed at points of the barycentric grid
+    that include the edges u = 0, v = 0, u + v = 1 and the vertices, each also nudged by one ulp. Every
+    hit/miss decision and every t, u, v bit equals the oracle's (the reference traversal restated, GPU
+    accept rule), for closest and any hit. The edges lie on faces of the triangle's flat bounding box,
+    so rays aimed at them also exercise the rounded slab test there. At a = 3.16e-3, a^2 < 1e-5: every
+    ray misses."""
+    p0 = np.array([0.25, 0.5, 0.1], np.float32)
+    tv = np.concatenate([p0, p0 + np.float32([a, 0, 0]), p0 + np.float32([0, a, 0])]).astype(np.float32)[None, :]
+    b = P.build_sbvh(tv)
+    scene = P.Scene(b.nodes, b.verts)
+    g = np.array([0.0, 0.25, 0.5, 0.75, 1.0], np.float32)
+    uv = np.array([(u, v) for u in g for v in g if u + v <= 1.0], np.float32)
+    aim = p0 + uv[:, :1] * np.float32(a) * np.float32([1, 0, 0]) + uv[:, 1:] * np.float32(a) * np.float32([0, 1, 0])
+    aim = aim.astype(np.float32)
+    aim = np.concatenate([aim, np.nextafter(aim, np.float32(-1)), np.nextafter(aim, np.float32(2))])
+    dz = np.linspace(-1.0, -0.9, 64, dtype=np.float32)              # |d.z| from 1 down to 0.9
+    az = np.linspace(0, 2 * np.pi, 7, endpoint=False)
+    rays = []
+    for z in dz:
+        for phi in az:
+            sxy = np.sqrt(1 - z * z)
+            d = np.array([sxy * np.cos(phi), sxy * np.sin(phi), z], np.float32)
+            o = (aim - d * np.float32(0.3)).astype(np.float32)
+            r = np.zeros(len(aim), P.RAY_IN_DTYPE)
+            r["origin"], r["dir"], r["tMin"], r["tMax"] = o, d, np.float32(1e-4), np.float32(3.4028235e38)
+            rays.append(r)
+    rays = np.concatenate(rays)
+    bf = O.cast_rays(b.nodes, b.verts, rays, mode=O.MODE_GPU)
+    gpu = _gpu_closest(scene, rays)
+    hit = gpu["triangleIndex"] != 0xFFFFFFFF
+    assert np.array_equal(hit, bf["triangleIndex"] != 0xFFFFFFFF)
+    if a * a < 1e-5:
+        assert not hit.any()                                         # every |det| is below the epsilon
+    else:
+        assert 0.02 < hit.mean() < 0.95, hit.mean()                  # both sides of the epsilon and the edges
+    for f in ("t", "u", "v"):
+        assert np.array_equal(gpu[f][hit].view(np.uint32), bf[f][hit].view(np.uint32)), f
+    assert np.array_equal(_gpu_any(scene, rays), (bf["triangleIndex"] == 0xFFFFFFFF).astype(np.uint8))
