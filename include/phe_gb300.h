@@ -349,11 +349,12 @@ phe_status phe_renderer_result(const phe_renderer* renderer, phe_render_result* 
  * 3 = roughness: 4 bytes per pixel; 4 = TAA velocity: 2 floats per pixel, in uv units). Synchronises
  * `stream`. The headless stand-in for reading the GL result texture. */
 phe_status phe_renderer_read(const phe_renderer* renderer, int which, void* hostDst, void* stream);
-/* Asynchronous read-back for frame pipelines: snapshots the buffer into one of two device staging
- * slots on `stream` (so the next frames may overwrite it) and copies the snapshot to `hostDst` on the
- * renderer's copy stream, overlapping the frames queued after it. Returns at once. `hostDst` must be
- * pinned for the copy to be asynchronous, and holds the image once phe_renderer_read_wait returns (or
- * two read_async calls later, whose snapshot waits for this copy). */
+/* Asynchronous read-back for frame pipelines: copies the buffer to `hostDst` on the renderer's copy
+ * stream after the work queued on `stream`, overlapping the frames queued after it. Returns at once.
+ * Colour, history and velocity are kept per side of the frame parity and copied in place (the frame
+ * after next, which rewrites that side, waits for the copy); raw colour and roughness are first
+ * snapshot into one of two device staging slots on `stream`. `hostDst` must be pinned for the copy to
+ * be asynchronous, and holds the image once phe_renderer_read_wait returns. */
 phe_status phe_renderer_read_async(phe_renderer* renderer, int which, void* hostDst, void* stream);
 /* Waits until every read_async copy issued so far has landed in host memory. */
 phe_status phe_renderer_read_wait(phe_renderer* renderer);

@@ -58,6 +58,12 @@ struct phe_renderer {
 	cudaEvent_t snapEvents[2] = {}, doneEvents[2] = {};
 	bool readPending[2] = {false, false};
 	uint32_t readSlot = 0;
+	// Results kept per side of the frame parity (TAA colour, history, velocity) are copied out directly:
+	// sideDone[s] follows the last copy from side s, and the next frame that writes side s (the one
+	// after next) waits for it (sideGuard[s]).
+	cudaEvent_t readyEvent = nullptr;
+	cudaEvent_t sideDone[2] = {};
+	bool sideGuard[2] = {false, false};
 };
 
 static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
@@ -107,7 +113,7 @@ static phe_status allocate(phe_renderer* r, uint32_t resX, uint32_t resY, uint32
 		P * sizeof(float4),           // rawColor
 		P * sizeof(float4),           // history[0]
 		P * sizeof(float4),           // history[1]
-		P * sizeof(float4),           // color
+		P * sizeof(float4),           // color[0]
 		kNumCounters * sizeof(uint32_t),
 		P * sizeof(phe_ray_hit),      // primaryHits
 		P * sizeof(phe_ray_hit),      // bounceHits
@@ -115,6 +121,7 @@ static phe_status allocate(phe_renderer* r, uint32_t resX, uint32_t resY, uint32
 		P * sizeof(uint32_t),         // bouncePerm
 		P * sizeof(float2),           // velocity[0]
 		P * sizeof(float2),           // velocity[1]
+		P * sizeof(float4),           // color[1]
 	};
 	size_t total = 0;
 	for (size_t s : sizes) total += align256(s);
@@ -135,7 +142,7 @@ static phe_status allocate(phe_renderer* r, uint32_t resX, uint32_t resY, uint32
 	fb.rawColor = (float4*)take(8);
 	fb.history[0] = (float4*)take(9);
 	fb.history[1] = (float4*)take(10);
-	fb.color = (float4*)take(11);
+	fb.color[0] = (float4*)take(11);
 	fb.counters = (uint32_t*)take(12);
 	fb.primaryHits = (phe_ray_hit*)take(13);
 	fb.bounceHits = (phe_ray_hit*)take(14);
@@ -143,6 +150,7 @@ static phe_status allocate(phe_renderer* r, uint32_t resX, uint32_t resY, uint32
 	fb.bouncePerm = (uint32_t*)take(16);
 	fb.velocity[0] = (float2*)take(17);
 	fb.velocity[1] = (float2*)take(18);
+	fb.color[1] = (float4*)take(19);
 	fb.sortWindow = r->sortWindow;
 	fb.capacityLP = (uint32_t)LP;
 	fb.refill = r->refill;
@@ -290,7 +298,9 @@ extern "C" phe_status phe_renderer_destroy(phe_renderer* r)
 		if (r->staging[i]) cudaFree(r->staging[i]);
 		if (r->snapEvents[i]) cudaEventDestroy(r->snapEvents[i]);
 		if (r->doneEvents[i]) cudaEventDestroy(r->doneEvents[i]);
+		if (r->sideDone[i]) cudaEventDestroy(r->sideDone[i]);
 	}
+	if (r->readyEvent) cudaEventDestroy(r->readyEvent);
 	if (r->copyStream) cudaStreamDestroy(r->copyStream);
 	if (r->streams.side) cudaStreamDestroy(r->streams.side);
 	if (r->streams.fork) cudaEventDestroy(r->streams.fork);
@@ -367,10 +377,24 @@ extern "C" phe_status phe_renderer_set_graph(phe_renderer* r, int enable)
 	return PHE_OK;
 }
 
+// Orders work on `s` that rewrites side `side` of the parity buffers after the asynchronous copies
+// still reading it.
+static phe_status guard_side(phe_renderer* r, uint32_t side, cudaStream_t s)
+{
+	if (!r->sideGuard[side]) return PHE_OK;
+	PHE_CUDA_TRY(cudaStreamWaitEvent(s, r->sideDone[side], 0), "wait for read-back of the side");
+	r->sideGuard[side] = false;
+	return PHE_OK;
+}
+
 extern "C" phe_status phe_renderer_reset_taa(phe_renderer* r, void* stream)
 {
 	if (!r || !r->allocation) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_reset_taa: no frame buffers");
 	size_t P = (size_t)r->resX * r->resY;
+	for (uint32_t side = 0; side < 2; side++) {
+		phe_status st = guard_side(r, side, (cudaStream_t)stream);
+		if (st) return st;
+	}
 	PHE_CUDA_TRY(cudaMemsetAsync(r->fb.history[0], 0, P * sizeof(float4), (cudaStream_t)stream), "reset TAA");
 	PHE_CUDA_TRY(cudaMemsetAsync(r->fb.history[1], 0, P * sizeof(float4), (cudaStream_t)stream), "reset TAA");
 	r->hasPrevCam = false;
@@ -438,6 +462,10 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 	fp.seed = r->seed;
 	std::memset(fp.lights, 0, sizeof(fp.lights));
 	if (numLights) std::memcpy(fp.lights, lights, sizeof(phe_sphere_light) * numLights);
+	{
+		phe_status gst = guard_side(r, outSide, s);   // this frame rewrites side outSide
+		if (gst) return gst;
+	}
 	PHE_CUDA_TRY(cudaMemcpyAsync(r->dParams, &fp, sizeof(FrameParamsDev), cudaMemcpyHostToDevice, s),
 	             "upload frame parameters");
 	PHE_CUDA_TRY(cudaEventRecord(r->paramEvents[slot], s), "record parameter slot");
@@ -495,7 +523,7 @@ extern "C" phe_status phe_renderer_result(const phe_renderer* r, phe_render_resu
 	if (!r || !out) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_result: null argument");
 	out->resX = r->resX;
 	out->resY = r->resY;
-	out->color = (const float*)r->fb.color;
+	out->color = (const float*)r->fb.color[r->parity];   // written by the last frame
 	out->history = (const float*)r->fb.history[r->parity];   // written by the last frame
 	out->rawColor = (const float*)r->fb.rawColor;
 	out->roughness = r->fb.roughness;
@@ -521,7 +549,7 @@ static phe_status read_source(const phe_renderer* r, int which, const void** src
 	size_t P = (size_t)r->resX * r->resY;
 	*bytes = P * sizeof(float4);
 	switch (which) {
-	case 0: *src = r->fb.color; break;
+	case 0: *src = r->fb.color[r->parity]; break;
 	case 1: *src = r->fb.history[r->parity]; break;
 	case 2: *src = r->fb.rawColor; break;
 	case 3: *src = r->fb.roughness; *bytes = P * sizeof(float); break;
@@ -561,7 +589,20 @@ extern "C" phe_status phe_renderer_read_async(phe_renderer* r, int which, void* 
 		for (int i = 0; i < 2; i++) {
 			PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->snapEvents[i], cudaEventDisableTiming), "create read event");
 			PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->doneEvents[i], cudaEventDisableTiming), "create read event");
+			PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->sideDone[i], cudaEventDisableTiming), "create read event");
 		}
+		PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->readyEvent, cudaEventDisableTiming), "create read event");
+	}
+	// TAA colour, history and a stored velocity live on the side the last frame wrote; the next frame
+	// only reads that side, so the copy reads it in place and the frame after next waits for the copy.
+	if (src && (which == 0 || which == 1 || which == 4)) {
+		const uint32_t side = r->parity;
+		PHE_CUDA_TRY(cudaEventRecord(r->readyEvent, s), "record frame end");
+		PHE_CUDA_TRY(cudaStreamWaitEvent(r->copyStream, r->readyEvent, 0), "order read-back");
+		PHE_CUDA_TRY(cudaMemcpyAsync(hostDst, src, bytes, cudaMemcpyDeviceToHost, r->copyStream), "read result");
+		PHE_CUDA_TRY(cudaEventRecord(r->sideDone[side], r->copyStream), "record read-back");
+		r->sideGuard[side] = true;
+		return PHE_OK;
 	}
 	if (bytes > r->stagingBytes) {   // grow both slots once no copy uses them
 		if ((st = phe_renderer_read_wait(r))) return st;
@@ -594,6 +635,8 @@ extern "C" phe_status phe_renderer_read_wait(phe_renderer* r)
 			PHE_CUDA_TRY(cudaEventSynchronize(r->doneEvents[i]), "wait for read-back");
 			r->readPending[i] = false;
 		}
+	for (int i = 0; i < 2; i++)   // an event never recorded counts as complete
+		if (r->sideDone[i]) PHE_CUDA_TRY(cudaEventSynchronize(r->sideDone[i]), "wait for read-back");
 	return PHE_OK;
 }
 

@@ -75,10 +75,13 @@ struct Wave {
 	bool busy = false;
 };
 
-// Device bytes a render slot holds for a frame of P pixels and L lights (the renderer's buffers).
+// Device bytes a render slot holds for a frame of P pixels and L lights (the renderer's buffers):
+// per light and pixel, two contributions, visibilities, shadow rays and slots; per pixel, the bounce
+// ray, pixel, throughput and permutation, roughness, raw colour, two histories, two TAA colours, two
+// hit records and two velocities.
 uint64_t render_bytes(uint64_t P, uint64_t L)
 {
-	return 2 * L * P * (16 + 1 + 32 + 4) + P * (32 + 4 + 16 + 4 + 16 * 4 + 16 * 2) + 4096;
+	return 2 * L * P * (16 + 1 + 32 + 4) + P * (32 + 4 + 16 + 4 + 4 + 16 + 16 * 2 + 16 * 2 + 16 * 2 + 8 * 2) + 4096;
 }
 
 uint64_t query_bytes(const phe_request& r)

@@ -571,7 +571,7 @@ __global__ void resolve_taa_kernel(const FrameParamsDev* __restrict__ fpp, Frame
 		taa_pixel(x, y, fp.resX, fp.resY, cur, fb.history[fp.parity], fp.velocity, fp.prevVelocity, fb.roughness[pid],
 		          oc, oh);
 		fb.rawColor[pid] = cur;
-		fb.color[pid] = oc;
+		fb.color[fp.parity ^ 1u][pid] = oc;
 		fb.history[fp.parity ^ 1u][pid] = oh;
 		return;
 	}
@@ -592,7 +592,7 @@ __global__ void resolve_taa_kernel(const FrameParamsDev* __restrict__ fpp, Frame
 	float4 oc, oh;
 	taa_blend(cur, h, clampf(__fsub_rn(1.0f, __fmul_rn(glsl_mix(3.0f, 1.0f, rough), 0.0f)), 0.0f, 1.0f), oc, oh);
 	st_stream(fb.rawColor + pid, cur);
-	st_stream(fb.color + pid, oc);
+	st_stream(fb.color[fp.parity ^ 1u] + pid, oc);
 	st_stream(fb.history[fp.parity ^ 1u] + pid, oh);
 }
 

@@ -54,7 +54,7 @@ struct FrameBuffers {
 	float4* rawColor;         // [P] resolved colour before TAA
 	float4* history[2];       // [P] TAA history ping-pong (rgb + effective sample count)
 	float2* velocity[2];      // [P] uv velocity ping-pong (same side as the history)
-	float4* color;            // [P] TAA output
+	float4* color[2];         // [P] TAA output ping-pong (same side as the history it was blended into)
 	uint32_t* counters;       // [kNumCounters]
 	uint32_t capacityLP;      // L * P
 	phe_ray_hit* primaryHits; // [P] closest hits of the primary rays, in 8x8-tile ray order

@@ -114,8 +114,9 @@ def test_wide_layout_frame_gives_the_binary_frame(graph):
 
 
 def test_async_read_back_matches_the_blocking_read():
-    """read_async snapshots each frame while later frames overwrite the buffer; after read_wait every
-    host image equals the blocking read of the same frame."""
+    """read_async copies each frame's result while later frames render (colour and history from the
+    side of the frame parity they were written to, roughness through a snapshot); after read_wait
+    every host image equals the blocking read of the same frame."""
     import torch
     res = (320, 184)
     s, b, datas, scene, cam, cam_pos, lights, r = _setup("c2_256_2000", res, [(0.5, 0.5, 2.0)], graph=True)
@@ -126,20 +127,23 @@ def test_async_read_back_matches_the_blocking_read():
     for f in range(frames):
         r.set_camera_def(cam_struct(cam), cam_pos, P.halton_jitter(f))
         r.render(lights)
-        want.append((r.read(READ_COLOR), r.read(READ_ROUGHNESS)))
+        want.append((r.read(READ_COLOR), r.read(READ_ROUGHNESS), r.read(READ_HISTORY)))
     got = [torch.empty((res[1], res[0], 4), dtype=torch.float32, pin_memory=True).numpy() for _ in range(frames)]
+    hist = [torch.empty((res[1], res[0], 4), dtype=torch.float32, pin_memory=True).numpy() for _ in range(frames)]
     rough = np.empty((res[1], res[0]), np.float32)        # pageable destination works too
     r.set_seed(3, 0)
     r.resetTAA()
     for f in range(frames):
         r.set_camera_def(cam_struct(cam), cam_pos, P.halton_jitter(f))
         r.render(lights)
-        r.read_async(got[f])
+        r.read_async(got[f])                              # colour and history: copied in place
+        r.read_async(hist[f], READ_HISTORY)
         if f == frames - 1:
-            r.read_async(rough, READ_ROUGHNESS)
+            r.read_async(rough, READ_ROUGHNESS)           # single-buffered: copied through a snapshot
     r.read_wait()
     for f in range(frames):
         assert np.array_equal(got[f], want[f][0]), f
+        assert np.array_equal(hist[f], want[f][2]), f
     assert np.array_equal(rough, want[-1][1])
     with pytest.raises(ValueError):
         r.read_async(np.empty(10, np.float32))
