@@ -252,21 +252,20 @@ void upload_scene_table(phe_server* s)
 	s->sceneTableDirty = false;
 }
 
-// Serial baseline: one request at a time with plain launches, waiting for each.
-void serve_serial(phe_server* s, Request* r)
+// Serial baseline: one request at a time with plain launches, waiting for each. Called with the lock
+// held; it is released only while waiting for the GPU, with the request in `inflight`, so that
+// drain() and the stop condition still see it and every change of shared state happens under the lock.
+void serve_serial(phe_server* s, Request* r, std::unique_lock<std::mutex>& lock)
 {
 	const phe_request& d = r->desc;
 	r->tAdmit = now_ms(s->t0);
 	phe_status ps = PHE_OK;
+	cudaStream_t wait = nullptr;
+	RenderSlot* slot = nullptr;
 	if (d.kind == PHE_REQ_RENDER) {
-		RenderSlot& slot = s->slots[0];
-		ps = issue_render(s, r, slot);
-		if (!ps) {
-			s->inflight.pop_back();
-			cudaStreamSynchronize(slot.stream);
-			r->rays = slot.totals[0] + slot.totals[1] + slot.totals[2] + slot.totals[3];
-			slot.busy = nullptr;
-		}
+		slot = &s->slots[0];
+		ps = issue_render(s, r, *slot);   // on success the request is in inflight
+		if (!ps) wait = slot->stream;
 	} else {
 		ps = admit_query(s, r);
 		if (!ps) {
@@ -279,11 +278,23 @@ void serve_serial(phe_server* s, Request* r)
 			if (!ps) cudaMemcpyAsync(d.out, out, outBytes, cudaMemcpyDeviceToHost, s->waveStream);
 			cudaFreeAsync(r->dMem, s->waveStream);
 			r->dMem = nullptr;
-			cudaStreamSynchronize(s->waveStream);
 			r->rays = d.numRays;
+			r->state = kIssued;
+			s->inflight.push_back(r);
+			wait = s->waveStream;
 		}
 	}
-	if (r->done) { s->eventPool.push_back(r->done); r->done = nullptr; }
+	if (wait) {
+		lock.unlock();
+		cudaError_t e = cudaStreamSynchronize(wait);
+		lock.lock();
+		s->inflight.erase(std::find(s->inflight.begin(), s->inflight.end(), r));
+		if (slot) {
+			r->rays = slot->totals[0] + slot->totals[1] + slot->totals[2] + slot->totals[3];
+			slot->busy = nullptr;
+		}
+		if (e != cudaSuccess && !ps) ps = cuda_fail(e, "request");
+	}
 	finish(s, r, ps);
 }
 
@@ -301,9 +312,7 @@ void worker_loop(phe_server* s)
 				Request* r = s->pending.front();
 				s->pending.pop_front();
 				s->bytesInUse += r->bytes;
-				lock.unlock();
-				serve_serial(s, r);
-				lock.lock();
+				serve_serial(s, r, lock);
 				s->cvDone.notify_all();
 				continue;
 			}

@@ -261,3 +261,27 @@ def test_concurrent_submitters_and_cancellers(scenes):
     st = server.stats()
     assert st["pending"] == 0 and st["in_flight"] == 0
     server.close()
+
+
+@pytest.mark.parametrize("serial", [True, False])
+def test_drain_returns_after_every_request(scenes, serial):
+    """drain() returns only once every submitted request is done: none polls as not ready afterwards,
+    including the last request of the serial baseline, which its worker serves with the lock released
+    while it waits for the GPU."""
+    server = Server(serial=serial, render_slots=1)
+    ids = [server.add_scene(x[2]) for x in scenes]
+    s = scenes[0][0]
+    for rep in range(3):
+        subs = []
+        for i in range(6):
+            n = 2000 + 3000 * i
+            rays = pinned(n, P.RAY_IN_DTYPE)
+            rays[:] = random_rays(n, [0, 0, 0.02], [s.scale, s.scale, 0.4 * s.scale], 40 + 10 * rep + i)
+            out = pinned(n * 16, np.uint8)
+            subs.append((server.submit_rays(ids[i % 2], rays, out, REQ_CLOSEST), rays, out))
+        server.drain()
+        for rid, rays, out in subs:
+            st = server.poll(rid)
+            assert st is not None and st.status == 0, (rep, rid)
+            server.release(rid)
+    server.close()
