@@ -71,6 +71,11 @@ static const uint32_t kParamSlots = 8;
 
 static void free_buffers(phe_renderer* r)
 {
+	// in-place read-backs may still be copying out of these buffers
+	for (int i = 0; i < 2; i++) {
+		if (r->sideDone[i]) cudaEventSynchronize(r->sideDone[i]);
+		r->sideGuard[i] = false;
+	}
 	if (r->graphExec) cudaGraphExecDestroy(r->graphExec);
 	r->graphExec = nullptr;
 	if (r->allocation) cudaFree(r->allocation);
@@ -290,6 +295,7 @@ extern "C" phe_status phe_renderer_destroy(phe_renderer* r)
 {
 	if (!r) return PHE_OK;
 	cudaDeviceSynchronize();
+	free_buffers(r);   // first: it waits on the read-back events destroyed below
 	for (int i = 0; i <= kFrameKernels; i++)
 		if (r->events[i]) cudaEventDestroy(r->events[i]);
 	for (uint32_t i = 0; i < kParamSlots; i++)
@@ -299,13 +305,13 @@ extern "C" phe_status phe_renderer_destroy(phe_renderer* r)
 		if (r->snapEvents[i]) cudaEventDestroy(r->snapEvents[i]);
 		if (r->doneEvents[i]) cudaEventDestroy(r->doneEvents[i]);
 		if (r->sideDone[i]) cudaEventDestroy(r->sideDone[i]);
+		r->sideDone[i] = nullptr;
 	}
 	if (r->readyEvent) cudaEventDestroy(r->readyEvent);
 	if (r->copyStream) cudaStreamDestroy(r->copyStream);
 	if (r->streams.side) cudaStreamDestroy(r->streams.side);
 	if (r->streams.fork) cudaEventDestroy(r->streams.fork);
 	if (r->streams.join) cudaEventDestroy(r->streams.join);
-	free_buffers(r);
 	cudaFree(r->dParams);
 	cudaFreeHost(r->hParams);
 	delete r;

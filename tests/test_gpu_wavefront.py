@@ -329,3 +329,37 @@ def test_renderer_lifecycle_lights_resolutions_and_resets():
         r.read_async(out)
         r.read_wait()
         assert np.array_equal(out, r.read(READ_COLOR))
+
+
+def test_async_read_back_across_a_reallocation():
+    """An in-place read-back still in flight when a larger frame makes the renderer reallocate its
+    buffers lands intact: the reallocation waits for it."""
+    import torch
+    s, b = built_scene("c1_64_100")
+    scene = P.Scene(b.nodes, b.verts, b.slot_datas(s.datas), s.materials)
+    k = s.scale
+    cam_pos = (0.5 * k, -0.3 * k, 0.6 * k)
+    lights = make_lights(np.array([(0.5, 0.5, 2.0)] * 8, np.float32) * np.float32(k), range_=1000.0 * k)
+    r = CudaTracerRenderer(use_graph=True)
+    r.setStaticScene(scene)
+    small, big = (64, 48), (512, 384)
+    r.setTargetResolution(small)
+    r.set_seed(5, 0)
+    r.resetTAA()
+    r.set_camera_def(cam_struct(O.camera_def(cam_pos, C1_CAM["dir"], C1_CAM["up"], math.radians(60), small)), cam_pos,
+                     P.halton_jitter(0))
+    r.render(lights[:1])
+    want_color, want_hist = r.read(READ_COLOR), r.read(READ_HISTORY)
+    out = torch.empty((small[1], small[0], 4), dtype=torch.float32, pin_memory=True).numpy()
+    hist = torch.empty((small[1], small[0], 4), dtype=torch.float32, pin_memory=True).numpy()
+    r.read_async(out)
+    r.read_async(hist, READ_HISTORY)
+    r.setTargetResolution(big)              # more pixels and lights: new frame buffers
+    r.resetTAA()
+    r.set_camera_def(cam_struct(O.camera_def(cam_pos, C1_CAM["dir"], C1_CAM["up"], math.radians(60), big)), cam_pos,
+                     P.halton_jitter(1))
+    r.render(lights)
+    r.read_wait()
+    assert np.array_equal(out, want_color)
+    assert np.array_equal(hist, want_hist)
+    assert r.read(READ_COLOR).shape[:2] == (big[1], big[0])
