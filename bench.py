@@ -62,10 +62,11 @@ def parse():
                     help="shadow-pass schedule: one pass over both queues after the bounce pass (default), the "
                          "primary shadow pass beside the bounce pass, or each after its own pass")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--workload", choices=["frame", "plain", "batch", "large", "serve"], default="frame",
+    ap.add_argument("--workload", choices=["frame", "plain", "batch", "large", "serve", "sizes"], default="frame",
                     help="frame (default, the headline): 1080p wavefront frame; batch: 64 uneven batches over 4 "
                          "scenes in one launch vs 64 plain launches; large: 8.6M-triangle scene, 4096x4096, 4 "
-                         "lights; serve: Poisson request arrivals through the serving loop")
+                         "lights; serve: Poisson request arrivals through the serving loop; sizes: launch time "
+                         "against rays per launch (16K..16M) for each ray-cast entry point")
     ap.add_argument("--rates", default="200,500,1000", help="serve: arrival rates (requests/s)")
     ap.add_argument("--duration", type=float, default=2.0, help="serve: seconds of arrivals per rate")
     ap.add_argument("--render-slots", type=int, default=8, help="serve: concurrent render requests")
@@ -618,6 +619,50 @@ def run_batch(args):
     print(json.dumps(line), flush=True)
 
 
+def run_sizes(args):
+    """Launch time against batch size on the 155,072-triangle scene: 16K..16M rays per launch through
+    phe_cast_closest (persistent warps), phe_cast_closest_plain (one ray per thread) and phe_cast_any,
+    for coherent rays (a 4096x4096 pinhole camera, 8x8-tile order) and incoherent rays (uniform origins
+    above the terrain, uniform directions, seeded). L2 flushed before each timed launch; median of
+    args.steps launches."""
+    import torch
+    import phantasyenginetestbed_gb300 as P
+    torch.cuda.set_device(0)
+    stream = torch.cuda.current_stream()
+    s, b, _ = _scene_with_bvh("c2_256_2000")
+    scene = P.Scene(b.nodes, b.verts)
+    k = s.scale
+    res = (4096, 4096)
+    N = res[0] * res[1]
+    coherent = torch.empty(N * 32, dtype=torch.uint8, device="cuda")
+    P.gen_primary_rays(coherent, P.camera_def((0.5 * k, -0.3 * k, 0.6 * k), CAM_DIR, CAM_UP, 60.0, res), res, order=1)
+    rng = np.random.default_rng(SEED)
+    inc = np.zeros(N, P.RAY_IN_DTYPE)
+    inc["origin"] = rng.uniform([0, 0, 0.02 * k], [k, k, 0.3 * k], (N, 3)).astype(np.float32)
+    d = rng.normal(size=(N, 3))
+    inc["dir"] = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    inc["tMin"], inc["tMax"] = np.float32(1e-4), np.float32(3.4028235e38)
+    incoherent = torch.from_numpy(inc.view(np.uint8)).cuda()
+    hits = torch.empty(N * 16, dtype=torch.uint8, device="cuda")
+    vis = torch.empty(N, dtype=torch.uint8, device="cuda")
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    out = {}
+    for rname, rays in (("coherent", coherent), ("incoherent", incoherent)):
+        for n in (1 << 14, 1 << 16, 1 << 18, 1 << 20, 1 << 22, 1 << 24):
+            row = {}
+            for name, fn in (("closest_persistent", lambda: P.cast_closest(scene, rays, hits, n, stream=stream)),
+                             ("closest_plain", lambda: P.cast_closest_plain(scene, rays, hits, n, stream=stream)),
+                             ("any", lambda: P.cast_any(scene, rays, vis, n, stream=stream))):
+                for _ in range(args.warmup):
+                    fn()
+                t = statistics.median(_timed(fn, args.steps, stream, flush))
+                row[name] = {"ms": round(t, 4), "Mrays_s": round(n / t / 1e3, 1)}
+            out[f"{rname}_{n}"] = row
+    line = {"workload": "sizes", "metric": METRIC, "unit": "Mrays/s", "triangles": int(len(s.tri_verts)),
+            "launches": out, "l2": "flushed before every timed launch"}
+    print(json.dumps(line), flush=True)
+
+
 def run_large(args):
     """8.63M-triangle scene (2048x2048-cell heightfield + 20,000 cubes, world x32), 4096x4096 frame with
     4 point lights: 16.8M primary rays, ~16M bounce rays (cosine-weighted), shadow rays to 4 lights."""
@@ -794,7 +839,8 @@ def main():
     elif args.workload == "frame":
         run_ours(args, world, rank, local)
     else:
-        {"plain": run_plain, "batch": run_batch, "large": run_large, "serve": run_serve}[args.workload](args)
+        {"plain": run_plain, "batch": run_batch, "large": run_large, "serve": run_serve,
+         "sizes": run_sizes}[args.workload](args)
 
 
 if __name__ == "__main__":
