@@ -188,10 +188,22 @@ def cpu_frame_rate(s, b, cam_pos, lights, min_seconds=8.0, max_frames=40, warm=1
     return rays / el / 1e6, threads, frames, times
 
 
+FRAME_WORKLOAD = (f"wavefront frame {RES[0]}x{RES[1]}: primary closest -> shade + 1 any-hit shadow ray per light -> "
+                  "cosine bounce closest -> shade + shadow -> resolve + TAA")
+FRAME_DATA = "synthetic (seeded heightfield + cubes scene, 155,072 triangles; the reference's Sponza is not in its tree)"
+
+
+def frame_config(s, b, build_s) -> dict:
+    """The frame workload's identifying keys, the same in both arms."""
+    return {"workload": FRAME_WORKLOAD, "scene": SCENE, "triangles": int(len(s.tri_verts)),
+            "bvh_nodes": int(len(b.nodes)), "bvh_slots": int(len(b.verts)), "sbvh_build_s": round(build_s, 2),
+            "lights": 1}
+
+
 def run_reference(args, world, rank):
     if rank != 0:
         return
-    s, b, cam_pos, lights, _ = frame_inputs()
+    s, b, cam_pos, lights, build_s = frame_inputs()
     from oracle import oracle as O
     import phantasyenginetestbed_gb300 as P
     cam = O.camera_def(cam_pos, CAM_DIR, CAM_UP, math.radians(60.0), RES)
@@ -222,9 +234,8 @@ def run_reference(args, world, rank):
         "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total / args.steps * 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded heightfield + cubes scene, 155,072 triangles)",
-        "config": {"workload": f"wavefront frame {RES[0]}x{RES[1]}, 1 point light, Halton jitter", "scene": SCENE,
-                   "parallelism": "host threads"},
+        "data": FRAME_DATA,
+        "config": {**frame_config(s, b, build_s), "parallelism": f"host threads x{threads}"},
         "latency_ms": {"p50": round(lat[len(lat) // 2], 3), "p99": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 3)},
         "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
                          "sample": (f"{args.steps} frames of the {RES[0]}x{RES[1]} workload through the castRay "
@@ -402,11 +413,8 @@ def run_ours(args, world, rank, local):
         "metric": METRIC, "value": round(value, 2), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
-        "data": "synthetic (seeded heightfield + cubes scene, 155,072 triangles; the reference's Sponza is not in its tree)",
-        "config": {"workload": f"wavefront frame {RES[0]}x{RES[1]}: primary closest -> shade + 1 any-hit shadow ray per "
-                               "light -> cosine bounce closest -> shade + shadow -> resolve + TAA",
-                   "scene": SCENE, "triangles": int(len(s.tri_verts)), "bvh_nodes": int(len(b.nodes)),
-                   "bvh_slots": int(len(b.verts)), "sbvh_build_s": round(build_s, 2), "lights": 1,
+        "data": FRAME_DATA,
+        "config": {**frame_config(s, b, build_s),
                    "rays_per_frame": round(rays_per_frame, 1), "rays_by_pass": {k: round(v, 1) for k, v in stage_rays.items()},
                    "cuda_graph": not args.no_graph, "pipeline": args.pipeline,
                    "refill_threshold": args.refill, "sort_window": args.sort_window,
