@@ -231,3 +231,62 @@ def test_bvh_cache_python_wrappers(tmp_path):
     assert nodes.tobytes() == b.nodes.tobytes() and verts.tobytes() == b.verts.tobytes()
     assert d2.tobytes() == datas.tobytes()
     assert P.validate_bvh(nodes, len(verts)) == b.max_depth
+
+
+def _tree_is_valid(nodes, num_slots, max_depth=64):
+    """The validation rules restated: from the root, every inner child index in range and reached once,
+    inner nodes shallower than max_depth, leaf ranges inside the slot array, counts >= 0, no NaN bound."""
+    n = len(nodes)
+    if n == 0 or num_slots == 0:
+        return False
+    seen = np.zeros(n, bool)
+    seen[0] = True
+    stack = [(0, 0)]
+    while stack:
+        i, d = stack.pop()
+        for c in range(2):
+            raw, count = int(nodes["iData"][i, c]), int(nodes["iData"][i, 2 + c])
+            if count < 0 or np.isnan(nodes["fData"][i, 6 * c: 6 * c + 6]).any():
+                return False
+            if count > 0:
+                if (~raw if raw < 0 else raw) + count > num_slots:
+                    return False
+            elif raw < 0 or raw >= n or seen[raw] or d + 1 >= max_depth:
+                return False
+            else:
+                seen[raw] = True
+                stack.append((raw, d + 1))
+    return True
+
+
+def test_validation_agrees_with_the_rules_on_random_corruptions():
+    """Hundreds of trees with random index, count and bound corruptions (small, negative, huge and
+    boundary values): phe_bvh_validate accepts exactly those the rules restated in Python accept, and
+    never crashes. Scene upload and every kernel rely on it to keep their indexing in bounds."""
+    s = P.generate_scene(8, 3, True, 5)
+    b = P.build_sbvh(s.tri_verts)
+    T, N = len(b.verts), len(b.nodes)
+    rng = np.random.default_rng(17)
+    specials = np.array([0, 1, -1, -2, N - 1, N, N + 1, T - 1, T, ~0, ~(T - 1), ~T, 2**31 - 1, -2**31], np.int64)
+    accepted = rejected = 0
+    for trial in range(600):
+        x = b.nodes.copy()
+        for _ in range(int(rng.integers(1, 4))):
+            i = int(rng.integers(0, N))
+            if rng.random() < 0.1:
+                x["fData"][i, int(rng.integers(0, 12))] = np.nan
+                continue
+            f = int(rng.integers(0, 4))
+            v = int(rng.choice(specials)) if rng.random() < 0.5 else int(rng.integers(-3 * N, 3 * N))
+            x["iData"][i, f] = np.int32(np.int64(v).astype(np.int32))
+        want = _tree_is_valid(x, T)
+        try:
+            P.validate_bvh(x, T)
+            got = True
+        except P.PheError as e:
+            assert e.status == native.PHE_ERR_INVALID_SCENE
+            got = False
+        assert got == want, trial
+        accepted += got
+        rejected += not got
+    assert accepted > 20 and rejected > 200, (accepted, rejected)
