@@ -1,7 +1,7 @@
 /* Test infrastructure only (the oracle). A plain-C restatement of the reference's CPU ray-cast
  * path, its any-hit semantics, primary-ray generation, wavefront shading, diffuse bounce and TAA
- * resolve. Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may load it; the
- * product never does.
+ * resolve. Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline and reference legs may
+ * load it; the product never does.
  *
  * Parity pin: oracle_cast_rays() in reference mode is checked bit-for-bit against the reference's
  * own castRay (compiled from its sources into oracle/_ref/libpheref.so) and against the committed

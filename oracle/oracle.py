@@ -1,8 +1,8 @@
 """Test infrastructure only: ctypes wrappers of the oracle (oracle/liboracle.so) and, where it was
 built from the reference sources, of the reference harness (oracle/_ref/libpheref.so).
 
-Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg may import this module; it is
-the checker, never the thing measured or shipped.
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline and reference legs may import this
+module; it checks results and times the CPU baseline, and is never the thing measured or shipped.
 """
 from __future__ import annotations
 
