@@ -67,6 +67,7 @@ def parse():
                          "scenes in one launch vs 64 plain launches; large: 8.6M-triangle scene, 4096x4096, 4 "
                          "lights; serve: Poisson request arrivals through the serving loop; sizes: launch time "
                          "against rays per launch (16K..16M) for each ray-cast entry point")
+    ap.add_argument("--res", type=int, default=4096, help="large: width and height of the frame")
     ap.add_argument("--rates", default="200,500,1000", help="serve: arrival rates (requests/s)")
     ap.add_argument("--duration", type=float, default=2.0, help="serve: seconds of arrivals per rate")
     ap.add_argument("--render-slots", type=int, default=8, help="serve: concurrent render requests")
@@ -678,7 +679,7 @@ def run_large(args):
     import phantasyenginetestbed_gb300 as P
     from phantasyenginetestbed_gb300.renderer import CudaTracerRenderer, make_lights
     torch.cuda.set_device(0)
-    res = (4096, 4096)
+    res = (args.res, args.res)
     s, b, build_s = _scene_with_bvh("c4_2048_20000")
     scene = P.Scene(b.nodes, b.verts, b.slot_datas(s.datas), s.materials)
     k = s.scale
