@@ -189,11 +189,11 @@ __global__ void __launch_bounds__(kWaveBlock, kWaveMinBlocks) primary_kernel(Dev
 			st_stream(fb.bounceThroughput + q, make_float4(thr.x, thr.y, thr.z, 0.0f));
 		} else if (active) {
 			// no primary hit: nothing to add for this pixel in either stage
+			// Visibility 0 marks both stages' slots as adding nothing, so the resolve reads no
+			// contribution for them (the sum stays +0, as with zero contributions marked visible).
 			for (uint32_t l = 0; l < L; l++) {
-				fb.contrib[(size_t)l * P + pid] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-				fb.inLight[(size_t)l * P + pid] = 1;
-				fb.contrib[(size_t)(L + l) * P + pid] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-				fb.inLight[(size_t)(L + l) * P + pid] = 1;
+				st_stream(fb.inLight + (size_t)l * P + pid, (uint8_t)0);
+				st_stream(fb.inLight + (size_t)(L + l) * P + pid, (uint8_t)0);
 			}
 		}
 		__syncwarp();
@@ -305,11 +305,8 @@ __global__ void __launch_bounds__(kWaveBlock, kBounceMinBlocks) bounce_kernel(De
 			hi.alpha = hi.roughness = hi.metallic = 0.0f;
 		}
 		shade_all_lights(fp, fb, 1, hit, hi, thr, toCamera, rng, pid);
-		if (active && !hit) {
-			for (uint32_t l = 0; l < L; l++) {
-				fb.contrib[(size_t)(L + l) * P + pid] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-				fb.inLight[(size_t)(L + l) * P + pid] = 1;
-			}
+		if (active && !hit) {   // the bounce ray escaped: nothing to add (visibility 0, no contribution read)
+			for (uint32_t l = 0; l < L; l++) st_stream(fb.inLight + (size_t)(L + l) * P + pid, (uint8_t)0);
 		}
 		__syncwarp();
 	}
@@ -438,11 +435,11 @@ __global__ void __launch_bounds__(kWaveBlock) primary_shade_kernel(DeviceScene s
 			st_stream(fb.bouncePixel + q, pid);
 			st_stream(fb.bounceThroughput + q, make_float4(thr.x, thr.y, thr.z, 0.0f));
 		} else if (active) {
+			// Visibility 0 marks both stages' slots as adding nothing, so the resolve reads no
+			// contribution for them (the sum stays +0, as with zero contributions marked visible).
 			for (uint32_t l = 0; l < L; l++) {
-				fb.contrib[(size_t)l * P + pid] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-				fb.inLight[(size_t)l * P + pid] = 1;
-				fb.contrib[(size_t)(L + l) * P + pid] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-				fb.inLight[(size_t)(L + l) * P + pid] = 1;
+				st_stream(fb.inLight + (size_t)l * P + pid, (uint8_t)0);
+				st_stream(fb.inLight + (size_t)(L + l) * P + pid, (uint8_t)0);
 			}
 		}
 	}
@@ -485,11 +482,8 @@ __global__ void __launch_bounds__(kWaveBlock) bounce_shade_kernel(DeviceScene s,
 			hi.alpha = hi.roughness = hi.metallic = 0.0f;
 		}
 		shade_all_lights(fp, fb, 1, hit, hi, thr, toCamera, rng, pid);
-		if (active && !hit) {
-			for (uint32_t l = 0; l < L; l++) {
-				fb.contrib[(size_t)(L + l) * P + pid] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-				fb.inLight[(size_t)(L + l) * P + pid] = 1;
-			}
+		if (active && !hit) {   // the bounce ray escaped: nothing to add (visibility 0, no contribution read)
+			for (uint32_t l = 0; l < L; l++) st_stream(fb.inLight + (size_t)(L + l) * P + pid, (uint8_t)0);
 		}
 	}
 }
