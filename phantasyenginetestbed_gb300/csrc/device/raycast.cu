@@ -8,6 +8,8 @@
 // instead of a file-static global reset by a second kernel (RayCastKernel.cu:172-177), so launches
 // on different streams do not share state.
 
+#include <atomic>
+
 #include "runtime.cuh"
 #include "traverse.cuh"
 
@@ -84,20 +86,23 @@ __global__ void __launch_bounds__(kPersistentBlock) any_persistent_kernel(Device
 	}
 }
 
-static int g_persistentBlocksPerSM[4] = {0, 0, 0, 0};   // [closest, any] x [binary, wide]
+// [closest, any] x [binary, wide]; filled on first use (threads that race store the same value)
+static std::atomic<int> g_persistentBlocksPerSM[4] = {};
 
 static phe_status persistent_grid(int which, const void* kernel, int* grid)
 {
 	DeviceInfo* d = nullptr;
 	phe_status st = device_info(&d);
 	if (st) return st;
-	if (g_persistentBlocksPerSM[which] == 0) {
+	int blocks = g_persistentBlocksPerSM[which].load(std::memory_order_relaxed);
+	if (blocks == 0) {
 		int b = 0;
 		PHE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, kPersistentBlock,
 		                                                           stack_smem_bytes(kPersistentBlock)), "occupancy");
-		g_persistentBlocksPerSM[which] = b > 0 ? b : 1;
+		blocks = b > 0 ? b : 1;
+		g_persistentBlocksPerSM[which].store(blocks, std::memory_order_relaxed);
 	}
-	*grid = g_persistentBlocksPerSM[which] * d->numSMs;
+	*grid = blocks * d->numSMs;
 	return PHE_OK;
 }
 

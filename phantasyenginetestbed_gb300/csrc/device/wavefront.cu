@@ -18,6 +18,7 @@
 // Queue counts stay on the device; persistent kernels read them when they start, so a frame needs
 // no host synchronisation and can be captured in a CUDA graph.
 
+#include <atomic>
 #include <cstring>
 #include <vector>
 
@@ -611,7 +612,8 @@ __global__ void taa_kernel(uint32_t W, uint32_t H, const float4* __restrict__ cu
 // The last three are the 4-wide instantiations of the fused kernels.
 enum { kGridPrimary = 0, kGridAnyQueue, kGridBounce, kGridPrimaryTrace, kGridAnyRefill, kGridBounceTrace,
        kGridPrimaryShade, kGridBounceShade, kGridPrimaryWide, kGridAnyQueueWide, kGridBounceWide, kGridCount };
-static int g_waveBlocksPerSM[kGridCount] = {};
+// filled on first use (threads that race store the same value)
+static std::atomic<int> g_waveBlocksPerSM[kGridCount] = {};
 
 static const void* wave_kernel(int which)
 {
@@ -635,14 +637,16 @@ static phe_status wave_grid(int which, int* grid)
 	DeviceInfo* d = nullptr;
 	phe_status st = device_info(&d);
 	if (st) return st;
-	if (g_waveBlocksPerSM[which] == 0) {
+	int blocks = g_waveBlocksPerSM[which].load(std::memory_order_relaxed);
+	if (blocks == 0) {
 		int b = 0;
 		const bool traverses = which != kGridPrimaryShade && which != kGridBounceShade;
 		PHE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, wave_kernel(which), kWaveBlock,
 		                                                           traverses ? kStackSmem : 0), "occupancy");
-		g_waveBlocksPerSM[which] = b > 0 ? b : 1;
+		blocks = b > 0 ? b : 1;
+		g_waveBlocksPerSM[which].store(blocks, std::memory_order_relaxed);
 	}
-	*grid = g_waveBlocksPerSM[which] * d->numSMs;
+	*grid = blocks * d->numSMs;
 	return PHE_OK;
 }
 
