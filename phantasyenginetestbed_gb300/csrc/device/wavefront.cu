@@ -538,7 +538,13 @@ __device__ __forceinline__ void taa_pixel(uint32_t x, uint32_t y, uint32_t W, ui
 	taa_blend(cur, h, trust, outColor, outHist);
 }
 
-__global__ void resolve_taa_kernel(const FrameParamsDev* __restrict__ fpp, FrameBuffers fb)
+// 12 resident blocks of 128 (40 registers): the still-camera path is bound by memory latency (a pixel's
+// contribution loads wait on its visibility bytes), so more threads in flight help: 39.5 us at 1080p
+// vs 42.3 us uncapped (44 registers, 10 blocks); 16 blocks (32 registers) gave 38.9 us but spilled
+// 104 bytes in the camera-motion path, 12 blocks spill 8.
+constexpr int kResolveMinBlocks = 12;
+__global__ void __launch_bounds__(128, kResolveMinBlocks) resolve_taa_kernel(const FrameParamsDev* __restrict__ fpp,
+                                                                           FrameBuffers fb)
 {
 	const FrameParamsDev& fp = *fpp;
 	uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
