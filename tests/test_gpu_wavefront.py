@@ -363,3 +363,43 @@ def test_async_read_back_across_a_reallocation():
     assert np.array_equal(out, want_color)
     assert np.array_equal(hist, want_hist)
     assert r.read(READ_COLOR).shape[:2] == (big[1], big[0])
+
+
+def test_async_read_back_of_velocity_and_colour_with_a_moving_camera():
+    """With the camera moving, the per-pixel velocity is stored on the frame's parity side like the TAA
+    colour; read_async of both every frame, without waiting in between, equals the blocking reads of
+    the same frames (the frame after next waits for each in-place copy)."""
+    import torch
+    res = (256, 160)
+    s, b, datas, scene, cam, cam_pos, lights, r = _setup("c2_256_2000", res, [(0.5, 0.5, 2.0)], graph=True)
+    k = s.scale
+    d0 = np.array(C1_CAM["dir"], np.float64)
+    p0 = np.array(cam_pos, np.float64)
+    path = [p0 + np.array([0.002 * k * f, 0.0005 * k * f, 0.0]) for f in range(6)]
+
+    def cam_at(f):
+        up = np.cross(np.cross(d0, np.array(C1_CAM["up"])), d0)
+        up = -up if up[2] < 0 else up
+        return cam_struct(O.camera_def(path[f], d0, up, math.radians(60), res))
+
+    want = []
+    r.set_seed(8, 0)
+    r.resetTAA()
+    for f in range(len(path)):
+        r.set_camera_def(cam_at(f), path[f], P.halton_jitter(f))
+        r.render(lights)
+        want.append((r.read(READ_COLOR), r.read(READ_VELOCITY)))
+    assert all(np.abs(v).max() > 0 for _, v in want[1:])
+    col = [torch.empty((res[1], res[0], 4), dtype=torch.float32, pin_memory=True).numpy() for _ in path]
+    vel = [torch.empty((res[1], res[0], 2), dtype=torch.float32, pin_memory=True).numpy() for _ in path]
+    r.set_seed(8, 0)
+    r.resetTAA()
+    for f in range(len(path)):
+        r.set_camera_def(cam_at(f), path[f], P.halton_jitter(f))
+        r.render(lights)
+        r.read_async(col[f])
+        r.read_async(vel[f], READ_VELOCITY)
+    r.read_wait()
+    for f in range(len(path)):
+        assert np.array_equal(col[f], want[f][0]), f
+        assert np.array_equal(vel[f], want[f][1]), f
