@@ -46,8 +46,13 @@ __device__ __forceinline__ uint32_t find_item(const BatchItemDev* __restrict__ i
 	return lo;
 }
 
+// Compiled for 1,280 resident threads per SM (48 registers), like the frame's bounce kernel: on the
+// uneven-batch mix over 10K..2M-triangle scenes 2.553 ms vs 2.617 ms with the compiler's own budget
+// (48-56 registers), and 2.932 ms at 40 registers (spills); the autotuner then picks the resident
+// blocks below that limit.
+constexpr int kBatchThreadsPerSM = 1280;
 template <int BLOCK, bool WIDE, int SN>
-__global__ void __launch_bounds__(BLOCK) batch_kernel(BatchTableDev t, uint32_t* __restrict__ counter,
+__global__ void __launch_bounds__(BLOCK, kBatchThreadsPerSM / BLOCK) batch_kernel(BatchTableDev t, uint32_t* __restrict__ counter,
                                                       uint32_t* __restrict__ status)
 {
 	const uint32_t lane = threadIdx.x & 31u;
