@@ -238,8 +238,9 @@ phe_status phe_gen_primary_rays(phe_ray_in* rays, const phe_camera_def* cam, uin
 phe_status phe_scene_set_layout(phe_scene* scene, int layout);
 phe_status phe_scene_get_layout(const phe_scene* scene, int* layout, int* wideAvailable);
 
-/* OR of error bits raised by kernels on this scene (1 = traversal stack overflow; never set for a
- * scene that passed validation). Synchronous. */
+/* OR of error bits raised by kernels on this scene: single casts, frames, batches, no-alloc batches
+ * and serving waves (1 = traversal stack overflow, never set for a scene that passed validation;
+ * 2 = a node or slot index outside its array, checked build only). Synchronous. */
 phe_status phe_scene_status(const phe_scene* scene, uint32_t* bits);
 
 /* ---------------------------------------------------------------------------------------------
@@ -275,7 +276,9 @@ typedef struct phe_batch_params {
 } phe_batch_params;
 typedef struct phe_batch_tuning_row { phe_batch_params params; float ms; } phe_batch_tuning_row;
 void phe_batch_default_params(phe_batch_params* params);
-/* The batch keeps the scene handles and the item table (device buffers stay owned by the caller). */
+/* The batch keeps the scene handles and the item table (device buffers stay owned by the caller).
+ * Every scene must live on the current device (PHE_ERR_INVALID_ARGUMENT otherwise). Traversal errors
+ * of a launch are ORed into each item's scene status word (phe_scene_status). */
 phe_status phe_batch_create(const phe_scene* const* scenes, uint32_t numScenes, const phe_batch_item* items,
                             uint32_t numItems, const phe_batch_params* params, phe_batch** out);
 /* New buffers / counts for the same number of items (the captured graph is rebuilt on next launch). */
@@ -296,10 +299,13 @@ phe_status phe_batch_destroy(phe_batch* batch);
  * renderer or a plugin host with its own allocator and memory budget; cudaMalloc may also wait for
  * the whole device). The descriptor table, scene table and work counter live in a fixed 11,520-byte
  * array inside the library (per GPU, until exit) instead of device memory the call allocates.
- * At most 256 batch items and 32 scenes per call (PHE_ERR_TOO_LARGE beyond). All calls share the
- * array: calls whose GPU work overlaps race, so serialise them on one stream. The first call on a
- * device looks up the array's address on that (current) device; make it before any stream capture.
- * Asynchronous on `stream`; results as phe_batch_launch. */
+ * At most 256 batch items and 32 scenes per call (PHE_ERR_TOO_LARGE beyond); every scene must live
+ * on the current device (PHE_ERR_INVALID_ARGUMENT). All calls share the array: calls whose GPU work
+ * overlaps race, so serialise them on one stream. The first call on a device looks up the array's
+ * address on that (current) device; make it before any stream capture. The tables travel to the
+ * GPU as a kernel parameter (no host-to-device copy), so the call queues two kernels on `stream`
+ * and returns without waiting for the GPU; results as phe_batch_launch. Traversal errors are ORed
+ * into each item's scene status word: read them with phe_scene_status. */
 phe_status phe_batch_cast_noalloc(const phe_scene* const* scenes, uint32_t numScenes, const phe_batch_item* items,
                                   uint32_t numItems, void* stream);
 

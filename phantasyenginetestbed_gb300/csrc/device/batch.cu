@@ -50,10 +50,11 @@ __device__ __forceinline__ uint32_t find_item(const BatchItemDev* __restrict__ i
 // uneven-batch mix over 10K..2M-triangle scenes 2.553 ms vs 2.617 ms with the compiler's own budget
 // (48-56 registers), and 2.932 ms at 40 registers (spills); the autotuner then picks the resident
 // blocks below that limit.
+// Traversal errors (stack overflow; an index outside its array in the checked build) are ORed into the
+// status word of the item's scene, which phe_scene_status reads.
 constexpr int kBatchThreadsPerSM = 1280;
 template <int BLOCK, bool WIDE, int SN>
-__global__ void __launch_bounds__(BLOCK, kBatchThreadsPerSM / BLOCK) batch_kernel(BatchTableDev t, uint32_t* __restrict__ counter,
-                                                      uint32_t* __restrict__ status)
+__global__ void __launch_bounds__(BLOCK, kBatchThreadsPerSM / BLOCK) batch_kernel(BatchTableDev t, uint32_t* __restrict__ counter)
 {
 	const uint32_t lane = threadIdx.x & 31u;
 	for (;;) {
@@ -77,7 +78,7 @@ __global__ void __launch_bounds__(BLOCK, kBatchThreadsPerSM / BLOCK) batch_kerne
 				err = trace<true, WIDE, SN>(s, r, h);
 				((uint8_t*)item.out)[i] = h.slot == ~0u ? 1 : 0;
 			}
-			if (err) atomicOr(status, err);
+			if (err) atomicOr(s.status, err);
 		}
 		__syncwarp();
 	}
@@ -87,7 +88,7 @@ __global__ void __launch_bounds__(BLOCK, kBatchThreadsPerSM / BLOCK) batch_kerne
 // `stackShared` (0 or kBatchStackShared) the one keeping that many stack entries in shared memory.
 template <int BLOCK>
 static phe_status launch_batch_kernel(const BatchTableDev& t, bool wide, int stackShared, int blocksPerSM, int numSMs,
-                                      uint32_t* counter, uint32_t* status, cudaStream_t stream, int* occupancyOut)
+                                      uint32_t* counter, cudaStream_t stream, int* occupancyOut)
 {
 	const bool sh = stackShared > 0;
 	auto kernel = wide ? (sh ? batch_kernel<BLOCK, true, kBatchStackShared> : batch_kernel<BLOCK, true, 0>)
@@ -104,7 +105,7 @@ static phe_status launch_batch_kernel(const BatchTableDev& t, bool wide, int sta
 	uint32_t grid = (uint32_t)(b * numSMs);
 	uint32_t need = (t.totalPadded + BLOCK - 1) / BLOCK;
 	if (grid > need) grid = need > 0 ? need : 1;
-	kernel<<<grid, BLOCK, smem, stream>>>(t, counter, status);
+	kernel<<<grid, BLOCK, smem, stream>>>(t, counter);
 	PHE_CUDA_TRY(cudaGetLastError(), "batch_kernel launch");
 	return PHE_OK;
 }
@@ -142,8 +143,8 @@ __global__ void __launch_bounds__(kOctantBlock) batch_sort_kernel(BatchTableDev 
 }
 
 phe_status launch_batch_table(const BatchItemDev* items, uint32_t numItems, uint32_t totalPadded,
-                              const DeviceScene* scenes, uint32_t* counter, uint32_t* status, int blockSize,
-                              int blocksPerSM, cudaStream_t stream, bool wide)
+                              const DeviceScene* scenes, uint32_t* counter, int blockSize, int blocksPerSM,
+                              cudaStream_t stream, bool wide)
 {
 	DeviceInfo* d = nullptr;
 	phe_status st = device_info(&d);
@@ -151,9 +152,9 @@ phe_status launch_batch_table(const BatchItemDev* items, uint32_t numItems, uint
 	if (totalPadded == 0) return PHE_OK;
 	BatchTableDev t{items, scenes, numItems, totalPadded, nullptr};
 	switch (blockSize) {
-	case 64: return launch_batch_kernel<64>(t, wide, 0, blocksPerSM, d->numSMs, counter, status, stream, nullptr);
-	case 256: return launch_batch_kernel<256>(t, wide, 0, blocksPerSM, d->numSMs, counter, status, stream, nullptr);
-	default: return launch_batch_kernel<128>(t, wide, 0, blocksPerSM, d->numSMs, counter, status, stream, nullptr);
+	case 64: return launch_batch_kernel<64>(t, wide, 0, blocksPerSM, d->numSMs, counter, stream, nullptr);
+	case 256: return launch_batch_kernel<256>(t, wide, 0, blocksPerSM, d->numSMs, counter, stream, nullptr);
+	default: return launch_batch_kernel<128>(t, wide, 0, blocksPerSM, d->numSMs, counter, stream, nullptr);
 	}
 }
 
@@ -167,11 +168,10 @@ struct phe_batch {
 	std::vector<DeviceScene> scenes;
 	std::vector<const phe_scene*> sceneHandles;
 	phe_batch_params params{};
-	void* allocation = nullptr;            // items table + scene table + counter + status
+	void* allocation = nullptr;            // items table + scene table + counter
 	BatchItemDev* dItems = nullptr;
 	DeviceScene* dScenes = nullptr;
 	uint32_t* dCounter = nullptr;
-	uint32_t* dStatus = nullptr;
 	uint32_t totalPadded = 0;
 	uint64_t totalRays = 0;
 	cudaGraphExec_t graph = nullptr;
@@ -318,6 +318,10 @@ extern "C" phe_status phe_batch_create(const phe_scene* const* scenes, uint32_t 
 	if (params && (st = check_params(params))) return st;
 	DeviceInfo* d = nullptr;
 	if ((st = device_info(&d))) return st;
+	for (uint32_t i = 0; i < numScenes; i++)
+		if (scenes[i]->device != d->device)
+			return fail(PHE_ERR_INVALID_ARGUMENT, "phe_batch_create: scene %u lives on device %d, not on the current device %d",
+			            i, scenes[i]->device, d->device);
 	phe_batch* b = new phe_batch();
 	if (params) b->params = *params;
 	else phe_batch_default_params(&b->params);
@@ -338,7 +342,6 @@ extern "C" phe_status phe_batch_create(const phe_scene* const* scenes, uint32_t 
 	b->dItems = (BatchItemDev*)base;
 	b->dScenes = (DeviceScene*)(base + itemBytes);
 	b->dCounter = (uint32_t*)(base + itemBytes + sceneBytes);
-	b->dStatus = b->dCounter + 1;
 	cudaMemset(b->dCounter, 0, 256);
 	e = cudaMemcpy(b->dScenes, b->scenes.data(), numScenes * sizeof(DeviceScene), cudaMemcpyHostToDevice);
 	if (e != cudaSuccess) {
@@ -383,9 +386,9 @@ static phe_status batch_enqueue(phe_batch* b, cudaStream_t stream)
 	const bool wide = b->params.layout == PHE_LAYOUT_WIDE4;
 	const int sh = b->params.stackShared;
 	switch (b->params.blockSize) {
-	case 64: return launch_batch_kernel<64>(t, wide, sh, b->params.blocksPerSM, d->numSMs, b->dCounter, b->dStatus, stream, nullptr);
-	case 256: return launch_batch_kernel<256>(t, wide, sh, b->params.blocksPerSM, d->numSMs, b->dCounter, b->dStatus, stream, nullptr);
-	case 128: return launch_batch_kernel<128>(t, wide, sh, b->params.blocksPerSM, d->numSMs, b->dCounter, b->dStatus, stream, nullptr);
+	case 64: return launch_batch_kernel<64>(t, wide, sh, b->params.blocksPerSM, d->numSMs, b->dCounter, stream, nullptr);
+	case 256: return launch_batch_kernel<256>(t, wide, sh, b->params.blocksPerSM, d->numSMs, b->dCounter, stream, nullptr);
+	case 128: return launch_batch_kernel<128>(t, wide, sh, b->params.blocksPerSM, d->numSMs, b->dCounter, stream, nullptr);
 	default: return fail(PHE_ERR_INVALID_ARGUMENT, "batch block size must be 64, 128 or 256");
 	}
 }
@@ -403,9 +406,9 @@ extern "C" phe_status phe_batch_launch(phe_batch* b, void* stream)
 		const bool wide = b->params.layout == PHE_LAYOUT_WIDE4;
 		const int sh = b->params.stackShared;
 		switch (b->params.blockSize) {
-		case 64: launch_batch_kernel<64>(t, wide, sh, 0, 1, nullptr, nullptr, nullptr, &occ); break;
-		case 256: launch_batch_kernel<256>(t, wide, sh, 0, 1, nullptr, nullptr, nullptr, &occ); break;
-		default: launch_batch_kernel<128>(t, wide, sh, 0, 1, nullptr, nullptr, nullptr, &occ); break;
+		case 64: launch_batch_kernel<64>(t, wide, sh, 0, 1, nullptr, nullptr, &occ); break;
+		case 256: launch_batch_kernel<256>(t, wide, sh, 0, 1, nullptr, nullptr, &occ); break;
+		default: launch_batch_kernel<128>(t, wide, sh, 0, 1, nullptr, nullptr, &occ); break;
 		}
 		cudaStream_t cap = nullptr;
 		PHE_CUDA_TRY(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking), "create capture stream");
@@ -495,9 +498,9 @@ extern "C" phe_status phe_batch_autotune(phe_batch* b, int repeats, void* stream
 	for (int bs : blocks) {
 		int occ = 0;
 		BatchTableDev t{};
-		if (bs == 64) launch_batch_kernel<64>(t, false, 0, 0, 1, nullptr, nullptr, nullptr, &occ);
-		else if (bs == 128) launch_batch_kernel<128>(t, false, 0, 0, 1, nullptr, nullptr, nullptr, &occ);
-		else launch_batch_kernel<256>(t, false, 0, 0, 1, nullptr, nullptr, nullptr, &occ);
+		if (bs == 64) launch_batch_kernel<64>(t, false, 0, 0, 1, nullptr, nullptr, &occ);
+		else if (bs == 128) launch_batch_kernel<128>(t, false, 0, 0, 1, nullptr, nullptr, &occ);
+		else launch_batch_kernel<256>(t, false, 0, 0, 1, nullptr, nullptr, &occ);
 		for (int ord : orders)
 			for (int q : occFrac)
 				for (int lay : layouts)
@@ -565,17 +568,24 @@ done:
 // Some callers own every byte of device memory through their own allocator or memory budget (a game
 // engine's renderer, a plugin host) and do not let a library call cudaMalloc: it can block until the
 // whole device is idle and it takes memory outside their accounting. For them this entry point keeps
-// its scratch (the batch descriptor table, the scene table, the work counter and the status word) in
-// the fixed array below, which lives in the library image. The caller passes the scenes, rays and
-// output buffers as usual.
+// its scratch (the batch descriptor table, the scene table and the work counter) in the fixed array
+// below, which lives in the library image. The caller passes the scenes, rays and output buffers as
+// usual.
+//
+// The host builds the two tables on its stack and hands them to a one-block staging kernel as its
+// by-value (__grid_constant__) parameter; the staging kernel copies them into the array and clears
+// the counter, and the batch kernel then runs from the array. No host-to-device copy is queued, so
+// nothing waits for pageable memory and the call returns as soon as both kernels are queued.
 //
 // Limits and sharing rules:
 //   * at most kNoAllocMaxItems batches and kNoAllocMaxScenes scenes per call (11,520 bytes of scratch,
 //     held by every GPU that loads the library until the process exits); larger calls fail with
 //     PHE_ERR_TOO_LARGE;
-//   * every call uses the same array and leaves its table there; the counter and status word are
-//     cleared at the start of each call. Two calls whose work overlaps on the GPU (for example on two
-//     streams at once) race on the array: serialise them on one stream;
+//   * every call uses the same array and leaves its tables there; the counter is cleared at the start
+//     of each call. Two calls whose work overlaps on the GPU (for example on two streams at once) race
+//     on the array: serialise them on one stream;
+//   * traversal errors are ORed into each scene's own status word (phe_scene_status), not kept in the
+//     array;
 //   * the first call on a device looks up the array's device address for that device (the call
 //     must be made with that device current); make that first call before any stream capture.
 // ------------------------------------------------------------------------------------------------
@@ -586,26 +596,49 @@ constexpr uint32_t kNoAllocMaxItems = 256;
 constexpr uint32_t kNoAllocMaxScenes = 32;
 constexpr size_t kNoAllocItemsBytes = kNoAllocMaxItems * sizeof(BatchItemDev);          // 8192
 constexpr size_t kNoAllocScenesBytes = kNoAllocMaxScenes * sizeof(DeviceScene);         // 3072
-constexpr size_t kNoAllocScratchBytes = kNoAllocItemsBytes + kNoAllocScenesBytes + 256; // + counter, status
+constexpr size_t kNoAllocScratchBytes = kNoAllocItemsBytes + kNoAllocScenesBytes + 256; // + counter
 static_assert(sizeof(DeviceScene) % 16 == 0, "scene table entries stay 16-byte aligned");
 static_assert(kNoAllocScratchBytes == 11520, "the documented scratch size");
 
 static __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocScratchBytes];
 
+// Both tables as one kernel parameter (11,264 bytes, inside the 32,764-byte limit of kernel parameters).
+struct NoAllocTables {
+	BatchItemDev items[kNoAllocMaxItems];
+	DeviceScene scenes[kNoAllocMaxScenes];
+};
+static_assert(sizeof(NoAllocTables) == kNoAllocItemsBytes + kNoAllocScenesBytes, "tables fill the scratch head");
+static_assert(sizeof(NoAllocTables) % 16 == 0, "tables copy as 16-byte words");
+
+constexpr int kNoAllocStageBlock = 256;
+
+// Copies the used part of both tables from the parameter into the scratch and clears the counter.
+// `scratch` is the array's device address looked up by the host.
+__global__ void __launch_bounds__(kNoAllocStageBlock) noalloc_stage_kernel(const __grid_constant__ NoAllocTables tab,
+                                                                          uint32_t numItems, uint32_t numScenes,
+                                                                          unsigned char* __restrict__ scratch)
+{
+	const uint4* src = reinterpret_cast<const uint4*>(&tab);
+	uint4* dst = reinterpret_cast<uint4*>(scratch);
+	const uint32_t itemWords = numItems * (uint32_t)(sizeof(BatchItemDev) / 16);
+	const uint32_t sceneWords = numScenes * (uint32_t)(sizeof(DeviceScene) / 16);
+	const uint32_t sceneFirst = (uint32_t)(kNoAllocItemsBytes / 16);
+	for (uint32_t k = threadIdx.x; k < itemWords; k += blockDim.x) dst[k] = src[k];
+	for (uint32_t k = threadIdx.x; k < sceneWords; k += blockDim.x) dst[sceneFirst + k] = src[sceneFirst + k];
+	if (threadIdx.x == 0) *reinterpret_cast<uint32_t*>(scratch + kNoAllocItemsBytes + kNoAllocScenesBytes) = 0u;
+}
+
 static std::mutex g_noallocMutex;
 static unsigned char* g_noallocAddr[64] = {};   // device address of g_noallocScratch, per device
 
 // Looks up (once per device) the device address of the scratch array on the current device.
-static phe_status noalloc_scratch(unsigned char** out)
+static phe_status noalloc_scratch(int dev, unsigned char** out)
 {
-	int dev = 0;
-	cudaError_t e = cudaGetDevice(&dev);
-	if (e != cudaSuccess) return fail(PHE_ERR_NO_DEVICE, "no CUDA device: %s", cudaGetErrorString(e));
 	if (dev < 0 || dev >= 64) return fail(PHE_ERR_NO_DEVICE, "device ordinal %d out of range", dev);
 	std::lock_guard<std::mutex> lock(g_noallocMutex);
 	if (!g_noallocAddr[dev]) {
 		void* p = nullptr;
-		e = cudaGetSymbolAddress(&p, g_noallocScratch);
+		cudaError_t e = cudaGetSymbolAddress(&p, g_noallocScratch);
 		if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(no-alloc scratch)");
 		g_noallocAddr[dev] = (unsigned char*)p;
 	}
@@ -630,52 +663,55 @@ extern "C" phe_status phe_batch_cast_noalloc(const phe_scene* const* scenes, uin
 		if (!scenes[i]) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_batch_cast_noalloc: scene %u is null", i);
 	phe_status st = check_items(items, numItems, numScenes);
 	if (st) return st;
+	// Padded ray total (a warp's 32-ray fetch never straddles two batches).
+	uint64_t total = 0;
+	for (uint32_t k = 0; k < numItems; k++) {
+		total += ((uint64_t)items[k].count + 31u) / 32u * 32u;
+		if (total > kMaxPersistentRays)
+			return fail(PHE_ERR_TOO_LARGE, "phe_batch_cast_noalloc: more than %u rays (padded)", kMaxPersistentRays);
+	}
+	int dev = 0;
+	cudaError_t e = cudaGetDevice(&dev);
+	if (e != cudaSuccess) return fail(PHE_ERR_NO_DEVICE, "no CUDA device: %s", cudaGetErrorString(e));
+	for (uint32_t i = 0; i < numScenes; i++)
+		if (scenes[i]->device != dev)
+			return fail(PHE_ERR_INVALID_ARGUMENT, "phe_batch_cast_noalloc: scene %u lives on device %d, not on the current device %d",
+			            i, scenes[i]->device, dev);
 	unsigned char* scratch = nullptr;
-	if ((st = noalloc_scratch(&scratch))) return st;
+	if ((st = noalloc_scratch(dev, &scratch))) return st;
+	if (total == 0) return PHE_OK;
 
-	// Tables are built on the stack (no heap, no device allocation) and copied into the scratch.
-	BatchItemDev table[kNoAllocMaxItems];
-	DeviceScene sceneTable[kNoAllocMaxScenes];
+	// Both tables on the host stack, passed by value to the staging kernel (no heap, no device allocation).
+	NoAllocTables tab;
 	uint32_t base = 0;
 	for (uint32_t k = 0; k < numItems; k++) {
-		table[k].scene = items[k].scene;
-		table[k].kind = items[k].kind;
-		table[k].count = items[k].count;
-		table[k].base = base;
-		table[k].rays = items[k].rays;
-		table[k].out = items[k].out;
-		uint64_t next = (uint64_t)base + ((uint64_t)items[k].count + 31u) / 32u * 32u;
-		if (next > kMaxPersistentRays)
-			return fail(PHE_ERR_TOO_LARGE, "phe_batch_cast_noalloc: more than %u rays (padded)", kMaxPersistentRays);
-		base = (uint32_t)next;
+		tab.items[k].scene = items[k].scene;
+		tab.items[k].kind = items[k].kind;
+		tab.items[k].count = items[k].count;
+		tab.items[k].base = base;
+		tab.items[k].rays = items[k].rays;
+		tab.items[k].out = items[k].out;
+		base += (items[k].count + 31u) / 32u * 32u;
 	}
 	bool wide = false;
 	for (uint32_t i = 0; i < numScenes; i++) {
-		sceneTable[i] = scenes[i]->dev;
+		tab.scenes[i] = scenes[i]->dev;
 		wide = wide || scenes[i]->dev.nodes4 != nullptr;
 	}
-	BatchItemDev* dItems = (BatchItemDev*)scratch;
-	DeviceScene* dScenes = (DeviceScene*)(scratch + kNoAllocItemsBytes);
-	uint32_t* dCounter = (uint32_t*)(scratch + kNoAllocItemsBytes + kNoAllocScenesBytes);
-	uint32_t* dStatus = dCounter + 1;
 	cudaStream_t s = (cudaStream_t)stream;
-	if (numItems)
-		PHE_CUDA_TRY(cudaMemcpyAsync(dItems, table, numItems * sizeof(BatchItemDev), cudaMemcpyHostToDevice, s),
-		             "copy batch table into scratch");
-	PHE_CUDA_TRY(cudaMemcpyAsync(dScenes, sceneTable, numScenes * sizeof(DeviceScene), cudaMemcpyHostToDevice, s),
-	             "copy scene table into scratch");
-	PHE_CUDA_TRY(cudaMemsetAsync(dCounter, 0, 2 * sizeof(uint32_t), s), "clear scratch counter");
-	if (base == 0) return PHE_OK;
-	int dev = 0, numSMs = 0, perSM = 0;
-	PHE_CUDA_TRY(cudaGetDevice(&dev), "cudaGetDevice");
+	noalloc_stage_kernel<<<1, kNoAllocStageBlock, 0, s>>>(tab, numItems, numScenes, scratch);
+	PHE_CUDA_TRY(cudaGetLastError(), "no-alloc staging kernel launch");
+
+	int numSMs = 0, perSM = 0;
 	PHE_CUDA_TRY(cudaDeviceGetAttribute(&numSMs, cudaDevAttrMultiProcessorCount, dev), "SM count");
 	auto kernel = wide ? batch_kernel<128, true, 0> : batch_kernel<128, false, 0>;
 	PHE_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSM, kernel, 128, 0), "occupancy");
 	uint32_t grid = (uint32_t)(perSM > 0 ? perSM : 1) * (uint32_t)numSMs;
 	uint32_t need = (base + 127u) / 128u;
 	if (grid > need) grid = need;
-	BatchTableDev t{dItems, dScenes, numItems, base, nullptr};
-	kernel<<<grid, 128, 0, s>>>(t, dCounter, dStatus);
+	BatchTableDev t{(const BatchItemDev*)scratch, (const DeviceScene*)(scratch + kNoAllocItemsBytes), numItems, base,
+	                nullptr};
+	kernel<<<grid, 128, 0, s>>>(t, (uint32_t*)(scratch + kNoAllocItemsBytes + kNoAllocScenesBytes));
 	PHE_CUDA_TRY(cudaGetLastError(), "batch_kernel launch (no-alloc)");
 	return PHE_OK;
 }

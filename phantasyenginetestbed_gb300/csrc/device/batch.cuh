@@ -22,8 +22,9 @@ static_assert(sizeof(BatchItemDev) == 32, "BatchItemDev is 32 bytes");
 // `totalPadded` global ray indices. `counter` must be zero when the kernel starts (the caller
 // clears it on `stream`). blockSize 64/128/256; blocksPerSM 0 = occupancy limit. `wide` must be set
 // when some scene of the table has its 4-wide layout selected (DeviceScene::nodes4 non-null).
+// Traversal errors go to each item's scene status word (DeviceScene::status).
 phe_status launch_batch_table(const BatchItemDev* items, uint32_t numItems, uint32_t totalPadded,
-                              const DeviceScene* scenes, uint32_t* counter, uint32_t* status, int blockSize,
-                              int blocksPerSM, cudaStream_t stream, bool wide);
+                              const DeviceScene* scenes, uint32_t* counter, int blockSize, int blocksPerSM,
+                              cudaStream_t stream, bool wide);
 
 } // namespace phe_gb300

@@ -43,9 +43,9 @@ struct DeviceScene {
 	const float4* tris;
 	const phe_triangle_data* datas;
 	const phe_material* materials;
-	uint32_t numNodes, numSlots, numMaterials, maxDepth;
+	uint32_t numNodes, numSlots, numMaterials, numNodes4;
 	const float4* nodes4;
-	uint32_t numNodes4, maxDepth4;
+	uint32_t* status;   // device word: OR of the error bits any kernel raised on this scene
 	const DeviceTexture* textures;
 	const uint8_t* texels;
 	const float* srgb;

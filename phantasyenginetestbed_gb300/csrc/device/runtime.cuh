@@ -17,7 +17,8 @@ struct phe_scene {
 	uint64_t generation = 0;      // bumped whenever `dev` changes (layout, materials): graphs re-capture
 	int64_t maxMaterialIndex = -1; // largest materialIndex of the triangle data (-1 without data)
 	uint32_t* status = nullptr;   // device word: OR of error bits raised by kernels on this scene
-	int device = 0;
+	uint32_t maxDepth = 0, maxDepth4 = 0;   // deepest leaf level of the binary and 4-wide trees
+	int device = 0;               // ordinal of the device holding the scene
 };
 
 namespace phe_gb300 {

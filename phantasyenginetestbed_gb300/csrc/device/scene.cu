@@ -379,7 +379,7 @@ extern "C" phe_status phe_scene_create(const phe_bvh_node* nodes, uint32_t numNo
 	sc->dev.numNodes = numNodes;
 	sc->dev.numSlots = numSlots;
 	sc->dev.numMaterials = 0;
-	sc->dev.maxDepth = maxDepth;
+	sc->maxDepth = maxDepth;
 	sc->dev.textures = nullptr;
 	sc->dev.texels = nullptr;
 	sc->dev.srgb = nullptr;
@@ -388,10 +388,11 @@ extern "C" phe_status phe_scene_create(const phe_bvh_node* nodes, uint32_t numNo
 	sc->dev.nodes4 = nullptr;   // binary layout unless phe_scene_set_layout selects the 4-wide one
 	sc->nodes4 = dNodes4;
 	sc->dev.numNodes4 = (uint32_t)(dn4.size() / 8);
-	sc->dev.maxDepth4 = depth4;
+	sc->maxDepth4 = depth4;
 	sc->allocation = base;
 	sc->bytes = total;
 	sc->status = dStatus;
+	sc->dev.status = dStatus;
 	sc->device = dinfo->device;
 	if (!hm.empty() && (s = upload_shading(sc, hm.data(), (uint32_t)hm.size(), nullptr, 0))) {
 		phe_scene_destroy(sc);

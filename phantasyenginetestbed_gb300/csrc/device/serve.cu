@@ -70,7 +70,7 @@ struct RenderSlot {
 struct Wave {
 	BatchItemDev* hostItems = nullptr;   // pinned [kMaxWaveItems]
 	BatchItemDev* devItems = nullptr;    // [kMaxWaveItems]
-	uint32_t* counter = nullptr;         // [2]: work counter, status
+	uint32_t* counter = nullptr;         // work counter of the wave
 	cudaEvent_t done = nullptr;
 	bool busy = false;
 };
@@ -185,7 +185,7 @@ phe_status launch_wave(phe_server* s, Wave& w)
 	PHE_CUDA_TRY(cudaMemcpyAsync(w.devItems, w.hostItems, n * sizeof(BatchItemDev), cudaMemcpyHostToDevice, st),
 	             "upload wave table");
 	PHE_CUDA_TRY(cudaMemsetAsync(w.counter, 0, 2 * sizeof(uint32_t), st), "clear wave counter");
-	phe_status ps = launch_batch_table(w.devItems, n, base, s->dScenes, w.counter, w.counter + 1, 128, 0, st,
+	phe_status ps = launch_batch_table(w.devItems, n, base, s->dScenes, w.counter, 128, 0, st,
 	                                   s->wideScenes);
 	if (ps) return ps;
 	for (uint32_t i = 0; i < n; i++) {

@@ -1,6 +1,6 @@
 """The checked build (libphe_gb300_checked.so: the same sources with PHE_DEVICE_CHECKS=1, every node and
 slot index tested against its array before it is read, an error bit instead of an out-of-bounds read)
-passes the ray-cast and frame parity tests with no error bit raised. Runs them in a child process that
+passes the ray-cast, frame, batch and no-alloc batch parity tests with no error bit raised. Runs them in a child process that
 loads the checked library."""
 import os
 import subprocess
@@ -13,7 +13,8 @@ ROOT = Path(__file__).resolve().parents[1]
 pytestmark = pytest.mark.gpu
 
 SUBSET = ["tests/test_gpu_raycast.py", "tests/test_gpu_wavefront.py::test_frame_matches_oracle_small",
-          "tests/test_gpu_textures.py::test_textured_frame_matches_oracle"]
+          "tests/test_gpu_textures.py::test_textured_frame_matches_oracle", "tests/test_gpu_batch.py",
+          "tests/test_zz_no_alloc.py"]
 
 
 def test_checked_build_passes_the_parity_tests():
