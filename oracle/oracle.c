@@ -447,6 +447,22 @@ static v3 sample_ggx(float r1, float r2, float a, v3 reflection, v3 surfaceNorma
 	return normalize3(add(vec, muls(surfaceNormal, off)));
 }
 
+/* reflect (CudaDeviceHelpers.cuh:44-47): in - 2 dot(n, in) n */
+static v3 reflect3(v3 in, v3 n) { return sub(in, muls(n, 2.0f * dot(n, in))); }
+
+/* The GGX branch of the bounce (MaterialKernel.cu:293-299): a = roughness^2 around reflect(fromCamera, n). */
+static v3 bounce_ggx(float r1, float r2, float roughness, v3 fromCamera, v3 normal)
+{
+	return sample_ggx(r1, r2, roughness * roughness, reflect3(fromCamera, normal), normal);
+}
+
+void oracle_sample_ggx_bounce(float r1, float r2, float roughness, const float fromCamera[3], const float nn[3],
+                              float out[3])
+{
+	v3 d = bounce_ggx(r1, r2, roughness, ld3(fromCamera), ld3(nn));
+	out[0] = d.x; out[1] = d.y; out[2] = d.z;
+}
+
 /* ---------------------------------------------------------------------------------------------
  * Wavefront frame
  * ------------------------------------------------------------------------------------------- */
@@ -474,22 +490,49 @@ static const uint8_t* texel_at(const or_texture* t, float u, float v)
 	return t->data + (size_t)jj * t->pitch + (size_t)i * t->bytesPerPixel;
 }
 
+/* retrieveTriData (InterpretRayHitKernel.cu:13-37): position and interpolated normal at a hit. */
+static void retrieve_tri_data(const or_tri_data* d, const or_ray* r, const or_hit* h, v3* pos, v3* normal)
+{
+	*pos = add(ld3(r->o), muls(ld3(r->d), h->t));
+	v3 n0 = ld3(d->n0), n1 = ld3(d->n1), n2 = ld3(d->n2);
+	*normal = normalize3(add(add(n0, muls(sub(n1, n0), h->u)), muls(sub(n2, n0), h->v)));
+}
+
+/* uv at a hit: uv0 + (uv1 - uv0) u + (uv2 - uv0) v, left to right */
+static void hit_uv(const or_tri_data* d, const or_hit* h, float* tu, float* tv)
+{
+	*tu = (d->uv0[0] + (d->uv1[0] - d->uv0[0]) * h->u) + (d->uv2[0] - d->uv0[0]) * h->v;
+	*tv = (d->uv0[1] + (d->uv1[1] - d->uv0[1]) * h->u) + (d->uv2[1] - d->uv0[1]) * h->v;
+}
+
+void oracle_retrieve_tri_data(uint32_t n, const or_tri_data* datas, const or_ray* rays, const or_hit* hits, float* out,
+                              uint32_t* materialIndex)
+{
+	for (uint32_t i = 0; i < n; i++) {
+		v3 pos, normal;
+		retrieve_tri_data(&datas[i], &rays[i], &hits[i], &pos, &normal);
+		float* o = out + 8 * (size_t)i;
+		o[0] = pos.x; o[1] = pos.y; o[2] = pos.z;
+		o[3] = normal.x; o[4] = normal.y; o[5] = normal.z;
+		hit_uv(&datas[i], &hits[i], &o[6], &o[7]);
+		materialIndex[i] = datas[i].materialIndex;
+	}
+}
+
 static hit_info interpret(const or_tri_data* datas, const or_frame_params* fp, const float* srgb, const or_ray* r,
                           const or_hit* h)
 {
 	/* retrieveTriData + material lookup (InterpretRayHitKernel.cu:13-37, 60-121) */
 	hit_info hi;
 	const or_tri_data* d = &datas[h->tri];
-	hi.pos = add(ld3(r->o), muls(ld3(r->d), h->t));
-	v3 n0 = ld3(d->n0), n1 = ld3(d->n1), n2 = ld3(d->n2);
-	hi.normal = normalize3(add(add(n0, muls(sub(n1, n0), h->u)), muls(sub(n2, n0), h->v)));
+	retrieve_tri_data(d, r, h, &hi.pos, &hi.normal);
 	const or_material* m = &fp->materials[d->materialIndex];
 	for (int k = 0; k < 4; k++) hi.surf.albedo[k] = m->albedo[k];
 	hi.surf.roughness = m->roughness;
 	hi.surf.metallic = m->metallic;
 	if (m->texIndex[0] >= 0 || m->texIndex[1] >= 0 || m->texIndex[2] >= 0) {
-		float tu = (d->uv0[0] + (d->uv1[0] - d->uv0[0]) * h->u) + (d->uv2[0] - d->uv0[0]) * h->v;
-		float tv = (d->uv0[1] + (d->uv1[1] - d->uv0[1]) * h->u) + (d->uv2[1] - d->uv0[1]) * h->v;
+		float tu, tv;
+		hit_uv(d, h, &tu, &tv);
 		if (m->texIndex[0] >= 0) {
 			const uint8_t* c = texel_at(&fp->textures[m->texIndex[0]], tu, tv);
 			for (int k = 0; k < 3; k++) hi.surf.albedo[k] = srgb[c[k]];
@@ -501,9 +544,10 @@ static hit_info interpret(const or_tri_data* datas, const or_frame_params* fp, c
 	return hi;
 }
 
-/* shadeHit (MaterialKernel.cu:49-112) for one light: contribution and, when cast, the shadow ray. */
+/* shadeHit (MaterialKernel.cu:49-112) for one light: contribution and, when cast, the shadow ray. The
+ * two uniform numbers of the soft-shadow offset come from `rng`, or from fixedR[0..1] when rng is NULL. */
 static int shade_light(const or_light* light, v3 mask, v3 normal, v3 toCamera, v3 pos, const or_surface* m,
-                       or_pcg* rng, float contrib[3], or_ray* shadowRay)
+                       or_pcg* rng, const float* fixedR, float contrib[3], or_ray* shadowRay)
 {
 	v3 lp = ld3(light->pos);
 	v3 toLight = sub(lp, pos);
@@ -522,8 +566,8 @@ static int shade_light(const or_light* light, v3 mask, v3 normal, v3 toCamera, v
 	v3 circleU = fabsf(normal.z) > 0.01f ? normalize3(mk(0.0f, -normal.z, normal.y))
 	                                     : normalize3(mk(-normal.y, normal.x, 0.0f));
 	v3 circleV = cross(circleU, l);
-	float r1 = oracle_pcg_uniform(rng);
-	float r2 = oracle_pcg_uniform(rng);
+	float r1 = rng ? oracle_pcg_uniform(rng) : fixedR[0];
+	float r2 = rng ? oracle_pcg_uniform(rng) : fixedR[1];
 	float centerDistance = light->radius * (2.0f * r2 - 1.0f);
 	float s, c;
 	oracle_sincos_2pi(r1, &s, &c);
@@ -535,6 +579,17 @@ static int shade_light(const or_light* light, v3 mask, v3 normal, v3 toCamera, v
 	shadowRay->tmin = 0.001f;
 	shadowRay->tmax = length3(diff);
 	return 1;
+}
+
+int oracle_shade_hit(const or_light* light, const float mask[3], const float normal[3], const float toCamera[3],
+                     const float pos[3], const float albedo[3], float metallic, float roughness, const float r12[2],
+                     float contrib[3], or_ray* shadowRay)
+{
+	or_surface m;
+	m.albedo[0] = albedo[0]; m.albedo[1] = albedo[1]; m.albedo[2] = albedo[2]; m.albedo[3] = 1.0f;
+	m.roughness = roughness;
+	m.metallic = metallic;
+	return shade_light(light, ld3(mask), ld3(normal), ld3(toCamera), ld3(pos), &m, NULL, r12, contrib, shadowRay);
 }
 
 typedef struct {
@@ -610,7 +665,7 @@ static void frame_pixel(frame_job* j, uint32_t x, uint32_t y)
 			float c[3];
 			or_ray sr;
 			int inLight = 1;
-			if (shade_light(&fp->lights[li], mk(1.0f, 1.0f, 1.0f), hi.normal, toCamera, hi.pos, &hi.surf, &rng, c, &sr)) {
+			if (shade_light(&fp->lights[li], mk(1.0f, 1.0f, 1.0f), hi.normal, toCamera, hi.pos, &hi.surf, &rng, NULL, c, &sr)) {
 				or_hit sh;
 				counts[1]++;
 				if (cast1(j, &sr, &sh, 1)) atomic_fetch_add(&j->overflows, 1);
@@ -638,9 +693,7 @@ static void frame_pixel(frame_job* j, uint32_t x, uint32_t y)
 				oracle_sample_lambert(r1, r2, na, o3);
 				bdir = ld3(o3);
 			} else {
-				v3 refl = sub(fromCamera, muls(hi.normal, 2.0f * dot(hi.normal, fromCamera)));
-				float a = m->roughness * m->roughness;
-				bdir = sample_ggx(r1, r2, a, refl, hi.normal);
+				bdir = bounce_ggx(r1, r2, m->roughness, fromCamera, hi.normal);
 			}
 			throughput = muls(throughput, 0.6f);
 		} else {
@@ -661,7 +714,7 @@ static void frame_pixel(frame_job* j, uint32_t x, uint32_t y)
 				float c[3];
 				or_ray sr;
 				int inLight = 1;
-				if (shade_light(&fp->lights[li], throughput, bi.normal, toCam2, bi.pos, &bi.surf, &rng2, c, &sr)) {
+				if (shade_light(&fp->lights[li], throughput, bi.normal, toCam2, bi.pos, &bi.surf, &rng2, NULL, c, &sr)) {
 					or_hit sh;
 					counts[3]++;
 					if (cast1(j, &sr, &sh, 3)) atomic_fetch_add(&j->overflows, 1);

@@ -100,6 +100,20 @@ float oracle_falloff(float toLightDist, float range);
 
 /* Cosine-weighted bounce direction (sampleLambertian + hemisphereToWorld, MaterialKernel.cu:206-246). */
 void oracle_sample_lambert(float r1, float r2, const float n[3], float out[3]);
+/* The GGX branch of the bounce (createSecondaryRaysKernel, MaterialKernel.cu:293-299): sampleGgx with
+ * a = roughness^2 around reflect(fromCamera, n) (CudaDeviceHelpers.cuh:44-47, MaterialKernel.cu:221-237). */
+void oracle_sample_ggx_bounce(float r1, float r2, float roughness, const float fromCamera[3], const float n[3],
+                              float out[3]);
+/* retrieveTriData (InterpretRayHitKernel.cu:13-37) for n hits, row i reading datas[i]: out receives
+ * pos.xyz, normal.xyz, uv.xy (8 floats per row). */
+void oracle_retrieve_tri_data(uint32_t n, const or_tri_data* datas, const or_ray* rays, const or_hit* hits, float* out,
+                              uint32_t* materialIndex);
+/* shadeHit (MaterialKernel.cu:49-112) for one light with the two uniform numbers r12 of its soft-shadow
+ * offset: contribution = mask * falloff * shade(...); returns 1 and fills shadowRay when the light
+ * casts a shadow ray, 0 where the reference writes its dummy ray. */
+int oracle_shade_hit(const or_light* light, const float mask[3], const float normal[3], const float toCamera[3],
+                     const float pos[3], const float albedo[3], float metallic, float roughness, const float r12[2],
+                     float contrib[3], or_ray* shadowRay);
 
 /* Wavefront frame (CudaTracerRenderer.cpp:612-728 normal path, with the raster G-buffer replaced
  * by ray-cast primary hits): primary closest hit -> shade + one shadow ray per light -> cosine

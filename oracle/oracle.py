@@ -16,7 +16,10 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 ORACLE_SO = HERE / "liboracle.so"
 REF_SO = HERE / "_ref" / "libpheref.so"
-REFERENCE_ROOT = Path(os.environ.get("PHE_REFERENCE_ROOT", "/root/reference"))
+REF_SHADING_SO = HERE / "_ref" / "libpheref_shading.so"
+# The reference files the harnesses compile: baseline/_ref, where oracle/stage_reference.py stages them
+# (git-ignored; it travels with the repository), unless PHE_REFERENCE_ROOT names another tree.
+REFERENCE_ROOT = Path(os.environ.get("PHE_REFERENCE_ROOT") or HERE.parent / "baseline" / "_ref")
 
 MODE_CPU = 0   # castRay accept rule: t < closest && tMin <= t <= tMax (BVHTraversal.hpp:176)
 MODE_GPU = 1   # rayCastKernel accept rule: tMin <= t < current (RayCastKernel.cu:361)
@@ -73,8 +76,14 @@ def srgb_table():
 
 
 def build() -> None:
-    """Builds liboracle.so, and the reference harness when the reference sources are present."""
+    """Builds liboracle.so, and the reference harnesses when the reference sources are present (staging
+    them into baseline/_ref first when a reference checkout is at hand and they are not staged yet)."""
     subprocess.run(["make", "-s", "-C", str(HERE), "oracle"], check=True)
+    if "PHE_REFERENCE_ROOT" not in os.environ:
+        from oracle import stage_reference as S
+        src = S.source_root()
+        if src is not None and not S.staged():
+            S.stage(src)
     if (REFERENCE_ROOT / "source").exists():
         subprocess.run(["make", "-s", "-C", str(HERE), "ref", f"REF={REFERENCE_ROOT}"], check=True)
 
@@ -124,12 +133,48 @@ def lib():
         L.oracle_pcg_uniform.restype = C.c_float
         L.oracle_pcg_next.argtypes = [V]
         L.oracle_pcg_next.restype = C.c_uint32
+        L.oracle_shade.argtypes = [V, V, V, V, C.c_float, C.c_float, V, C.c_float, V, C.c_float, V]
+        L.oracle_shade.restype = None
+        L.oracle_falloff.argtypes = [C.c_float, C.c_float]
+        L.oracle_falloff.restype = C.c_float
+        L.oracle_sample_lambert.argtypes = [C.c_float, C.c_float, V, V]
+        L.oracle_sample_lambert.restype = None
+        L.oracle_sample_ggx_bounce.argtypes = [C.c_float, C.c_float, C.c_float, V, V, V]
+        L.oracle_sample_ggx_bounce.restype = None
+        L.oracle_retrieve_tri_data.argtypes = [C.c_uint32, V, V, V, V, V]
+        L.oracle_retrieve_tri_data.restype = None
+        L.oracle_shade_hit.argtypes = [V, V, V, V, V, V, C.c_float, C.c_float, V, V, V]
+        L.oracle_shade_hit.restype = C.c_int
         _o = L
     return _o
 
 
 def ref_available() -> bool:
     return REF_SO.exists()
+
+
+def ref_shading_available() -> bool:
+    return REF_SHADING_SO.exists()
+
+
+_rs = None
+
+
+def ref_shading():
+    """The reference's shading, sampling and hit-interpretation functions compiled as host code
+    (oracle/ref_shading.cpp)."""
+    global _rs
+    if _rs is None:
+        L = C.CDLL(str(REF_SHADING_SO))
+        V = C.c_void_p
+        for name, args in (("ref_shade", [C.c_uint32, V, V]), ("ref_falloff", [C.c_uint32, V, V, V]),
+                           ("ref_sample_lambertian", [C.c_uint32, V, V]), ("ref_sample_ggx", [C.c_uint32, V, V]),
+                           ("ref_retrieve_tri_data", [C.c_uint32, V, V, V, V, V]),
+                           ("ref_shade_hit", [C.c_uint32, V, V, V, V])):
+            getattr(L, name).argtypes = args
+            getattr(L, name).restype = None
+        _rs = L
+    return _rs
 
 
 def ref():
@@ -341,3 +386,128 @@ def postprocess(linear, gamma=2.2):
     out = np.empty_like(lin)
     lib().oracle_postprocess(lin.size // 4, _p(lin), gamma, _p(out))
     return out
+
+
+# ---------------------------------------------------------------------------------------------
+# shading, sampling and hit interpretation on rows of inputs: the oracle (left) and the reference's
+# own functions (ref_*, oracle/ref_shading.cpp) take the same row layouts
+#   shade:      22 floats  p.xyz n.xyz v.xyz albedo.rgb roughness metallic l.xyz toLightDist strength.rgb range
+#   lambert:     5 floats  r1 r2 n.xyz
+#   ggx:         9 floats  r1 r2 roughness fromCamera.xyz n.xyz
+#   shade_hit:  28 floats  mask.rgb n.xyz toCamera.xyz pos.xyz albedo.rgb metallic roughness
+#                          light.pos.xyz light.radius light.range light.strength.rgb light.staticShadows r1 r2
+
+TRI_DATA_DTYPE = np.dtype([("n0", "<f4", (3,)), ("n1", "<f4", (3,)), ("n2", "<f4", (3,)), ("uv0", "<f4", (2,)),
+                           ("uv1", "<f4", (2,)), ("uv2", "<f4", (2,)), ("materialIndex", "<u4")])
+
+
+def _rows(a, width):
+    a = np.ascontiguousarray(a, np.float32)
+    assert a.ndim == 2 and a.shape[1] == width
+    return a
+
+
+def shade_rows(rows):
+    rows = _rows(rows, 22)
+    out = np.empty((len(rows), 3), np.float32)
+    L = lib()
+    for i, r in enumerate(rows):
+        L.oracle_shade(_p(r[0:3]), _p(r[3:6]), _p(r[6:9]), _p(r[9:12]), float(r[12]), float(r[13]), _p(r[14:17]),
+                       float(r[17]), _p(r[18:21]), float(r[21]), _p(out[i]))
+    return out
+
+
+def falloff_rows(dist, rng):
+    return np.array([lib().oracle_falloff(float(d), float(r)) for d, r in zip(dist, rng)], np.float32)
+
+
+def lambert_rows(rows):
+    rows = _rows(rows, 5)
+    out = np.empty((len(rows), 3), np.float32)
+    for i, r in enumerate(rows):
+        lib().oracle_sample_lambert(float(r[0]), float(r[1]), _p(r[2:5]), _p(out[i]))
+    return out
+
+
+def ggx_rows(rows):
+    rows = _rows(rows, 9)
+    out = np.empty((len(rows), 3), np.float32)
+    for i, r in enumerate(rows):
+        lib().oracle_sample_ggx_bounce(float(r[0]), float(r[1]), float(r[2]), _p(r[3:6]), _p(r[6:9]), _p(out[i]))
+    return out
+
+
+def retrieve_tri_data(datas, rays, hits):
+    datas = np.ascontiguousarray(datas, TRI_DATA_DTYPE)
+    rays = np.ascontiguousarray(rays, RAY_IN_DTYPE)
+    hits = np.ascontiguousarray(hits, RAY_HIT_DTYPE)
+    out = np.empty((len(datas), 8), np.float32)
+    mat = np.empty(len(datas), np.uint32)
+    lib().oracle_retrieve_tri_data(len(datas), _p(datas), _p(rays), _p(hits), _p(out), _p(mat))
+    return out, mat
+
+
+def shade_hit_rows(rows):
+    rows = _rows(rows, 28)
+    contrib = np.empty((len(rows), 3), np.float32)
+    rays = np.zeros((len(rows), 8), np.float32)
+    cast = np.empty(len(rows), np.uint8)
+    light = np.zeros(1, LIGHT_DTYPE)
+    L = lib()
+    for i, r in enumerate(rows):
+        light["pos"] = r[17:20]
+        light["radius"] = r[20]
+        light["range"] = r[21]
+        light["strength"] = r[22:25]
+        light["staticShadows"] = int(r[25] != 0)
+        cast[i] = L.oracle_shade_hit(_p(light), _p(r[0:3]), _p(r[3:6]), _p(r[6:9]), _p(r[9:12]), _p(r[12:15]),
+                                     float(r[15]), float(r[16]), _p(r[26:28]), _p(contrib[i]), _p(rays[i]))
+    return contrib, rays, cast
+
+
+def ref_shade_rows(rows):
+    rows = _rows(rows, 22)
+    out = np.empty((len(rows), 3), np.float32)
+    ref_shading().ref_shade(len(rows), _p(rows), _p(out))
+    return out
+
+
+def ref_falloff_rows(dist, rng):
+    dist = np.ascontiguousarray(dist, np.float32)
+    rng = np.ascontiguousarray(rng, np.float32)
+    out = np.empty(len(dist), np.float32)
+    ref_shading().ref_falloff(len(dist), _p(dist), _p(rng), _p(out))
+    return out
+
+
+def ref_lambert_rows(rows):
+    rows = _rows(rows, 5)
+    out = np.empty((len(rows), 3), np.float32)
+    ref_shading().ref_sample_lambertian(len(rows), _p(rows), _p(out))
+    return out
+
+
+def ref_ggx_rows(rows):
+    rows = _rows(rows, 9)
+    out = np.empty((len(rows), 3), np.float32)
+    ref_shading().ref_sample_ggx(len(rows), _p(rows), _p(out))
+    return out
+
+
+def ref_retrieve_tri_data(datas, rays, hits):
+    datas = np.ascontiguousarray(datas, TRI_DATA_DTYPE)
+    rays = np.ascontiguousarray(rays, RAY_IN_DTYPE)
+    hits = np.ascontiguousarray(hits, RAY_HIT_DTYPE)
+    out = np.empty((len(datas), 8), np.float32)
+    mat = np.empty(len(datas), np.uint32)
+    ref_shading().ref_retrieve_tri_data(len(datas), _p(datas), _p(rays), _p(hits), _p(out), _p(mat))
+    return out, mat
+
+
+def ref_shade_hit_rows(rows):
+    rows = _rows(rows, 28)
+    contrib = np.empty((len(rows), 3), np.float32)
+    rays = np.empty((len(rows), 8), np.float32)
+    cast = np.empty(len(rows), np.uint8)
+    ref_shading().ref_shade_hit(len(rows), _p(rows), _p(contrib), _p(rays), _p(cast))
+    return contrib, rays, cast

@@ -1,7 +1,7 @@
 """Generates the golden fixtures in tests/golden/ from the reference's own CPU code.
 
-Needs the reference sources (default /root/reference, or PHE_REFERENCE_ROOT) to build
-oracle/_ref/libpheref.so, a harness around the reference's buildStaticFrom + sanitizeBVH, castRay /
+Needs the reference sources (staged into baseline/_ref by oracle/stage_reference.py, or the tree
+named by PHE_REFERENCE_ROOT) to build oracle/_ref/libpheref.so, a harness around the reference's buildStaticFrom + sanitizeBVH, castRay /
 castDebugRay, the triangle test and generateCameraDef. Inputs come from the project's seeded scene
 generator and the oracle's primary-ray generator, both of which are deterministic across platforms.
 
@@ -12,8 +12,11 @@ Fixtures (npz, compressed):
                   the 512x512 primary rays, and 4096 incoherent rays with their hits
   ref_isect.npz   2000 ray/triangle pairs through the reference triangle test
   ref_halton.npy  the reference's 16-entry Halton table parsed from GameScreen.cpp
+  ref_shading.npz 4096 input rows each through the reference's own shade, falloffFactor,
+                  sampleLambertian, sampleGgx (as the bounce calls it), retrieveTriData and shadeHit
+                  (oracle/_ref/libpheref_shading.so, the functions compiled as host code), with outputs
 
-Run:  python tests/golden/make_golden.py
+Run:  python tests/golden/make_golden.py [--only shading]
 """
 from __future__ import annotations
 
@@ -52,8 +55,39 @@ def incoherent_rays(scene_scale: float, n: int, seed: int) -> np.ndarray:
     return rays
 
 
+def shading_digest(x: dict) -> str:
+    """sha256 over every input row of the shading fixture (the test regenerates them and compares)."""
+    h = hashlib.sha256()
+    for k in ("shade", "falloff", "lambert", "ggx", "shade_hit"):
+        h.update(np.ascontiguousarray(x[k]).tobytes())
+    for a in x["tri_data"]:
+        h.update(np.ascontiguousarray(a).tobytes())
+    return h.hexdigest()
+
+
+def shading() -> None:
+    """Reference outputs of the shading functions on the seeded rows of tests.helpers.shading_inputs."""
+    from tests.helpers import shading_inputs
+    if not O.ref_shading_available():
+        raise SystemExit("reference shading harness not built: the reference sources are needed")
+    x = shading_inputs(4096, 7)
+    d, r, h = x["tri_data"]
+    td, tm = O.ref_retrieve_tri_data(d, r, h)
+    hc, hr, hk = O.ref_shade_hit_rows(x["shade_hit"])
+    np.savez_compressed(HERE / "ref_shading.npz", seed=np.array([4096, 7], np.int64),
+                        digest=np.array(shading_digest(x)),
+                        shade=O.ref_shade_rows(x["shade"]),
+                        falloff=O.ref_falloff_rows(x["falloff"][:, 0], x["falloff"][:, 1]),
+                        lambert=O.ref_lambert_rows(x["lambert"]), ggx=O.ref_ggx_rows(x["ggx"]),
+                        tri_data=td, tri_material=tm, shade_hit_contrib=hc, shade_hit_ray=hr, shade_hit_cast=hk)
+
+
 def main() -> None:
     O.build()
+    if "--only" in sys.argv and sys.argv[sys.argv.index("--only") + 1] == "shading":
+        shading()
+        print("shading fixture written to", HERE)
+        return
     if not O.ref_available():
         raise SystemExit("reference harness not built: the reference sources are needed")
 
@@ -107,6 +141,7 @@ def main() -> None:
     block = block[:block.index("};")]
     vals = [float(x) for x in re.findall(r"([0-9]*\.[0-9]+)f", block)]
     np.save(HERE / "ref_halton.npy", np.array(vals, np.float32).reshape(-1, 2))
+    shading()
     print("fixtures written to", HERE)
 
 

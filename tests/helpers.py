@@ -118,3 +118,68 @@ def from_device(t, dtype) -> np.ndarray:
 def device_empty(n: int, dtype):
     import torch
     return torch.empty(n * np.dtype(dtype).itemsize, dtype=torch.uint8, device="cuda")
+
+
+# --- seeded inputs for the shading comparison against the reference's own functions ---------------
+
+def _unit(rng, n):
+    d = rng.normal(size=(n, 3))
+    return (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+
+
+def shading_inputs(n: int, seed: int) -> dict:
+    """Rows for shade / falloff / sampleLambertian / sampleGgx / retrieveTriData / shadeHit in the layouts
+    of oracle.oracle's *_rows functions. Includes the edge cases of each function: lights behind the
+    surface and beyond their range, l = -v (a zero half vector), roughness and metallic at 0 and 1,
+    normals within 0.001 of +-z (the other up vector), point and sphere lights, shadows off."""
+    rng = np.random.default_rng(seed)
+    f32 = np.float32
+    out = {}
+    nrm = _unit(rng, n)
+    v = _unit(rng, n)
+    l = _unit(rng, n)
+    l[::97] = -v[::97]
+    rough = rng.uniform(0, 1, n).astype(f32)
+    rough[::11] = 0.0
+    rough[5::11] = 1.0
+    metal = rng.uniform(0, 1, n).astype(f32)
+    metal[::7] = 0.0
+    metal[3::7] = 1.0
+    rngs = rng.uniform(0.5, 4.0, n).astype(f32)
+    dist = (rngs * rng.uniform(0.01, 1.3, n)).astype(f32)
+    shade = np.concatenate([rng.uniform(-2, 2, (n, 3)), nrm, v, rng.uniform(0, 1, (n, 3)), rough[:, None],
+                            metal[:, None], l, dist[:, None], rng.uniform(0, 10, (n, 3)), rngs[:, None]], axis=1)
+    out["shade"] = shade.astype(f32)
+    out["falloff"] = np.stack([dist, rngs], axis=1)
+    zn = _unit(rng, n)
+    zn[::5] = np.array([0.0, 0.0, 1.0], f32)
+    zn[1::5] = np.array([0.0, 0.0, -1.0], f32)
+    zn[2::5, 2] = np.sign(zn[2::5, 2]) * rng.uniform(0.998, 1.0, len(zn[2::5])).astype(f32)
+    zn = (zn / np.linalg.norm(zn, axis=1, keepdims=True)).astype(f32)
+    r12 = rng.uniform(0, 1, (n, 2)).astype(f32)
+    out["lambert"] = np.concatenate([r12, zn], axis=1).astype(f32)
+    out["ggx"] = np.concatenate([r12, rough[:, None], _unit(rng, n), zn], axis=1).astype(f32)
+    datas = np.zeros(n, P.TRI_DATA_DTYPE)
+    for k in ("n0", "n1", "n2"):
+        datas[k] = rng.normal(size=(n, 3)).astype(f32)
+    for k in ("uv0", "uv1", "uv2"):
+        datas[k] = rng.uniform(-2, 2, (n, 2)).astype(f32)
+    datas["materialIndex"] = rng.integers(0, 1 << 20, n).astype(np.uint32)
+    rays = np.zeros(n, P.RAY_IN_DTYPE)
+    rays["origin"] = rng.uniform(-4, 4, (n, 3)).astype(f32)
+    rays["dir"] = _unit(rng, n)
+    hits = np.zeros(n, P.RAY_HIT_DTYPE)
+    hits["t"] = rng.uniform(0, 10, n).astype(f32)
+    uu = rng.uniform(0, 1, n)
+    vv = rng.uniform(0, 1, n) * (1 - uu)
+    hits["u"], hits["v"] = uu.astype(f32), vv.astype(f32)
+    out["tri_data"] = (datas, rays, hits)
+    pos = rng.uniform(0, 2, (n, 3)).astype(f32)
+    lpos = (pos + rng.uniform(-2, 2, (n, 3))).astype(f32)
+    radius = np.where(rng.uniform(size=n) < 0.5, 0.0, rng.uniform(0, 0.5, n)).astype(f32)
+    shadows = (rng.uniform(size=n) < 0.85).astype(f32)
+    out["shade_hit"] = np.concatenate(
+        [rng.uniform(0, 1, (n, 3)), nrm, v, pos, rng.uniform(0, 1, (n, 3)), metal[:, None], rough[:, None], lpos,
+         radius[:, None], rng.uniform(0.5, 4.0, (n, 1)), rng.uniform(0, 10, (n, 3)), shadows[:, None], r12],
+        axis=1).astype(f32)
+    return out
