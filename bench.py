@@ -7,9 +7,18 @@ per-pass rates and per-frame p50/p99 latency are reported beside it.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
---impl reference times the reference's CPU ray-cast path for the same frame on the host cores:
-the reference sources do not exist on the GPU host, so this is the oracle restatement of castRay
-(pinned bit-for-bit to the reference, tests/test_oracle.py) with all host threads.
+The scene's SBVH comes from the reference's own host builder (buildStaticFrom + sanitizeBVH,
+StaticBVHBuilder.cpp:213-260, compiled from the reference sources staged in baseline/_ref): the tree a
+drop-in caller of the reference's ray-cast path hands the library. Building it is input preparation,
+outside every timed region, like generating the scene; where the reference sources are absent the
+project's own SBVH builder stands in, and `config.bvh_builder` says which.
+
+--impl reference times the reference's CPU ray-cast path on the host cores: the reference's own
+castRay (BVHTraversal.hpp:37-128, compiled from its sources) over exactly the rays each frame casts
+(primary and bounce rays closest hit, shadow rays any hit as castRay != miss), with all host threads;
+the rays themselves are produced untimed by the oracle's frame. Where the reference sources are
+absent it falls back to the oracle's restatement of castRay (pinned bit for bit, tests/test_oracle.py)
+and says so (`cpu_baseline.kind` "port").
 Under torchrun (N > 1) every rank renders its own frames (replicas; weak scaling) and the time is
 the max over ranks.
 """
@@ -34,7 +43,10 @@ sys.path.insert(0, str(ROOT))
 METRIC = "Mrays/s closest-/any-hit (plain vs batched/served, 1 GB300) + p50/p99 latency"
 SCENE = "c2_256_2000"
 RES = (1920, 1080)
-REF_BUDGET_S = 90.0   # host seconds the reference arm spends in its timed steps
+LAYOUTS = {"binary": 0, "wide4": 1, "wide8": 2}
+DEFAULT_LAYOUT = "binary"
+REF_BUDGET_S = 60.0   # host seconds the reference arm spends in its timed steps
+CPU_LEG_BUDGET_S = 12.0   # host seconds of the cpu_baseline leg of the GPU arm
 SEED = 2024
 CAM_DIR = (0.0, 0.8, -0.6)
 CAM_UP = (0.0, 0.6, 0.8)
@@ -62,12 +74,14 @@ def parse():
                     help="shadow-pass schedule: one pass over both queues after the bounce pass (default), the "
                          "primary shadow pass beside the bounce pass, or each after its own pass")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--layout", choices=["binary", "wide4", "wide8"], default=DEFAULT_LAYOUT,
+                    help="node layout of the frame's scene (every layout gives the same results)")
     ap.add_argument("--workload", choices=["frame", "plain", "batch", "large", "serve", "sizes"], default="frame",
                     help="frame (default, the headline): 1080p wavefront frame; batch: 64 uneven batches over 4 "
                          "scenes in one launch vs 64 plain launches; large: 8.6M-triangle scene, 4096x4096, 4 "
-                         "lights; serve: Poisson request arrivals through the serving loop; sizes: launch time "
+                         "lights (16M diffuse + 16M shadow rays per launch); serve: Poisson request arrivals through the serving loop; sizes: launch time "
                          "against rays per launch (16K..16M) for each ray-cast entry point")
-    ap.add_argument("--res", type=int, default=4096, help="large: width and height of the frame")
+    ap.add_argument("--res", type=int, default=4096, help="large: width and height of the primary pass")
     ap.add_argument("--rates", default="200,500,1000", help="serve: arrival rates (requests/s)")
     ap.add_argument("--duration", type=float, default=2.0, help="serve: seconds of arrivals per rate")
     ap.add_argument("--render-slots", type=int, default=8, help="serve: concurrent render requests")
@@ -153,40 +167,91 @@ def aggregate_over_ranks(rays_this_rank: float, ms_this_rank: float, dist=None, 
     return r, m, r / (m / 1e3) / 1e6
 
 
+class ReferenceTree:
+    """An SBVH in the reference layout with its slot -> input-triangle map."""
+
+    def __init__(self, nodes, verts, slot_to_tri):
+        self.nodes, self.verts, self.slot_to_tri = nodes, verts, slot_to_tri
+
+    def slot_datas(self, datas):
+        return np.ascontiguousarray(datas[self.slot_to_tri])
+
+
+def reference_tree(s):
+    """The scene's SBVH from the reference's own host builder, or None where the reference sources were
+    not present when the harness was built. Input preparation (untimed); the GPU arm's timed path runs
+    only libphe_gb300.so."""
+    from oracle import oracle as O
+    if not O.ref_available():
+        return None
+    nodes, verts, s2t = O.ref_build_sbvh(s.tri_verts)
+    return ReferenceTree(nodes, verts, s2t)
+
+
+BUILDER_REFERENCE = "reference buildStaticFrom + sanitizeBVH (StaticBVHBuilder.cpp:213-260), compiled from its sources"
+BUILDER_PROJECT = "this project's SBVH builder (the reference sources were not present)"
+
+
 def frame_inputs():
     import phantasyenginetestbed_gb300 as P
     from phantasyenginetestbed_gb300.renderer import make_lights
     s = P.standard_scene(SCENE)
     t = time.perf_counter()
-    b = P.build_sbvh(s.tri_verts)
+    b = reference_tree(s)
+    builder = BUILDER_REFERENCE
+    if b is None:
+        b, builder = P.build_sbvh(s.tri_verts), BUILDER_PROJECT
     build_s = time.perf_counter() - t
     k = s.scale
     cam_pos = (0.5 * k, -0.3 * k, 0.6 * k)
     lights = make_lights(np.array([[0.5, 0.5, 2.0]], np.float32) * np.float32(k), range_=1000.0 * k)
-    return s, b, cam_pos, lights, build_s
+    return s, b, cam_pos, lights, build_s, builder
 
 
-def cpu_frame_rate(s, b, cam_pos, lights, min_seconds=8.0, max_frames=40, warm=1):
-    """The oracle (castRay restatement + shading) rendering the same frames on all host threads."""
+def cpu_castray_rate(s, b, cam_pos, lights, budget_s, steps, first_frame=0):
+    """The CPU ray-cast path on all host threads over the frame's own rays. Each step takes frame
+    first_frame + k, has the oracle's frame produce (untimed) the rays of a band of rows of it — primary,
+    primary shadow, bounce and bounce shadow rays — and times casting exactly those rays: the
+    reference's castRay compiled from its sources (closest hit for primary and bounce rays; castRay !=
+    miss for the shadow rays), or the oracle's restatement where the reference is absent. The band
+    (moving down the frame) is sized so that the timed steps take about budget_s.
+    Returns (Mrays/s, kind, threads, rows per band, per-step seconds)."""
     from oracle import oracle as O
     import phantasyenginetestbed_gb300 as P
     cam = O.camera_def(cam_pos, CAM_DIR, CAM_UP, math.radians(60.0), RES)
     datas = b.slot_datas(s.datas)
     threads = O.threads()
-    for f in range(warm):
+    kind = "reference" if O.ref_available() else "port"
+
+    def band_rays(f, rows):
+        dump = [np.empty(RES[0] * (rows[1] - rows[0]), O.RAY_IN_DTYPE) for _ in range(4)]
         O.render_frame(b.nodes, b.verts, datas, s.materials, lights, cam, RES, P.halton_jitter(f), cam_pos, SEED, f,
-                       nthreads=threads)
-    rays, frames, t0 = 0, 0, time.perf_counter()
-    times = []
-    while frames < max_frames and (time.perf_counter() - t0) < min_seconds:
+                       nthreads=threads, rows=rows, dump=dump)
+        return dump
+
+    def cast(dump):
+        closest = np.concatenate([dump[0], dump[2]])
+        shadow = np.concatenate([dump[1], dump[3]])
         t = time.perf_counter()
-        _, _, counts = O.render_frame(b.nodes, b.verts, datas, s.materials, lights, cam, RES, P.halton_jitter(frames),
-                                      cam_pos, SEED, frames, nthreads=threads)
-        times.append(time.perf_counter() - t)
-        rays += int(counts.sum())
-        frames += 1
-    el = time.perf_counter() - t0
-    return rays / el / 1e6, threads, frames, times
+        if kind == "reference":
+            O.ref_cast_rays(b.nodes, b.verts, closest, nthreads=threads)
+            O.ref_any_rays(b.nodes, b.verts, shadow, nthreads=threads)
+        else:
+            O.cast_rays(b.nodes, b.verts, closest, nthreads=threads)
+            O.any_rays(b.nodes, b.verts, shadow, nthreads=threads)
+        return time.perf_counter() - t, len(closest) + len(shadow)
+
+    # Calibration on a 64-row band (untimed): rays per row and the rate.
+    el, n = cast(band_rays(first_frame, (RES[1] // 2 - 32, RES[1] // 2 + 32)))
+    rate = n / max(el, 1e-6)
+    rows = int(max(8, min(RES[1], budget_s / steps * rate / (n / 64))))
+    rays, times = 0, []
+    for k in range(steps):
+        r0 = (k * rows) % RES[1]
+        el, n = cast(band_rays(first_frame + k, (r0, min(RES[1], r0 + rows))))
+        times.append(el)
+        rays += n
+    return rays / sum(times) / 1e6, kind, threads, rows, times
 
 
 FRAME_WORKLOAD = (f"wavefront frame {RES[0]}x{RES[1]}: primary closest -> shade + 1 any-hit shadow ray per light -> "
@@ -194,58 +259,82 @@ FRAME_WORKLOAD = (f"wavefront frame {RES[0]}x{RES[1]}: primary closest -> shade 
 FRAME_DATA = "synthetic (seeded heightfield + cubes scene, 155,072 triangles; the reference's Sponza is not in its tree)"
 
 
-def frame_config(s, b, build_s) -> dict:
-    """The frame workload's identifying keys, the same in both arms."""
+L2_NOTE = "GPU arm: L2 flushed (512 MiB write) before every timed frame"
+
+
+def frame_config(s, b, builder, world) -> dict:
+    """The frame workload's identifying keys, identical in both arms (the GPU arm's node layout is
+    reported beside them, under "frame")."""
     return {"workload": FRAME_WORKLOAD, "scene": SCENE, "triangles": int(len(s.tri_verts)),
-            "bvh_nodes": int(len(b.nodes)), "bvh_slots": int(len(b.verts)), "sbvh_build_s": round(build_s, 2),
-            "lights": 1}
+            "resolution": f"{RES[0]}x{RES[1]}", "bvh_builder": builder, "bvh_nodes": int(len(b.nodes)),
+            "bvh_slots": int(len(b.verts)), "lights": 1, "seed": SEED, "l2": L2_NOTE, "parallelism": f"replicas x{world}"}
 
 
 def run_reference(args, world, rank):
     if rank != 0:
         return
-    s, b, cam_pos, lights, build_s = frame_inputs()
-    from oracle import oracle as O
-    import phantasyenginetestbed_gb300 as P
-    cam = O.camera_def(cam_pos, CAM_DIR, CAM_UP, math.radians(60.0), RES)
-    datas = b.slot_datas(s.datas)
-    threads = O.threads()
-    full = []
-    for f in range(max(1, args.warmup)):
-        t = time.perf_counter()
-        O.render_frame(b.nodes, b.verts, datas, s.materials, lights, cam, RES, P.halton_jitter(f), cam_pos, SEED, f,
-                       nthreads=threads)
-        full.append(time.perf_counter() - t)
-    # Each step renders a band of rows sized so that all steps take about REF_BUDGET_S (whole frames
-    # when the steps are few); the band moves down the frame from step to step.
-    rows = max(8, min(RES[1], int(RES[1] * (REF_BUDGET_S / args.steps) / min(full))))
-    rays, times = 0, []
-    for f in range(args.steps):
-        r0 = (f * rows) % RES[1]
-        band = (r0, min(RES[1], r0 + rows))
-        t = time.perf_counter()
-        _, _, counts = O.render_frame(b.nodes, b.verts, datas, s.materials, lights, cam, RES, P.halton_jitter(f),
-                                      cam_pos, SEED, f, nthreads=threads, rows=band)
-        times.append(time.perf_counter() - t)
-        rays += int(counts.sum())
+    s, b, cam_pos, lights, build_s, builder = frame_inputs()
+    value, kind, threads, rows, times = cpu_castray_rate(s, b, cam_pos, lights, REF_BUDGET_S, args.steps,
+                                                         first_frame=args.warmup)
     total = sum(times)
-    value = rays / total / 1e6
     lat = sorted(t * 1e3 for t in times)
+    what = ("the reference's castRay compiled from its sources (BVHTraversal.hpp:37-128)" if kind == "reference"
+            else "the oracle's restatement of castRay (the reference sources were not present)")
     line = {
         "impl": "reference", "metric": METRIC, "value": round(value, 3), "unit": "Mrays/s", "n_gpus": args.gpus,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(total / args.steps * 1e3, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": FRAME_DATA,
-        "config": {**frame_config(s, b, build_s), "parallelism": f"host threads x{threads}"},
+        "config": frame_config(s, b, builder, world),
+        "sbvh_build_s": round(build_s, 2),
         "latency_ms": {"p50": round(lat[len(lat) // 2], 3), "p99": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 3)},
-        "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": threads, "kind": "port",
-                         "sample": (f"{args.steps} frames of the {RES[0]}x{RES[1]} workload through the castRay "
-                                    f"restatement, a band of up to {rows} rows of each (moving down the frame; whole "
-                                    f"frames take {min(full):.2f} s here); the reference sources are not on "
-                                    "the GPU host")},
+        "cpu_baseline": {"value": round(value, 3), "unit": "Mrays/s", "cores": threads, "kind": kind,
+                         "sample": (f"{args.steps} frames of the {RES[0]}x{RES[1]} workload: per frame the rays of a "
+                                    f"band of {rows} rows (moving down the frame; primary, shadow, bounce and bounce-"
+                                    f"shadow rays as the frame casts them, produced untimed by the oracle's frame) "
+                                    f"cast through {what}; shading is not timed")},
         "e2e": {"value": round(value, 3), "unit": "Mrays/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+# frame pass -> its kernel function and the committed ncu summary of that kernel on this workload
+PASS_KERNEL = {"primary": "primary_kernel", "bounce": "bounce_kernel", "shadows": "any_queue_kernel",
+               "primary_shadow": "any_queue_kernel", "bounce_shadow": "any_queue_kernel",
+               "primary_trace": "primary_trace_kernel", "bounce_trace": "bounce_trace_kernel"}
+
+
+def frame_roofline(dominant, entry, clock, num_sms, builder, layout) -> dict:
+    """Roofline of the dominant frame kernel. The frame's scene is L2-resident, so no memory roofline
+    binds; the limit is instruction issue (4 warp instructions per SM cycle). achieved = the kernel's
+    warp instructions per launch (the ncu count of that kernel on this workload, per ray, times the rays
+    of the live launch) / (the live CUDA-event launch duration x SMs x the median SM clock sampled under
+    load). Beside it: SIMD efficiency, DRAM / L2 / L1 fractions and DRAM bytes per launch from the same
+    ncu capture, and the HBM-effective figure (algorithmic bytes / live duration / measured HBM copy
+    peak), which counts bytes mostly served by L1 and L2."""
+    kernel = PASS_KERNEL.get(dominant, dominant)
+    peaks_path = ROOT / "MEASURED_PEAKS.json"
+    peaks = json.loads(peaks_path.read_text()) if peaks_path.exists() else {}
+    hbm_peak, peak_src = (float(peaks["hbm_gbs"]), "measured") if "hbm_gbs" in peaks else (6800.0, "fallback")
+    mhz = clock.get("sm_mhz") or float(peaks.get("sm_max_mhz", 2070.0))
+    out = {"bound": "issue", "kernel": kernel, "pass": dominant, "achieved": None, "peak": 4.0,
+           "unit": "warp instructions / SM cycle", "frac": None, "traffic": None,
+           "hbm_effective": {"achieved": entry.get("GB_s"), "peak": hbm_peak, "unit": "GB/s", "peak_source": peak_src,
+                             "frac": round(entry["GB_s"] / hbm_peak, 4) if entry.get("GB_s") else None}}
+    prof = ROOT / "profiles" / "ncu_kernels.json"
+    nc = json.loads(prof.read_text()).get(f"{kernel}/{layout}") if prof.exists() else None
+    if nc and nc.get("bvh_builder") == builder:
+        inst = nc["warp_inst_per_ray"] * entry["rays"]
+        ipc = inst / (entry["ms"] * 1e-3 * num_sms * mhz * 1e6)
+        out.update({"achieved": round(ipc, 3), "frac": round(ipc / 4.0, 4), "traffic": nc.get("dram_bytes_per_launch"),
+                    "traffic_rays": nc.get("rays_per_launch"), "simd_efficiency": nc.get("simd_efficiency"),
+                    "dram_frac": nc.get("dram_frac"), "l2_frac": nc.get("l2_frac"), "l1_frac": nc.get("l1_frac"),
+                    "ncu_inst_per_active_cycle": nc.get("inst_per_active_cycle"), "source": nc.get("source"),
+                    "how": f"{nc['warp_inst_per_ray']:.1f} warp instructions per ray (ncu) x {entry['rays']:.0f} rays / "
+                           f"({entry['ms']:.4f} ms x {num_sms} SMs x {mhz:.0f} MHz)"})
+    else:
+        out["note"] = f"no ncu summary of {kernel} on this tree and layout ({layout}) in profiles/ncu_kernels.json"
+    return out
 
 
 def run_ours(args, world, rank, local):
@@ -259,8 +348,9 @@ def run_ours(args, world, rank, local):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    s, b, cam_pos, lights, build_s = frame_inputs()
+    s, b, cam_pos, lights, build_s, builder = frame_inputs()
     scene = P.Scene(b.nodes, b.verts, b.slot_datas(s.datas), s.materials)
+    scene.set_layout(LAYOUTS[args.layout])
     r = CudaTracerRenderer(use_graph=not args.no_graph)
     r.set_pipeline(fused=args.pipeline == "fused", refill=args.refill, sort_window=args.sort_window)
     r.set_shadow_schedule({"in-order": 0, "beside": 1, "merged": 2}[args.shadows])
@@ -350,7 +440,8 @@ def run_ours(args, world, rank, local):
             dist.destroy_process_group()
         return
 
-    work = json.loads((ROOT / "profiles" / "work_per_ray.json").read_text())["stages"]
+    work = json.loads((ROOT / "profiles" / "work_per_ray.json").read_text())["trees"][
+        "reference" if builder == BUILDER_REFERENCE else "project"]["stages"]
     io = {"primary": 48, "primary_shadow": 33, "bounce": 48, "bounce_shadow": 33}
     stage_rays = dict(zip(["primary", "primary_shadow", "bounce", "bounce_shadow"], (counts / args.steps).tolist()))
     per_kernel = {}
@@ -382,55 +473,32 @@ def run_ours(args, world, rank, local):
                           "GB_s": round(n * bytes_per_ray / (avg_kernel_ms[i] / 1e3) / 1e9, 1)})
         per_kernel[name] = entry
     dominant = max((k for k in names if "rays" in per_kernel[k]), key=lambda k: per_kernel[k]["ms"])
-    peaks_path = ROOT / "MEASURED_PEAKS.json"
-    if peaks_path.exists():
-        peak = float(json.loads(peaks_path.read_text())["hbm_gbs"])
-        peak_src = "measured"
-    else:
-        peak, peak_src = 6800.0, "fallback"
-    traffic, issue = None, None
-    tpath = ROOT / "profiles" / "ncu_traffic.json"
-    if tpath.exists():
-        nc = json.loads(tpath.read_text())
-        traffic = nc.get(dominant)
-        if f"{dominant}_inst_per_cycle" in nc:
-            # the limit that binds (the scene is L2-resident): issue, from the committed ncu capture
-            issue = {"inst_per_cycle": nc[f"{dominant}_inst_per_cycle"], "of": 4,
-                     "frac": round(nc[f"{dominant}_inst_per_cycle"] / 4, 3),
-                     "simd_efficiency": nc.get(f"{dominant}_simd_efficiency"),
-                     "dram_frac": nc.get(f"{dominant}_dram_throughput"),
-                     "l2_frac": nc.get(f"{dominant}_l2_throughput"), "l1_frac": nc.get(f"{dominant}_l1_throughput"),
-                     "l2_bytes": nc.get(f"{dominant}_l2_bytes"), "source": "profiles/bounce_kernel_1080p_ncu.md"}
-    dom = per_kernel[dominant]
-    achieved = dom.get("GB_s")
     lat = sorted(per)
+    clock = clocks.summary()
+    roofline = frame_roofline(dominant, per_kernel[dominant], clock, torch.cuda.get_device_properties(local).multi_processor_count,
+                              builder, args.layout)
     cpu = None
     if not args.no_cpu_baseline and world == 1:
-        v, cores, frames, _ = cpu_frame_rate(s, b, cam_pos, lights)
-        cpu = {"value": round(v, 3), "unit": "Mrays/s", "cores": cores, "kind": "port",
-               "sample": f"{frames} full {RES[0]}x{RES[1]} frames (~8 s) through the castRay restatement"}
+        v, kind, cores, rows, times = cpu_castray_rate(s, b, cam_pos, lights, CPU_LEG_BUDGET_S, 4, first_frame=first)
+        what = "the reference's castRay compiled from its sources" if kind == "reference" else "the castRay restatement"
+        cpu = {"value": round(v, 3), "unit": "Mrays/s", "cores": cores, "kind": kind,
+               "sample": (f"4 frames x a band of {rows} rows: the band's primary, shadow, bounce and bounce-shadow rays "
+                          f"(produced untimed by the oracle's frame) cast through {what} ({sum(times):.1f} s)")}
     launches_per_frame = len(names)
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": "Mrays/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": FRAME_DATA,
-        "config": {**frame_config(s, b, build_s),
-                   "rays_per_frame": round(rays_per_frame, 1), "rays_by_pass": {k: round(v, 1) for k, v in stage_rays.items()},
-                   "cuda_graph": not args.no_graph, "pipeline": args.pipeline,
-                   "refill_threshold": args.refill, "sort_window": args.sort_window,
-                   "shadow_schedule": args.shadows if args.pipeline == "fused" else "in-order", "l2": "flushed before every timed frame (512 MiB write)",
-                   "parallelism": f"replicas x{world}"},
+        "config": frame_config(s, b, builder, world),
+        "frame": {"rays_per_frame": round(rays_per_frame, 1), "rays_by_pass": {k: round(v, 1) for k, v in stage_rays.items()},
+                  "cuda_graph": not args.no_graph, "pipeline": args.pipeline, "refill_threshold": args.refill,
+                  "sort_window": args.sort_window, "sbvh_build_s": round(build_s, 2), "node_layout": args.layout,
+                  "shadow_schedule": args.shadows if args.pipeline == "fused" else "in-order"},
         "latency_ms": {"p50": round(lat[len(lat) // 2], 4), "p99": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 4)},
         "passes": per_kernel,
-        "roofline": {"bound": "hbm", "kernel": dominant, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4) if achieved else None, "traffic": traffic,
-                     "peak_source": peak_src, "issue": issue,
-                     "note": "algorithmic bytes = ray I/O + 64 B x nodes + 48 B x triangle tests per ray (oracle "
-                             "castDebugRay means, profiles/work_per_ray.json); the scene is L2-resident, so most of "
-                             "it is served from L1/L2 (traffic = DRAM bytes per launch) and frac is an effective "
-                             "bandwidth; the binding limit is instruction issue (see issue)"},
-        "clocks": clocks.summary(),
+        "roofline": roofline,
+        "clocks": clock,
         "e2e": {"value": round(e2e_value, 2), "unit": "Mrays/s",
                 "h2d_bytes_per_step": int(native.lib().phe_renderer_frame_param_bytes()),
                 "d2h_bytes_per_step": RES[0] * RES[1] * 16,
@@ -515,7 +583,7 @@ def run_plain(args):
     vis = torch.empty(n, dtype=torch.uint8, device="cuda")
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
     out = {}
-    for layout, lname in ((0, "binary"), (1, "wide4")):
+    for layout, lname in ((0, "binary"), (1, "wide4"), (2, "wide8")):
         scene.set_layout(layout)
         for name, fn in (("closest_persistent", lambda: P.cast_closest(scene, rays, hits, n, stream=stream)),
                          ("closest_plain", lambda: P.cast_closest_plain(scene, rays, hits, n, stream=stream)),
@@ -672,58 +740,118 @@ def run_sizes(args):
     print(json.dumps(line), flush=True)
 
 
+def large_rays(s, b, prim_rays, prim_hits, n, lights, seed):
+    """The large workload's secondary rays, from the hit points of the primary pass (cycled where fewer
+    than n pixels hit): n diffuse rays, cosine-weighted about the hit triangle's geometric normal
+    (flipped to face the incoming ray), directions from a seeded PCG64 stream; and n any-hit shadow
+    rays, ray i from hit point i // 4 toward light i % 4, tMin 1e-3, tMax = the distance to the light."""
+    import phantasyenginetestbed_gb300 as P
+    hit = prim_hits["triangleIndex"] != 0xFFFFFFFF
+    r, h = prim_rays[hit], prim_hits[hit]
+    pos = r["origin"] + r["dir"] * h["t"][:, None]
+    tv = b.verts[h["triangleIndex"]]
+    nrm = np.cross(tv["v1"][:, :3] - tv["v0"][:, :3], tv["v2"][:, :3] - tv["v0"][:, :3])
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    nrm = np.where(((nrm * r["dir"]).sum(1) > 0)[:, None], -nrm, nrm).astype(np.float32)
+    H = len(pos)
+    rng = np.random.default_rng(seed)   # PCG64
+    idx = np.arange(n) % H
+    r1, r2 = rng.random(n, np.float32), rng.random(n, np.float32)
+    phi = 2.0 * np.pi * r1
+    st, ct = np.sqrt(r2), np.sqrt(1.0 - r2)
+    nn = nrm[idx]
+    up = np.where(np.abs(nn[:, 2:3]) < 0.999, np.array([0, 0, 1], np.float32), np.array([1, 0, 0], np.float32))
+    u = np.cross(up, nn)
+    u /= np.linalg.norm(u, axis=1, keepdims=True)
+    v = np.cross(nn, u)
+    d = u * (st * np.cos(phi))[:, None] + v * (st * np.sin(phi))[:, None] + nn * ct[:, None]
+    diffuse = np.zeros(n, P.RAY_IN_DTYPE)
+    diffuse["origin"] = pos[idx]
+    diffuse["dir"] = (d / np.linalg.norm(d, axis=1, keepdims=True)).astype(np.float32)
+    diffuse["tMin"], diffuse["tMax"] = np.float32(1e-3), np.float32(3.4028235e38)
+    lp = np.asarray([l["pos"] for l in lights], np.float32)
+    o = pos[(np.arange(n) // 4) % H]
+    to = lp[np.arange(n) % 4] - o
+    dist = np.linalg.norm(to, axis=1)
+    shadow = np.zeros(n, P.RAY_IN_DTYPE)
+    shadow["origin"] = o
+    shadow["dir"] = (to / dist[:, None]).astype(np.float32)
+    shadow["tMin"], shadow["tMax"] = np.float32(1e-3), dist.astype(np.float32)
+    return diffuse, shadow, H
+
+
 def run_large(args):
-    """8.63M-triangle scene (2048x2048-cell heightfield + 20,000 cubes, world x32), 4096x4096 frame with
-    4 point lights: 16.8M primary rays, ~16M bounce rays (cosine-weighted), shadow rays to 4 lights."""
+    """The large incoherent workload: 8.63M-triangle scene (2048x2048-cell heightfield + 20,000 cubes,
+    world x32). A 4096x4096 pinhole primary pass gives the hit points; then ONE launch of 16M diffuse
+    closest-hit rays from them (cosine-weighted, seeded PCG64 directions) and ONE launch of 16M any-hit
+    shadow rays toward 4 point lights, each timed over args.steps launches from a cold L2 (the scene is
+    ~0.9 GB, 7x the L2), on every node layout the scene offers. HBM traffic per launch comes from a
+    one-kernel ncu capture (profiles/large_workload_ncu.md)."""
     import torch
     import phantasyenginetestbed_gb300 as P
-    from phantasyenginetestbed_gb300.renderer import CudaTracerRenderer, make_lights
+    from phantasyenginetestbed_gb300.renderer import make_lights
     torch.cuda.set_device(0)
+    stream = torch.cuda.current_stream()
     res = (args.res, args.res)
+    N = 16 << 20
     s, b, build_s = _scene_with_bvh("c4_2048_20000")
-    scene = P.Scene(b.nodes, b.verts, b.slot_datas(s.datas), s.materials)
+    scene = P.Scene(b.nodes, b.verts)
     k = s.scale
-    cam_pos = (0.5 * k, -0.3 * k, 0.6 * k)
+    cam = P.camera_def((0.5 * k, -0.3 * k, 0.6 * k), CAM_DIR, CAM_UP, 60.0, res)
     lights = make_lights(np.array([[0.5, 0.5, 2.0], [0.1, 0.1, 1.0], [0.9, 0.2, 1.5], [0.3, 0.9, 0.8]], np.float32)
                          * np.float32(k), range_=1000.0 * k)
-    r = CudaTracerRenderer(use_graph=True)
-    r.setStaticScene(scene)
-    r.setTargetResolution(res)
-    stream = torch.cuda.current_stream()
-    r.set_seed(SEED, 0)
-    for f in range(args.warmup):
-        r.updateCamera(cam_pos, CAM_DIR, CAM_UP, 60.0, P.halton_jitter(f))
-        r.render(lights, stream=stream)
-    steps = max(3, min(args.steps, 10))
-    r.set_graph(False)
-    r.set_kernel_timing(True)
-    r.set_seed(SEED, args.warmup)
-    counts = np.zeros(4, np.int64)
-    walls = []
-    for f in range(steps):
-        r.updateCamera(cam_pos, CAM_DIR, CAM_UP, 60.0, P.halton_jitter(f))
-        r.render(lights, stream=stream)
-        counts += r.ray_counts(stream=stream).astype(np.int64)
-    kms, frames = r.kernel_times()
-    avg = kms / frames
-    counts = counts / steps
-    frame_ms = float(avg.sum())
-    names = ["primary", "bounce", "shadows", "resolve_taa"]   # the default (merged) shadow schedule
-    passes = {}
-    for i, nm in enumerate(names):
-        e = {"ms": round(float(avg[i]), 3)}
-        if nm == "shadows":
-            n = counts[1] + counts[3]
-            e.update({"rays": int(n), "Mrays_s": round(n / avg[i] / 1e3, 1),
-                      "primary_shadow_rays": int(counts[1]), "bounce_shadow_rays": int(counts[3])})
-        elif nm in TRACE_PASS:
-            n = counts[["primary", "primary_shadow", "bounce", "bounce_shadow"].index(TRACE_PASS[nm])]
-            e.update({"rays": int(n), "Mrays_s": round(n / avg[i] / 1e3, 1)})
-        passes[nm] = e
+    npix = res[0] * res[1]
+    prim = torch.empty(npix * 32, dtype=torch.uint8, device="cuda")
+    P.gen_primary_rays(prim, cam, res, order=1)
+    prim_hits = torch.empty(npix * 16, dtype=torch.uint8, device="cuda")
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    P.cast_closest(scene, prim, prim_hits, npix, stream=stream)
+    torch.cuda.synchronize()
+    t_prim = statistics.median(_timed(lambda: P.cast_closest(scene, prim, prim_hits, npix, stream=stream), 3, stream, flush))
+    diffuse, shadow, H = large_rays(s, b, prim.cpu().numpy().view(P.RAY_IN_DTYPE),
+                                    prim_hits.cpu().numpy().view(P.RAY_HIT_DTYPE), N, lights, SEED)
+    d_diffuse = torch.from_numpy(diffuse.view(np.uint8)).cuda()
+    d_shadow = torch.from_numpy(shadow.view(np.uint8)).cuda()
+    hits = torch.empty(N * 16, dtype=torch.uint8, device="cuda")
+    vis = torch.empty(N, dtype=torch.uint8, device="cuda")
+    layouts = {}
+    lay0, avail = scene.layout()
+    for layout, name in ((0, "binary"), (1, "wide4"), (2, "wide8")):
+        if layout and not (avail & layout):
+            continue
+        scene.set_layout(layout)
+        row = {}
+        for pas, fn in (("diffuse_closest", lambda: P.cast_closest(scene, d_diffuse, hits, N, stream=stream)),
+                        ("shadow_any", lambda: P.cast_any(scene, d_shadow, vis, N, stream=stream))):
+            for _ in range(args.warmup):
+                fn()
+            t = _timed(fn, max(3, min(args.steps, 20)), stream, flush)
+            m = statistics.median(t)
+            row[pas] = {"ms": round(m, 3), "Mrays_s": round(N / m / 1e3, 1), "latency_ms": _percentiles(t)}
+        layouts[name] = row
+    scene.set_layout(0)
+    torch.cuda.synchronize()
     line = {"workload": "large", "metric": METRIC, "unit": "Mrays/s", "triangles": int(len(s.tri_verts)),
-            "bvh_nodes": int(len(b.nodes)), "bvh_slots": int(len(b.verts)), "sbvh_build_s": round(build_s, 1),
-            "scene_bytes": scene.device_bytes(), "res": res, "lights": 4, "frame_ms": round(frame_ms, 3),
-            "rays_per_frame": int(counts.sum()), "value": round(counts.sum() / frame_ms / 1e3, 1), "passes": passes}
+            "bvh_builder": "this project's SBVH builder", "bvh_nodes": int(len(b.nodes)), "bvh_slots": int(len(b.verts)),
+            "sbvh_build_s": round(build_s, 1), "scene_bytes": scene.device_bytes(),
+            "primary": {"res": res, "rays": npix, "hits": int(H), "ms": round(t_prim, 3),
+                        "Mrays_s": round(npix / t_prim / 1e3, 1)},
+            "rays_per_launch": N, "lights": 4, "layouts": layouts,
+            "l2": "flushed (512 MiB write) before every timed launch"}
+    ncu = ROOT / "profiles" / "large_workload_ncu.json"
+    if ncu.exists():
+        peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (ROOT / "MEASURED_PEAKS.json").exists() else {}
+        hbm = float(peaks.get("hbm_gbs", 6800.0))
+        roof = {}
+        for pas, rec in json.loads(ncu.read_text()).get("passes", {}).items():
+            ms = layouts.get(rec.get("layout", "binary"), {}).get(pas, {}).get("ms")
+            if ms:
+                bytes_launch = rec["dram_bytes_per_ray"] * N
+                roof[pas] = {"bound": "hbm", "traffic": int(bytes_launch), "achieved": round(bytes_launch / ms / 1e6, 1),
+                             "peak": hbm, "unit": "GB/s", "frac": round(bytes_launch / ms / 1e6 / hbm, 4),
+                             "how": f"{rec['dram_bytes_per_ray']:.1f} DRAM bytes per ray (ncu, {rec['source']}) x {N} rays / "
+                                    f"live launch time"}
+        line["roofline"] = roof
     print(json.dumps(line), flush=True)
 
 

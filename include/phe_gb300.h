@@ -155,6 +155,15 @@ void phe_host_bvh_free(phe_host_bvh* bvh);
  * PHE_ERR_INVALID_SCENE; `maxDepth` (optional) receives the deepest leaf level. */
 phe_status phe_bvh_validate(const phe_bvh_node* nodes, uint32_t numNodes, uint32_t numSlots, uint32_t* maxDepth);
 
+/* The 8-wide compressed node layout (PHE_LAYOUT_WIDE8) that scene upload builds from a tree, on the
+ * host: 20 words per node and 8 words per leaf record (format in csrc/host/wide8.hpp). Either output
+ * array may be NULL to query the counts first. PHE_ERR_INVALID_SCENE (reason in phe_last_error) when the
+ * tree allows no 8-wide layout: a child box outside its parent's box, inverted or not finite. No
+ * reference counterpart (the reference traverses its binary nodes only). */
+phe_status phe_bvh_wide8_build(const phe_bvh_node* nodes, uint32_t numNodes, uint32_t numSlots, uint32_t* nodeWords,
+                               uint32_t maxNodes, uint32_t* leafWords, uint32_t maxLeaves, uint32_t* numNodes8,
+                               uint32_t* numLeaves8, uint32_t* depth);
+
 /* BVH cache file (testbed_application/Main.cpp:105-154): three headerless raw arrays
  * <base>_nodes.bin, <base>_verts.bin, <base>_datas.bin. Read sizes come from the file sizes;
  * datas must have as many entries as verts (the reference's only check, Main.cpp:131-133). Writes
@@ -235,7 +244,16 @@ phe_status phe_gen_primary_rays(phe_ray_in* rays, const phe_camera_def* cam, uin
  * Rays with a non-finite 1/dir always use the binary nodes. Kernels read the layout when launched. */
 #define PHE_LAYOUT_BINARY 0
 #define PHE_LAYOUT_WIDE4 1
+/* PHE_LAYOUT_WIDE8: the tree collapsed to nodes of up to 8 children whose boxes are stored as 8-bit
+ * offsets on a per-node power-of-two grid rounded outward (80 bytes per node, after Ylitie, Karras and
+ * Laine, HPG 2017), with one 32-byte record per leaf holding its exact box and slot range. Child
+ * boxes are tested with directed rounding (entry distance down, exit up), so a quantized box passes
+ * whenever the exact one does; a leaf's exact box is re-tested with the reference arithmetic before
+ * its triangles, so the same leaves are intersected as with the binary nodes and results are the
+ * same. Built at upload when every child box lies inside its parent box and no box is inverted. */
+#define PHE_LAYOUT_WIDE8 2
 phe_status phe_scene_set_layout(phe_scene* scene, int layout);
+/* `wideAvailable` (optional) receives a mask of the wide layouts the tree allows: 1 = 4-wide, 2 = 8-wide. */
 phe_status phe_scene_get_layout(const phe_scene* scene, int* layout, int* wideAvailable);
 
 /* OR of error bits raised by kernels on this scene: single casts, frames, batches, no-alloc batches
@@ -266,7 +284,7 @@ typedef struct phe_batch_params {
 	int32_t blocksPerSM;     /* resident blocks per SM (0 = occupancy limit) */
 	int32_t order;           /* PHE_BATCH_ORDER_* */
 	int32_t useGraph;        /* 1 = replay from a CUDA graph captured on first launch */
-	int32_t layout;          /* PHE_LAYOUT_* for every scene of the batch (wide only where available) */
+	int32_t layout;          /* PHE_LAYOUT_* for every scene of the batch (a wide layout only where the scene has it) */
 	int32_t stackShared;     /* traversal-stack entries kept in shared memory: 0 or 16 (the rest: local) */
 	int32_t sortWindow;      /* ray-sort granularity: 0 = rays in the given order, else 256..4096 (a
 	                          * multiple of 256): within windows of that many rays of a batch, rays are
@@ -297,7 +315,7 @@ phe_status phe_batch_destroy(phe_batch* batch);
 /* The batched launch without any device allocation (no counterpart in the reference). For callers
  * that manage all device memory themselves and cannot let a library call cudaMalloc (an engine's
  * renderer or a plugin host with its own allocator and memory budget; cudaMalloc may also wait for
- * the whole device). The descriptor table, scene table and work counter live in a fixed 11,520-byte
+ * the whole device). The descriptor table, scene table and work counter live in a fixed 12,544-byte
  * array inside the library (per GPU, until exit) instead of device memory the call allocates.
  * At most 256 batch items and 32 scenes per call (PHE_ERR_TOO_LARGE beyond); every scene must live
  * on the current device (PHE_ERR_INVALID_ARGUMENT). All calls share the array: calls whose GPU work

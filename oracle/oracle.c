@@ -597,10 +597,15 @@ typedef struct {
 	const or_hit* primaryHits; float* color; float* roughnessOut;
 	float srgb[256];
 	atomic_uint next; atomic_ullong counts[4]; atomic_ullong work[8]; atomic_int overflows;
+	atomic_uint dumpNext[4];
 } frame_job;
 
 static int cast1(frame_job* j, const or_ray* r, or_hit* h, int stage)
 {
+	if (j->fp->dump[stage]) {
+		uint32_t k = atomic_fetch_add(&j->dumpNext[stage], 1u);
+		if (k < j->fp->dumpCapacity[stage]) j->fp->dump[stage][k] = *r;
+	}
 	uint32_t nv = 0, nt = 0;
 	int rc = oracle_cast_ray(j->nodes, j->tris, r, OR_MODE_REFERENCE_GPU, h, &nv, &nt);
 	atomic_fetch_add(&j->work[2 * stage], (unsigned long long)nv);
@@ -754,6 +759,7 @@ int oracle_render_frame(const or_node* nodes, const or_tri* tris, const or_tri_d
 	atomic_init(&j.next, 0u);
 	for (int i = 0; i < 4; i++) atomic_init(&j.counts[i], 0ull);
 	for (int i = 0; i < 8; i++) atomic_init(&j.work[i], 0ull);
+	for (int i = 0; i < 4; i++) atomic_init(&j.dumpNext[i], 0u);
 	atomic_init(&j.overflows, 0);
 	if (threads < 1) threads = 1;
 	pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * (size_t)threads);
@@ -768,6 +774,8 @@ int oracle_render_frame(const or_node* nodes, const or_tri* tris, const or_tri_d
 		for (int i = 0; i < 4; i++) rayCounts[i] = atomic_load(&j.counts[i]);
 	if (workSums)
 		for (int i = 0; i < 8; i++) workSums[i] = atomic_load(&j.work[i]);
+	if (fp->dumpCount)
+		for (int i = 0; i < 4; i++) fp->dumpCount[i] = atomic_load(&j.dumpNext[i]);
 	return atomic_load(&j.overflows);
 }
 

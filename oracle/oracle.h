@@ -5,7 +5,9 @@
  *
  * Parity pin: oracle_cast_rays() in reference mode is checked bit-for-bit against the reference's
  * own castRay (compiled from its sources into oracle/_ref/libpheref.so) and against the committed
- * fixtures in tests/golden/ that the reference produced.
+ * fixtures in tests/golden/ that the reference produced; the shading, sampling and hit-interpretation
+ * functions are checked against the reference's own ones compiled as host code
+ * (oracle/_ref/libpheref_shading.so) to within 1e-4 absolute, and against their committed outputs.
  *
  * Paths below are relative to the reference project root. Every float operation is written in the
  * reference's source order and the library is built without FP contraction or fast-math, so results
@@ -136,6 +138,12 @@ typedef struct {
 	 * miss) in `cam` minus its uv in `prevCam`, both without jitter; (2, 2) behind either camera. */
 	or_camera prevCam;
 	float* velocity;
+	/* Ray dump (optional): every ray cast at stage s (primary, primary shadow, bounce, bounce shadow) is
+	 * also written to dump[s] (up to dumpCapacity[s] rays, in no particular order); dumpCount[s] receives
+	 * the number cast. Lets a CPU baseline time another traversal on exactly the frame's rays. */
+	or_ray* dump[4];
+	uint32_t dumpCapacity[4];
+	uint32_t* dumpCount;
 } or_frame_params;
 /* `rayCounts` (optional, 4): rays cast per stage (primary, primary shadow, bounce, bounce shadow);
  * `workSums` (optional, 8): castDebugRay's nodesVisited and triangleIntersectionTests summed per stage. */

@@ -37,7 +37,8 @@ class FrameParams(C.Structure):
                 ("camPos", C.c_float * 3), ("lights", C.c_void_p), ("numLights", C.c_uint32),
                 ("materials", C.c_void_p), ("seed", C.c_uint64), ("frame", C.c_uint32),
                 ("textures", C.c_void_p), ("numTextures", C.c_uint32), ("rowBegin", C.c_uint32),
-                ("rowEnd", C.c_uint32), ("prevCam", C.c_float * 12), ("velocity", C.c_void_p)]
+                ("rowEnd", C.c_uint32), ("prevCam", C.c_float * 12), ("velocity", C.c_void_p),
+                ("dump", C.c_void_p * 4), ("dumpCapacity", C.c_uint32 * 4), ("dumpCount", C.c_void_p)]
 
 
 class Texture(C.Structure):
@@ -188,6 +189,8 @@ def ref():
         L.ref_bvh_copy.argtypes = [V, V, V, V]
         L.ref_bvh_free.argtypes = [V]
         L.ref_cast_rays.argtypes = [V, V, V, C.c_uint32, V, V, C.c_int]
+        L.ref_any_rays.argtypes = [V, V, V, C.c_uint32, V, C.c_int]
+        L.ref_any_rays.restype = None
         L.ref_intersect_tri.argtypes = [V, V, V, V]
         L.ref_camera_def.argtypes = [V, V, V, C.c_float, C.c_float, C.c_float, V]
         _r = L
@@ -263,12 +266,14 @@ def sincos_2pi(r):
 
 def render_frame(nodes, verts, slot_datas, materials, lights, cam12, res, jitter, cam_pos, seed, frame,
                  primary_hits=None, nthreads=None, work=None, textures=(), rows=None, prev_cam=None,
-                 velocity_out=None):
+                 velocity_out=None, dump=None):
     """Oracle frame: (color (H, W, 4), roughness (H, W), ray counts per stage). `work` (optional
     uint64 array of 8) receives nodesVisited / triangle tests summed per stage; `textures` are
     (H, W, C) uint8 images indexed by the materials' texture indices; `rows` = (begin, end) renders
     only those rows (the rest of the image is left unset, the counts cover those rows); `velocity_out`
-    ((H, W, 2) float32) receives the TAA velocity against the previous camera `prev_cam`."""
+    ((H, W, 2) float32) receives the TAA velocity against the previous camera `prev_cam`; `dump` (a list
+    of 4 RAY_IN_DTYPE arrays) receives the rays cast per stage (primary, primary shadow, bounce, bounce
+    shadow), and is replaced by the filled prefixes."""
     fp = FrameParams()
     fp.resX, fp.resY = res
     fp.cam[:] = [float(x) for x in cam12]
@@ -289,6 +294,13 @@ def render_frame(nodes, verts, slot_datas, materials, lights, cam12, res, jitter
         assert velocity_out.dtype == np.float32 and velocity_out.shape == (res[1], res[0], 2)
         fp.prevCam[:] = [float(x) for x in (cam12 if prev_cam is None else prev_cam)]
         fp.velocity = velocity_out.ctypes.data
+    dump_count = np.zeros(4, np.uint32)
+    if dump is not None:
+        for k in range(4):
+            assert dump[k].dtype == RAY_IN_DTYPE and dump[k].flags.c_contiguous
+            fp.dump[k] = dump[k].ctypes.data
+            fp.dumpCapacity[k] = len(dump[k])
+        fp.dumpCount = dump_count.ctypes.data
     color = np.empty((res[1], res[0], 4), np.float32)
     rough = np.empty((res[1], res[0]), np.float32)
     counts = np.zeros(4, np.uint64)
@@ -296,6 +308,9 @@ def render_frame(nodes, verts, slot_datas, materials, lights, cam12, res, jitter
                                    _p(rough), _p(counts), _p(work), nthreads or threads())
     if rc:
         raise RuntimeError(f"oracle: {rc} rays overflowed the traversal stack")
+    if dump is not None:
+        assert (dump_count <= np.array([len(d) for d in dump])).all(), "ray dump capacity exceeded"
+        dump[:] = [d[:int(c)] for d, c in zip(dump, dump_count)]
     return color, rough, counts
 
 
@@ -329,6 +344,14 @@ def ref_cast_rays(nodes, verts, rays, debug=False, nthreads=None):
     dbg = np.empty((n, 2), np.uint32) if debug else None
     ref().ref_cast_rays(_p(nodes), _p(verts), _p(rays), n, _p(hits), _p(dbg), nthreads or threads())
     return (hits, dbg) if debug else hits
+
+
+def ref_any_rays(nodes, verts, rays, nthreads=None):
+    """Any hit through the reference castRay: 1 where it finds no triangle in [tMin, tMax]."""
+    out = np.empty(len(rays), np.uint8)
+    ref().ref_any_rays(_p(nodes), _p(verts), _p(np.ascontiguousarray(rays, RAY_IN_DTYPE)), len(rays), _p(out),
+                       nthreads or threads())
+    return out
 
 
 def ref_camera_def(pos, direction, up, vfov_rad, res):

@@ -125,6 +125,32 @@ void ref_cast_rays(const void* nodes, const void* verts, const float* rays, uint
 	for (auto& th : threads) th.join();
 }
 
+// Any hit through the reference castRay, the way the reference's CPU path would answer a shadow
+// query (it has no any-hit traversal): inLight[i] = 1 when castRay(ray, tMin, tMax) finds no triangle.
+void ref_any_rays(const void* nodes, const void* verts, const float* rays, uint32_t n, uint8_t* inLight,
+                  int numThreads)
+{
+	const BVHNode* nd = (const BVHNode*)nodes;
+	const TriangleVertices* tv = (const TriangleVertices*)verts;
+	if (numThreads < 1) numThreads = 1;
+	auto work = [&](uint32_t begin, uint32_t end) {
+		for (uint32_t i = begin; i < end; i++) {
+			const float* r = rays + 8 * size_t(i);
+			Ray ray(sfz::vec3(r[0], r[1], r[2]), sfz::vec3(r[4], r[5], r[6]));
+			RayCastResult res = castRay(nd, tv, ray, r[3], r[7]);
+			inLight[i] = res.triangleIndex == ~0u ? 1 : 0;
+		}
+	};
+	std::vector<std::thread> threads;
+	uint32_t chunk = (n + numThreads - 1) / numThreads;
+	for (int t = 0; t < numThreads; t++) {
+		uint32_t b = t * chunk, e = b + chunk < n ? b + chunk : n;
+		if (b >= e) break;
+		threads.emplace_back(work, b, e);
+	}
+	for (auto& th : threads) th.join();
+}
+
 // The reference triangle test on one triangle (TriangleVertices layout).
 int ref_intersect_tri(const float* tri, const float* origin, const float* dir, float* tuv)
 {

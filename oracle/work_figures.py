@@ -7,6 +7,9 @@ Algorithmic bytes per ray (used by bench.py's roofline.achieved):
   any hit:     33 B ray I/O (32 in + 1 out)  + 64 * n_node + 48 * n_tri
   a shaded hit adds 64 B of TriangleData.
 
+Frame figures are written for the tree of the reference's own builder ("reference", the tree the
+frame benchmark uses) and for this project's builder ("project").
+
 Run: python oracle/work_figures.py
 """
 from __future__ import annotations
@@ -32,9 +35,19 @@ CAM_DIR = (0.0, 0.8, -0.6)
 CAM_UP = (0.0, 0.6, 0.8)
 
 
-def frame_setup(scene_name=FRAME_SCENE, res=FRAME_RES):
+class _Tree:
+    def __init__(self, nodes, verts, s2t):
+        self.nodes, self.verts, self.slot_to_tri = nodes, verts, s2t
+
+    def slot_datas(self, datas):
+        return np.ascontiguousarray(datas[self.slot_to_tri])
+
+
+def frame_setup(scene_name=FRAME_SCENE, res=FRAME_RES, builder="project"):
+    """builder "reference": the reference's own buildStaticFrom + sanitizeBVH (oracle/_ref); "project":
+    this project's SBVH builder."""
     s = P.standard_scene(scene_name)
-    b = P.build_sbvh(s.tri_verts)
+    b = _Tree(*O.ref_build_sbvh(s.tri_verts)) if builder == "reference" else P.build_sbvh(s.tri_verts)
     k = s.scale
     cam_pos = (0.5 * k, -0.3 * k, 0.6 * k)
     cam = O.camera_def(cam_pos, CAM_DIR, CAM_UP, math.radians(60.0), res)
@@ -42,18 +55,28 @@ def frame_setup(scene_name=FRAME_SCENE, res=FRAME_RES):
     return s, b, cam, cam_pos, lights
 
 
-def main() -> None:
-    s, b, cam, cam_pos, lights = frame_setup()
+def frame_work(builder):
+    s, b, cam, cam_pos, lights = frame_setup(builder=builder)
     work = np.zeros(8, np.uint64)
     jit = P.halton_jitter(0)
     _, _, counts = O.render_frame(b.nodes, b.verts, b.slot_datas(s.datas), s.materials, lights, cam, FRAME_RES, jit,
                                   cam_pos, FRAME_SEED, 0, work=work)
     stages = ["primary", "primary_shadow", "bounce", "bounce_shadow"]
-    out = {"workload": f"wavefront frame {FRAME_SCENE} {FRAME_RES[0]}x{FRAME_RES[1]} seed {FRAME_SEED} frame 0",
-           "bvh": {"nodes": len(b.nodes), "slots": len(b.verts)}, "stages": {}}
+    out = {"bvh": {"nodes": len(b.nodes), "slots": len(b.verts)}, "stages": {}}
     for i, st in enumerate(stages):
         n = int(counts[i])
         out["stages"][st] = {"rays": n, "n_node": float(work[2 * i]) / n, "n_tri": float(work[2 * i + 1]) / n}
+    return out
+
+
+def main() -> None:
+    out = {"workload": f"wavefront frame {FRAME_SCENE} {FRAME_RES[0]}x{FRAME_RES[1]} seed {FRAME_SEED} frame 0",
+           "trees": {}}
+    # the tree the frame benchmark uses (the reference's own builder) and this project's builder
+    for builder in ("reference", "project"):
+        if builder == "reference" and not O.ref_available():
+            continue
+        out["trees"][builder] = frame_work(builder)
     # plain closest-hit primary rays of the 64x64-cell scene, 512x512
     s1 = P.standard_scene("c1_64_100")
     b1 = P.build_sbvh(s1.tri_verts)

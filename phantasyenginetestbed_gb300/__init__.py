@@ -25,7 +25,7 @@ from .native import (LIGHT_DTYPE, MATERIAL_DTYPE, NODE_DTYPE, RAY_HIT_DTYPE, RAY
 
 __all__ = [
     "CameraDef", "PheError", "Scene", "HostBVH", "SceneArrays", "generate_scene", "build_sbvh", "camera_def",
-    "halton_jitter", "write_bvh_cache", "read_bvh_cache", "cast_closest", "cast_closest_plain", "cast_any", "gen_primary_rays", "STANDARD_SCENES",
+    "halton_jitter", "wide8_build", "write_bvh_cache", "read_bvh_cache", "cast_closest", "cast_closest_plain", "cast_any", "gen_primary_rays", "STANDARD_SCENES",
     "NODE_DTYPE", "TRI_VERTS_DTYPE", "TRI_DATA_DTYPE", "RAY_IN_DTYPE", "RAY_HIT_DTYPE", "MATERIAL_DTYPE", "LIGHT_DTYPE",
 ]
 
@@ -128,6 +128,20 @@ def validate_bvh(nodes: np.ndarray, num_slots: int) -> int:
     return int(md.value)
 
 
+def wide8_build(nodes: np.ndarray, num_slots: int):
+    """The 8-wide compressed layout scene upload builds from a tree (phe_bvh_wide8_build): (node words
+    (N, 20) uint32, leaf records (L, 8) uint32, depth)."""
+    nodes = np.ascontiguousarray(nodes)
+    nn, nl, dp = C.c_uint32(), C.c_uint32(), C.c_uint32()
+    check(lib().phe_bvh_wide8_build(ptr(nodes), len(nodes), num_slots, None, 0, None, 0, C.byref(nn), C.byref(nl),
+                                    C.byref(dp)), "phe_bvh_wide8_build")
+    w = np.empty((nn.value, 20), np.uint32)
+    lv = np.empty((nl.value, 8), np.uint32)
+    check(lib().phe_bvh_wide8_build(ptr(nodes), len(nodes), num_slots, ptr(w), nn.value, ptr(lv), nl.value,
+                                    C.byref(nn), C.byref(nl), C.byref(dp)), "phe_bvh_wide8_build")
+    return w, lv, int(dp.value)
+
+
 def camera_def(pos, direction, up, vfov_deg: float, res) -> CameraDef:
     """generateCameraDef (GenerateRays.cpp:12-35)."""
     out = CameraDef()
@@ -189,13 +203,15 @@ class Scene:
               "phe_scene_set_materials_and_textures")
 
     def set_layout(self, layout: int) -> None:
-        """0 = binary nodes (default), 1 = 4-wide nodes (same results; see phe_scene_set_layout)."""
+        """0 = binary nodes (default), 1 = 4-wide nodes, 2 = 8-wide compressed nodes (same results; see
+        phe_scene_set_layout)."""
         check(lib().phe_scene_set_layout(self.handle, layout), "phe_scene_set_layout")
 
     def layout(self):
+        """(selected layout, mask of the wide layouts the tree allows: 1 = 4-wide, 2 = 8-wide)."""
         lay, avail = C.c_int(), C.c_int()
         check(lib().phe_scene_get_layout(self.handle, C.byref(lay), C.byref(avail)), "phe_scene_get_layout")
-        return int(lay.value), bool(avail.value)
+        return int(lay.value), int(avail.value)
 
     def status(self) -> int:
         """Error bits raised by kernels on this scene so far (1 = traversal stack overflow, 2 = index

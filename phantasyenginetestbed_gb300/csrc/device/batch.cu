@@ -207,8 +207,8 @@ static phe_status check_params(const phe_batch_params* p)
 	                           p->sortWindow % kOctantBlock))
 		return fail(PHE_ERR_INVALID_ARGUMENT, "batch sortWindow must be 0 or a multiple of %d up to %d", kOctantBlock,
 		            kMaxOctantWindow);
-	if (p->layout != PHE_LAYOUT_BINARY && p->layout != PHE_LAYOUT_WIDE4)
-		return fail(PHE_ERR_INVALID_ARGUMENT, "batch layout must be PHE_LAYOUT_BINARY or PHE_LAYOUT_WIDE4");
+	if (p->layout != PHE_LAYOUT_BINARY && p->layout != PHE_LAYOUT_WIDE4 && p->layout != PHE_LAYOUT_WIDE8)
+		return fail(PHE_ERR_INVALID_ARGUMENT, "batch layout must be PHE_LAYOUT_BINARY, PHE_LAYOUT_WIDE4 or PHE_LAYOUT_WIDE8");
 	return PHE_OK;
 }
 
@@ -249,8 +249,11 @@ static phe_status upload_table(phe_batch* b)
 	PHE_CUDA_TRY(cudaMemcpy(b->dItems, dev.data(), n * sizeof(BatchItemDev), cudaMemcpyHostToDevice), "upload batch table");
 	std::vector<DeviceScene> st(b->sceneHandles.size());
 	for (size_t i = 0; i < st.size(); i++) {
-		st[i] = b->sceneHandles[i]->dev;
-		st[i].nodes4 = b->params.layout == PHE_LAYOUT_WIDE4 ? b->sceneHandles[i]->nodes4 : nullptr;
+		const phe_scene* sc = b->sceneHandles[i];
+		st[i] = sc->dev;
+		st[i].nodes4 = b->params.layout == PHE_LAYOUT_WIDE4 ? sc->nodes4 : nullptr;
+		st[i].nodes8 = b->params.layout == PHE_LAYOUT_WIDE8 ? sc->nodes8 : nullptr;
+		st[i].leaves8 = b->params.layout == PHE_LAYOUT_WIDE8 ? sc->leaves8 : nullptr;
 	}
 	if (!st.empty())
 		PHE_CUDA_TRY(cudaMemcpy(b->dScenes, st.data(), st.size() * sizeof(DeviceScene), cudaMemcpyHostToDevice),
@@ -383,7 +386,7 @@ static phe_status batch_enqueue(phe_batch* b, cudaStream_t stream)
 		                                                    b->dPerm);
 		PHE_CUDA_TRY(cudaGetLastError(), "batch_sort_kernel launch");
 	}
-	const bool wide = b->params.layout == PHE_LAYOUT_WIDE4;
+	const bool wide = b->params.layout == PHE_LAYOUT_WIDE4 || b->params.layout == PHE_LAYOUT_WIDE8;
 	const int sh = b->params.stackShared;
 	switch (b->params.blockSize) {
 	case 64: return launch_batch_kernel<64>(t, wide, sh, b->params.blocksPerSM, d->numSMs, b->dCounter, stream, nullptr);
@@ -403,7 +406,7 @@ extern "C" phe_status phe_batch_launch(phe_batch* b, void* stream)
 		// Resolve occupancy outside capture.
 		int occ = 0;
 		BatchTableDev t{};
-		const bool wide = b->params.layout == PHE_LAYOUT_WIDE4;
+		const bool wide = b->params.layout == PHE_LAYOUT_WIDE4 || b->params.layout == PHE_LAYOUT_WIDE8;
 		const int sh = b->params.stackShared;
 		switch (b->params.blockSize) {
 		case 64: launch_batch_kernel<64>(t, wide, sh, 0, 1, nullptr, nullptr, &occ); break;
@@ -475,7 +478,7 @@ extern "C" phe_status phe_batch_autotune(phe_batch* b, int repeats, void* stream
 	const int blocks[] = {64, 128, 256};
 	const int orders[] = {PHE_BATCH_ORDER_GIVEN, PHE_BATCH_ORDER_LARGEST_FIRST};
 	const int occFrac[] = {4, 3, 2};  // quarters of the occupancy limit: 4/4, 3/4, 2/4
-	const int layouts[] = {PHE_LAYOUT_BINARY, PHE_LAYOUT_WIDE4};
+	const int layouts[] = {PHE_LAYOUT_BINARY, PHE_LAYOUT_WIDE4, PHE_LAYOUT_WIDE8};
 	const int stacks[] = {0, kBatchStackShared};
 	const int sorts[] = {0, 1024, 4096};
 	// Candidates are timed from a cold L2 (the condition of a batch that arrives after other work): a
@@ -578,7 +581,7 @@ done:
 // nothing waits for pageable memory and the call returns as soon as both kernels are queued.
 //
 // Limits and sharing rules:
-//   * at most kNoAllocMaxItems batches and kNoAllocMaxScenes scenes per call (11,520 bytes of scratch,
+//   * at most kNoAllocMaxItems batches and kNoAllocMaxScenes scenes per call (12,544 bytes of scratch,
 //     held by every GPU that loads the library until the process exits); larger calls fail with
 //     PHE_ERR_TOO_LARGE;
 //   * every call uses the same array and leaves its tables there; the counter is cleared at the start
@@ -595,14 +598,14 @@ namespace phe_gb300 {
 constexpr uint32_t kNoAllocMaxItems = 256;
 constexpr uint32_t kNoAllocMaxScenes = 32;
 constexpr size_t kNoAllocItemsBytes = kNoAllocMaxItems * sizeof(BatchItemDev);          // 8192
-constexpr size_t kNoAllocScenesBytes = kNoAllocMaxScenes * sizeof(DeviceScene);         // 3072
+constexpr size_t kNoAllocScenesBytes = kNoAllocMaxScenes * sizeof(DeviceScene);         // 4096
 constexpr size_t kNoAllocScratchBytes = kNoAllocItemsBytes + kNoAllocScenesBytes + 256; // + counter
 static_assert(sizeof(DeviceScene) % 16 == 0, "scene table entries stay 16-byte aligned");
-static_assert(kNoAllocScratchBytes == 11520, "the documented scratch size");
+static_assert(kNoAllocScratchBytes == 12544, "the documented scratch size");
 
 static __device__ __align__(256) unsigned char g_noallocScratch[kNoAllocScratchBytes];
 
-// Both tables as one kernel parameter (11,264 bytes, inside the 32,764-byte limit of kernel parameters).
+// Both tables as one kernel parameter (12,288 bytes, inside the 32,764-byte limit of kernel parameters).
 struct NoAllocTables {
 	BatchItemDev items[kNoAllocMaxItems];
 	DeviceScene scenes[kNoAllocMaxScenes];
@@ -696,7 +699,7 @@ extern "C" phe_status phe_batch_cast_noalloc(const phe_scene* const* scenes, uin
 	bool wide = false;
 	for (uint32_t i = 0; i < numScenes; i++) {
 		tab.scenes[i] = scenes[i]->dev;
-		wide = wide || scenes[i]->dev.nodes4 != nullptr;
+		wide = wide || scenes[i]->dev.nodes4 || scenes[i]->dev.nodes8;
 	}
 	cudaStream_t s = (cudaStream_t)stream;
 	noalloc_stage_kernel<<<1, kNoAllocStageBlock, 0, s>>>(tab, numItems, numScenes, scratch);

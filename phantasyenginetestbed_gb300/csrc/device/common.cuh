@@ -29,6 +29,8 @@ namespace phe_gb300 {
 //        of padding. Every child box is a box of the binary tree (a grandchild when the binary child
 //        is inner), and it is built only when each grandchild box lies inside its parent box, so the
 //        4-wide test of a grandchild passes only if the skipped binary test of its parent would pass.
+// nodes8 / leaves8 (optional): the 8-wide compressed layout, 80 B per node and 32 B per leaf record
+//        (format in host/wide8.hpp, traversal in traverse8.cuh).
 // Textures of a scene: texels of texture k start at texels + offset (rows rowBytes apart, tightly
 // packed); srgb[b] = powf(b / 255, 2.2) correctly rounded.
 struct DeviceTexture {
@@ -50,8 +52,11 @@ struct DeviceScene {
 	const uint8_t* texels;
 	const float* srgb;
 	uint32_t numTextures, pad;
+	const uint4* nodes8;    // set only while the 8-wide layout is selected (host/wide8.hpp)
+	const float4* leaves8;  // its leaf records
+	uint32_t numNodes8, numLeaves8, pad2[2];
 };
-static_assert(sizeof(DeviceScene) == 96, "DeviceScene is 96 bytes");
+static_assert(sizeof(DeviceScene) == 128, "DeviceScene is 128 bytes");
 
 constexpr int32_t kEmptyChild = 0x7FFFFFFE;
 

@@ -126,7 +126,7 @@ extern "C" phe_status phe_cast_closest_plain(const phe_scene* scene, const phe_r
 	if (((uintptr_t)hits & 15u) != 0) return fail(PHE_ERR_INVALID_ARGUMENT, "hit buffer must be 16-byte aligned");
 	if (n == 0) return PHE_OK;
 	uint32_t grid = (n + kPlainBlock - 1) / kPlainBlock;
-	auto kernel = scene->dev.nodes4 ? closest_plain_kernel<true> : closest_plain_kernel<false>;
+	auto kernel = (scene->dev.nodes4 || scene->dev.nodes8) ? closest_plain_kernel<true> : closest_plain_kernel<false>;
 	kernel<<<grid, kPlainBlock, stack_smem_bytes(kPlainBlock), (cudaStream_t)stream>>>(scene->dev, rays, hits, n,
 	                                                                                   scene->status);
 	PHE_CUDA_TRY(cudaGetLastError(), "closest_plain_kernel launch");
@@ -141,7 +141,7 @@ extern "C" phe_status phe_cast_closest(const phe_scene* scene, const phe_ray_in*
 	if (((uintptr_t)hits & 15u) != 0) return fail(PHE_ERR_INVALID_ARGUMENT, "hit buffer must be 16-byte aligned");
 	if (n == 0) return PHE_OK;
 	if (n > kMaxPersistentRays) return fail(PHE_ERR_TOO_LARGE, "phe_cast_closest: at most %u rays per launch", kMaxPersistentRays);
-	const bool wide = scene->dev.nodes4 != nullptr;
+	const bool wide = scene->dev.nodes4 || scene->dev.nodes8;
 	auto kernel = wide ? closest_persistent_kernel<true> : closest_persistent_kernel<false>;
 	int grid = 0;
 	if ((st = persistent_grid(wide ? 2 : 0, (const void*)kernel, &grid))) return st;
@@ -163,7 +163,7 @@ extern "C" phe_status phe_cast_any(const phe_scene* scene, const phe_ray_in* ray
 	if (st) return st;
 	if (n == 0) return PHE_OK;
 	if (n > kMaxPersistentRays) return fail(PHE_ERR_TOO_LARGE, "phe_cast_any: at most %u rays per launch", kMaxPersistentRays);
-	const bool wide = scene->dev.nodes4 != nullptr;
+	const bool wide = scene->dev.nodes4 || scene->dev.nodes8;
 	auto kernel = wide ? any_persistent_kernel<true> : any_persistent_kernel<false>;
 	int grid = 0;
 	if ((st = persistent_grid(wide ? 3 : 1, (const void*)kernel, &grid))) return st;

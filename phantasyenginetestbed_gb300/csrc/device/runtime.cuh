@@ -9,8 +9,11 @@
 #include "common.cuh"
 
 struct phe_scene {
-	phe_gb300::DeviceScene dev;         // dev.nodes4 is set only while the 4-wide layout is selected
+	phe_gb300::DeviceScene dev;         // dev.nodes4 / dev.nodes8 are set only while that layout is selected
 	const float4* nodes4 = nullptr;     // 4-wide nodes, when the tree allows them (else null)
+	const uint4* nodes8 = nullptr;      // 8-wide compressed nodes and their leaf records, when the tree
+	const float4* leaves8 = nullptr;    // allows them (else null)
+	uint32_t numNodes8 = 0, numLeaves8 = 0, maxDepth8 = 0;
 	void* allocation = nullptr;   // one cudaMalloc holding nodes, 4-wide nodes, tris, datas, status
 	void* shading = nullptr;      // one cudaMalloc holding materials, texture table, sRGB table, texels
 	uint64_t bytes = 0, shadingBytes = 0;

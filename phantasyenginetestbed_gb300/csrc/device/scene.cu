@@ -10,6 +10,7 @@
 #include <mutex>
 #include <vector>
 
+#include "../host/wide8.hpp"
 #include "runtime.cuh"
 
 namespace phe_gb300 {
@@ -344,13 +345,21 @@ extern "C" phe_status phe_scene_create(const phe_bvh_node* nodes, uint32_t numNo
 	uint32_t depth4 = 0;
 	bool wide = collapse4(dn, dn4, depth4);
 	if (!wide) dn4.clear();
+	Wide8Tree w8;
+	std::string why8;
+	if (!build_wide8(hn.data(), numNodes, w8, why8)) {
+		w8.nodes.clear();
+		w8.leaves.clear();
+	}
 
 	size_t nodeBytes = align256(dn.size() * sizeof(float4));
 	size_t node4Bytes = align256(dn4.size() * sizeof(float4));
+	size_t node8Bytes = align256(w8.nodes.size() * sizeof(uint32_t));
+	size_t leaf8Bytes = align256(w8.leaves.size() * sizeof(uint32_t));
 	size_t triBytes = align256(dt.size() * sizeof(float4));
 	size_t dataBytes = align256(hd.size() * sizeof(phe_triangle_data));
 	size_t statusBytes = 256;
-	size_t total = nodeBytes + node4Bytes + triBytes + dataBytes + statusBytes;
+	size_t total = nodeBytes + node4Bytes + node8Bytes + leaf8Bytes + triBytes + dataBytes + statusBytes;
 	char* base = nullptr;
 	cudaError_t e = cudaMalloc(&base, total);
 	if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(scene)");
@@ -358,6 +367,8 @@ extern "C" phe_status phe_scene_create(const phe_bvh_node* nodes, uint32_t numNo
 	char* p = base;
 	float4* dNodes = (float4*)p; p += nodeBytes;
 	float4* dNodes4 = dn4.empty() ? nullptr : (float4*)p; p += node4Bytes;
+	uint4* dNodes8 = w8.nodes.empty() ? nullptr : (uint4*)p; p += node8Bytes;
+	float4* dLeaves8 = w8.leaves.empty() ? nullptr : (float4*)p; p += leaf8Bytes;
 	float4* dTris = (float4*)p; p += triBytes;
 	phe_triangle_data* dDatas = hd.empty() ? nullptr : (phe_triangle_data*)p; p += dataBytes;
 	uint32_t* dStatus = (uint32_t*)p;
@@ -365,6 +376,10 @@ extern "C" phe_status phe_scene_create(const phe_bvh_node* nodes, uint32_t numNo
 		return cleanup(cuda_fail(e, "upload nodes"));
 	if (dNodes4 && (e = cudaMemcpy(dNodes4, dn4.data(), dn4.size() * sizeof(float4), cudaMemcpyHostToDevice)) != cudaSuccess)
 		return cleanup(cuda_fail(e, "upload 4-wide nodes"));
+	if (dNodes8 && (e = cudaMemcpy(dNodes8, w8.nodes.data(), w8.nodes.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess)
+		return cleanup(cuda_fail(e, "upload 8-wide nodes"));
+	if (dLeaves8 && (e = cudaMemcpy(dLeaves8, w8.leaves.data(), w8.leaves.size() * 4, cudaMemcpyHostToDevice)) != cudaSuccess)
+		return cleanup(cuda_fail(e, "upload 8-wide leaf records"));
 	if ((e = cudaMemcpy(dTris, dt.data(), dt.size() * sizeof(float4), cudaMemcpyHostToDevice)) != cudaSuccess)
 		return cleanup(cuda_fail(e, "upload triangles"));
 	if (dDatas && (e = cudaMemcpy(dDatas, hd.data(), hd.size() * sizeof(phe_triangle_data), cudaMemcpyHostToDevice)) != cudaSuccess)
@@ -385,8 +400,17 @@ extern "C" phe_status phe_scene_create(const phe_bvh_node* nodes, uint32_t numNo
 	sc->dev.srgb = nullptr;
 	sc->dev.numTextures = 0;
 	sc->maxMaterialIndex = maxMaterialIndex;
-	sc->dev.nodes4 = nullptr;   // binary layout unless phe_scene_set_layout selects the 4-wide one
+	sc->dev.nodes4 = nullptr;   // binary layout unless phe_scene_set_layout selects a wide one
+	sc->dev.nodes8 = nullptr;
+	sc->dev.leaves8 = nullptr;
 	sc->nodes4 = dNodes4;
+	sc->nodes8 = dNodes8;
+	sc->leaves8 = dLeaves8;
+	sc->numNodes8 = (uint32_t)(w8.nodes.size() / kWide8NodeWords);
+	sc->numLeaves8 = (uint32_t)(w8.leaves.size() / kWide8LeafWords);
+	sc->maxDepth8 = w8.depth;
+	sc->dev.numNodes8 = sc->numNodes8;
+	sc->dev.numLeaves8 = sc->numLeaves8;
 	sc->dev.numNodes4 = (uint32_t)(dn4.size() / 8);
 	sc->maxDepth4 = depth4;
 	sc->allocation = base;
@@ -444,23 +468,34 @@ extern "C" phe_status phe_scene_status(const phe_scene* scene, uint32_t* bits)
 extern "C" phe_status phe_scene_set_layout(phe_scene* scene, int layout)
 {
 	if (!scene) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_scene_set_layout: null scene");
-	if (layout == PHE_LAYOUT_BINARY) {
-		if (scene->dev.nodes4) scene->generation++;
-		scene->dev.nodes4 = nullptr;
-		return PHE_OK;
+	const float4* n4 = nullptr;
+	const uint4* n8 = nullptr;
+	const float4* l8 = nullptr;
+	if (layout == PHE_LAYOUT_WIDE4) {
+		if (!scene->nodes4)
+			return fail(PHE_ERR_INVALID_SCENE, "phe_scene_set_layout: this tree has child boxes outside their parent box");
+		n4 = scene->nodes4;
+	} else if (layout == PHE_LAYOUT_WIDE8) {
+		if (!scene->nodes8)
+			return fail(PHE_ERR_INVALID_SCENE, "phe_scene_set_layout: this tree allows no 8-wide layout (a child box "
+			                                   "outside its parent box, inverted or not finite)");
+		n8 = scene->nodes8;
+		l8 = scene->leaves8;
+	} else if (layout != PHE_LAYOUT_BINARY) {
+		return fail(PHE_ERR_INVALID_ARGUMENT, "phe_scene_set_layout: unknown layout %d", layout);
 	}
-	if (layout != PHE_LAYOUT_WIDE4) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_scene_set_layout: unknown layout %d", layout);
-	if (!scene->nodes4)
-		return fail(PHE_ERR_INVALID_SCENE, "phe_scene_set_layout: this tree has child boxes outside their parent box");
-	if (scene->dev.nodes4 != scene->nodes4) scene->generation++;
-	scene->dev.nodes4 = scene->nodes4;
+	if (scene->dev.nodes4 != n4 || scene->dev.nodes8 != n8) scene->generation++;
+	scene->dev.nodes4 = n4;
+	scene->dev.nodes8 = n8;
+	scene->dev.leaves8 = l8;
 	return PHE_OK;
 }
 
 extern "C" phe_status phe_scene_get_layout(const phe_scene* scene, int* layout, int* wideAvailable)
 {
 	if (!scene) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_scene_get_layout: null scene");
-	if (layout) *layout = scene->dev.nodes4 ? PHE_LAYOUT_WIDE4 : PHE_LAYOUT_BINARY;
-	if (wideAvailable) *wideAvailable = scene->nodes4 ? 1 : 0;
+	if (layout)
+		*layout = scene->dev.nodes8 ? PHE_LAYOUT_WIDE8 : scene->dev.nodes4 ? PHE_LAYOUT_WIDE4 : PHE_LAYOUT_BINARY;
+	if (wideAvailable) *wideAvailable = (scene->nodes4 ? 1 : 0) | (scene->nodes8 ? 2 : 0);
 	return PHE_OK;
 }

@@ -246,7 +246,7 @@ void upload_scene_table(phe_server* s)
 	s->wideScenes = false;
 	for (const phe_scene* sc : s->scenes) {
 		t.push_back(sc->dev);
-		s->wideScenes = s->wideScenes || sc->dev.nodes4 != nullptr;
+		s->wideScenes = s->wideScenes || sc->dev.nodes4 || sc->dev.nodes8;
 	}
 	if (!t.empty()) cudaMemcpy(s->dScenes, t.data(), t.size() * sizeof(DeviceScene), cudaMemcpyHostToDevice);
 	s->sceneTableDirty = false;

@@ -314,14 +314,23 @@ __device__ __forceinline__ uint32_t traverse4(const float4* __restrict__ nodes4,
 	return err;
 }
 
-// WIDE = false compiles the binary traversal only; kernels are instantiated for both layouts and
-// the host launches the WIDE one only for scenes whose 4-wide layout is selected, so binary
-// launches carry neither the 4-wide code nor its larger stack.
+} // namespace phe_gb300
+
+#include "traverse8.cuh"
+
+namespace phe_gb300 {
+
+// WIDE = false compiles the binary traversal only; kernels are instantiated for both and the host
+// launches the WIDE one only for scenes whose 4-wide or 8-wide layout is selected, so binary launches
+// carry neither the wide code nor its stacks. Rays with a non-finite 1/dir always take the binary
+// nodes (the wide tests assume finite slab distances).
 template <bool ANY, bool WIDE = false, int SN = kSmemStack>
 __device__ __forceinline__ uint32_t trace(const DeviceScene& s, const RayState& r, HitRecord& hit)
 {
 	if (r.safe) {
 		if constexpr (WIDE) {
+			if (s.nodes8)
+				return traverse8<ANY>(s.nodes8, s.leaves8, s.tris, Wide8Bounds{s.numNodes8, s.numLeaves8, s.numSlots}, r, hit);
 			if (s.nodes4) return traverse4<ANY>(s.nodes4, s.tris, TraversalBounds{s.numNodes4, s.numSlots}, r, hit);
 		}
 		return traverse<true, ANY, SN>(s.nodes, s.tris, TraversalBounds{s.numNodes, s.numSlots}, r, hit);

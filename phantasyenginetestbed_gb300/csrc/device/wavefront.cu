@@ -686,7 +686,7 @@ phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, c
 	int binGrid = dinfo->numSMs * 4;
 	mark();
 	if (fused) {
-		const bool wide = scene->dev.nodes4 != nullptr;
+		const bool wide = scene->dev.nodes4 || scene->dev.nodes8;
 		auto primary = wide ? primary_kernel<true> : primary_kernel<false>;
 		auto anyQueue = wide ? any_queue_kernel<true> : any_queue_kernel<false>;
 		auto bounce = wide ? bounce_kernel<true> : bounce_kernel<false>;

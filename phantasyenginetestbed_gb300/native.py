@@ -34,6 +34,7 @@ PTR_HOST = 0
 PTR_DEVICE = 1
 LAYOUT_BINARY = 0
 LAYOUT_WIDE4 = 1
+LAYOUT_WIDE8 = 2
 
 # numpy views of the reference layouts
 NODE_DTYPE = np.dtype([("fData", "<f4", (12,)), ("iData", "<i4", (4,))])            # phe::BVHNode, 64 B
@@ -138,6 +139,8 @@ SIGNATURES: dict[str, tuple] = {
     "phe_host_bvh_copy": (_I32, [_VP, _VP, _VP, _VP]),
     "phe_host_bvh_free": (None, [_VP]),
     "phe_bvh_validate": (_I32, [_VP, _U32, _U32, C.POINTER(_U32)]),
+    "phe_bvh_wide8_build": (_I32, [_VP, _U32, _U32, _VP, _U32, _VP, _U32, C.POINTER(_U32), C.POINTER(_U32),
+                                   C.POINTER(_U32)]),
     "phe_bvh_cache_write": (_I32, [C.c_char_p, _VP, _U32, _VP, _VP, _U32]),
     "phe_bvh_cache_sizes": (_I32, [C.c_char_p, C.POINTER(_U32), C.POINTER(_U32)]),
     "phe_bvh_cache_read": (_I32, [C.c_char_p, _VP, _U32, _VP, _VP, _U32]),

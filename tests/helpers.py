@@ -51,6 +51,25 @@ def golden_scene(name: str):
     return s, nodes, verts, s2t
 
 
+class RefTree:
+    """A BVH built by the reference's own builder (buildStaticFrom + sanitizeBVH, compiled from the
+    reference sources into oracle/_ref/libpheref.so), with the slot -> input-triangle map."""
+
+    def __init__(self, nodes, verts, slot_to_tri):
+        self.nodes, self.verts, self.slot_to_tri = nodes, verts, slot_to_tri
+
+    def slot_datas(self, datas: np.ndarray) -> np.ndarray:
+        return np.ascontiguousarray(datas[self.slot_to_tri])
+
+
+@lru_cache(maxsize=None)
+def ref_built_scene(name: str):
+    """(scene arrays, RefTree) of a standard scene, built by the reference builder."""
+    s = P.standard_scene(name)
+    nodes, verts, s2t = O.ref_build_sbvh(s.tri_verts)
+    return s, RefTree(nodes, verts, s2t)
+
+
 @lru_cache(maxsize=None)
 def built_scene(name: str):
     """(scene arrays, HostBVH from the project's builder) of a standard scene."""

@@ -233,13 +233,15 @@ def test_small_scenes_every_ray_vs_brute_force(T):
     assert np.array_equal(_gpu_any(scene, rays), O.any_rays(b.nodes, b.verts, rays))
 
 
-def test_wide_layout_gives_the_binary_results():
-    """The 4-wide node layout visits the leaves the binary layout visits: closest hits (same slots
-    except documented near-ties) and any hits identical, on coherent, incoherent and axis-aligned rays."""
+@pytest.mark.parametrize("layout", [1, 2], ids=["wide4", "wide8"])
+def test_wide_layout_gives_the_binary_results(layout):
+    """The 4-wide and the 8-wide compressed node layouts reach the leaves the binary layout reaches:
+    closest hits (same slots except documented near-ties) and any hits identical, on coherent,
+    incoherent and axis-aligned rays."""
     s, b = built_scene("c2_256_2000")
     scene = P.Scene(b.nodes, b.verts)
     lay, avail = scene.layout()
-    assert lay == 0 and avail
+    assert lay == 0 and avail == 3
     k = s.scale
     cam = O.camera_def((0.5 * k, -0.3 * k, 0.6 * k), C1_CAM["dir"], C1_CAM["up"], math.radians(60), (640, 360))
     rays = np.concatenate([O.gen_primary(cam, (640, 360)), random_rays(100000, [0, 0, 0.02], [k, k, 0.3 * k], 9)])
@@ -247,8 +249,8 @@ def test_wide_layout_gives_the_binary_results():
     rays["dir"][::7] = axes[np.arange(len(rays[::7])) % 3]
     binary = _gpu_closest(scene, rays)
     binary_any = _gpu_any(scene, rays)
-    scene.set_layout(1)
-    assert scene.layout() == (1, True)
+    scene.set_layout(layout)
+    assert scene.layout() == (layout, 3)
     for kind in ("persistent", "plain"):
         wide = _gpu_closest(scene, rays, kind)
         _check(O.compare_closest(wide, binary, rays, b.slot_to_tri, b.verts), len(rays))
@@ -260,7 +262,7 @@ def test_wide_layout_gives_the_binary_results():
 def test_inverted_child_box_keeps_the_binary_layout():
     """A child box stored with lo > hi on one axis is valid input (the reference's min/max slab test
     treats it as the swapped interval) but breaks the box nesting the 4-wide collapse relies on: the
-    scene offers the binary layout only, refuses the 4-wide one, and its casts match the oracle."""
+    scene offers the binary layout only, refuses the wide ones, and its casts match the oracle."""
     s, b = built_scene("c1_64_100")
     nodes = b.nodes.copy()
     root = nodes[0]
@@ -271,9 +273,10 @@ def test_inverted_child_box_keeps_the_binary_layout():
     box[0], box[3] = box[3], box[0]          # first child box of that node: swap lo.x and hi.x
     assert box[0] > box[3]
     scene = P.Scene(nodes, b.verts)
-    assert scene.layout() == (0, False)
-    with pytest.raises(P.PheError):
-        scene.set_layout(1)
+    assert scene.layout() == (0, 0)
+    for layout in (1, 2):
+        with pytest.raises(P.PheError):
+            scene.set_layout(layout)
     k = s.scale
     cam = O.camera_def((0.5 * k, -0.3 * k, 0.6 * k), C1_CAM["dir"], C1_CAM["up"], math.radians(60), (256, 256))
     rays = np.concatenate([O.gen_primary(cam, (256, 256)), random_rays(20000, [0, 0, 0.02], [k, k, 0.3 * k], 4)])

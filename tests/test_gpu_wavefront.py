@@ -96,11 +96,12 @@ def test_shadow_schedules_give_the_same_frame(graph):
 
 @pytest.mark.parametrize("graph", [False, True])
 def test_wide_layout_frame_gives_the_binary_frame(graph):
-    """Switching the scene to 4-wide nodes between frames (graph re-captured) renders the same frame."""
+    """Switching the scene to 4-wide or 8-wide nodes between frames (graph re-captured) renders the same
+    frame."""
     res = (256, 160)
     s, b, datas, scene, cam, cam_pos, lights, r = _setup("c2_256_2000", res, [(0.5, 0.5, 2.0)], graph)
     out = []
-    for layout in (0, 1, 0):
+    for layout in (0, 1, 0, 2, 0):
         scene.set_layout(layout)
         r.set_seed(5, 0)
         r.resetTAA()
@@ -109,7 +110,7 @@ def test_wide_layout_frame_gives_the_binary_frame(graph):
             r.render(lights)
         out.append((r.read(READ_RAW), r.ray_counts()))
     for raw, counts in out[1:]:
-        _compare(raw, out[0][0], "4-wide vs binary frame")     # same hits up to documented near-ties
+        _compare(raw, out[0][0], "wide vs binary frame")     # same hits up to documented near-ties
         assert np.abs(counts.astype(np.int64) - out[0][1].astype(np.int64)).max() <= 2
 
 

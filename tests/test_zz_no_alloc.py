@@ -5,7 +5,7 @@ their accounting and can wait for the whole device). Its scratch lives in a fixe
 library instead.
 
 Checked through the C ABI on two calls in a row against the allocating entry point (phe_batch_create +
-phe_batch_launch) and against the oracle, with a 4-wide scene in the table, empty batches, exactly the
+phe_batch_launch) and against the oracle, with a 4-wide or 8-wide scene in the table, empty batches, exactly the
 largest accepted item count, and the size refusals. The file name sorts last so that pytest collects it
 after every other test: a run that stops at the first failure has run all the others before it."""
 import ctypes as C
@@ -25,14 +25,14 @@ MAX_ITEMS = 256
 MAX_SCENES = 32
 
 
-def _scenes(wide_second=False):
+def _scenes(wide_second=0):
     out = []
     for args in [(16, 10, False, 61), (48, 40, True, 62)]:
         s = P.generate_scene(*args)
         b = P.build_sbvh(s.tri_verts)
         out.append((s, b, P.Scene(b.nodes, b.verts)))
     if wide_second:
-        out[1][2].set_layout(N.LAYOUT_WIDE4)
+        out[1][2].set_layout(wide_second)
     return out
 
 
@@ -74,7 +74,7 @@ def _check_against_oracle(scenes, items, host, got, call):
             assert np.array_equal(g[:n], O.any_rays(b.nodes, b.verts, rays)), call
 
 
-@pytest.mark.parametrize("wide", [False, True], ids=["binary", "wide4_scene"])
+@pytest.mark.parametrize("wide", [0, N.LAYOUT_WIDE4, N.LAYOUT_WIDE8], ids=["binary", "wide4_scene", "wide8_scene"])
 def test_noalloc_matches_allocating_launch_and_oracle_on_two_calls(wide):
     import torch
     scenes = _scenes(wide_second=wide)
