@@ -82,6 +82,7 @@ def parse():
                          "lights (16M diffuse + 16M shadow rays per launch); serve: Poisson request arrivals through the serving loop; sizes: launch time "
                          "against rays per launch (16K..16M) for each ray-cast entry point")
     ap.add_argument("--res", type=int, default=4096, help="large: width and height of the primary pass")
+    ap.add_argument("--rays", type=int, default=16 << 20, help="large: rays per diffuse / shadow launch")
     ap.add_argument("--rates", default="200,500,1000", help="serve: arrival rates (requests/s)")
     ap.add_argument("--duration", type=float, default=2.0, help="serve: seconds of arrivals per rate")
     ap.add_argument("--render-slots", type=int, default=8, help="serve: concurrent render requests")
@@ -793,7 +794,7 @@ def run_large(args):
     torch.cuda.set_device(0)
     stream = torch.cuda.current_stream()
     res = (args.res, args.res)
-    N = 16 << 20
+    N = args.rays
     s, b, build_s = _scene_with_bvh("c4_2048_20000")
     scene = P.Scene(b.nodes, b.verts)
     k = s.scale

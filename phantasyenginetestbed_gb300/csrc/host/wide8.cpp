@@ -117,17 +117,16 @@ bool build_wide8(const phe_bvh_node* nodes, uint32_t numNodes, Wide8Tree& out, s
 			}
 		}
 	}
-	struct Job { uint32_t binary, wide, depth; };
-	std::deque<Job> jobs{{0, 0, 1}};
-	out.nodes.assign(kWide8NodeWords, 0u);
-	while (!jobs.empty()) {
-		Job job = jobs.front();
-		jobs.pop_front();
-		out.depth = std::max(out.depth, job.depth);
+	// 1. Collapse: each wide node starts from a binary node's two children and repeatedly replaces the
+	//    inner child with the largest surface area by its two children, up to 8 children.
+	struct WNode { std::vector<Kid> kids; std::vector<int32_t> sub; };
+	std::vector<WNode> wn(1);
+	std::vector<uint32_t> src{0};   // binary node of each wide node
+	for (size_t w = 0; w < wn.size(); w++) {
 		Kid kids[8];
 		int n = 0;
-		kids[n++] = kid_of(nodes[job.binary], 0);
-		kids[n++] = kid_of(nodes[job.binary], 1);
+		kids[n++] = kid_of(nodes[src[w]], 0);
+		kids[n++] = kid_of(nodes[src[w]], 1);
 		while (n < 8) {
 			int best = -1;
 			float bestArea = -1.0f;
@@ -141,6 +140,28 @@ bool build_wide8(const phe_bvh_node* nodes, uint32_t numNodes, Wide8Tree& out, s
 			kids[best] = kid_of(x, 0);
 			kids[n++] = kid_of(x, 1);
 		}
+		for (int i = 0; i < n; i++) {
+			wn[w].kids.push_back(kids[i]);
+			int32_t sub = -1;
+			if (!kids[i].count) {
+				sub = (int32_t)wn.size();
+				wn.emplace_back();
+				src.push_back((uint32_t)kids[i].node);
+			}
+			wn[w].sub.push_back(sub);
+		}
+	}
+	// 2. Emit breadth-first, so that each node's inner children are contiguous.
+	struct Job { int32_t w; uint32_t index, depth; };
+	std::deque<Job> jobs{{0, 0, 1}};
+	out.nodes.assign(kWide8NodeWords, 0u);
+	while (!jobs.empty()) {
+		Job job = jobs.front();
+		jobs.pop_front();
+		out.depth = std::max(out.depth, job.depth);
+		const WNode& W = wn[job.w];
+		const int n = (int)W.kids.size();
+		const Kid* kids = W.kids.data();
 		// Slots: child c in slot s comes first for rays of octant s; greedy assignment by the projection
 		// of the child's centre (relative to the node's) on the octant's diagonal.
 		float cen[3] = {0, 0, 0};
@@ -181,7 +202,7 @@ bool build_wide8(const phe_bvh_node* nodes, uint32_t numNodes, Wide8Tree& out, s
 			used[bc] = true;
 			slotKid[bs] = bc;
 		}
-		uint32_t* w = &out.nodes[(size_t)job.wide * kWide8NodeWords];
+		uint32_t* w = &out.nodes[(size_t)job.index * kWide8NodeWords];
 		uint32_t imask = 0, valid = 0;
 		for (int s = 0; s < 8; s++) {
 			if (slotKid[s] < 0) continue;
@@ -235,7 +256,7 @@ bool build_wide8(const phe_bvh_node* nodes, uint32_t numNodes, Wide8Tree& out, s
 		w[6] = valid;
 		w[7] = 0;
 		uint32_t nInner = (uint32_t)__builtin_popcount(imask);
-		out.nodes.resize(out.nodes.size() + (size_t)nInner * kWide8NodeWords, 0u);
+		out.nodes.resize(out.nodes.size() + (size_t)nInner * kWide8NodeWords, 0u);   // w is not used past here
 		uint32_t innerRank = 0;
 		for (int s = 0; s < 8; s++) {
 			if (slotKid[s] < 0) continue;
@@ -245,7 +266,7 @@ bool build_wide8(const phe_bvh_node* nodes, uint32_t numNodes, Wide8Tree& out, s
 				                                 f2u(kd.hi[0]), f2u(kd.hi[1]), f2u(kd.hi[2]), kd.count};
 				out.leaves.insert(out.leaves.end(), rec, rec + kWide8LeafWords);
 			} else {
-				jobs.push_back({(uint32_t)kd.node, childBase + innerRank++, job.depth + 1});
+				jobs.push_back({W.sub[slotKid[s]], childBase + innerRank++, job.depth + 1});
 			}
 		}
 	}
