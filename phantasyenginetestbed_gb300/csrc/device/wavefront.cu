@@ -18,6 +18,7 @@
 // Queue counts stay on the device; persistent kernels read them when they start, so a frame needs
 // no host synchronisation and can be captured in a CUDA graph.
 
+#include <algorithm>
 #include <atomic>
 #include <cstring>
 #include <vector>
@@ -690,9 +691,15 @@ phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, c
 		auto primary = wide ? primary_kernel<true> : primary_kernel<false>;
 		auto anyQueue = wide ? any_queue_kernel<true> : any_queue_kernel<false>;
 		auto bounce = wide ? bounce_kernel<true> : bounce_kernel<false>;
-		const int gPrimary = g[wide ? kGridPrimaryWide : kGridPrimary];
-		const int gAny = g[wide ? kGridAnyQueueWide : kGridAnyQueue];
-		const int gBounce = g[wide ? kGridBounceWide : kGridBounce];
+		// Persistent grids, but never more blocks than the frame's rays can keep busy: a small frame (a
+		// 256x256 render of the serving loop) then leaves the other SMs to concurrent requests.
+		const uint64_t P = (uint64_t)resX * resY;
+		auto clamp = [](int grid, uint64_t rays) {
+			return (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)grid, (rays + kWaveBlock - 1) / kWaveBlock));
+		};
+		const int gPrimary = clamp(g[wide ? kGridPrimaryWide : kGridPrimary], P);
+		const int gAny = clamp(g[wide ? kGridAnyQueueWide : kGridAnyQueue], 2 * (uint64_t)fb.capacityLP);
+		const int gBounce = clamp(g[wide ? kGridBounceWide : kGridBounce], P);
 		const phe_ray_in* rays1 = fb.shadowRays + fb.capacityLP;
 		const uint32_t* slots1 = fb.shadowSlots + fb.capacityLP;
 		primary<<<gPrimary, kWaveBlock, kStackSmem, stream>>>(scene->dev, dParams, fb, scene->status);
