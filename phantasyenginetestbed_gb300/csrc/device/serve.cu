@@ -3,8 +3,9 @@
 //
 // A scheduler thread owns the GPU work:
 //   * admission — a request is admitted when it fits the device-memory budget (resident scenes
-//     count against it), the in-flight limit, and, for renders, a free render slot. Its device state
-//     (rays and results; a render slot's frame buffers) stays on the GPU until it completes.
+//     count against it), the in-flight limit, and, for renders, a free render slot (queries behind a
+//     render that waits for a slot are admitted past it). Its device state (rays and results; a render
+//     slot's frame buffers) stays on the GPU until it completes.
 //   * ray queries — every admitted query whose rays are on the device joins the next WAVE: one
 //     batched persistent launch over all of them (any scenes, closest and any hit mixed). Requests that
 //     arrive while a wave runs are admitted and go into the following wave (up to two waves queued).
@@ -163,6 +164,11 @@ phe_status admit_query(phe_server* s, Request* r)
 	return PHE_OK;
 }
 
+// Host callback queued after a wave's or a render's completion event: wakes the scheduler so that it
+// retires the requests at once instead of at its next timed poll. It only notifies (no CUDA call, no
+// lock); phe_server_destroy synchronises the device before the server is freed.
+void CUDART_CB wake_scheduler(void* server) { static_cast<phe_server*>(server)->cvWork.notify_all(); }
+
 // Launches one wave over every admitted query (called with the lock held).
 phe_status launch_wave(phe_server* s, Wave& w)
 {
@@ -202,6 +208,7 @@ phe_status launch_wave(phe_server* s, Wave& w)
 		s->inflight.push_back(r);
 	}
 	PHE_CUDA_TRY(cudaEventRecord(w.done, st), "record wave event");
+	PHE_CUDA_TRY(cudaLaunchHostFunc(st, wake_scheduler, s), "queue wave completion callback");
 	w.busy = true;
 	s->admitted.erase(s->admitted.begin(), s->admitted.begin() + n);
 	s->wavesLaunched++;
@@ -233,6 +240,7 @@ phe_status issue_render(phe_server* s, Request* r, RenderSlot& slot)
 	if ((ps = phe_renderer_ray_totals_async(R, slot.totals, st))) return ps;
 	r->done = take_event(s);
 	PHE_CUDA_TRY(cudaEventRecord(r->done, st), "record request event");
+	if (!s->cfg.serial) PHE_CUDA_TRY(cudaLaunchHostFunc(st, wake_scheduler, s), "queue render completion callback");
 	r->slot = (int)(&slot - s->slots.data());
 	slot.busy = r;
 	r->state = kIssued;
@@ -336,18 +344,26 @@ void worker_loop(phe_server* s)
 				if (w.busy && cudaEventQuery(w.done) != cudaErrorNotReady) w.busy = false;
 			if (progress) s->cvDone.notify_all();
 
-			// 2. admission, in arrival order
-			while (!s->pending.empty()) {
-				Request* r = s->pending.front();
+			// 2. admission, in arrival order. A render waiting for a free slot does not hold back the
+			//    queries behind it (renders keep their order among themselves); a request that does not
+			//    fit the memory budget or the in-flight limit stops admission.
+			bool renderWaits = false;
+			for (size_t pi = 0; pi < s->pending.size();) {
+				Request* r = s->pending[pi];
 				if (s->inflight.size() + s->admitted.size() >= s->cfg.maxInFlight) break;
 				if (s->sceneBytes + s->bytesInUse + r->bytes > s->cfg.memoryBudget) break;
 				RenderSlot* freeSlot = nullptr;
 				if (r->desc.kind == PHE_REQ_RENDER) {
-					for (RenderSlot& sl : s->slots)
-						if (!sl.busy) { freeSlot = &sl; break; }
-					if (!freeSlot) break;
+					if (!renderWaits)
+						for (RenderSlot& sl : s->slots)
+							if (!sl.busy) { freeSlot = &sl; break; }
+					if (!freeSlot) {
+						renderWaits = true;
+						pi++;
+						continue;
+					}
 				}
-				s->pending.pop_front();
+				s->pending.erase(s->pending.begin() + pi);
 				s->bytesInUse += r->bytes;
 				r->tAdmit = now_ms(s->t0);
 				r->state = kAdmitted;
@@ -386,7 +402,7 @@ void worker_loop(phe_server* s)
 			if (s->inflight.empty() && s->pending.empty() && s->admitted.empty())
 				s->cvWork.wait(lock, [&] { return s->stop || !s->pending.empty(); });
 			else
-				s->cvWork.wait_for(lock, std::chrono::microseconds(50));
+				s->cvWork.wait_for(lock, std::chrono::microseconds(20));
 		}
 	}
 }

@@ -285,3 +285,45 @@ def test_drain_returns_after_every_request(scenes, serial):
             assert st is not None and st.status == 0, (rep, rid)
             server.release(rid)
     server.close()
+
+
+def test_queries_pass_a_render_that_waits_for_a_slot(scenes):
+    """With one render slot busy, a second render waits for it; ray queries submitted behind that render
+    are admitted past it instead of waiting too, and the second render is admitted only once the first
+    one has completed. The queries' results equal the oracle."""
+    server = Server(render_slots=1)
+    ids = [server.add_scene(x[2]) for x in scenes]
+    s, b, _ = scenes[0]
+    k = s.scale
+    res = (1024, 1024)
+    cam_pos = (0.5 * k, -0.3 * k, 0.6 * k)
+    cam = cam_struct(O.camera_def(cam_pos, C1_CAM["dir"], C1_CAM["up"], math.radians(60), res))
+    lights = make_lights(np.array([[0.5, 0.5, 2.0]], np.float32) * np.float32(k), range_=1000.0 * k)
+    frames = [pinned((res[1], res[0], 4), np.float32) for _ in range(2)]
+    queries = []
+    for i in range(4):
+        rays = pinned(5000, P.RAY_IN_DTYPE)
+        rays[:] = random_rays(5000, [0, 0, 0.02], [k, k, 0.4 * k], 900 + i)
+        queries.append((rays, pinned(5000 * 16, np.uint8)))
+    r1 = server.submit_render(ids[0], res, 8, cam, cam_pos, lights, 5, frames[0])
+    r2 = server.submit_render(ids[0], res, 8, cam, cam_pos, lights, 6, frames[1])
+    qids = [server.submit_rays(ids[0], rays, out, REQ_CLOSEST) for rays, out in queries]
+    server.drain()
+    first, second = server.poll(r1), server.poll(r2)
+    assert first.status == 0 and second.status == 0
+    assert second.admitMs >= first.doneMs - 1e-3   # the one slot was busy until the first render completed
+    behind = 0
+    for qid, (rays, out) in zip(qids, queries):
+        st = server.poll(qid)
+        assert st is not None and st.status == 0
+        if st.submitMs < first.doneMs:
+            behind += 1
+            assert st.admitMs < second.admitMs, (st.submitMs, st.admitMs, first.doneMs, second.admitMs)
+        rep = O.compare_closest(out.view(P.RAY_HIT_DTYPE), O.cast_rays(b.nodes, b.verts, rays), rays,
+                                b.slot_to_tri, b.verts)
+        assert rep["ok"], rep
+        server.release(qid)
+    assert behind > 0
+    server.release(r1)
+    server.release(r2)
+    server.close()
