@@ -6,7 +6,7 @@ Host API over the C ABI of libphe_gb300.so (include/phe_gb300.h):
 * scene tools (host): :func:`generate_scene`, :func:`build_sbvh`, :func:`camera_def`, :func:`halton_jitter`
 * device scenes: :class:`Scene` (``setStaticScene``, CudaTracerRenderer.cpp:251-315)
 * ray casting: :func:`cast_closest`, :func:`cast_closest_plain`, :func:`cast_any`, :func:`gen_primary_rays`
-* the reference's own launch functions: :mod:`phantasyenginetestbed_gb300.kernels`
+* the reference's renderer: :class:`phantasyenginetestbed_gb300.renderer.CudaTracerRenderer`
 
 Device buffers are torch CUDA tensors (or raw device addresses); torch supplies memory and streams
 only, every computation runs in the library's CUDA kernels.

@@ -4,7 +4,8 @@
 // A scheduler thread owns the GPU work:
 //   * admission — a request is admitted when it fits the device-memory budget (resident scenes
 //     count against it), the in-flight limit, and, for renders, a free render slot (queries behind a
-//     render that waits for a slot are admitted past it). Its device state (rays and results; a render
+//     render that waits for a slot are admitted past it; a render on a scene a slot is rendering may
+//     go before a bounded number of earlier renders). Its device state (rays and results; a render
 //     slot's frame buffers) stays on the GPU until it completes.
 //   * ray queries — every admitted query whose rays are on the device joins the next WAVE: one
 //     batched persistent launch over all of them (any scenes, closest and any hit mixed). Requests that
@@ -36,6 +37,8 @@ namespace {
 
 constexpr uint32_t kWaveRing = 2;          // waves in flight at once
 constexpr uint32_t kMaxWaveItems = 1024;   // queries per wave
+constexpr size_t kAffinityLookAhead = 16;  // pending entries searched for a render on a scene in use
+constexpr uint32_t kMaxPassed = 8;         // a render is passed over at most this many times
 
 double now_ms(std::chrono::steady_clock::time_point t0)
 {
@@ -57,6 +60,7 @@ struct Request {
 	void* dMem = nullptr;           // query: rays then results
 	cudaEvent_t done = nullptr;
 	int slot = -1;                  // render slot
+	uint32_t passed = 0;            // times a later render on a busier scene was admitted before it
 	uint64_t rays = 0;
 	std::string error;              // message of a failed request (set on the scheduler thread)
 };
@@ -248,6 +252,32 @@ phe_status issue_render(phe_server* s, Request* r, RenderSlot& slot)
 	return PHE_OK;
 }
 
+// Scene affinity of render admission: the render at pending[pi] is next in order and a slot is free.
+// If no slot is rendering its scene, a later render (within kAffinityLookAhead entries) on a scene that
+// a slot is rendering goes first instead, its tree being warm in L2; every render passed over counts
+// it, and one passed kMaxPassed times is taken in order. Returns the index of the render to admit.
+size_t pick_render(phe_server* s, size_t pi)
+{
+	auto inUse = [&](uint32_t scene) {
+		for (const RenderSlot& sl : s->slots)
+			if (sl.busy && sl.busy->desc.scene == scene) return true;
+		return false;
+	};
+	const Request* r = s->pending[pi];
+	if (r->passed >= kMaxPassed || inUse(r->desc.scene)) return pi;
+	const size_t end = std::min(s->pending.size(), pi + 1 + kAffinityLookAhead);
+	for (size_t j = pi + 1; j < end; j++) {
+		const Request* q = s->pending[j];
+		if (q->desc.kind == PHE_REQ_RENDER && inUse(q->desc.scene) &&
+		    s->sceneBytes + s->bytesInUse + q->bytes <= s->cfg.memoryBudget) {
+			for (size_t k = pi; k < j; k++)
+				if (s->pending[k]->desc.kind == PHE_REQ_RENDER) s->pending[k]->passed++;
+			return j;
+		}
+	}
+	return pi;
+}
+
 void upload_scene_table(phe_server* s)
 {
 	std::vector<DeviceScene> t;
@@ -345,14 +375,16 @@ void worker_loop(phe_server* s)
 			if (progress) s->cvDone.notify_all();
 
 			// 2. admission, in arrival order. A render waiting for a free slot does not hold back the
-			//    queries behind it (renders keep their order among themselves); a request that does not
-			//    fit the memory budget or the in-flight limit stops admission.
+			//    queries behind it; renders are taken in order except for the bounded scene affinity of
+			//    pick_render; a request that does not fit the memory budget or the in-flight limit stops
+			//    admission.
 			bool renderWaits = false;
 			for (size_t pi = 0; pi < s->pending.size();) {
 				Request* r = s->pending[pi];
 				if (s->inflight.size() + s->admitted.size() >= s->cfg.maxInFlight) break;
 				if (s->sceneBytes + s->bytesInUse + r->bytes > s->cfg.memoryBudget) break;
 				RenderSlot* freeSlot = nullptr;
+				size_t take = pi;
 				if (r->desc.kind == PHE_REQ_RENDER) {
 					if (!renderWaits)
 						for (RenderSlot& sl : s->slots)
@@ -362,8 +394,10 @@ void worker_loop(phe_server* s)
 						pi++;
 						continue;
 					}
+					take = pick_render(s, pi);
+					r = s->pending[take];
 				}
-				s->pending.erase(s->pending.begin() + pi);
+				s->pending.erase(s->pending.begin() + take);
 				s->bytesInUse += r->bytes;
 				r->tAdmit = now_ms(s->t0);
 				r->state = kAdmitted;

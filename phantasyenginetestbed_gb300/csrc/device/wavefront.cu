@@ -539,63 +539,93 @@ __device__ __forceinline__ void taa_pixel(uint32_t x, uint32_t y, uint32_t W, ui
 	taa_blend(cur, h, trust, outColor, outHist);
 }
 
-// 12 resident blocks of 128 (40 registers): the still-camera path is bound by memory latency (a pixel's
-// contribution loads wait on its visibility bytes), so more threads in flight help: 39.5 us at 1080p
-// vs 42.3 us uncapped (44 registers, 10 blocks); 16 blocks (32 registers) gave 38.9 us but spilled
-// 104 bytes in the camera-motion path, 12 blocks spill 8.
-constexpr int kResolveMinBlocks = 12;
-__global__ void __launch_bounds__(128, kResolveMinBlocks) resolve_taa_kernel(const FrameParamsDev* __restrict__ fpp,
-                                                                           FrameBuffers fb)
+// Two pixels a thread, 128 apart (a block covers 256 consecutive pixels, so every load and store of a
+// warp stays coalesced). The still-camera path is bound by memory latency: a pixel's contribution loads
+// wait on its visibility bytes. Here the visibility loads of both pixels (kResolveChunk slots each) are
+// issued together, then the contribution loads of the visible slots, so a thread keeps two independent
+// chains in flight; the per-pixel sums keep the slot order.
+constexpr int kResolveBlock = 128;
+constexpr int kResolveMinBlocks = 8;
+constexpr uint32_t kResolveChunk = 4;   // light slots whose loads are issued together
+__global__ void __launch_bounds__(kResolveBlock, kResolveMinBlocks)
+resolve_taa_kernel(const FrameParamsDev* __restrict__ fpp, FrameBuffers fb)
 {
 	const FrameParamsDev& fp = *fpp;
-	uint32_t x = blockIdx.x * blockDim.x + threadIdx.x;
-	uint32_t y = blockIdx.y * blockDim.y + threadIdx.y;
-	if (x >= fp.resX || y >= fp.resY) return;
 	const uint32_t P = fp.numPixels, L = fp.numLights;
-	uint32_t pid = y * fp.resX + x;
-	if (pid == 0) {
+	const uint32_t p0 = blockIdx.x * (2u * kResolveBlock) + threadIdx.x, p1 = p0 + kResolveBlock;
+	if (p0 >= P) return;
+	if (p0 == 0) {
 		atomicAdd(&fb.rayTotals[0], (unsigned long long)P);
 		atomicAdd(&fb.rayTotals[1], (unsigned long long)fb.counters[kCtrShadow0]);
 		atomicAdd(&fb.rayTotals[2], (unsigned long long)fb.counters[kCtrBounce]);
 		atomicAdd(&fb.rayTotals[3], (unsigned long long)fb.counters[kCtrShadow1]);
 	}
 	if (fp.velocity || fp.prevVelocity) {   // camera motion: the full TAA with reprojected history
-		f3 acc = mk3(0.0f, 0.0f, 0.0f);
-		for (uint32_t k = 0; k < 2 * L; k++) {
-			size_t slot = (size_t)k * P + pid;
-			if (fb.inLight[slot]) {
-				float4 c = fb.contrib[slot];
-				acc = add3(acc, mk3(c.x, c.y, c.z));
+		for (uint32_t pid = p0; pid <= p1 && pid < P; pid += kResolveBlock) {
+			f3 acc = mk3(0.0f, 0.0f, 0.0f);
+			for (uint32_t k = 0; k < 2 * L; k++) {
+				size_t slot = (size_t)k * P + pid;
+				if (fb.inLight[slot]) {
+					float4 c = fb.contrib[slot];
+					acc = add3(acc, mk3(c.x, c.y, c.z));
+				}
 			}
+			float4 cur = make_float4(acc.x, acc.y, acc.z, 1.0f);
+			float4 oc, oh;
+			taa_pixel(pid % fp.resX, pid / fp.resX, fp.resX, fp.resY, cur, fb.history[fp.parity], fp.velocity,
+			          fp.prevVelocity, fb.roughness[pid], oc, oh);
+			fb.rawColor[pid] = cur;
+			fb.color[fp.parity ^ 1u][pid] = oc;
+			fb.history[fp.parity ^ 1u][pid] = oh;
 		}
-		float4 cur = make_float4(acc.x, acc.y, acc.z, 1.0f);
-		float4 oc, oh;
-		taa_pixel(x, y, fp.resX, fp.resY, cur, fb.history[fp.parity], fp.velocity, fp.prevVelocity, fb.roughness[pid],
-		          oc, oh);
-		fb.rawColor[pid] = cur;
-		fb.color[fp.parity ^ 1u][pid] = oc;
-		fb.history[fp.parity ^ 1u][pid] = oh;
 		return;
 	}
-	// Still camera. Every load this pixel needs is issued before the first store (the stores could
-	// alias them for the compiler). With zero velocity the history texel is the pixel itself and both
-	// velocity lengths are 0, so velocityDistrust = 0 and trust = clamp(1 - roughnessDistrust * 0).
-	const float4 h = ld_stream(fb.history[fp.parity] + pid);
-	const float rough = ld_stream(fb.roughness + pid);
-	uint8_t lit[2 * kMaxLights];
-	for (uint32_t k = 0; k < 2 * L; k++) lit[k] = ld_stream(fb.inLight + (size_t)k * P + pid);
-	f3 acc = mk3(0.0f, 0.0f, 0.0f);
-	for (uint32_t k = 0; k < 2 * L; k++)
-		if (lit[k]) {
-			float4 c = ld_stream(fb.contrib + (size_t)k * P + pid);
-			acc = add3(acc, mk3(c.x, c.y, c.z));
+	// Still camera. Every load a pixel needs is issued before the first store (the stores could alias
+	// them for the compiler). With zero velocity the history texel is the pixel itself and both velocity
+	// lengths are 0, so velocityDistrust = 0 and trust = clamp(1 - roughnessDistrust * 0). At the end of
+	// the frame the second pixel may not exist: it then repeats the first and its stores are skipped.
+	const bool two = p1 < P;
+	const uint32_t q = two ? p1 : p0;
+	const float4 h0 = ld_stream(fb.history[fp.parity] + p0), h1 = ld_stream(fb.history[fp.parity] + q);
+	const float r0 = ld_stream(fb.roughness + p0), r1 = ld_stream(fb.roughness + q);
+	const uint32_t n = 2 * L;
+	f3 a0 = mk3(0.0f, 0.0f, 0.0f), a1 = a0;
+	for (uint32_t k0 = 0; k0 < n; k0 += kResolveChunk) {
+		uint8_t v0[kResolveChunk], v1[kResolveChunk];
+#pragma unroll
+		for (uint32_t j = 0; j < kResolveChunk; j++) {
+			const size_t base = (size_t)(k0 + j) * P;
+			const bool in = k0 + j < n;
+			v0[j] = in ? ld_stream(fb.inLight + base + p0) : (uint8_t)0;
+			v1[j] = in ? ld_stream(fb.inLight + base + q) : (uint8_t)0;
 		}
-	float4 cur = make_float4(acc.x, acc.y, acc.z, 1.0f);
-	float4 oc, oh;
-	taa_blend(cur, h, clampf(__fsub_rn(1.0f, __fmul_rn(glsl_mix(3.0f, 1.0f, rough), 0.0f)), 0.0f, 1.0f), oc, oh);
-	st_stream(fb.rawColor + pid, cur);
-	st_stream(fb.color[fp.parity ^ 1u] + pid, oc);
-	st_stream(fb.history[fp.parity ^ 1u] + pid, oh);
+		float4 c0[kResolveChunk], c1[kResolveChunk];
+#pragma unroll
+		for (uint32_t j = 0; j < kResolveChunk; j++) {
+			const size_t base = (size_t)(k0 + j) * P;
+			c0[j] = v0[j] ? ld_stream(fb.contrib + base + p0) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+			c1[j] = v1[j] ? ld_stream(fb.contrib + base + q) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+		}
+#pragma unroll
+		for (uint32_t j = 0; j < kResolveChunk; j++) {
+			if (v0[j]) a0 = add3(a0, mk3(c0[j].x, c0[j].y, c0[j].z));
+			if (v1[j]) a1 = add3(a1, mk3(c1[j].x, c1[j].y, c1[j].z));
+		}
+	}
+	const float4 cur0 = make_float4(a0.x, a0.y, a0.z, 1.0f), cur1 = make_float4(a1.x, a1.y, a1.z, 1.0f);
+	float4 oc0, oh0, oc1, oh1;
+	taa_blend(cur0, h0, clampf(__fsub_rn(1.0f, __fmul_rn(glsl_mix(3.0f, 1.0f, r0), 0.0f)), 0.0f, 1.0f), oc0, oh0);
+	taa_blend(cur1, h1, clampf(__fsub_rn(1.0f, __fmul_rn(glsl_mix(3.0f, 1.0f, r1), 0.0f)), 0.0f, 1.0f), oc1, oh1);
+	float4* color = fb.color[fp.parity ^ 1u];
+	float4* hist = fb.history[fp.parity ^ 1u];
+	st_stream(fb.rawColor + p0, cur0);
+	st_stream(color + p0, oc0);
+	st_stream(hist + p0, oh0);
+	if (two) {
+		st_stream(fb.rawColor + p1, cur1);
+		st_stream(color + p1, oc1);
+		st_stream(hist + p1, oh1);
+	}
 }
 
 __global__ void taa_kernel(uint32_t W, uint32_t H, const float4* __restrict__ cur, const float4* __restrict__ hist,
@@ -680,8 +710,6 @@ phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, c
 	PHE_CUDA_TRY(cudaMemsetAsync(fb.counters, 0, sizeof(uint32_t) * kNumCounters, stream), "clear frame counters");
 	int e = 0;
 	auto mark = [&]() { if (ev) cudaEventRecord(ev[e++], stream); };
-	dim3 block(16, 8);
-	dim3 grid((resX + 15) / 16, (resY + 7) / 8);
 	DeviceInfo* dinfo = nullptr;
 	if ((st = device_info(&dinfo))) return st;
 	int binGrid = dinfo->numSMs * 4;
@@ -760,7 +788,8 @@ phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, c
 		                                                                 scene->status);
 		mark();
 	}
-	resolve_taa_kernel<<<grid, block, 0, stream>>>(dParams, fb);
+	const uint32_t resolveGrid = (uint32_t)(((uint64_t)resX * resY + 2 * kResolveBlock - 1) / (2 * kResolveBlock));
+	resolve_taa_kernel<<<resolveGrid, kResolveBlock, 0, stream>>>(dParams, fb);
 	mark();
 	PHE_CUDA_TRY(cudaGetLastError(), "frame kernel launch");
 	return PHE_OK;
