@@ -83,7 +83,8 @@ def parse():
                          "against rays per launch (16K..16M) for each ray-cast entry point")
     ap.add_argument("--res", type=int, default=4096, help="large: width and height of the primary pass")
     ap.add_argument("--rays", type=int, default=16 << 20, help="large: rays per diffuse / shadow launch")
-    ap.add_argument("--rates", default="200,500,1000", help="serve: arrival rates (requests/s)")
+    ap.add_argument("--rates", default="200,500,1000,2000,4000,8000",
+                    help="serve: arrival rates (requests/s); 2000 and above saturate the serial baseline")
     ap.add_argument("--duration", type=float, default=2.0, help="serve: seconds of arrivals per rate")
     ap.add_argument("--render-slots", type=int, default=8, help="serve: concurrent render requests")
     ap.add_argument("--batch-window-us", type=int, default=0, help="serve: wave batching window")

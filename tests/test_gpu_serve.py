@@ -327,3 +327,42 @@ def test_queries_pass_a_render_that_waits_for_a_slot(scenes):
     server.release(r1)
     server.release(r2)
     server.close()
+
+
+def test_render_on_a_scene_in_use_goes_first(scenes):
+    """Scene affinity: when a render slot frees and the next pending render's scene is not being
+    rendered by any slot, a later pending render on a scene that a slot is rendering is admitted first.
+    R1 (long) and R2 (shorter) render scene 0 in the two slots; R3 (scene 1) and R4 (scene 0) wait. When
+    R2 completes, R1 still renders scene 0, so R4 goes before R3. Both frames equal the same renders
+    made alone."""
+    server = Server(render_slots=2)
+    ids = [server.add_scene(x[2]) for x in scenes]
+
+    def render_args(si, res):
+        k = scenes[si][0].scale
+        cam_pos = (0.5 * k, -0.3 * k, 0.6 * k)
+        cam = cam_struct(O.camera_def(cam_pos, C1_CAM["dir"], C1_CAM["up"], math.radians(60), res))
+        lights = make_lights(np.array([[0.5, 0.5, 2.0]], np.float32) * np.float32(k), range_=1000.0 * k)
+        return cam, cam_pos, lights
+
+    plan = [(0, (1920, 1080), 8), (0, (512, 512), 4), (1, (256, 256), 1), (0, (256, 256), 1)]
+    outs = [pinned((res[1], res[0], 4), np.float32) for _, res, _ in plan]
+    args = [render_args(si, res) for si, res, _ in plan]
+    rids = [server.submit_render(ids[si], res, spp, a[0], a[1], a[2], 30 + i, outs[i])
+            for i, ((si, res, spp), a) in enumerate(zip(plan, args))]
+    server.drain()
+    st = [server.poll(r) for r in rids]
+    assert all(x.status == 0 for x in st)
+    assert st[2].submitMs < st[1].doneMs and st[3].submitMs < st[1].doneMs   # both waited for a slot
+    assert st[0].doneMs > st[1].doneMs                                       # R1 still rendered scene 0
+    assert st[3].admitMs < st[2].admitMs, [(x.submitMs, x.admitMs, x.doneMs) for x in st]
+    for i in (2, 3):   # the reordered renders give the frames they give alone
+        si, res, spp = plan[i]
+        rid = server.submit_render(ids[si], res, spp, args[i][0], args[i][1], args[i][2], 30 + i,
+                                   alone := pinned((res[1], res[0], 4), np.float32))
+        assert server.wait(rid).status == 0
+        assert np.array_equal(alone, outs[i])
+        server.release(rid)
+    for r in rids:
+        server.release(r)
+    server.close()
