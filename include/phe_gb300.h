@@ -440,7 +440,10 @@ phe_status phe_taa_resolve(uint32_t resX, uint32_t resY, const float* cur, const
  * Serving (no reference counterpart): continuous batching of ray-query and render requests against
  * device-resident scenes. A scheduler thread admits requests in arrival order while they fit the
  * device-memory budget (resident scenes count against it), the in-flight limit and, for renders, a
- * free render slot. Admitted ray queries whose rays are on the device join the next wave, ONE batched
+ * free render slot. A render waiting for a slot does not hold back the ray queries behind it; when a
+ * slot frees, a render on a scene that another slot is rendering may go before up to 16 earlier
+ * pending entries (a render is passed over at most 8 times). Admitted ray queries whose rays are on
+ * the device join the next wave, ONE batched
  * persistent launch over all of them; requests arriving meanwhile join the following wave. Renders
  * run their spp frames (wavefront frame + TAA with Halton jitter) on their slot's own stream, so they
  * overlap each other and the query waves. Results go straight to the caller's host buffers (pinned
