@@ -69,6 +69,9 @@ def parse():
     ap.add_argument("--pipeline", choices=["fused", "split"], default="fused",
                     help="fused: traversal + shading in one kernel per bounce (4 kernels with merged shadows); split: 7 kernels")
     ap.add_argument("--refill", type=int, default=28, help="lane-refill threshold of the split pipeline")
+    ap.add_argument("--frames-in-flight", type=int, default=1, choices=(1, 2),
+                    help="frame: 2 = consecutive frames overlap on the renderer's own streams (same bytes); "
+                         "with 1, the line also reports 2 in flight without L2 flushes as a secondary figure")
     ap.add_argument("--sort-window", type=int, default=0, help="bin bounce rays by octant in windows of N (0 = off)")
     ap.add_argument("--shadows", choices=["merged", "beside", "in-order"], default="merged",
                     help="shadow-pass schedule: one pass over both queues after the bounce pass (default), the "
@@ -339,6 +342,53 @@ def frame_roofline(dominant, entry, clock, num_sms, builder, layout) -> dict:
     return out
 
 
+def two_in_flight(r, frame, stream, first, steps, rays_per_frame):
+    """Secondary figures with two frames in flight (consecutive frames overlapping on the renderer's own
+    streams, the same bytes as one at a time): device throughput over `steps` frames (CUDA events from
+    before the first frame to the join after the last), per-frame GPU latency from the renderer's
+    records, and end to end with the colour image read back asynchronously every frame. No L2 flush
+    between frames: the frames overlap, so there is no point between them, and a flush on the caller's
+    stream would run inside the next frame."""
+    import torch
+    from phantasyenginetestbed_gb300.renderer import READ_COLOR
+    r.set_frames_in_flight(2)
+    try:
+        for k in range(100):   # the first pipelined frames after the switch run slower in some runs
+            frame(first + k)
+        torch.cuda.synchronize()
+        region = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+        r.set_seed(SEED, first)
+        region[0].record(stream)
+        for k in range(steps):
+            frame(first + k)
+        r.join(stream)
+        region[1].record(stream)
+        torch.cuda.synchronize()
+        ms = region[0].elapsed_time(region[1])
+        r.set_seed(SEED, first)
+        r.set_latency_recording(True)
+        for k in range(steps):
+            frame(first + k)
+        lat = sorted(float(x) for x in r.frame_latencies())
+        r.set_latency_recording(False)
+        host_imgs = [torch.empty((RES[1], RES[0], 4), dtype=torch.float32, pin_memory=True).numpy() for _ in range(2)]
+        torch.cuda.synchronize()
+        r.set_seed(SEED, first)
+        t0 = time.perf_counter()
+        for k in range(steps):
+            frame(first + k)
+            r.read_async(host_imgs[k & 1], READ_COLOR, stream=stream)
+        r.read_wait()
+        e2e_s = time.perf_counter() - t0
+    finally:
+        r.set_frames_in_flight(1)
+    return {"Mrays_s": round(rays_per_frame * steps / (ms / 1e3) / 1e6, 2), "ms_per_frame": round(ms / steps, 4),
+            "latency_ms": {"p50": round(lat[len(lat) // 2], 4), "p99": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 4),
+                           "of": "per frame on the GPU, first kernel start to resolve end"},
+            "e2e_Mrays_s": round(rays_per_frame * steps / e2e_s / 1e6, 2),
+            "l2": "not flushed between frames: overlapping frames have no point between them"}
+
+
 def run_ours(args, world, rank, local):
     import torch
     import phantasyenginetestbed_gb300 as P
@@ -358,9 +408,11 @@ def run_ours(args, world, rank, local):
     r.set_shadow_schedule({"in-order": 0, "beside": 1, "merged": 2}[args.shadows])
     r.setStaticScene(scene)
     r.setTargetResolution(RES)
+    r.set_frames_in_flight(args.frames_in_flight)
     r.set_seed(SEED, 0)
     r.resetTAA()
     stream = torch.cuda.current_stream()
+    inflight = args.frames_in_flight
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")   # 4x the 126 MiB L2
 
     def frame(f):
@@ -372,24 +424,47 @@ def run_ours(args, world, rank, local):
     torch.cuda.synchronize()
     first = args.warmup
 
-    # Timed region: K frames, L2 flushed before each (outside the per-frame events).
+    # Timed region: K frames, L2 flushed before each. One frame in flight: CUDA events around each
+    # frame on the render stream (the flushes fall outside them). Two in flight: frames overlap on the
+    # renderer's streams, so the region runs from before the first flush to the join after the last
+    # frame (flushes included); per-frame latency comes from the renderer's latency records of a
+    # second, identical pass.
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    region = (torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
     if dist:
         dist.barrier()
     torch.cuda.synchronize()
     r.set_seed(SEED, first)
     with ClockSampler(local) as clocks:
-        for k in range(args.steps):
-            flush.zero_()
-            starts[k].record(stream)
-            frame(first + k)
-            ends[k].record(stream)
+        if inflight == 1:
+            for k in range(args.steps):
+                flush.zero_()
+                starts[k].record(stream)
+                frame(first + k)
+                ends[k].record(stream)
+        else:
+            region[0].record(stream)
+            for k in range(args.steps):
+                flush.zero_()
+                frame(first + k)
+            r.join(stream)
+            region[1].record(stream)
         torch.cuda.synchronize()
     if dist:
         dist.barrier()
-    per = [a.elapsed_time(e) for a, e in zip(starts, ends)]
-    total_ms = sum(per)
+    if inflight == 1:
+        per = [a.elapsed_time(e) for a, e in zip(starts, ends)]
+        total_ms = sum(per)
+    else:
+        total_ms = region[0].elapsed_time(region[1])
+        r.set_seed(SEED, first)
+        r.set_latency_recording(True)
+        for k in range(args.steps):
+            flush.zero_()
+            frame(first + k)
+        per = [float(x) for x in r.frame_latencies()]
+        r.set_latency_recording(False)
     # Rays cast by the timed frames: the frames are deterministic, so replaying them with the same
     # seed and frame indices and reading the queue counters after each gives the exact counts.
     r.set_seed(SEED, first)
@@ -436,6 +511,7 @@ def run_ours(args, world, rank, local):
         frame(first + k)
         r.read(READ_COLOR, out=host_imgs[0], stream=stream)
     e2e_blocking = rays_per_frame * args.steps * world / (time.perf_counter() - t0) / 1e6
+    overlap = two_in_flight(r, frame, stream, first, args.steps, rays_per_frame) if inflight == 1 else None
 
     if rank != 0:
         if dist:
@@ -494,10 +570,14 @@ def run_ours(args, world, rank, local):
         "data": FRAME_DATA,
         "config": frame_config(s, b, builder, world),
         "frame": {"rays_per_frame": round(rays_per_frame, 1), "rays_by_pass": {k: round(v, 1) for k, v in stage_rays.items()},
-                  "cuda_graph": not args.no_graph, "pipeline": args.pipeline, "refill_threshold": args.refill,
+                  "frames_in_flight": inflight, "two_frames_in_flight": overlap,
+                  "cuda_graph": not args.no_graph and inflight == 1,
+                  "pipeline": args.pipeline, "refill_threshold": args.refill,
                   "sort_window": args.sort_window, "sbvh_build_s": round(build_s, 2), "node_layout": args.layout,
                   "shadow_schedule": args.shadows if args.pipeline == "fused" else "in-order"},
-        "latency_ms": {"p50": round(lat[len(lat) // 2], 4), "p99": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 4)},
+        "latency_ms": {"p50": round(lat[len(lat) // 2], 4), "p99": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 4),
+                       "of": ("per frame, CUDA events around it" if inflight == 1 else
+                              "per frame on the GPU, first kernel start to resolve end, 2 frames in flight")},
         "passes": per_kernel,
         "roofline": roofline,
         "clocks": clock,
@@ -505,7 +585,7 @@ def run_ours(args, world, rank, local):
                 "h2d_bytes_per_step": int(native.lib().phe_renderer_frame_param_bytes()),
                 "d2h_bytes_per_step": RES[0] * RES[1] * 16,
                 "mode": "pipelined: colour image read back asynchronously (two pinned host images) while the "
-                        "next frame renders; clock stops when the last image is in host memory",
+                        "next frames render; clock stops when the last image is in host memory",
                 "blocking_value": round(e2e_blocking, 2)},
         "gpu_launches": launches_per_frame * args.steps,
         "cpu_baseline": cpu,

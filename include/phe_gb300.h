@@ -410,6 +410,25 @@ phe_status phe_renderer_set_kernel_timing(phe_renderer* renderer, int enable);
 /* Bytes copied host -> device per frame (the frame parameter block: camera, jitter, lights). */
 uint32_t phe_renderer_frame_param_bytes(void);
 phe_status phe_renderer_kernel_times(phe_renderer* renderer, double msTotal[8], uint32_t* numKernels, uint32_t* frames);
+/* Frames in flight (no reference counterpart; the reference renders and presents one frame at a time).
+ * 1 (default): a frame's kernels run on the stream given to phe_renderer_render. 2: frame k's traversal
+ * kernels run on the renderer's traversal stream k % 2 with per-frame buffers of their own, after the
+ * work enqueued on the caller's stream before the call and after the resolve that last used those
+ * buffers; its resolve + TAA runs on the renderer's resolve stream after the previous frame's resolve.
+ * Consecutive frames overlap on the GPU; every frame gives exactly the bytes it gives with 1. The
+ * caller's stream is NOT ordered after the frame: phe_renderer_read / read_async / ray_counts /
+ * reset_taa / the ray-total calls wait for the last frame themselves, phe_renderer_join orders a stream
+ * after it (needed before using the pointers of phe_renderer_result on the GPU). Frames timed per
+ * kernel run in order on the caller's stream, and the BESIDE_BOUNCE shadow schedule runs IN_ORDER.
+ * Changing the setting waits for the frames in flight; 2 adds a second set of per-frame buffers
+ * (~410 MB at 1080p with one light). */
+phe_status phe_renderer_set_frames_in_flight(phe_renderer* renderer, int frames);
+phe_status phe_renderer_join(phe_renderer* renderer, void* stream);
+/* With 2 frames in flight and recording enabled, each frame's GPU latency (start of its first kernel to
+ * the end of its resolve) is recorded. frame_latencies with capacity 0 returns how many are recorded;
+ * otherwise it waits for and removes up to `capacity` of them, oldest first, into ms[]. */
+phe_status phe_renderer_set_latency_recording(phe_renderer* renderer, int enable);
+phe_status phe_renderer_frame_latencies(phe_renderer* renderer, float* ms, uint32_t capacity, uint32_t* count);
 
 /* Ray totals per pass summed over the frames since the last reset (device counters): reset clears them
  * on `stream`; totals_async copies the 4 totals (primary, primary shadow, bounce, bounce shadow) to

@@ -6,9 +6,20 @@
 // Buffers are (re)allocated in set_target_resolution, as targetResolutionUpdated does
 // (CudaTracerRenderer.cpp:735-793). A frame is either launched directly or replayed from a CUDA
 // graph captured on first use; per-frame values travel in one small parameter copy.
+//
+// Two frames in flight (phe_renderer_set_frames_in_flight): frame k's traversal kernels run on the
+// renderer's traversal stream k % 2 with their own per-frame buffers (slot k % 2: queues,
+// contributions, visibility, roughness, counters, parameters), after the caller's work enqueued before
+// the call and after the resolve that last read that slot; its resolve + TAA runs on the renderer's
+// resolve stream, after the previous frame's. Consecutive frames thus overlap on the GPU while the TAA
+// chain keeps its order, and every frame computes exactly what it computes alone. The caller's stream
+// is not made to wait (that would serialise the next frame): reads wait for the frame themselves, and
+// phe_renderer_join orders a stream after the last frame.
 
 #include <cmath>
 #include <cstring>
+#include <utility>
+#include <vector>
 
 #include "runtime.cuh"
 #include "wavefront.cuh"
@@ -18,8 +29,22 @@ using namespace phe_gb300;
 struct phe_renderer {
 	const phe_scene* scene = nullptr;
 	uint32_t resX = 0, resY = 0, numLights = 0;
-	FrameBuffers fb{};
+	FrameBuffers fb{};                   // slot 0 per-frame buffers + the shared ones
 	void* allocation = nullptr;
+	FrameBuffers fb1{};                  // slot 1: fb with its per-frame buffers replaced
+	void* allocation1 = nullptr;
+	int inFlight = 1;
+	FrameParamsDev* dParams1 = nullptr;  // parameters of slot 1
+	cudaStream_t travStream[2] = {}, resolveStream = nullptr;
+	cudaEvent_t callEvent = nullptr;     // the caller's work before a render
+	cudaEvent_t travDone[2] = {}, resolveDone[2] = {};
+	bool slotUsed[2] = {false, false};   // resolveDone[slot] marks the last frame that used the slot
+	uint32_t nextSlot = 0, lastSlot = 0;
+	bool framePending = false;           // a frame in flight that no caller stream has been ordered after
+	// Latency recording of frames in flight: (start, end) event pairs, drained by frame_latencies.
+	bool recordLatency = false;
+	std::vector<cudaEvent_t> latencyPool;
+	std::vector<std::pair<cudaEvent_t, cudaEvent_t>> latencyPending;
 	FrameParamsDev* dParams = nullptr;
 	FrameParamsDev* hParams = nullptr;   // pinned staging ring of kParamSlots
 	cudaEvent_t paramEvents[8] = {};     // last copy out of each staging slot
@@ -48,10 +73,16 @@ struct phe_renderer {
 	FrameStreams streams;                  // second stream for PHE_SHADOWS_BESIDE_BOUNCE
 	int shadowSchedule = PHE_SHADOWS_MERGED;
 	// Asynchronous read-back: two device staging slots copied to the host on copyStream.
-	// Camera motion (TAA velocity): the last rendered camera and which velocity sides are all zero.
+	// Camera motion (TAA velocity): the last rendered camera and a ring of three velocity buffers
+	// (frame k writes entry velNext, its resolve reads the previous frame's entry velLast; with two
+	// frames in flight, frame k+1 must not overwrite what frame k's resolve still reads).
 	phe_camera_def prevCam{};
 	bool hasPrevCam = false;
-	bool velocityZero[2] = {true, true};
+	float2* vel[3] = {};
+	bool velZero[3] = {true, true, true};
+	uint32_t velLast = 0, velNext = 1;
+	cudaEvent_t velDone[3] = {};         // last asynchronous copy out of each velocity buffer
+	bool velGuard[3] = {false, false, false};
 	cudaStream_t copyStream = nullptr;
 	void* staging[2] = {nullptr, nullptr};
 	size_t stagingBytes = 0;
@@ -69,19 +100,112 @@ struct phe_renderer {
 static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 static const uint32_t kParamSlots = 8;
 
+// Waits for the frames in flight on the renderer's own streams (none in sequential mode).
+static void drain_streams(phe_renderer* r)
+{
+	for (int j = 0; j < 2; j++)
+		if (r->travStream[j]) cudaStreamSynchronize(r->travStream[j]);
+	if (r->resolveStream) cudaStreamSynchronize(r->resolveStream);
+}
+
 static void free_buffers(phe_renderer* r)
 {
+	drain_streams(r);
 	// in-place read-backs may still be copying out of these buffers
 	for (int i = 0; i < 2; i++) {
 		if (r->sideDone[i]) cudaEventSynchronize(r->sideDone[i]);
 		r->sideGuard[i] = false;
 	}
+	for (int i = 0; i < 3; i++) {
+		if (r->velDone[i]) cudaEventSynchronize(r->velDone[i]);
+		r->velGuard[i] = false;
+	}
 	if (r->graphExec) cudaGraphExecDestroy(r->graphExec);
 	r->graphExec = nullptr;
 	if (r->allocation) cudaFree(r->allocation);
-	r->allocation = nullptr;
+	if (r->allocation1) cudaFree(r->allocation1);
+	r->allocation = r->allocation1 = nullptr;
 	std::memset(&r->fb, 0, sizeof(r->fb));
+	std::memset(&r->fb1, 0, sizeof(r->fb1));
+	for (int i = 0; i < 3; i++) r->vel[i] = nullptr;
+	r->slotUsed[0] = r->slotUsed[1] = false;
+	r->framePending = false;
 	r->capacityP = r->capacityL = 0;
+}
+
+// Per-frame buffers of one slot: everything a frame's traversal writes and its resolve reads. Sizes
+// for P pixels and L lights, in carving order.
+static const int kPerFrameParts = 12;
+static void per_frame_sizes(size_t P, size_t L, size_t sizes[kPerFrameParts])
+{
+	const size_t LP = P * L;
+	const size_t v[kPerFrameParts] = {
+		2 * LP * sizeof(float4),          // contrib
+		2 * LP,                           // inLight
+		2 * LP * sizeof(phe_ray_in),      // shadowRays
+		2 * LP * sizeof(uint32_t),        // shadowSlots
+		P * sizeof(phe_ray_in),           // bounceRays
+		P * sizeof(uint32_t),             // bouncePixel
+		P * sizeof(float4),               // bounceThroughput
+		P * sizeof(float),                // roughness
+		kNumCounters * sizeof(uint32_t),  // counters
+		P * sizeof(phe_ray_hit),          // primaryHits
+		P * sizeof(phe_ray_hit),          // bounceHits
+		P * sizeof(uint32_t),             // bouncePerm
+	};
+	for (int i = 0; i < kPerFrameParts; i++) sizes[i] = v[i];
+}
+
+static size_t per_frame_bytes(size_t P, size_t L)
+{
+	size_t sizes[kPerFrameParts], total = 0;
+	per_frame_sizes(P, L, sizes);
+	for (size_t x : sizes) total += align256(x);
+	return total;
+}
+
+// Points fb's per-frame buffers into `base` (per_frame_bytes(P, L) bytes); returns the end.
+static char* carve_per_frame(char* base, size_t P, size_t L, FrameBuffers& fb)
+{
+	size_t sizes[kPerFrameParts];
+	per_frame_sizes(P, L, sizes);
+	char* p = base;
+	auto take = [&](int i) { char* q = p; p += align256(sizes[i]); return q; };
+	fb.contrib = (float4*)take(0);
+	fb.inLight = (uint8_t*)take(1);
+	fb.shadowRays = (phe_ray_in*)take(2);
+	fb.shadowSlots = (uint32_t*)take(3);
+	fb.bounceRays = (phe_ray_in*)take(4);
+	fb.bouncePixel = (uint32_t*)take(5);
+	fb.bounceThroughput = (float4*)take(6);
+	fb.roughness = (float*)take(7);
+	fb.counters = (uint32_t*)take(8);
+	fb.primaryHits = (phe_ray_hit*)take(9);
+	fb.bounceHits = (phe_ray_hit*)take(10);
+	fb.bouncePerm = (uint32_t*)take(11);
+	return p;
+}
+
+// Slot 1 shares everything with slot 0 but its per-frame buffers.
+static void make_fb1(phe_renderer* r)
+{
+	if (!r->allocation1) return;
+	r->fb1 = r->fb;
+	carve_per_frame((char*)r->allocation1, r->capacityP, r->capacityL, r->fb1);
+}
+
+static phe_status allocate_slot1(phe_renderer* r)
+{
+	if (r->allocation1 || !r->allocation) return PHE_OK;
+	const size_t bytes = per_frame_bytes(r->capacityP, r->capacityL);
+	cudaError_t e = cudaMalloc(&r->allocation1, bytes);
+	if (e != cudaSuccess) {
+		r->allocation1 = nullptr;
+		return cuda_fail(e, "cudaMalloc(frame buffers of the second frame in flight)");
+	}
+	if ((e = cudaMemset(r->allocation1, 0, bytes)) != cudaSuccess) return cuda_fail(e, "clear frame buffers");
+	make_fb1(r);
+	return PHE_OK;
 }
 
 static phe_status allocate(phe_renderer* r, uint32_t resX, uint32_t resY, uint32_t numLights)
@@ -90,7 +214,7 @@ static phe_status allocate(phe_renderer* r, uint32_t resX, uint32_t resY, uint32
 	const size_t L = numLights ? numLights : 1;
 	if (resX != r->resX || resY != r->resY) {   // velocities of another resolution do not carry over
 		r->hasPrevCam = false;
-		r->velocityZero[0] = r->velocityZero[1] = true;
+		r->velZero[0] = r->velZero[1] = r->velZero[2] = true;
 	}
 	if (r->allocation && P <= r->capacityP && L <= r->capacityL) {
 		// Keep the buffers: every stride is computed from the current resolution at launch time. A
@@ -105,59 +229,34 @@ static phe_status allocate(phe_renderer* r, uint32_t resX, uint32_t resY, uint32
 		return PHE_OK;
 	}
 	free_buffers(r);
-	const size_t LP = P * L;
-	size_t sizes[] = {
-		2 * LP * sizeof(float4),      // contrib
-		2 * LP,                       // inLight
-		2 * LP * sizeof(phe_ray_in),  // shadowRays
-		2 * LP * sizeof(uint32_t),    // shadowSlots
-		P * sizeof(phe_ray_in),       // bounceRays
-		P * sizeof(uint32_t),         // bouncePixel
-		P * sizeof(float4),           // bounceThroughput
-		P * sizeof(float),            // roughness
-		P * sizeof(float4),           // rawColor
-		P * sizeof(float4),           // history[0]
-		P * sizeof(float4),           // history[1]
-		P * sizeof(float4),           // color[0]
-		kNumCounters * sizeof(uint32_t),
-		P * sizeof(phe_ray_hit),      // primaryHits
-		P * sizeof(phe_ray_hit),      // bounceHits
-		4 * sizeof(unsigned long long), // rayTotals
-		P * sizeof(uint32_t),         // bouncePerm
-		P * sizeof(float2),           // velocity[0]
-		P * sizeof(float2),           // velocity[1]
-		P * sizeof(float4),           // color[1]
+	const size_t shared[] = {
+		P * sizeof(float4),               // rawColor
+		P * sizeof(float4),               // history[0]
+		P * sizeof(float4),               // history[1]
+		P * sizeof(float4),               // color[0]
+		P * sizeof(float4),               // color[1]
+		4 * sizeof(unsigned long long),   // rayTotals
+		P * sizeof(float2),               // velocity ring
+		P * sizeof(float2),
+		P * sizeof(float2),
 	};
-	size_t total = 0;
-	for (size_t s : sizes) total += align256(s);
+	size_t total = per_frame_bytes(P, L);
+	for (size_t x : shared) total += align256(x);
 	char* base = nullptr;
 	cudaError_t e = cudaMalloc(&base, total);
 	if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc(frame buffers)");
-	char* p = base;
-	auto take = [&](size_t i) { char* q = p; p += align256(sizes[i]); return q; };
 	FrameBuffers& fb = r->fb;
-	fb.contrib = (float4*)take(0);
-	fb.inLight = (uint8_t*)take(1);
-	fb.shadowRays = (phe_ray_in*)take(2);
-	fb.shadowSlots = (uint32_t*)take(3);
-	fb.bounceRays = (phe_ray_in*)take(4);
-	fb.bouncePixel = (uint32_t*)take(5);
-	fb.bounceThroughput = (float4*)take(6);
-	fb.roughness = (float*)take(7);
-	fb.rawColor = (float4*)take(8);
-	fb.history[0] = (float4*)take(9);
-	fb.history[1] = (float4*)take(10);
-	fb.color[0] = (float4*)take(11);
-	fb.counters = (uint32_t*)take(12);
-	fb.primaryHits = (phe_ray_hit*)take(13);
-	fb.bounceHits = (phe_ray_hit*)take(14);
-	fb.rayTotals = (unsigned long long*)take(15);
-	fb.bouncePerm = (uint32_t*)take(16);
-	fb.velocity[0] = (float2*)take(17);
-	fb.velocity[1] = (float2*)take(18);
-	fb.color[1] = (float4*)take(19);
+	char* p = carve_per_frame(base, P, L, fb);
+	auto take = [&](size_t i) { char* q = p; p += align256(shared[i]); return q; };
+	fb.rawColor = (float4*)take(0);
+	fb.history[0] = (float4*)take(1);
+	fb.history[1] = (float4*)take(2);
+	fb.color[0] = (float4*)take(3);
+	fb.color[1] = (float4*)take(4);
+	fb.rayTotals = (unsigned long long*)take(5);
+	for (int i = 0; i < 3; i++) r->vel[i] = (float2*)take(6 + i);
 	fb.sortWindow = r->sortWindow;
-	fb.capacityLP = (uint32_t)LP;
+	fb.capacityLP = (uint32_t)(P * L);
 	fb.refill = r->refill;
 	r->capacityP = P;
 	r->capacityL = L;
@@ -167,6 +266,7 @@ static phe_status allocate(phe_renderer* r, uint32_t resX, uint32_t resY, uint32
 	r->numLights = numLights;
 	if ((e = cudaMemset(base, 0, total)) != cudaSuccess) return cuda_fail(e, "clear frame buffers");
 	r->parity = 0;
+	if (r->inFlight == 2) return allocate_slot1(r);
 	return PHE_OK;
 }
 
@@ -220,6 +320,7 @@ extern "C" phe_status phe_renderer_set_pipeline(phe_renderer* r, int fused, int 
 	r->fb.refill = refill;
 	r->sortWindow = sortWindow;
 	r->fb.sortWindow = sortWindow;
+	make_fb1(r);
 	if (r->graphExec) {
 		cudaGraphExecDestroy(r->graphExec);
 		r->graphExec = nullptr;
@@ -270,11 +371,13 @@ extern "C" phe_status phe_renderer_create(phe_renderer** out)
 	if (st) return st;
 	phe_renderer* r = new phe_renderer();
 	cudaError_t e = cudaMalloc(&r->dParams, sizeof(FrameParamsDev));
+	if (e == cudaSuccess) e = cudaMalloc(&r->dParams1, sizeof(FrameParamsDev));
 	if (e == cudaSuccess) e = cudaMallocHost(&r->hParams, sizeof(FrameParamsDev) * kParamSlots);
 	for (uint32_t i = 0; i < kParamSlots && e == cudaSuccess; i++)
 		e = cudaEventCreateWithFlags(&r->paramEvents[i], cudaEventDisableTiming);
 	if (e != cudaSuccess) {
 		if (r->dParams) cudaFree(r->dParams);
+		if (r->dParams1) cudaFree(r->dParams1);
 		if (r->hParams) cudaFreeHost(r->hParams);
 		delete r;
 		return cuda_fail(e, "allocate frame parameters");
@@ -296,6 +399,20 @@ extern "C" phe_status phe_renderer_destroy(phe_renderer* r)
 	if (!r) return PHE_OK;
 	cudaDeviceSynchronize();
 	free_buffers(r);   // first: it waits on the read-back events destroyed below
+	for (int j = 0; j < 2; j++) {
+		if (r->travStream[j]) cudaStreamDestroy(r->travStream[j]);
+		if (r->travDone[j]) cudaEventDestroy(r->travDone[j]);
+		if (r->resolveDone[j]) cudaEventDestroy(r->resolveDone[j]);
+	}
+	if (r->resolveStream) cudaStreamDestroy(r->resolveStream);
+	if (r->callEvent) cudaEventDestroy(r->callEvent);
+	for (cudaEvent_t e : r->latencyPool) cudaEventDestroy(e);
+	for (auto& pr : r->latencyPending) {
+		cudaEventDestroy(pr.first);
+		cudaEventDestroy(pr.second);
+	}
+	for (int i = 0; i < 3; i++)
+		if (r->velDone[i]) cudaEventDestroy(r->velDone[i]);
 	for (int i = 0; i <= kFrameKernels; i++)
 		if (r->events[i]) cudaEventDestroy(r->events[i]);
 	for (uint32_t i = 0; i < kParamSlots; i++)
@@ -313,6 +430,7 @@ extern "C" phe_status phe_renderer_destroy(phe_renderer* r)
 	if (r->streams.fork) cudaEventDestroy(r->streams.fork);
 	if (r->streams.join) cudaEventDestroy(r->streams.join);
 	cudaFree(r->dParams);
+	cudaFree(r->dParams1);
 	cudaFreeHost(r->hParams);
 	delete r;
 	return PHE_OK;
@@ -393,24 +511,117 @@ static phe_status guard_side(phe_renderer* r, uint32_t side, cudaStream_t s)
 	return PHE_OK;
 }
 
+// The same for entry i of the velocity ring.
+static phe_status guard_velocity(phe_renderer* r, uint32_t i, cudaStream_t s)
+{
+	if (!r->velGuard[i]) return PHE_OK;
+	PHE_CUDA_TRY(cudaStreamWaitEvent(s, r->velDone[i], 0), "wait for read-back of a velocity buffer");
+	r->velGuard[i] = false;
+	return PHE_OK;
+}
+
+// Orders `s` after the last frame in flight (no-op in sequential mode, where frames run on `s`).
+static phe_status join_frames(const phe_renderer* r, cudaStream_t s)
+{
+	if (!r->framePending) return PHE_OK;
+	PHE_CUDA_TRY(cudaStreamWaitEvent(s, r->resolveDone[r->lastSlot], 0), "wait for the last frame");
+	return PHE_OK;
+}
+
+// Buffers of the last rendered frame's slot (slot 0 in sequential mode).
+static const FrameBuffers& last_fb(const phe_renderer* r) { return r->lastSlot ? r->fb1 : r->fb; }
+
+extern "C" phe_status phe_renderer_join(phe_renderer* r, void* stream)
+{
+	if (!r) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_join: null renderer");
+	return join_frames(r, (cudaStream_t)stream);
+}
+
+extern "C" phe_status phe_renderer_set_frames_in_flight(phe_renderer* r, int frames)
+{
+	if (!r) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_set_frames_in_flight: null renderer");
+	if (frames != 1 && frames != 2) return fail(PHE_ERR_INVALID_ARGUMENT, "frames in flight must be 1 or 2");
+	drain_streams(r);   // the slots and streams change hands only when no frame is in flight
+	r->slotUsed[0] = r->slotUsed[1] = false;
+	r->framePending = false;
+	r->nextSlot = r->lastSlot = 0;
+	r->inFlight = frames;
+	if (frames == 2) {
+		if (!r->resolveStream) {
+			for (int j = 0; j < 2; j++) {
+				PHE_CUDA_TRY(cudaStreamCreateWithFlags(&r->travStream[j], cudaStreamNonBlocking), "create frame stream");
+				PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->travDone[j], cudaEventDisableTiming), "create frame event");
+				PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->resolveDone[j], cudaEventDisableTiming), "create frame event");
+			}
+			PHE_CUDA_TRY(cudaStreamCreateWithFlags(&r->resolveStream, cudaStreamNonBlocking), "create frame stream");
+			PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->callEvent, cudaEventDisableTiming), "create frame event");
+		}
+		phe_status st = allocate_slot1(r);
+		if (st) return st;
+	}
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_renderer_set_latency_recording(phe_renderer* r, int enable)
+{
+	if (!r) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_set_latency_recording: null renderer");
+	r->recordLatency = enable != 0;
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_renderer_frame_latencies(phe_renderer* r, float* ms, uint32_t capacity, uint32_t* count)
+{
+	if (!r || !count || (capacity && !ms)) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_frame_latencies: null argument");
+	if (capacity == 0) {   // how many are recorded
+		*count = (uint32_t)r->latencyPending.size();
+		return PHE_OK;
+	}
+	const uint32_t n = (uint32_t)std::min<size_t>(capacity, r->latencyPending.size());
+	for (uint32_t i = 0; i < n; i++) {
+		const auto& pr = r->latencyPending[i];
+		PHE_CUDA_TRY(cudaEventSynchronize(pr.second), "wait for a recorded frame");
+		PHE_CUDA_TRY(cudaEventElapsedTime(&ms[i], pr.first, pr.second), "frame latency");
+		r->latencyPool.push_back(pr.first);
+		r->latencyPool.push_back(pr.second);
+	}
+	r->latencyPending.erase(r->latencyPending.begin(), r->latencyPending.begin() + n);
+	*count = n;
+	return PHE_OK;
+}
+
+static phe_status take_timing_event(phe_renderer* r, cudaEvent_t* e)
+{
+	if (!r->latencyPool.empty()) {
+		*e = r->latencyPool.back();
+		r->latencyPool.pop_back();
+		return PHE_OK;
+	}
+	PHE_CUDA_TRY(cudaEventCreate(e), "create latency event");
+	return PHE_OK;
+}
+
 extern "C" phe_status phe_renderer_reset_taa(phe_renderer* r, void* stream)
 {
 	if (!r || !r->allocation) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_reset_taa: no frame buffers");
 	size_t P = (size_t)r->resX * r->resY;
+	phe_status st = join_frames(r, (cudaStream_t)stream);   // the resolve of a frame in flight uses the history
+	if (st) return st;
 	for (uint32_t side = 0; side < 2; side++) {
-		phe_status st = guard_side(r, side, (cudaStream_t)stream);
+		st = guard_side(r, side, (cudaStream_t)stream);
 		if (st) return st;
 	}
 	PHE_CUDA_TRY(cudaMemsetAsync(r->fb.history[0], 0, P * sizeof(float4), (cudaStream_t)stream), "reset TAA");
 	PHE_CUDA_TRY(cudaMemsetAsync(r->fb.history[1], 0, P * sizeof(float4), (cudaStream_t)stream), "reset TAA");
 	r->hasPrevCam = false;
-	r->velocityZero[0] = r->velocityZero[1] = true;
+	r->velZero[0] = r->velZero[1] = r->velZero[2] = true;
 	return PHE_OK;
 }
 
 extern "C" phe_status phe_renderer_reset_ray_totals(phe_renderer* r, void* stream)
 {
 	if (!r || !r->allocation) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_reset_ray_totals: no frame buffers");
+	phe_status st = join_frames(r, (cudaStream_t)stream);
+	if (st) return st;
 	PHE_CUDA_TRY(cudaMemsetAsync(r->fb.rayTotals, 0, 4 * sizeof(unsigned long long), (cudaStream_t)stream),
 	             "reset ray totals");
 	return PHE_OK;
@@ -419,6 +630,8 @@ extern "C" phe_status phe_renderer_reset_ray_totals(phe_renderer* r, void* strea
 extern "C" phe_status phe_renderer_ray_totals_async(const phe_renderer* r, uint64_t* hostTotals4, void* stream)
 {
 	if (!r || !r->allocation || !hostTotals4) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_ray_totals_async: no frame");
+	phe_status st = join_frames(r, (cudaStream_t)stream);
+	if (st) return st;
 	PHE_CUDA_TRY(cudaMemcpyAsync(hostTotals4, r->fb.rayTotals, 4 * sizeof(uint64_t), cudaMemcpyDeviceToHost,
 	                             (cudaStream_t)stream), "read ray totals");
 	return PHE_OK;
@@ -439,22 +652,41 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 	uint32_t L = numLights ? numLights : 1;
 	if (L != r->numLights) {
 		// Contribution and queue buffers scale with the light count.
+		drain_streams(r);
 		cudaStreamSynchronize(s);
 		phe_status st = allocate(r, r->resX, r->resY, L);
 		if (st) return st;
+	}
+	// Two frames in flight, unless per-kernel timing wants the frame in order on one stream.
+	const bool pipelined = r->inFlight == 2 && !r->timing;
+	const uint32_t j = pipelined ? r->nextSlot : 0;
+	const FrameBuffers& fb = j ? r->fb1 : r->fb;
+	FrameParamsDev* dParams = j ? r->dParams1 : r->dParams;
+	cudaStream_t X = pipelined ? r->travStream[j] : s;   // traversal kernels
+	cudaStream_t R = pipelined ? r->resolveStream : s;   // resolve + TAA
+	if (pipelined) {
+		// after the caller's work so far, and after the resolve that last read this slot's buffers
+		PHE_CUDA_TRY(cudaEventRecord(r->callEvent, s), "record caller work");
+		PHE_CUDA_TRY(cudaStreamWaitEvent(X, r->callEvent, 0), "order frame after caller work");
+		if (r->slotUsed[j]) PHE_CUDA_TRY(cudaStreamWaitEvent(X, r->resolveDone[j], 0), "wait for the slot");
+	} else {
+		phe_status st = join_frames(r, s);   // frames still in flight from before per-kernel timing
+		if (st) return st;
+		r->framePending = false;
 	}
 	// Pinned staging ring: a slot is rewritten only after its previous copy has been consumed.
 	uint32_t slot = r->paramSlot;
 	r->paramSlot = (slot + 1) % kParamSlots;
 	PHE_CUDA_TRY(cudaEventSynchronize(r->paramEvents[slot]), "wait for a free parameter slot");
 	FrameParamsDev& fp = r->hParams[slot];
-	// Camera motion: this frame writes the velocity on the side of its output history, the previous
-	// frame's velocity is on the other side; a camera equal to the previous one has velocity 0.
-	const uint32_t outSide = r->parity ^ 1u, inSide = r->parity;
+	// Camera motion: this frame writes the next entry of the velocity ring and reads the previous
+	// frame's; a camera equal to the previous one has velocity 0 (nothing written or read).
+	const uint32_t outSide = r->parity ^ 1u;
+	const uint32_t vOut = r->velNext, vIn = r->velLast;
 	const bool moving = r->hasPrevCam && std::memcmp(&r->prevCam, &r->cam, sizeof(phe_camera_def)) != 0;
 	fp.prevCam = r->hasPrevCam ? r->prevCam : r->cam;
-	fp.velocity = moving ? r->fb.velocity[outSide] : nullptr;
-	fp.prevVelocity = r->velocityZero[inSide] ? nullptr : r->fb.velocity[inSide];
+	fp.velocity = moving ? r->vel[vOut] : nullptr;
+	fp.prevVelocity = r->velZero[vIn] ? nullptr : r->vel[vIn];
 	fp.cam = r->cam;
 	fp.jitter[0] = r->jitter[0];
 	fp.jitter[1] = r->jitter[1];
@@ -468,14 +700,38 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 	fp.seed = r->seed;
 	std::memset(fp.lights, 0, sizeof(fp.lights));
 	if (numLights) std::memcpy(fp.lights, lights, sizeof(phe_sphere_light) * numLights);
-	{
-		phe_status gst = guard_side(r, outSide, s);   // this frame rewrites side outSide
-		if (gst) return gst;
-	}
-	PHE_CUDA_TRY(cudaMemcpyAsync(r->dParams, &fp, sizeof(FrameParamsDev), cudaMemcpyHostToDevice, s),
+	phe_status gst = guard_velocity(r, vOut, X);   // the traversal rewrites this velocity buffer
+	if (!gst) gst = guard_side(r, outSide, R);     // the resolve rewrites this colour / history side
+	if (gst) return gst;
+	PHE_CUDA_TRY(cudaMemcpyAsync(dParams, &fp, sizeof(FrameParamsDev), cudaMemcpyHostToDevice, X),
 	             "upload frame parameters");
-	PHE_CUDA_TRY(cudaEventRecord(r->paramEvents[slot], s), "record parameter slot");
-	if (r->useGraph) {
+	PHE_CUDA_TRY(cudaEventRecord(r->paramEvents[slot], X), "record parameter slot");
+	if (pipelined) {
+		cudaEvent_t t0 = nullptr, t1 = nullptr;
+		if (r->recordLatency) {
+			phe_status st = take_timing_event(r, &t0);
+			if (!st) st = take_timing_event(r, &t1);
+			if (st) return st;
+			PHE_CUDA_TRY(cudaEventRecord(t0, X), "record frame start");
+		}
+		phe_status st = launch_frame(r->scene, dParams, fb, r->resX, r->resY, X, nullptr, r->fused, r->shadowSchedule,
+		                             nullptr, kFrameTraversal);
+		if (st) return st;
+		PHE_CUDA_TRY(cudaEventRecord(r->travDone[j], X), "record frame traversal");
+		PHE_CUDA_TRY(cudaStreamWaitEvent(R, r->travDone[j], 0), "order resolve after traversal");
+		st = launch_frame(r->scene, dParams, fb, r->resX, r->resY, R, nullptr, r->fused, r->shadowSchedule, nullptr,
+		                  kFrameResolve);
+		if (st) return st;
+		PHE_CUDA_TRY(cudaEventRecord(r->resolveDone[j], R), "record frame end");
+		if (r->recordLatency) {
+			PHE_CUDA_TRY(cudaEventRecord(t1, R), "record frame end");
+			r->latencyPending.emplace_back(t0, t1);
+		}
+		r->slotUsed[j] = true;
+		r->lastSlot = j;
+		r->nextSlot = j ^ 1u;
+		r->framePending = true;
+	} else if (r->useGraph) {
 		if (r->graphExec && r->graphGeneration != r->scene->generation) {   // scene arrays or layout changed
 			cudaGraphExecDestroy(r->graphExec);
 			r->graphExec = nullptr;
@@ -502,6 +758,7 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 			r->graphGeneration = r->scene->generation;
 		}
 		PHE_CUDA_TRY(cudaGraphLaunch(r->graphExec, s), "launch frame graph");
+		r->lastSlot = 0;
 	} else {
 		phe_status st;
 		if (r->timing) {
@@ -515,8 +772,11 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 			                  r->shadowSchedule, &r->streams);
 		}
 		if (st) return st;
+		r->lastSlot = 0;
 	}
-	r->velocityZero[outSide] = !moving;
+	r->velZero[vOut] = !moving;
+	r->velLast = vOut;
+	r->velNext = (vOut + 1) % 3;
 	r->prevCam = r->cam;
 	r->hasPrevCam = true;
 	r->frame++;
@@ -532,16 +792,19 @@ extern "C" phe_status phe_renderer_result(const phe_renderer* r, phe_render_resu
 	out->color = (const float*)r->fb.color[r->parity];   // written by the last frame
 	out->history = (const float*)r->fb.history[r->parity];   // written by the last frame
 	out->rawColor = (const float*)r->fb.rawColor;
-	out->roughness = r->fb.roughness;
-	out->velocity = r->velocityZero[r->parity] ? nullptr : (const float*)r->fb.velocity[r->parity];
+	out->roughness = last_fb(r).roughness;
+	out->velocity = r->velZero[r->velLast] ? nullptr : (const float*)r->vel[r->velLast];
 	return PHE_OK;
 }
 
 extern "C" phe_status phe_renderer_ray_counts(const phe_renderer* r, uint64_t counts[4], void* stream)
 {
 	if (!r || !counts || !r->fb.counters) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_ray_counts: no frame");
+	phe_status st = join_frames(r, (cudaStream_t)stream);
+	if (st) return st;
 	uint32_t c[kNumCounters];
-	PHE_CUDA_TRY(cudaMemcpyAsync(c, r->fb.counters, sizeof(c), cudaMemcpyDeviceToHost, (cudaStream_t)stream), "read counters");
+	PHE_CUDA_TRY(cudaMemcpyAsync(c, last_fb(r).counters, sizeof(c), cudaMemcpyDeviceToHost, (cudaStream_t)stream),
+	             "read counters");
 	PHE_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream), "read counters");
 	counts[0] = (uint64_t)r->resX * r->resY;
 	counts[1] = c[kCtrShadow0];
@@ -558,8 +821,8 @@ static phe_status read_source(const phe_renderer* r, int which, const void** src
 	case 0: *src = r->fb.color[r->parity]; break;
 	case 1: *src = r->fb.history[r->parity]; break;
 	case 2: *src = r->fb.rawColor; break;
-	case 3: *src = r->fb.roughness; *bytes = P * sizeof(float); break;
-	case 4: *src = r->velocityZero[r->parity] ? nullptr : r->fb.velocity[r->parity]; *bytes = P * sizeof(float2); break;
+	case 3: *src = last_fb(r).roughness; *bytes = P * sizeof(float); break;
+	case 4: *src = r->velZero[r->velLast] ? nullptr : r->vel[r->velLast]; *bytes = P * sizeof(float2); break;
 	default: return fail(PHE_ERR_INVALID_ARGUMENT, "renderer read: which must be 0..4");
 	}
 	return PHE_OK;
@@ -572,6 +835,7 @@ extern "C" phe_status phe_renderer_read(const phe_renderer* r, int which, void* 
 	size_t bytes = 0;
 	phe_status st = read_source(r, which, &src, &bytes);
 	if (st) return st;
+	if ((st = join_frames(r, (cudaStream_t)stream))) return st;
 	if (!src) {   // a velocity that is 0 everywhere is not stored
 		PHE_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream), "read result");
 		std::memset(hostDst, 0, bytes);
@@ -597,19 +861,34 @@ extern "C" phe_status phe_renderer_read_async(phe_renderer* r, int which, void* 
 			PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->doneEvents[i], cudaEventDisableTiming), "create read event");
 			PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->sideDone[i], cudaEventDisableTiming), "create read event");
 		}
+		for (int i = 0; i < 3; i++)
+			PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->velDone[i], cudaEventDisableTiming), "create read event");
 		PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->readyEvent, cudaEventDisableTiming), "create read event");
 	}
-	// TAA colour, history and a stored velocity live on the side the last frame wrote; the next frame
-	// only reads that side, so the copy reads it in place and the frame after next waits for the copy.
+	// TAA colour and history live on the side the last frame wrote, a stored velocity in the last entry
+	// of the ring; the next frame only reads them, so the copy reads them in place and the frame that
+	// rewrites them waits for the copy. The copy waits for the last frame itself: with frames in flight
+	// the caller's stream is not ordered after them, and ordering it would hold back the next frame.
 	if (src && (which == 0 || which == 1 || which == 4)) {
-		const uint32_t side = r->parity;
-		PHE_CUDA_TRY(cudaEventRecord(r->readyEvent, s), "record frame end");
-		PHE_CUDA_TRY(cudaStreamWaitEvent(r->copyStream, r->readyEvent, 0), "order read-back");
+		if (r->framePending) {
+			PHE_CUDA_TRY(cudaStreamWaitEvent(r->copyStream, r->resolveDone[r->lastSlot], 0), "order read-back");
+		} else {
+			PHE_CUDA_TRY(cudaEventRecord(r->readyEvent, s), "record frame end");
+			PHE_CUDA_TRY(cudaStreamWaitEvent(r->copyStream, r->readyEvent, 0), "order read-back");
+		}
 		PHE_CUDA_TRY(cudaMemcpyAsync(hostDst, src, bytes, cudaMemcpyDeviceToHost, r->copyStream), "read result");
-		PHE_CUDA_TRY(cudaEventRecord(r->sideDone[side], r->copyStream), "record read-back");
-		r->sideGuard[side] = true;
+		if (which == 4) {
+			PHE_CUDA_TRY(cudaEventRecord(r->velDone[r->velLast], r->copyStream), "record read-back");
+			r->velGuard[r->velLast] = true;
+		} else {
+			PHE_CUDA_TRY(cudaEventRecord(r->sideDone[r->parity], r->copyStream), "record read-back");
+			r->sideGuard[r->parity] = true;
+		}
 		return PHE_OK;
 	}
+	// Raw colour and roughness are rewritten by the next frame: a snapshot on the caller's stream, which
+	// is first ordered after the last frame (with frames in flight this also orders the next frame after it).
+	if ((st = join_frames(r, s))) return st;
 	if (bytes > r->stagingBytes) {   // grow both slots once no copy uses them
 		if ((st = phe_renderer_read_wait(r))) return st;
 		for (int i = 0; i < 2; i++) {
@@ -643,6 +922,8 @@ extern "C" phe_status phe_renderer_read_wait(phe_renderer* r)
 		}
 	for (int i = 0; i < 2; i++)   // an event never recorded counts as complete
 		if (r->sideDone[i]) PHE_CUDA_TRY(cudaEventSynchronize(r->sideDone[i]), "wait for read-back");
+	for (int i = 0; i < 3; i++)
+		if (r->velDone[i]) PHE_CUDA_TRY(cudaEventSynchronize(r->velDone[i]), "wait for read-back");
 	return PHE_OK;
 }
 

@@ -699,7 +699,7 @@ phe_status prepare_frame()
 
 phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, const FrameBuffers& fb, uint32_t resX,
                         uint32_t resY, cudaStream_t stream, cudaEvent_t* ev, bool fused, int schedule,
-                        const FrameStreams* streams)
+                        const FrameStreams* streams, int parts)
 {
 	// Timed frames keep one stream so that the per-kernel events measure one kernel each.
 	const bool beside = schedule == PHE_SHADOWS_BESIDE_BOUNCE && streams && streams->side && !ev;
@@ -707,90 +707,94 @@ phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, c
 	int g[kGridCount];
 	for (int k = 0; k < kGridCount; k++)
 		if ((st = wave_grid(k, &g[k]))) return st;
-	PHE_CUDA_TRY(cudaMemsetAsync(fb.counters, 0, sizeof(uint32_t) * kNumCounters, stream), "clear frame counters");
 	int e = 0;
 	auto mark = [&]() { if (ev) cudaEventRecord(ev[e++], stream); };
 	DeviceInfo* dinfo = nullptr;
 	if ((st = device_info(&dinfo))) return st;
 	int binGrid = dinfo->numSMs * 4;
-	mark();
-	if (fused) {
-		const bool wide = scene->dev.nodes4 || scene->dev.nodes8;
-		auto primary = wide ? primary_kernel<true> : primary_kernel<false>;
-		auto anyQueue = wide ? any_queue_kernel<true> : any_queue_kernel<false>;
-		auto bounce = wide ? bounce_kernel<true> : bounce_kernel<false>;
-		// Persistent grids, but never more blocks than the frame's rays can keep busy: a small frame (a
-		// 256x256 render of the serving loop) then leaves the other SMs to concurrent requests.
-		const uint64_t P = (uint64_t)resX * resY;
-		auto clamp = [](int grid, uint64_t rays) {
-			return (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)grid, (rays + kWaveBlock - 1) / kWaveBlock));
-		};
-		const int gPrimary = clamp(g[wide ? kGridPrimaryWide : kGridPrimary], P);
-		const int gAny = clamp(g[wide ? kGridAnyQueueWide : kGridAnyQueue], 2 * (uint64_t)fb.capacityLP);
-		const int gBounce = clamp(g[wide ? kGridBounceWide : kGridBounce], P);
-		const phe_ray_in* rays1 = fb.shadowRays + fb.capacityLP;
-		const uint32_t* slots1 = fb.shadowSlots + fb.capacityLP;
-		primary<<<gPrimary, kWaveBlock, kStackSmem, stream>>>(scene->dev, dParams, fb, scene->status);
+	if (parts & kFrameTraversal) {
+		PHE_CUDA_TRY(cudaMemsetAsync(fb.counters, 0, sizeof(uint32_t) * kNumCounters, stream), "clear frame counters");
 		mark();
-		if (schedule != PHE_SHADOWS_MERGED) {
-			cudaStream_t shadowStream = stream;
-			if (beside) {
-				PHE_CUDA_TRY(cudaEventRecord(streams->fork, stream), "fork frame");
-				PHE_CUDA_TRY(cudaStreamWaitEvent(streams->side, streams->fork, 0), "fork frame");
-				shadowStream = streams->side;
+		if (fused) {
+			const bool wide = scene->dev.nodes4 || scene->dev.nodes8;
+			auto primary = wide ? primary_kernel<true> : primary_kernel<false>;
+			auto anyQueue = wide ? any_queue_kernel<true> : any_queue_kernel<false>;
+			auto bounce = wide ? bounce_kernel<true> : bounce_kernel<false>;
+			// Persistent grids, but never more blocks than the frame's rays can keep busy: a small frame (a
+			// 256x256 render of the serving loop) then leaves the other SMs to concurrent requests.
+			const uint64_t P = (uint64_t)resX * resY;
+			auto clamp = [](int grid, uint64_t rays) {
+				return (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)grid, (rays + kWaveBlock - 1) / kWaveBlock));
+			};
+			const int gPrimary = clamp(g[wide ? kGridPrimaryWide : kGridPrimary], P);
+			const int gAny = clamp(g[wide ? kGridAnyQueueWide : kGridAnyQueue], 2 * (uint64_t)fb.capacityLP);
+			const int gBounce = clamp(g[wide ? kGridBounceWide : kGridBounce], P);
+			const phe_ray_in* rays1 = fb.shadowRays + fb.capacityLP;
+			const uint32_t* slots1 = fb.shadowSlots + fb.capacityLP;
+			primary<<<gPrimary, kWaveBlock, kStackSmem, stream>>>(scene->dev, dParams, fb, scene->status);
+			mark();
+			if (schedule != PHE_SHADOWS_MERGED) {
+				cudaStream_t shadowStream = stream;
+				if (beside) {
+					PHE_CUDA_TRY(cudaEventRecord(streams->fork, stream), "fork frame");
+					PHE_CUDA_TRY(cudaStreamWaitEvent(streams->side, streams->fork, 0), "fork frame");
+					shadowStream = streams->side;
+				}
+				anyQueue<<<gAny, kWaveBlock, kStackSmem, shadowStream>>>(scene->dev, fb.shadowRays, fb.shadowSlots,
+				                                                 fb.counters + kCtrShadow0, nullptr, nullptr, nullptr,
+				                                                 fb.inLight, fb.counters + kCtrWork2, scene->status);
+				if (beside) PHE_CUDA_TRY(cudaEventRecord(streams->join, shadowStream), "join frame");
+				mark();
 			}
-			anyQueue<<<gAny, kWaveBlock, kStackSmem, shadowStream>>>(scene->dev, fb.shadowRays, fb.shadowSlots,
-			                                                 fb.counters + kCtrShadow0, nullptr, nullptr, nullptr,
-			                                                 fb.inLight, fb.counters + kCtrWork2, scene->status);
-			if (beside) PHE_CUDA_TRY(cudaEventRecord(streams->join, shadowStream), "join frame");
+			if (fb.sortWindow > 0) {
+				bin_bounce_kernel<<<binGrid, kBinBlock, 0, stream>>>(fb);
+				mark();
+			}
+			bounce<<<gBounce, kWaveBlock, kStackSmem, stream>>>(scene->dev, dParams, fb, scene->status);
 			mark();
-		}
-		if (fb.sortWindow > 0) {
-			bin_bounce_kernel<<<binGrid, kBinBlock, 0, stream>>>(fb);
+			if (schedule == PHE_SHADOWS_MERGED) {
+				// bounce shadows first: their incoherent rays start early and the primary ones fill the tail
+				anyQueue<<<gAny, kWaveBlock, kStackSmem, stream>>>(scene->dev, rays1, slots1, fb.counters + kCtrShadow1,
+				                                           fb.shadowRays, fb.shadowSlots, fb.counters + kCtrShadow0,
+				                                           fb.inLight, fb.counters + kCtrWork3, scene->status);
+			} else {
+				anyQueue<<<gAny, kWaveBlock, kStackSmem, stream>>>(scene->dev, rays1, slots1, fb.counters + kCtrShadow1, nullptr,
+				                                           nullptr, nullptr, fb.inLight, fb.counters + kCtrWork3,
+				                                           scene->status);
+			}
 			mark();
-		}
-		bounce<<<gBounce, kWaveBlock, kStackSmem, stream>>>(scene->dev, dParams, fb, scene->status);
-		mark();
-		if (schedule == PHE_SHADOWS_MERGED) {
-			// bounce shadows first: their incoherent rays start early and the primary ones fill the tail
-			anyQueue<<<gAny, kWaveBlock, kStackSmem, stream>>>(scene->dev, rays1, slots1, fb.counters + kCtrShadow1,
-			                                           fb.shadowRays, fb.shadowSlots, fb.counters + kCtrShadow0,
-			                                           fb.inLight, fb.counters + kCtrWork3, scene->status);
+			if (beside) PHE_CUDA_TRY(cudaStreamWaitEvent(stream, streams->join, 0), "join frame");
 		} else {
-			anyQueue<<<gAny, kWaveBlock, kStackSmem, stream>>>(scene->dev, rays1, slots1, fb.counters + kCtrShadow1, nullptr,
-			                                           nullptr, nullptr, fb.inLight, fb.counters + kCtrWork3,
-			                                           scene->status);
-		}
-		mark();
-		if (beside) PHE_CUDA_TRY(cudaStreamWaitEvent(stream, streams->join, 0), "join frame");
-	} else {
-		primary_trace_kernel<<<g[kGridPrimaryTrace], kWaveBlock, kStackSmem, stream>>>(scene->dev, dParams, fb, scene->status);
-		mark();
-		primary_shade_kernel<<<g[kGridPrimaryShade], kWaveBlock, 0, stream>>>(scene->dev, dParams, fb);
-		mark();
-		any_refill_kernel<<<g[kGridAnyRefill], kWaveBlock, kStackSmem, stream>>>(scene->dev, fb.shadowRays, fb.shadowSlots,
-		                                                                 fb.counters + kCtrShadow0, fb.inLight,
-		                                                                 fb.counters + kCtrWork2, fb.refill,
-		                                                                 scene->status);
-		mark();
-		if (fb.sortWindow > 0) {
-			bin_bounce_kernel<<<binGrid, kBinBlock, 0, stream>>>(fb);
+			primary_trace_kernel<<<g[kGridPrimaryTrace], kWaveBlock, kStackSmem, stream>>>(scene->dev, dParams, fb, scene->status);
+			mark();
+			primary_shade_kernel<<<g[kGridPrimaryShade], kWaveBlock, 0, stream>>>(scene->dev, dParams, fb);
+			mark();
+			any_refill_kernel<<<g[kGridAnyRefill], kWaveBlock, kStackSmem, stream>>>(scene->dev, fb.shadowRays, fb.shadowSlots,
+			                                                                 fb.counters + kCtrShadow0, fb.inLight,
+			                                                                 fb.counters + kCtrWork2, fb.refill,
+			                                                                 scene->status);
+			mark();
+			if (fb.sortWindow > 0) {
+				bin_bounce_kernel<<<binGrid, kBinBlock, 0, stream>>>(fb);
+				mark();
+			}
+			bounce_trace_kernel<<<g[kGridBounceTrace], kWaveBlock, kStackSmem, stream>>>(scene->dev, fb, scene->status);
+			mark();
+			bounce_shade_kernel<<<g[kGridBounceShade], kWaveBlock, 0, stream>>>(scene->dev, dParams, fb);
+			mark();
+			any_refill_kernel<<<g[kGridAnyRefill], kWaveBlock, kStackSmem, stream>>>(scene->dev, fb.shadowRays + fb.capacityLP,
+			                                                                 fb.shadowSlots + fb.capacityLP,
+			                                                                 fb.counters + kCtrShadow1, fb.inLight,
+			                                                                 fb.counters + kCtrWork3, fb.refill,
+			                                                                 scene->status);
 			mark();
 		}
-		bounce_trace_kernel<<<g[kGridBounceTrace], kWaveBlock, kStackSmem, stream>>>(scene->dev, fb, scene->status);
-		mark();
-		bounce_shade_kernel<<<g[kGridBounceShade], kWaveBlock, 0, stream>>>(scene->dev, dParams, fb);
-		mark();
-		any_refill_kernel<<<g[kGridAnyRefill], kWaveBlock, kStackSmem, stream>>>(scene->dev, fb.shadowRays + fb.capacityLP,
-		                                                                 fb.shadowSlots + fb.capacityLP,
-		                                                                 fb.counters + kCtrShadow1, fb.inLight,
-		                                                                 fb.counters + kCtrWork3, fb.refill,
-		                                                                 scene->status);
+	}
+	if (parts & kFrameResolve) {
+		const uint32_t resolveGrid = (uint32_t)(((uint64_t)resX * resY + 2 * kResolveBlock - 1) / (2 * kResolveBlock));
+		resolve_taa_kernel<<<resolveGrid, kResolveBlock, 0, stream>>>(dParams, fb);
 		mark();
 	}
-	const uint32_t resolveGrid = (uint32_t)(((uint64_t)resX * resY + 2 * kResolveBlock - 1) / (2 * kResolveBlock));
-	resolve_taa_kernel<<<resolveGrid, kResolveBlock, 0, stream>>>(dParams, fb);
-	mark();
 	PHE_CUDA_TRY(cudaGetLastError(), "frame kernel launch");
 	return PHE_OK;
 }

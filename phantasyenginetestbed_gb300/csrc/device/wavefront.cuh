@@ -53,7 +53,6 @@ struct FrameBuffers {
 	float* roughness;         // [P] roughness at the primary hit (0 on a miss), read by TAA
 	float4* rawColor;         // [P] resolved colour before TAA
 	float4* history[2];       // [P] TAA history ping-pong (rgb + effective sample count)
-	float2* velocity[2];      // [P] uv velocity ping-pong (same side as the history)
 	float4* color[2];         // [P] TAA output ping-pong (same side as the history it was blended into)
 	uint32_t* counters;       // [kNumCounters]
 	uint32_t capacityLP;      // L * P
@@ -91,8 +90,11 @@ struct FrameStreams {
 	cudaStream_t side = nullptr;
 	cudaEvent_t fork = nullptr, join = nullptr;
 };
+// `parts` selects the traversal kernels (counter reset, primary, bounce, shadow passes), the resolve +
+// TAA kernel, or both: a renderer with two frames in flight launches them on different streams.
+enum { kFrameTraversal = 1, kFrameResolve = 2, kFrameAll = 3 };
 phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, const FrameBuffers& fb, uint32_t resX,
                         uint32_t resY, cudaStream_t stream, cudaEvent_t* events, bool fused, int schedule,
-                        const FrameStreams* streams);
+                        const FrameStreams* streams, int parts = kFrameAll);
 
 } // namespace phe_gb300

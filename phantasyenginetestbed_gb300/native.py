@@ -177,6 +177,10 @@ SIGNATURES: dict[str, tuple] = {
     "phe_renderer_set_shadow_schedule": (_I32, [_VP, _I32]),
     "phe_renderer_read_async": (_I32, [_VP, _I32, _VP, _VP]),
     "phe_renderer_read_wait": (_I32, [_VP]),
+    "phe_renderer_set_frames_in_flight": (_I32, [_VP, _I32]),
+    "phe_renderer_join": (_I32, [_VP, _VP]),
+    "phe_renderer_set_latency_recording": (_I32, [_VP, _I32]),
+    "phe_renderer_frame_latencies": (_I32, [_VP, _PF, _U32, C.POINTER(_U32)]),
     "phe_batch_default_params": (None, [C.POINTER(BatchParams)]),
     "phe_batch_create": (_I32, [C.POINTER(_VP), _U32, C.POINTER(BatchItem), _U32, C.POINTER(BatchParams), C.POINTER(_VP)]),
     "phe_batch_update": (_I32, [_VP, C.POINTER(BatchItem), _U32]),

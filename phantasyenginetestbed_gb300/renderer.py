@@ -132,6 +132,31 @@ class CudaTracerRenderer:
         check(lib().phe_renderer_set_pipeline(self.handle, 1 if fused else 0, refill, sort_window),
               "phe_renderer_set_pipeline")
 
+    def set_frames_in_flight(self, frames: int) -> None:
+        """1 (default): each frame runs on the caller's stream. 2: consecutive frames overlap on the
+        renderer's own streams (same results); the caller's stream is not ordered after a frame: reads
+        wait for it, join() orders a stream after the last frame."""
+        check(lib().phe_renderer_set_frames_in_flight(self.handle, int(frames)), "phe_renderer_set_frames_in_flight")
+
+    def join(self, stream=None) -> None:
+        """Orders `stream` after the last frame (a no-op with one frame in flight)."""
+        check(lib().phe_renderer_join(self.handle, _stream(stream)), "phe_renderer_join")
+
+    def set_latency_recording(self, enable: bool) -> None:
+        """With two frames in flight: record each frame's GPU latency (first kernel start to resolve end)."""
+        check(lib().phe_renderer_set_latency_recording(self.handle, 1 if enable else 0),
+              "phe_renderer_set_latency_recording")
+
+    def frame_latencies(self) -> np.ndarray:
+        """Latencies (ms) of the frames recorded since the last call, waiting for them."""
+        n = C.c_uint32(0)
+        check(lib().phe_renderer_frame_latencies(self.handle, None, 0, C.byref(n)), "phe_renderer_frame_latencies")
+        out = np.zeros(n.value, np.float32)
+        if n.value:
+            buf = out.ctypes.data_as(C.POINTER(C.c_float))
+            check(lib().phe_renderer_frame_latencies(self.handle, buf, n.value, C.byref(n)), "phe_renderer_frame_latencies")
+        return out[: n.value]
+
     def set_shadow_schedule(self, schedule: int = 2) -> None:
         """SHADOWS_IN_ORDER, SHADOWS_BESIDE_BOUNCE or SHADOWS_MERGED (default); same results."""
         check(lib().phe_renderer_set_shadow_schedule(self.handle, int(schedule)), "phe_renderer_set_shadow_schedule")

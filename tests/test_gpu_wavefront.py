@@ -406,3 +406,82 @@ def test_async_read_back_of_velocity_and_colour_with_a_moving_camera():
     for f in range(len(path)):
         assert np.array_equal(col[f], want[f][0]), f
         assert np.array_equal(vel[f], want[f][1]), f
+
+
+def _flight_plan(s, cam_pos):
+    """A frame sequence with camera motion, a TAA reset and a light-count change (2 lights, then 1)."""
+    k = s.scale
+    d0 = np.array(C1_CAM["dir"], np.float64)
+    d1 = d0 + np.array([0.03, 0.0, 0.01])
+    p0 = np.array(cam_pos, np.float64)
+    one = make_lights(np.asarray([(0.5, 0.5, 2.0)], np.float32) * np.float32(k), range_=1000.0 * k)
+    two = make_lights(np.asarray([(0.5, 0.5, 2.0), (0.1, 0.9, 1.0)], np.float32) * np.float32(k), range_=1000.0 * k)
+    moved = p0 + [0.008 * k, 0.0, 0.002 * k]
+    # (camera position, direction, lights, reset TAA before the frame)
+    return [(p0, d0, one, False), (p0, d0, one, False), (p0 + [0.004 * k, 0.001 * k, 0.0], d0, one, False),
+            (moved, d1, two, False), (moved, d1, two, False), (moved, d1, two, True), (moved, d1, one, False),
+            (p0, d0, one, False), (p0, d0, one, False)]
+
+
+def _flight_frame(r, f, step, res, stream):
+    pos, d, lights, reset = step
+    if reset:
+        r.resetTAA(stream=stream)
+    up = np.cross(np.cross(d, np.array(C1_CAM["up"])), d)
+    up = -up if up[2] < 0 else up
+    cam_f = O.camera_def(pos, d, up, math.radians(60), res)
+    r.set_camera_def(cam_struct(cam_f), pos, P.halton_jitter(f))
+    r.render(lights, stream=stream)
+
+
+@pytest.mark.parametrize("res", [(256, 160), (120, 40)])
+def test_frames_in_flight_give_the_sequential_frames(res):
+    """Two frames in flight (consecutive frames overlapping on the renderer's own streams) give, frame
+    after frame, the bytes of the same sequence rendered one frame at a time: TAA colour read back
+    asynchronously in place while later frames render, and, with blocking reads after every frame, raw
+    colour, history, roughness, velocity and ray counts. Latency recording returns one positive figure
+    per frame."""
+    import torch
+    s, b, datas, scene, cam, cam_pos, lights, seq = _setup("c2_256_2000", res, [(0.5, 0.5, 2.0)], graph=True)
+    pip = CudaTracerRenderer()
+    pip.setStaticScene(scene)
+    pip.setTargetResolution(res)
+    pip.set_frames_in_flight(2)
+    plan = _flight_plan(s, cam_pos)
+    stream = torch.cuda.Stream()
+    host = lambda: torch.empty((res[1], res[0], 4), dtype=torch.float32, pin_memory=True).numpy()
+    # pass 1: only asynchronous in-place colour reads while the frames run (overlapped on `pip`)
+    colours = {}
+    for name, r in (("seq", seq), ("pip", pip)):
+        r.set_seed(21, 0)
+        r.resetTAA(stream=stream)
+        if r is pip:
+            r.set_latency_recording(True)
+        colours[name] = [host() for _ in plan]
+        for f, step in enumerate(plan):
+            _flight_frame(r, f, step, res, stream)
+            r.read_async(colours[name][f], READ_COLOR, stream=stream)
+        r.read_wait()
+    for f in range(len(plan)):
+        assert np.array_equal(colours["seq"][f], colours["pip"][f]), f
+    lat = pip.frame_latencies()
+    pip.set_latency_recording(False)
+    assert len(lat) == len(plan) and np.all(lat > 0), lat
+    # pass 2: blocking reads of every output after every frame
+    for name, r in (("seq", seq), ("pip", pip)):
+        r.set_seed(22, 0)
+        r.resetTAA(stream=stream)
+    for f, step in enumerate(plan):
+        got = []
+        for r in (seq, pip):
+            _flight_frame(r, f, step, res, stream)
+            got.append([r.read(w, stream=stream) for w in (READ_COLOR, READ_HISTORY, READ_RAW, READ_ROUGHNESS,
+                                                             READ_VELOCITY)] + [r.ray_counts(stream=stream)])
+        for a, c in zip(*got):
+            assert np.array_equal(a, c), f
+    pip.join(stream)
+    stream.synchronize()
+    pip.set_frames_in_flight(1)   # back to one frame: the same renderer keeps rendering the sequence
+    _flight_frame(pip, len(plan), plan[0], res, stream)
+    _flight_frame(seq, len(plan), plan[0], res, stream)
+    assert np.array_equal(pip.read(READ_COLOR, stream=stream), seq.read(READ_COLOR, stream=stream))
