@@ -15,7 +15,14 @@ from __future__ import annotations
 
 import ctypes as C
 import math
+import os
 from dataclasses import dataclass
+
+# Hardware work queues between the host and the GPU (read when the CUDA context is created; a value the
+# process already set is kept). The serving loop runs a stream per render slot beside its query waves:
+# with the default of 8 queues those streams share queues and wait on each other, and 32 gave 5% more
+# served rays/s (4,905 vs 4,669 Mrays/s at 8,000 req/s); single-stream work is unaffected.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 import numpy as np
 

@@ -336,6 +336,11 @@ extern "C" phe_status phe_renderer_set_shadow_schedule(phe_renderer* r, int sche
 	if (!r) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_set_shadow_schedule: null renderer");
 	if (schedule != PHE_SHADOWS_IN_ORDER && schedule != PHE_SHADOWS_BESIDE_BOUNCE && schedule != PHE_SHADOWS_MERGED)
 		return fail(PHE_ERR_INVALID_ARGUMENT, "unknown shadow schedule %d", schedule);
+	if (schedule == PHE_SHADOWS_BESIDE_BOUNCE && !r->streams.side) {
+		PHE_CUDA_TRY(cudaStreamCreateWithFlags(&r->streams.side, cudaStreamNonBlocking), "create renderer stream");
+		PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->streams.fork, cudaEventDisableTiming), "create renderer event");
+		PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->streams.join, cudaEventDisableTiming), "create renderer event");
+	}
 	if (schedule != r->shadowSchedule && r->graphExec) {
 		cudaGraphExecDestroy(r->graphExec);
 		r->graphExec = nullptr;
@@ -383,13 +388,11 @@ extern "C" phe_status phe_renderer_create(phe_renderer** out)
 		return cuda_fail(e, "allocate frame parameters");
 	}
 	std::memset(r->hParams, 0, sizeof(FrameParamsDev) * kParamSlots);
-	if (cudaStreamCreateWithFlags(&r->streams.side, cudaStreamNonBlocking) != cudaSuccess ||
-	    cudaEventCreateWithFlags(&r->streams.fork, cudaEventDisableTiming) != cudaSuccess ||
-	    cudaEventCreateWithFlags(&r->streams.join, cudaEventDisableTiming) != cudaSuccess) {
-		cudaError_t e2 = cudaGetLastError();
-		phe_renderer_destroy(r);
-		return cuda_fail(e2, "create renderer streams");
-	}
+	// No stream of its own yet: CUDA maps streams onto a few hardware queues in creation order, so
+	// streams that sit unused (the side stream of a schedule not chosen) would make the streams of
+	// concurrent renderers share queues and wait on each other. The side stream comes with the
+	// BESIDE_BOUNCE schedule, the frame streams with two frames in flight, the copy stream with the
+	// first asynchronous read.
 	*out = r;
 	return PHE_OK;
 }
