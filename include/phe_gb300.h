@@ -418,8 +418,9 @@ phe_status phe_renderer_kernel_times(phe_renderer* renderer, double msTotal[8], 
  * Consecutive frames overlap on the GPU; every frame gives exactly the bytes it gives with 1. The
  * caller's stream is NOT ordered after the frame: phe_renderer_read / read_async / ray_counts /
  * reset_taa / the ray-total calls wait for the last frame themselves, phe_renderer_join orders a stream
- * after it (needed before using the pointers of phe_renderer_result on the GPU). Frames timed per
- * kernel run in order on the caller's stream, and the BESIDE_BOUNCE shadow schedule runs IN_ORDER.
+ * after it (needed before using the pointers of phe_renderer_result on the GPU). Frames in flight are
+ * launched directly (no graph replay); frames timed per kernel run in order on the caller's stream, and
+ * the BESIDE_BOUNCE shadow schedule runs IN_ORDER. phe_scene_destroy waits for all device work.
  * Changing the setting waits for the frames in flight; 2 adds a second set of per-frame buffers
  * (~410 MB at 1080p with one light). */
 phe_status phe_renderer_set_frames_in_flight(phe_renderer* renderer, int frames);

@@ -444,6 +444,9 @@ extern "C" phe_status phe_scene_set_materials_and_textures(phe_scene* scene, con
 extern "C" phe_status phe_scene_destroy(phe_scene* scene)
 {
 	if (!scene) return PHE_OK;
+	// Work on any stream may still read the scene: a renderer's own streams with two frames in flight
+	// are not ordered after the caller's.
+	cudaDeviceSynchronize();
 	if (scene->shading) cudaFree(scene->shading);
 	cudaError_t e = cudaFree(scene->allocation);
 	delete scene;
