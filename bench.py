@@ -69,6 +69,8 @@ def parse():
     ap.add_argument("--pipeline", choices=["fused", "split"], default="fused",
                     help="fused: traversal + shading in one kernel per bounce (4 kernels with merged shadows); split: 7 kernels")
     ap.add_argument("--refill", type=int, default=28, help="lane-refill threshold of the split pipeline")
+    ap.add_argument("--frame-parts", type=int, default=2, choices=(1, 2),
+                    help="frame: 2 = the even and odd tile rows run as two overlapping parts (same bytes), 1 = whole")
     ap.add_argument("--frames-in-flight", type=int, default=1, choices=(1, 2),
                     help="frame: 2 = consecutive frames overlap on the renderer's own streams (same bytes); "
                          "with 1, the line also reports 2 in flight without L2 flushes as a secondary figure")
@@ -342,7 +344,7 @@ def frame_roofline(dominant, entry, clock, num_sms, builder, layout) -> dict:
     return out
 
 
-def two_in_flight(r, frame, stream, first, steps, rays_per_frame):
+def two_in_flight(r, frame, stream, first, steps, rays_per_frame, parts=1):
     """Secondary figures with two frames in flight (consecutive frames overlapping on the renderer's own
     streams, the same bytes as one at a time): device throughput over `steps` frames (CUDA events from
     before the first frame to the join after the last), per-frame GPU latency from the renderer's
@@ -351,6 +353,7 @@ def two_in_flight(r, frame, stream, first, steps, rays_per_frame):
     stream would run inside the next frame."""
     import torch
     from phantasyenginetestbed_gb300.renderer import READ_COLOR
+    r.set_frame_parts(1)   # the two modes do not combine
     r.set_frames_in_flight(2)
     try:
         for k in range(100):   # the first pipelined frames after the switch run slower in some runs
@@ -382,6 +385,7 @@ def two_in_flight(r, frame, stream, first, steps, rays_per_frame):
         e2e_s = time.perf_counter() - t0
     finally:
         r.set_frames_in_flight(1)
+        r.set_frame_parts(parts)
     return {"Mrays_s": round(rays_per_frame * steps / (ms / 1e3) / 1e6, 2), "ms_per_frame": round(ms / steps, 4),
             "latency_ms": {"p50": round(lat[len(lat) // 2], 4), "p99": round(lat[min(len(lat) - 1, int(0.99 * len(lat)))], 4),
                            "of": "per frame on the GPU, first kernel start to resolve end"},
@@ -408,6 +412,7 @@ def run_ours(args, world, rank, local):
     r.set_shadow_schedule({"in-order": 0, "beside": 1, "merged": 2}[args.shadows])
     r.setStaticScene(scene)
     r.setTargetResolution(RES)
+    r.set_frame_parts(args.frame_parts)
     r.set_frames_in_flight(args.frames_in_flight)
     r.set_seed(SEED, 0)
     r.resetTAA()
@@ -511,7 +516,8 @@ def run_ours(args, world, rank, local):
         frame(first + k)
         r.read(READ_COLOR, out=host_imgs[0], stream=stream)
     e2e_blocking = rays_per_frame * args.steps * world / (time.perf_counter() - t0) / 1e6
-    overlap = two_in_flight(r, frame, stream, first, args.steps, rays_per_frame) if inflight == 1 else None
+    overlap = (two_in_flight(r, frame, stream, first, args.steps, rays_per_frame, args.frame_parts)
+               if inflight == 1 else None)
 
     if rank != 0:
         if dist:
@@ -570,7 +576,7 @@ def run_ours(args, world, rank, local):
         "data": FRAME_DATA,
         "config": frame_config(s, b, builder, world),
         "frame": {"rays_per_frame": round(rays_per_frame, 1), "rays_by_pass": {k: round(v, 1) for k, v in stage_rays.items()},
-                  "frames_in_flight": inflight, "two_frames_in_flight": overlap,
+                  "frame_parts": args.frame_parts, "frames_in_flight": inflight, "two_frames_in_flight": overlap,
                   "cuda_graph": not args.no_graph and inflight == 1,
                   "pipeline": args.pipeline, "refill_threshold": args.refill,
                   "sort_window": args.sort_window, "sbvh_build_s": round(build_s, 2), "node_layout": args.layout,

@@ -41,6 +41,13 @@ struct phe_renderer {
 	bool slotUsed[2] = {false, false};   // resolveDone[slot] marks the last frame that used the slot
 	uint32_t nextSlot = 0, lastSlot = 0;
 	bool framePending = false;           // a frame in flight that no caller stream has been ordered after
+	// A frame split into two parts (phe_renderer_set_frame_parts): part 1 (the odd tile rows) runs on
+	// partStream beside part 0 on the caller's stream, with the queues and counters of fb1 and the
+	// per-pixel buffers of fb; the caller's stream joins it at the end of the frame.
+	int frameParts = 1;
+	bool lastSplit = false;              // the last frame ran as two parts
+	cudaStream_t partStream = nullptr;
+	cudaEvent_t partFork = nullptr, partJoin = nullptr;
 	// Latency recording of frames in flight: (start, end) event pairs, drained by frame_latencies.
 	bool recordLatency = false;
 	std::vector<cudaEvent_t> latencyPool;
@@ -186,12 +193,18 @@ static char* carve_per_frame(char* base, size_t P, size_t L, FrameBuffers& fb)
 	return p;
 }
 
-// Slot 1 shares everything with slot 0 but its per-frame buffers.
+// Slot 1 shares everything with slot 0 but its per-frame buffers; as part 1 of a split frame it also
+// shares the per-pixel ones (the parts write disjoint pixels) and keeps only its queues and counters.
 static void make_fb1(phe_renderer* r)
 {
 	if (!r->allocation1) return;
 	r->fb1 = r->fb;
 	carve_per_frame((char*)r->allocation1, r->capacityP, r->capacityL, r->fb1);
+	if (r->frameParts == 2) {
+		r->fb1.contrib = r->fb.contrib;
+		r->fb1.inLight = r->fb.inLight;
+		r->fb1.roughness = r->fb.roughness;
+	}
 }
 
 static phe_status allocate_slot1(phe_renderer* r)
@@ -266,7 +279,7 @@ static phe_status allocate(phe_renderer* r, uint32_t resX, uint32_t resY, uint32
 	r->numLights = numLights;
 	if ((e = cudaMemset(base, 0, total)) != cudaSuccess) return cuda_fail(e, "clear frame buffers");
 	r->parity = 0;
-	if (r->inFlight == 2) return allocate_slot1(r);
+	if (r->inFlight == 2 || r->frameParts == 2) return allocate_slot1(r);
 	return PHE_OK;
 }
 
@@ -409,6 +422,9 @@ extern "C" phe_status phe_renderer_destroy(phe_renderer* r)
 	}
 	if (r->resolveStream) cudaStreamDestroy(r->resolveStream);
 	if (r->callEvent) cudaEventDestroy(r->callEvent);
+	if (r->partStream) cudaStreamDestroy(r->partStream);
+	if (r->partFork) cudaEventDestroy(r->partFork);
+	if (r->partJoin) cudaEventDestroy(r->partJoin);
 	for (cudaEvent_t e : r->latencyPool) cudaEventDestroy(e);
 	for (auto& pr : r->latencyPending) {
 		cudaEventDestroy(pr.first);
@@ -544,6 +560,8 @@ extern "C" phe_status phe_renderer_set_frames_in_flight(phe_renderer* r, int fra
 {
 	if (!r) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_set_frames_in_flight: null renderer");
 	if (frames != 1 && frames != 2) return fail(PHE_ERR_INVALID_ARGUMENT, "frames in flight must be 1 or 2");
+	if (frames == 2 && r->frameParts == 2)
+		return fail(PHE_ERR_INVALID_ARGUMENT, "two frames in flight and split frames cannot be combined");
 	drain_streams(r);   // the slots and streams change hands only when no frame is in flight
 	r->slotUsed[0] = r->slotUsed[1] = false;
 	r->framePending = false;
@@ -562,6 +580,32 @@ extern "C" phe_status phe_renderer_set_frames_in_flight(phe_renderer* r, int fra
 		phe_status st = allocate_slot1(r);
 		if (st) return st;
 	}
+	return PHE_OK;
+}
+
+extern "C" phe_status phe_renderer_set_frame_parts(phe_renderer* r, int parts)
+{
+	if (!r) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_set_frame_parts: null renderer");
+	if (parts != 1 && parts != 2) return fail(PHE_ERR_INVALID_ARGUMENT, "frame parts must be 1 or 2");
+	if (parts == 2 && r->inFlight == 2)
+		return fail(PHE_ERR_INVALID_ARGUMENT, "two frames in flight and split frames cannot be combined");
+	if (parts == r->frameParts) return PHE_OK;
+	cudaDeviceSynchronize();   // part 1's buffers change role
+	if (r->graphExec) {
+		cudaGraphExecDestroy(r->graphExec);
+		r->graphExec = nullptr;
+	}
+	r->frameParts = parts;
+	if (parts == 2) {
+		if (!r->partStream) {
+			PHE_CUDA_TRY(cudaStreamCreateWithFlags(&r->partStream, cudaStreamNonBlocking), "create part stream");
+			PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->partFork, cudaEventDisableTiming), "create part event");
+			PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->partJoin, cudaEventDisableTiming), "create part event");
+		}
+		phe_status st = allocate_slot1(r);
+		if (st) return st;
+	}
+	make_fb1(r);
 	return PHE_OK;
 }
 
@@ -640,6 +684,26 @@ extern "C" phe_status phe_renderer_ray_totals_async(const phe_renderer* r, uint6
 	return PHE_OK;
 }
 
+// One frame on `s`: whole, or split into its two parts, part 1 on the part stream between a fork and a
+// join on `s` (the same calls capture a split frame into a graph).
+static phe_status launch_whole_or_split(phe_renderer* r, cudaStream_t s, bool split, uint32_t n0, uint32_t n1)
+{
+	if (!split)
+		return launch_frame(r->scene, r->dParams, r->fb, r->resX, r->resY, s, nullptr, r->fused, r->shadowSchedule,
+		                    &r->streams);
+	PHE_CUDA_TRY(cudaEventRecord(r->partFork, s), "fork frame parts");
+	PHE_CUDA_TRY(cudaStreamWaitEvent(r->partStream, r->partFork, 0), "fork frame parts");
+	phe_status st = launch_frame(r->scene, r->dParams, r->fb, r->resX, r->resY, s, nullptr, r->fused,
+	                             r->shadowSchedule, nullptr, kFrameAll, n0);
+	if (st) return st;
+	st = launch_frame(r->scene, r->dParams1, r->fb1, r->resX, r->resY, r->partStream, nullptr, r->fused,
+	                  r->shadowSchedule, nullptr, kFrameAll, n1);
+	if (st) return st;
+	PHE_CUDA_TRY(cudaEventRecord(r->partJoin, r->partStream), "join frame parts");
+	PHE_CUDA_TRY(cudaStreamWaitEvent(s, r->partJoin, 0), "join frame parts");
+	return PHE_OK;
+}
+
 extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_light* lights, uint32_t numLights, void* stream)
 {
 	if (!r) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_render: null renderer");
@@ -667,6 +731,12 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 	FrameParamsDev* dParams = j ? r->dParams1 : r->dParams;
 	cudaStream_t X = pipelined ? r->travStream[j] : s;   // traversal kernels
 	cudaStream_t R = pipelined ? r->resolveStream : s;   // resolve + TAA
+	// A split frame: the even tile rows on `s`, the odd ones on the part stream (fused pipeline only;
+	// frames timed per kernel stay whole).
+	const uint32_t tileRows = r->resY / 8u;
+	const bool split = !pipelined && r->frameParts == 2 && r->fused && !r->timing && tileRows >= 2;
+	const uint32_t n0 = split ? (tileRows + 1) / 2 * 8u * r->resX : r->resX * r->resY;
+	const uint32_t n1 = split ? tileRows / 2 * 8u * r->resX : 0u;
 	if (pipelined) {
 		// after the caller's work so far, and after the resolve that last read this slot's buffers
 		PHE_CUDA_TRY(cudaEventRecord(r->callEvent, s), "record caller work");
@@ -701,6 +771,10 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 	fp.frame = r->frame;
 	fp.parity = r->parity;
 	fp.seed = r->seed;
+	fp.part = 0;
+	fp.parts = split ? 2u : 1u;
+	fp.partPixels = n0;
+	fp.pad = 0;
 	std::memset(fp.lights, 0, sizeof(fp.lights));
 	if (numLights) std::memcpy(fp.lights, lights, sizeof(phe_sphere_light) * numLights);
 	phe_status gst = guard_velocity(r, vOut, X);   // the traversal rewrites this velocity buffer
@@ -709,6 +783,18 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 	PHE_CUDA_TRY(cudaMemcpyAsync(dParams, &fp, sizeof(FrameParamsDev), cudaMemcpyHostToDevice, X),
 	             "upload frame parameters");
 	PHE_CUDA_TRY(cudaEventRecord(r->paramEvents[slot], X), "record parameter slot");
+	if (split) {   // part 1's parameters: the same but for its part index and pixel count
+		const uint32_t slot1 = r->paramSlot;
+		r->paramSlot = (slot1 + 1) % kParamSlots;
+		PHE_CUDA_TRY(cudaEventSynchronize(r->paramEvents[slot1]), "wait for a free parameter slot");
+		FrameParamsDev& fp1 = r->hParams[slot1];
+		fp1 = fp;
+		fp1.part = 1;
+		fp1.partPixels = n1;
+		PHE_CUDA_TRY(cudaMemcpyAsync(r->dParams1, &fp1, sizeof(FrameParamsDev), cudaMemcpyHostToDevice, s),
+		             "upload frame parameters");
+		PHE_CUDA_TRY(cudaEventRecord(r->paramEvents[slot1], s), "record parameter slot");
+	}
 	if (pipelined) {
 		cudaEvent_t t0 = nullptr, t1 = nullptr;
 		if (r->recordLatency) {
@@ -748,8 +834,7 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 			cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
 			phe_status st = PHE_OK;
 			if (e == cudaSuccess) {
-				st = launch_frame(r->scene, r->dParams, r->fb, r->resX, r->resY, cap, nullptr, r->fused,
-				                  r->shadowSchedule, &r->streams);
+				st = launch_whole_or_split(r, cap, split, n0, n1);
 				e = cudaStreamEndCapture(cap, &g);
 			}
 			cudaStreamDestroy(cap);
@@ -771,12 +856,12 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 			                  nullptr);
 			r->pendingTimes = true;
 		} else {
-			st = launch_frame(r->scene, r->dParams, r->fb, r->resX, r->resY, s, nullptr, r->fused,
-			                  r->shadowSchedule, &r->streams);
+			st = launch_whole_or_split(r, s, split, n0, n1);
 		}
 		if (st) return st;
 		r->lastSlot = 0;
 	}
+	r->lastSplit = split;
 	r->velZero[vOut] = !moving;
 	r->velLast = vOut;
 	r->velNext = (vOut + 1) % 3;
@@ -806,13 +891,17 @@ extern "C" phe_status phe_renderer_ray_counts(const phe_renderer* r, uint64_t co
 	phe_status st = join_frames(r, (cudaStream_t)stream);
 	if (st) return st;
 	uint32_t c[kNumCounters];
+	uint32_t c1[kNumCounters] = {};
 	PHE_CUDA_TRY(cudaMemcpyAsync(c, last_fb(r).counters, sizeof(c), cudaMemcpyDeviceToHost, (cudaStream_t)stream),
 	             "read counters");
+	if (r->lastSplit)   // part 1's queues
+		PHE_CUDA_TRY(cudaMemcpyAsync(c1, r->fb1.counters, sizeof(c1), cudaMemcpyDeviceToHost, (cudaStream_t)stream),
+		             "read counters");
 	PHE_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream), "read counters");
 	counts[0] = (uint64_t)r->resX * r->resY;
-	counts[1] = c[kCtrShadow0];
-	counts[2] = c[kCtrBounce];
-	counts[3] = c[kCtrShadow1];
+	counts[1] = (uint64_t)c[kCtrShadow0] + c1[kCtrShadow0];
+	counts[2] = (uint64_t)c[kCtrBounce] + c1[kCtrBounce];
+	counts[3] = (uint64_t)c[kCtrShadow1] + c1[kCtrShadow1];
 	return PHE_OK;
 }
 

@@ -132,20 +132,21 @@ __global__ void __launch_bounds__(kWaveBlock, kWaveMinBlocks) primary_kernel(Dev
                                                              FrameBuffers fb, uint32_t* __restrict__ status)
 {
 	const FrameParamsDev& fp = *fpp;
-	const uint32_t P = fp.numPixels, W = fp.resX, L = fp.numLights;
+	const uint32_t P = fp.numPixels, W = fp.resX, L = fp.numLights, n = fp.partPixels;
 	uint32_t* work = fb.counters + kCtrWork0;
 	for (;;) {
 		uint32_t base = 0;
 		if (lane_id() == 0) base = atomicAdd(work, 32u);
 		base = __shfl_sync(0xFFFFFFFFu, base, 0);
-		if (base >= P) break;
+		if (base >= n) break;
 		uint32_t i = base + lane_id();
-		bool active = i < P;
-		// 8x8-tile-major ray order (getRayIdx, CudaDeviceHelpers.cuh:49-62): coherent warps
+		bool active = i < n;
+		// 8x8-tile-major ray order (getRayIdx, CudaDeviceHelpers.cuh:49-62): coherent warps; this part's
+		// tile rows interleave with the other parts'
 		uint32_t tile = i >> 6, within = i & 63u;
 		uint32_t tilesX = W >> 3;
 		uint32_t x = (tile % tilesX) * 8u + (within & 7u);
-		uint32_t y = (tile / tilesX) * 8u + (within >> 3);
+		uint32_t y = ((tile / tilesX) * fp.parts + fp.part) * 8u + (within >> 3);
 		uint32_t pid = y * W + x;
 		RayState r;
 		HitRecord h;
@@ -551,17 +552,24 @@ __global__ void __launch_bounds__(kResolveBlock, kResolveMinBlocks)
 resolve_taa_kernel(const FrameParamsDev* __restrict__ fpp, FrameBuffers fb)
 {
 	const FrameParamsDev& fp = *fpp;
-	const uint32_t P = fp.numPixels, L = fp.numLights;
-	const uint32_t p0 = blockIdx.x * (2u * kResolveBlock) + threadIdx.x, p1 = p0 + kResolveBlock;
-	if (p0 >= P) return;
-	if (p0 == 0) {
-		atomicAdd(&fb.rayTotals[0], (unsigned long long)P);
+	const uint32_t P = fp.numPixels, L = fp.numLights, np = fp.partPixels, W = fp.resX;
+	// The thread's two pixels, indices q0 and q1 into this part's pixels in row order (the part's rows
+	// are its tile rows, which interleave with the other parts'; with one part, q is the pixel).
+	const uint32_t q0 = blockIdx.x * (2u * kResolveBlock) + threadIdx.x, q1 = q0 + kResolveBlock;
+	if (q0 >= np) return;
+	auto pixel = [&](uint32_t q) {
+		const uint32_t lr = q / W;
+		return (((lr >> 3) * fp.parts + fp.part) * 8u + (lr & 7u)) * W + q % W;
+	};
+	if (q0 == 0) {
+		atomicAdd(&fb.rayTotals[0], (unsigned long long)np);
 		atomicAdd(&fb.rayTotals[1], (unsigned long long)fb.counters[kCtrShadow0]);
 		atomicAdd(&fb.rayTotals[2], (unsigned long long)fb.counters[kCtrBounce]);
 		atomicAdd(&fb.rayTotals[3], (unsigned long long)fb.counters[kCtrShadow1]);
 	}
 	if (fp.velocity || fp.prevVelocity) {   // camera motion: the full TAA with reprojected history
-		for (uint32_t pid = p0; pid <= p1 && pid < P; pid += kResolveBlock) {
+		for (uint32_t q = q0; q <= q1 && q < np; q += kResolveBlock) {
+			const uint32_t pid = pixel(q);
 			f3 acc = mk3(0.0f, 0.0f, 0.0f);
 			for (uint32_t k = 0; k < 2 * L; k++) {
 				size_t slot = (size_t)k * P + pid;
@@ -584,10 +592,10 @@ resolve_taa_kernel(const FrameParamsDev* __restrict__ fpp, FrameBuffers fb)
 	// them for the compiler). With zero velocity the history texel is the pixel itself and both velocity
 	// lengths are 0, so velocityDistrust = 0 and trust = clamp(1 - roughnessDistrust * 0). At the end of
 	// the frame the second pixel may not exist: it then repeats the first and its stores are skipped.
-	const bool two = p1 < P;
-	const uint32_t q = two ? p1 : p0;
-	const float4 h0 = ld_stream(fb.history[fp.parity] + p0), h1 = ld_stream(fb.history[fp.parity] + q);
-	const float r0 = ld_stream(fb.roughness + p0), r1 = ld_stream(fb.roughness + q);
+	const bool two = q1 < np;
+	const uint32_t p0 = pixel(q0), p1 = two ? pixel(q1) : p0;
+	const float4 h0 = ld_stream(fb.history[fp.parity] + p0), h1 = ld_stream(fb.history[fp.parity] + p1);
+	const float r0 = ld_stream(fb.roughness + p0), r1 = ld_stream(fb.roughness + p1);
 	const uint32_t n = 2 * L;
 	f3 a0 = mk3(0.0f, 0.0f, 0.0f), a1 = a0;
 	for (uint32_t k0 = 0; k0 < n; k0 += kResolveChunk) {
@@ -597,14 +605,14 @@ resolve_taa_kernel(const FrameParamsDev* __restrict__ fpp, FrameBuffers fb)
 			const size_t base = (size_t)(k0 + j) * P;
 			const bool in = k0 + j < n;
 			v0[j] = in ? ld_stream(fb.inLight + base + p0) : (uint8_t)0;
-			v1[j] = in ? ld_stream(fb.inLight + base + q) : (uint8_t)0;
+			v1[j] = in ? ld_stream(fb.inLight + base + p1) : (uint8_t)0;
 		}
 		float4 c0[kResolveChunk], c1[kResolveChunk];
 #pragma unroll
 		for (uint32_t j = 0; j < kResolveChunk; j++) {
 			const size_t base = (size_t)(k0 + j) * P;
 			c0[j] = v0[j] ? ld_stream(fb.contrib + base + p0) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-			c1[j] = v1[j] ? ld_stream(fb.contrib + base + q) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+			c1[j] = v1[j] ? ld_stream(fb.contrib + base + p1) : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
 		}
 #pragma unroll
 		for (uint32_t j = 0; j < kResolveChunk; j++) {
@@ -699,7 +707,7 @@ phe_status prepare_frame()
 
 phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, const FrameBuffers& fb, uint32_t resX,
                         uint32_t resY, cudaStream_t stream, cudaEvent_t* ev, bool fused, int schedule,
-                        const FrameStreams* streams, int parts)
+                        const FrameStreams* streams, int parts, uint32_t partPixels)
 {
 	// Timed frames keep one stream so that the per-kernel events measure one kernel each.
 	const bool beside = schedule == PHE_SHADOWS_BESIDE_BOUNCE && streams && streams->side && !ev;
@@ -722,7 +730,7 @@ phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, c
 			auto bounce = wide ? bounce_kernel<true> : bounce_kernel<false>;
 			// Persistent grids, but never more blocks than the frame's rays can keep busy: a small frame (a
 			// 256x256 render of the serving loop) then leaves the other SMs to concurrent requests.
-			const uint64_t P = (uint64_t)resX * resY;
+			const uint64_t P = partPixels ? partPixels : (uint64_t)resX * resY;
 			auto clamp = [](int grid, uint64_t rays) {
 				return (int)std::max<uint64_t>(1, std::min<uint64_t>((uint64_t)grid, (rays + kWaveBlock - 1) / kWaveBlock));
 			};
@@ -791,7 +799,8 @@ phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, c
 		}
 	}
 	if (parts & kFrameResolve) {
-		const uint32_t resolveGrid = (uint32_t)(((uint64_t)resX * resY + 2 * kResolveBlock - 1) / (2 * kResolveBlock));
+		const uint64_t pixels = partPixels ? partPixels : (uint64_t)resX * resY;
+		const uint32_t resolveGrid = (uint32_t)((pixels + 2 * kResolveBlock - 1) / (2 * kResolveBlock));
 		resolve_taa_kernel<<<resolveGrid, kResolveBlock, 0, stream>>>(dParams, fb);
 		mark();
 	}

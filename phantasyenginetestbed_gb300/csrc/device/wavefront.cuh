@@ -40,6 +40,10 @@ struct FrameParamsDev {
 	phe_camera_def prevCam;
 	float2* velocity;
 	const float2* prevVelocity;
+	// A frame split into `parts` parts (phe_renderer_set_frame_parts): this part covers the tile rows r
+	// with r % parts == part, partPixels pixels; numPixels stays the whole frame (the stride of the
+	// per-pixel buffers the parts share).
+	uint32_t part, parts, partPixels, pad;
 };
 
 struct FrameBuffers {
@@ -93,8 +97,9 @@ struct FrameStreams {
 // `parts` selects the traversal kernels (counter reset, primary, bounce, shadow passes), the resolve +
 // TAA kernel, or both: a renderer with two frames in flight launches them on different streams.
 enum { kFrameTraversal = 1, kFrameResolve = 2, kFrameAll = 3 };
+// `partPixels` (0 = the whole frame) sizes the grids of one part of a split frame.
 phe_status launch_frame(const phe_scene* scene, const FrameParamsDev* dParams, const FrameBuffers& fb, uint32_t resX,
                         uint32_t resY, cudaStream_t stream, cudaEvent_t* events, bool fused, int schedule,
-                        const FrameStreams* streams, int parts = kFrameAll);
+                        const FrameStreams* streams, int parts = kFrameAll, uint32_t partPixels = 0);
 
 } // namespace phe_gb300

@@ -178,6 +178,7 @@ SIGNATURES: dict[str, tuple] = {
     "phe_renderer_read_async": (_I32, [_VP, _I32, _VP, _VP]),
     "phe_renderer_read_wait": (_I32, [_VP]),
     "phe_renderer_set_frames_in_flight": (_I32, [_VP, _I32]),
+    "phe_renderer_set_frame_parts": (_I32, [_VP, _I32]),
     "phe_renderer_join": (_I32, [_VP, _VP]),
     "phe_renderer_set_latency_recording": (_I32, [_VP, _I32]),
     "phe_renderer_frame_latencies": (_I32, [_VP, _PF, _U32, C.POINTER(_U32)]),

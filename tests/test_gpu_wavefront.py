@@ -485,3 +485,36 @@ def test_frames_in_flight_give_the_sequential_frames(res):
     _flight_frame(pip, len(plan), plan[0], res, stream)
     _flight_frame(seq, len(plan), plan[0], res, stream)
     assert np.array_equal(pip.read(READ_COLOR, stream=stream), seq.read(READ_COLOR, stream=stream))
+
+
+@pytest.mark.parametrize("res,graph", [((256, 160), True), ((256, 160), False), ((120, 40), True), ((8, 8), False)])
+def test_split_frames_give_the_whole_frames(res, graph):
+    """A frame split into two parts (even and odd tile rows on two streams, own queues over shared
+    per-pixel buffers) gives the bytes of the whole frame through camera motion, a TAA reset and a
+    light-count change: TAA colour, history, raw colour, roughness, velocity and ray counts. 8x8 has one
+    tile row, so it renders whole."""
+    import torch
+    s, b, datas, scene, cam, cam_pos, lights, whole = _setup("c2_256_2000", res, [(0.5, 0.5, 2.0)], graph=graph)
+    split = CudaTracerRenderer(use_graph=graph)
+    split.setStaticScene(scene)
+    split.setTargetResolution(res)
+    split.set_frame_parts(2)
+    plan = _flight_plan(s, cam_pos)
+    stream = torch.cuda.Stream()
+    for r in (whole, split):
+        r.set_seed(31, 0)
+        r.resetTAA(stream=stream)
+    for f, step in enumerate(plan):
+        got = []
+        for r in (whole, split):
+            _flight_frame(r, f, step, res, stream)
+            got.append([r.read(w, stream=stream) for w in (READ_COLOR, READ_HISTORY, READ_RAW, READ_ROUGHNESS,
+                                                             READ_VELOCITY)] + [r.ray_counts(stream=stream)])
+        for a, c in zip(*got):
+            assert np.array_equal(a, c), f
+    with pytest.raises(P.PheError):
+        split.set_frames_in_flight(2)
+    split.set_frame_parts(1)
+    _flight_frame(split, len(plan), plan[0], res, stream)
+    _flight_frame(whole, len(plan), plan[0], res, stream)
+    assert np.array_equal(split.read(READ_COLOR, stream=stream), whole.read(READ_COLOR, stream=stream))
