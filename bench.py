@@ -344,6 +344,32 @@ def frame_roofline(dominant, entry, clock, num_sms, builder, layout) -> dict:
     return out
 
 
+def frame_issue(stage_rays, ms_per_frame, clock, num_sms, builder, layout) -> dict | None:
+    """Issue use of the whole frame: the warp instructions of its three traversal kernels (ncu counts per
+    ray on this workload times the frame's rays of each pass; the resolve, ~1% of them, left out) / (the
+    frame time x SMs x the median SM clock). It counts what the overlap of a split frame's parts adds,
+    which the per-kernel roofline of whole-frame kernels does not see."""
+    prof = ROOT / "profiles" / "ncu_kernels.json"
+    if not prof.exists():
+        return None
+    nc = json.loads(prof.read_text())
+    rays = {"primary_kernel": stage_rays["primary"], "bounce_kernel": stage_rays["bounce"],
+            "any_queue_kernel": stage_rays["primary_shadow"] + stage_rays["bounce_shadow"]}
+    inst = 0.0
+    for kernel, n in rays.items():
+        e = nc.get(f"{kernel}/{layout}")
+        if not e or e.get("bvh_builder") != builder:
+            return None
+        inst += e["warp_inst_per_ray"] * n
+    peaks_path = ROOT / "MEASURED_PEAKS.json"
+    peaks = json.loads(peaks_path.read_text()) if peaks_path.exists() else {}
+    mhz = clock.get("sm_mhz") or float(peaks.get("sm_max_mhz", 2070.0))
+    ipc = inst / (ms_per_frame * 1e-3 * num_sms * mhz * 1e6)
+    return {"achieved": round(ipc, 3), "peak": 4.0, "unit": "warp instructions / SM cycle", "frac": round(ipc / 4.0, 4),
+            "warp_inst_per_frame": round(inst), "how": f"{inst / 1e6:.1f} M warp instructions per frame (ncu counts x this "
+            f"frame's rays) / ({ms_per_frame:.4f} ms x {num_sms} SMs x {mhz:.0f} MHz)"}
+
+
 def two_in_flight(r, frame, stream, first, steps, rays_per_frame, parts=1):
     """Secondary figures with two frames in flight (consecutive frames overlapping on the renderer's own
     streams, the same bytes as one at a time): device throughput over `steps` frames (CUDA events from
@@ -562,8 +588,9 @@ def run_ours(args, world, rank, local):
     dominant = max((k for k in names if "rays" in per_kernel[k]), key=lambda k: per_kernel[k]["ms"])
     lat = sorted(per)
     clock = clocks.summary()
-    roofline = frame_roofline(dominant, per_kernel[dominant], clock, torch.cuda.get_device_properties(local).multi_processor_count,
-                              builder, args.layout)
+    num_sms = torch.cuda.get_device_properties(local).multi_processor_count
+    roofline = frame_roofline(dominant, per_kernel[dominant], clock, num_sms, builder, args.layout)
+    roofline["frame_issue"] = frame_issue(stage_rays, total_ms / args.steps, clock, num_sms, builder, args.layout)
     cpu = None
     if not args.no_cpu_baseline and world == 1:
         v, kind, cores, rows, times = cpu_castray_rate(s, b, cam_pos, lights, CPU_LEG_BUDGET_S, 4, first_frame=first)
