@@ -69,8 +69,8 @@ def parse():
     ap.add_argument("--pipeline", choices=["fused", "split"], default="fused",
                     help="fused: traversal + shading in one kernel per bounce (4 kernels with merged shadows); split: 7 kernels")
     ap.add_argument("--refill", type=int, default=28, help="lane-refill threshold of the split pipeline")
-    ap.add_argument("--frame-parts", type=int, default=2, choices=(1, 2),
-                    help="frame: 2 = the even and odd tile rows run as two overlapping parts (same bytes), 1 = whole")
+    ap.add_argument("--frame-parts", type=int, default=2, choices=(1, 2, 3, 4),
+                    help="frame: the tile rows dealt to this many overlapping parts (same bytes); 1 = whole")
     ap.add_argument("--frames-in-flight", type=int, default=1, choices=(1, 2),
                     help="frame: 2 = consecutive frames overlap on the renderer's own streams (same bytes); "
                          "with 1, the line also reports 2 in flight without L2 flushes as a secondary figure")

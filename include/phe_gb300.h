@@ -424,14 +424,14 @@ phe_status phe_renderer_kernel_times(phe_renderer* renderer, double msTotal[8], 
  * Changing the setting waits for the frames in flight; 2 adds a second set of per-frame buffers
  * (~410 MB at 1080p with one light). */
 phe_status phe_renderer_set_frames_in_flight(phe_renderer* renderer, int frames);
-/* Split frames (no reference counterpart). 1 (default): a frame's kernels run as one sequence. 2: the
- * frame's even and odd tile rows (8-pixel rows) run as two parts, part 0 on the caller's stream and
- * part 1 on the renderer's part stream forked from it, each with its own ray queues and counters over
- * the shared per-pixel buffers, and the caller's stream joins part 1 at the end of the frame: the
- * stream semantics of one frame are unchanged and every pixel gets the bytes of the whole frame (each
- * pixel's work depends only on the pixel; TAA reads only the previous frame). The two parts' kernels
- * overlap on the GPU. Applies to the fused pipeline with at least two tile rows, not to frames timed per
- * kernel; cannot be combined with two frames in flight; adds a second set of ray queues. */
+/* Split frames (no reference counterpart). 1 (default): a frame's kernels run as one sequence. 2..4:
+ * the frame's tile rows (8-pixel rows) are dealt round-robin to `parts` parts, part 0 on the caller's
+ * stream and the others on the renderer's part streams forked from it, each with its own ray queues and
+ * counters over the shared per-pixel buffers, and the caller's stream joins them at the end of the frame:
+ * the stream semantics of one frame are unchanged and every pixel gets the bytes of the whole frame (each
+ * pixel's work depends only on the pixel; TAA reads only the previous frame). The parts' kernels overlap
+ * on the GPU. Applies to the fused pipeline (at most one part per tile row), not to frames timed per
+ * kernel; cannot be combined with two frames in flight; each part past the first adds a set of ray queues. */
 phe_status phe_renderer_set_frame_parts(phe_renderer* renderer, int parts);
 phe_status phe_renderer_join(phe_renderer* renderer, void* stream);
 /* With 2 frames in flight and recording enabled, each frame's GPU latency (start of its first kernel to

@@ -16,6 +16,7 @@
 // is not made to wait (that would serialise the next frame): reads wait for the frame themselves, and
 // phe_renderer_join orders a stream after the last frame.
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <utility>
@@ -25,6 +26,8 @@
 #include "wavefront.cuh"
 
 using namespace phe_gb300;
+
+constexpr int kMaxFrameParts = 4;
 
 struct phe_renderer {
 	const phe_scene* scene = nullptr;
@@ -41,13 +44,17 @@ struct phe_renderer {
 	bool slotUsed[2] = {false, false};   // resolveDone[slot] marks the last frame that used the slot
 	uint32_t nextSlot = 0, lastSlot = 0;
 	bool framePending = false;           // a frame in flight that no caller stream has been ordered after
-	// A frame split into two parts (phe_renderer_set_frame_parts): part 1 (the odd tile rows) runs on
-	// partStream beside part 0 on the caller's stream, with the queues and counters of fb1 and the
-	// per-pixel buffers of fb; the caller's stream joins it at the end of the frame.
+	// A frame split into parts (phe_renderer_set_frame_parts): part j (tile rows r with r % parts == j)
+	// runs on partStream[j] beside part 0 on the caller's stream, with queues and counters of its own
+	// (part 1: fb1's, parts 2..: partFb's) over the per-pixel buffers of fb; the caller's stream joins
+	// every part at the end of the frame.
 	int frameParts = 1;
-	bool lastSplit = false;              // the last frame ran as two parts
-	cudaStream_t partStream = nullptr;
-	cudaEvent_t partFork = nullptr, partJoin = nullptr;
+	uint32_t lastParts = 1;              // parts the last frame ran as
+	cudaStream_t partStream[kMaxFrameParts] = {};
+	cudaEvent_t partFork = nullptr, partJoin[kMaxFrameParts] = {};
+	void* partAlloc[kMaxFrameParts] = {};
+	FrameBuffers partFb[kMaxFrameParts] = {};
+	FrameParamsDev* partParams[kMaxFrameParts] = {};   // parameters of parts 2.. (part 1: dParams1)
 	// Latency recording of frames in flight: (start, end) event pairs, drained by frame_latencies.
 	bool recordLatency = false;
 	std::vector<cudaEvent_t> latencyPool;
@@ -105,6 +112,13 @@ struct phe_renderer {
 };
 
 static size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Buffers and parameters of part j of a split frame (part 0: the renderer's own).
+static const FrameBuffers& part_fb(const phe_renderer* r, uint32_t j) { return j == 0 ? r->fb : j == 1 ? r->fb1 : r->partFb[j]; }
+static FrameParamsDev* part_params(const phe_renderer* r, uint32_t j)
+{
+	return j == 0 ? r->dParams : j == 1 ? r->dParams1 : r->partParams[j];
+}
 static const uint32_t kParamSlots = 8;
 
 // Waits for the frames in flight on the renderer's own streams (none in sequential mode).
@@ -132,6 +146,10 @@ static void free_buffers(phe_renderer* r)
 	if (r->allocation) cudaFree(r->allocation);
 	if (r->allocation1) cudaFree(r->allocation1);
 	r->allocation = r->allocation1 = nullptr;
+	for (int j = 2; j < kMaxFrameParts; j++) {
+		if (r->partAlloc[j]) cudaFree(r->partAlloc[j]);
+		r->partAlloc[j] = nullptr;
+	}
 	std::memset(&r->fb, 0, sizeof(r->fb));
 	std::memset(&r->fb1, 0, sizeof(r->fb1));
 	for (int i = 0; i < 3; i++) r->vel[i] = nullptr;
@@ -193,18 +211,29 @@ static char* carve_per_frame(char* base, size_t P, size_t L, FrameBuffers& fb)
 	return p;
 }
 
+static void share_pixels(const phe_renderer* r, FrameBuffers& f)
+{
+	f.contrib = r->fb.contrib;
+	f.inLight = r->fb.inLight;
+	f.roughness = r->fb.roughness;
+}
+
 // Slot 1 shares everything with slot 0 but its per-frame buffers; as part 1 of a split frame it also
-// shares the per-pixel ones (the parts write disjoint pixels) and keeps only its queues and counters.
+// shares the per-pixel ones (the parts write disjoint pixels) and keeps only its queues and counters,
+// as parts 2.. do.
 static void make_fb1(phe_renderer* r)
 {
-	if (!r->allocation1) return;
-	r->fb1 = r->fb;
-	carve_per_frame((char*)r->allocation1, r->capacityP, r->capacityL, r->fb1);
-	if (r->frameParts == 2) {
-		r->fb1.contrib = r->fb.contrib;
-		r->fb1.inLight = r->fb.inLight;
-		r->fb1.roughness = r->fb.roughness;
+	if (r->allocation1) {
+		r->fb1 = r->fb;
+		carve_per_frame((char*)r->allocation1, r->capacityP, r->capacityL, r->fb1);
+		if (r->frameParts >= 2) share_pixels(r, r->fb1);
 	}
+	for (int j = 2; j < kMaxFrameParts; j++)
+		if (r->partAlloc[j]) {
+			r->partFb[j] = r->fb;
+			carve_per_frame((char*)r->partAlloc[j], r->capacityP, r->capacityL, r->partFb[j]);
+			share_pixels(r, r->partFb[j]);
+		}
 }
 
 static phe_status allocate_slot1(phe_renderer* r)
@@ -217,6 +246,24 @@ static phe_status allocate_slot1(phe_renderer* r)
 		return cuda_fail(e, "cudaMalloc(frame buffers of the second frame in flight)");
 	}
 	if ((e = cudaMemset(r->allocation1, 0, bytes)) != cudaSuccess) return cuda_fail(e, "clear frame buffers");
+	make_fb1(r);
+	return PHE_OK;
+}
+
+// Queue buffers of parts 2.. of a split frame.
+static phe_status allocate_parts(phe_renderer* r)
+{
+	if (!r->allocation) return PHE_OK;
+	const size_t bytes = per_frame_bytes(r->capacityP, r->capacityL);
+	for (int j = 2; j < r->frameParts; j++) {
+		if (r->partAlloc[j]) continue;
+		cudaError_t e = cudaMalloc(&r->partAlloc[j], bytes);
+		if (e != cudaSuccess) {
+			r->partAlloc[j] = nullptr;
+			return cuda_fail(e, "cudaMalloc(ray queues of a frame part)");
+		}
+		if ((e = cudaMemset(r->partAlloc[j], 0, bytes)) != cudaSuccess) return cuda_fail(e, "clear frame buffers");
+	}
 	make_fb1(r);
 	return PHE_OK;
 }
@@ -279,7 +326,11 @@ static phe_status allocate(phe_renderer* r, uint32_t resX, uint32_t resY, uint32
 	r->numLights = numLights;
 	if ((e = cudaMemset(base, 0, total)) != cudaSuccess) return cuda_fail(e, "clear frame buffers");
 	r->parity = 0;
-	if (r->inFlight == 2 || r->frameParts == 2) return allocate_slot1(r);
+	if (r->inFlight == 2 || r->frameParts >= 2) {
+		phe_status st = allocate_slot1(r);
+		if (!st && r->frameParts > 2) st = allocate_parts(r);
+		return st;
+	}
 	return PHE_OK;
 }
 
@@ -422,9 +473,12 @@ extern "C" phe_status phe_renderer_destroy(phe_renderer* r)
 	}
 	if (r->resolveStream) cudaStreamDestroy(r->resolveStream);
 	if (r->callEvent) cudaEventDestroy(r->callEvent);
-	if (r->partStream) cudaStreamDestroy(r->partStream);
+	for (int j = 0; j < kMaxFrameParts; j++) {
+		if (r->partStream[j]) cudaStreamDestroy(r->partStream[j]);
+		if (r->partJoin[j]) cudaEventDestroy(r->partJoin[j]);
+		if (r->partParams[j]) cudaFree(r->partParams[j]);
+	}
 	if (r->partFork) cudaEventDestroy(r->partFork);
-	if (r->partJoin) cudaEventDestroy(r->partJoin);
 	for (cudaEvent_t e : r->latencyPool) cudaEventDestroy(e);
 	for (auto& pr : r->latencyPending) {
 		cudaEventDestroy(pr.first);
@@ -560,7 +614,7 @@ extern "C" phe_status phe_renderer_set_frames_in_flight(phe_renderer* r, int fra
 {
 	if (!r) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_set_frames_in_flight: null renderer");
 	if (frames != 1 && frames != 2) return fail(PHE_ERR_INVALID_ARGUMENT, "frames in flight must be 1 or 2");
-	if (frames == 2 && r->frameParts == 2)
+	if (frames == 2 && r->frameParts >= 2)
 		return fail(PHE_ERR_INVALID_ARGUMENT, "two frames in flight and split frames cannot be combined");
 	drain_streams(r);   // the slots and streams change hands only when no frame is in flight
 	r->slotUsed[0] = r->slotUsed[1] = false;
@@ -586,8 +640,8 @@ extern "C" phe_status phe_renderer_set_frames_in_flight(phe_renderer* r, int fra
 extern "C" phe_status phe_renderer_set_frame_parts(phe_renderer* r, int parts)
 {
 	if (!r) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_renderer_set_frame_parts: null renderer");
-	if (parts != 1 && parts != 2) return fail(PHE_ERR_INVALID_ARGUMENT, "frame parts must be 1 or 2");
-	if (parts == 2 && r->inFlight == 2)
+	if (parts < 1 || parts > kMaxFrameParts) return fail(PHE_ERR_INVALID_ARGUMENT, "frame parts must be 1..%d", kMaxFrameParts);
+	if (parts >= 2 && r->inFlight == 2)
 		return fail(PHE_ERR_INVALID_ARGUMENT, "two frames in flight and split frames cannot be combined");
 	if (parts == r->frameParts) return PHE_OK;
 	cudaDeviceSynchronize();   // part 1's buffers change role
@@ -596,13 +650,18 @@ extern "C" phe_status phe_renderer_set_frame_parts(phe_renderer* r, int parts)
 		r->graphExec = nullptr;
 	}
 	r->frameParts = parts;
-	if (parts == 2) {
-		if (!r->partStream) {
-			PHE_CUDA_TRY(cudaStreamCreateWithFlags(&r->partStream, cudaStreamNonBlocking), "create part stream");
-			PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->partFork, cudaEventDisableTiming), "create part event");
-			PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->partJoin, cudaEventDisableTiming), "create part event");
+	if (parts >= 2) {
+		if (!r->partFork) PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->partFork, cudaEventDisableTiming), "create part event");
+		for (int j = 1; j < parts; j++) {
+			if (!r->partStream[j]) {
+				PHE_CUDA_TRY(cudaStreamCreateWithFlags(&r->partStream[j], cudaStreamNonBlocking), "create part stream");
+				PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->partJoin[j], cudaEventDisableTiming), "create part event");
+			}
+			if (j >= 2 && !r->partParams[j])
+				PHE_CUDA_TRY(cudaMalloc(&r->partParams[j], sizeof(FrameParamsDev)), "allocate part parameters");
 		}
 		phe_status st = allocate_slot1(r);
+		if (!st) st = allocate_parts(r);
 		if (st) return st;
 	}
 	make_fb1(r);
@@ -684,23 +743,25 @@ extern "C" phe_status phe_renderer_ray_totals_async(const phe_renderer* r, uint6
 	return PHE_OK;
 }
 
-// One frame on `s`: whole, or split into its two parts, part 1 on the part stream between a fork and a
-// join on `s` (the same calls capture a split frame into a graph).
-static phe_status launch_whole_or_split(phe_renderer* r, cudaStream_t s, bool split, uint32_t n0, uint32_t n1)
+// One frame on `s`: whole, or split into `parts` parts, parts 1.. on their part streams between a fork
+// and joins on `s` (the same calls capture a split frame into a graph).
+static phe_status launch_whole_or_split(phe_renderer* r, cudaStream_t s, uint32_t parts, const uint32_t* n)
 {
-	if (!split)
+	if (parts == 1)
 		return launch_frame(r->scene, r->dParams, r->fb, r->resX, r->resY, s, nullptr, r->fused, r->shadowSchedule,
 		                    &r->streams);
 	PHE_CUDA_TRY(cudaEventRecord(r->partFork, s), "fork frame parts");
-	PHE_CUDA_TRY(cudaStreamWaitEvent(r->partStream, r->partFork, 0), "fork frame parts");
-	phe_status st = launch_frame(r->scene, r->dParams, r->fb, r->resX, r->resY, s, nullptr, r->fused,
-	                             r->shadowSchedule, nullptr, kFrameAll, n0);
-	if (st) return st;
-	st = launch_frame(r->scene, r->dParams1, r->fb1, r->resX, r->resY, r->partStream, nullptr, r->fused,
-	                  r->shadowSchedule, nullptr, kFrameAll, n1);
-	if (st) return st;
-	PHE_CUDA_TRY(cudaEventRecord(r->partJoin, r->partStream), "join frame parts");
-	PHE_CUDA_TRY(cudaStreamWaitEvent(s, r->partJoin, 0), "join frame parts");
+	for (uint32_t j = 1; j < parts; j++)
+		PHE_CUDA_TRY(cudaStreamWaitEvent(r->partStream[j], r->partFork, 0), "fork frame parts");
+	for (uint32_t j = 0; j < parts; j++) {
+		cudaStream_t ps = j ? r->partStream[j] : s;
+		phe_status st = launch_frame(r->scene, part_params(r, j), part_fb(r, j), r->resX, r->resY, ps, nullptr, r->fused,
+		                             r->shadowSchedule, nullptr, kFrameAll, n[j]);
+		if (st) return st;
+		if (j) PHE_CUDA_TRY(cudaEventRecord(r->partJoin[j], ps), "join frame parts");
+	}
+	for (uint32_t j = 1; j < parts; j++)
+		PHE_CUDA_TRY(cudaStreamWaitEvent(s, r->partJoin[j], 0), "join frame parts");
 	return PHE_OK;
 }
 
@@ -731,12 +792,13 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 	FrameParamsDev* dParams = j ? r->dParams1 : r->dParams;
 	cudaStream_t X = pipelined ? r->travStream[j] : s;   // traversal kernels
 	cudaStream_t R = pipelined ? r->resolveStream : s;   // resolve + TAA
-	// A split frame: the even tile rows on `s`, the odd ones on the part stream (fused pipeline only;
-	// frames timed per kernel stay whole).
+	// A split frame: part j takes the tile rows r with r % parts == j, part 0 on `s`, the others on their
+	// part streams (fused pipeline only, at most one part per tile row; frames timed per kernel stay whole).
 	const uint32_t tileRows = r->resY / 8u;
-	const bool split = !pipelined && r->frameParts == 2 && r->fused && !r->timing && tileRows >= 2;
-	const uint32_t n0 = split ? (tileRows + 1) / 2 * 8u * r->resX : r->resX * r->resY;
-	const uint32_t n1 = split ? tileRows / 2 * 8u * r->resX : 0u;
+	const uint32_t parts = (!pipelined && r->frameParts >= 2 && r->fused && !r->timing)
+	                           ? std::min<uint32_t>((uint32_t)r->frameParts, tileRows) : 1u;
+	uint32_t n[kMaxFrameParts] = {};
+	for (uint32_t k = 0; k < parts; k++) n[k] = (tileRows - k + parts - 1) / parts * 8u * r->resX;
 	if (pipelined) {
 		// after the caller's work so far, and after the resolve that last read this slot's buffers
 		PHE_CUDA_TRY(cudaEventRecord(r->callEvent, s), "record caller work");
@@ -772,8 +834,8 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 	fp.parity = r->parity;
 	fp.seed = r->seed;
 	fp.part = 0;
-	fp.parts = split ? 2u : 1u;
-	fp.partPixels = n0;
+	fp.parts = parts;
+	fp.partPixels = n[0];
 	fp.pad = 0;
 	std::memset(fp.lights, 0, sizeof(fp.lights));
 	if (numLights) std::memcpy(fp.lights, lights, sizeof(phe_sphere_light) * numLights);
@@ -783,17 +845,17 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 	PHE_CUDA_TRY(cudaMemcpyAsync(dParams, &fp, sizeof(FrameParamsDev), cudaMemcpyHostToDevice, X),
 	             "upload frame parameters");
 	PHE_CUDA_TRY(cudaEventRecord(r->paramEvents[slot], X), "record parameter slot");
-	if (split) {   // part 1's parameters: the same but for its part index and pixel count
-		const uint32_t slot1 = r->paramSlot;
-		r->paramSlot = (slot1 + 1) % kParamSlots;
-		PHE_CUDA_TRY(cudaEventSynchronize(r->paramEvents[slot1]), "wait for a free parameter slot");
-		FrameParamsDev& fp1 = r->hParams[slot1];
-		fp1 = fp;
-		fp1.part = 1;
-		fp1.partPixels = n1;
-		PHE_CUDA_TRY(cudaMemcpyAsync(r->dParams1, &fp1, sizeof(FrameParamsDev), cudaMemcpyHostToDevice, s),
+	for (uint32_t k = 1; k < parts; k++) {   // the other parts' parameters: the same but for part and pixels
+		const uint32_t slotK = r->paramSlot;
+		r->paramSlot = (slotK + 1) % kParamSlots;
+		PHE_CUDA_TRY(cudaEventSynchronize(r->paramEvents[slotK]), "wait for a free parameter slot");
+		FrameParamsDev& fpk = r->hParams[slotK];
+		fpk = fp;
+		fpk.part = k;
+		fpk.partPixels = n[k];
+		PHE_CUDA_TRY(cudaMemcpyAsync(part_params(r, k), &fpk, sizeof(FrameParamsDev), cudaMemcpyHostToDevice, s),
 		             "upload frame parameters");
-		PHE_CUDA_TRY(cudaEventRecord(r->paramEvents[slot1], s), "record parameter slot");
+		PHE_CUDA_TRY(cudaEventRecord(r->paramEvents[slotK], s), "record parameter slot");
 	}
 	if (pipelined) {
 		cudaEvent_t t0 = nullptr, t1 = nullptr;
@@ -834,7 +896,7 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 			cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
 			phe_status st = PHE_OK;
 			if (e == cudaSuccess) {
-				st = launch_whole_or_split(r, cap, split, n0, n1);
+				st = launch_whole_or_split(r, cap, parts, n);
 				e = cudaStreamEndCapture(cap, &g);
 			}
 			cudaStreamDestroy(cap);
@@ -856,12 +918,12 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 			                  nullptr);
 			r->pendingTimes = true;
 		} else {
-			st = launch_whole_or_split(r, s, split, n0, n1);
+			st = launch_whole_or_split(r, s, parts, n);
 		}
 		if (st) return st;
 		r->lastSlot = 0;
 	}
-	r->lastSplit = split;
+	r->lastParts = parts;
 	r->velZero[vOut] = !moving;
 	r->velLast = vOut;
 	r->velNext = (vOut + 1) % 3;
@@ -891,17 +953,22 @@ extern "C" phe_status phe_renderer_ray_counts(const phe_renderer* r, uint64_t co
 	phe_status st = join_frames(r, (cudaStream_t)stream);
 	if (st) return st;
 	uint32_t c[kNumCounters];
-	uint32_t c1[kNumCounters] = {};
+	uint32_t cp[kMaxFrameParts][kNumCounters] = {};
 	PHE_CUDA_TRY(cudaMemcpyAsync(c, last_fb(r).counters, sizeof(c), cudaMemcpyDeviceToHost, (cudaStream_t)stream),
 	             "read counters");
-	if (r->lastSplit)   // part 1's queues
-		PHE_CUDA_TRY(cudaMemcpyAsync(c1, r->fb1.counters, sizeof(c1), cudaMemcpyDeviceToHost, (cudaStream_t)stream),
-		             "read counters");
+	for (uint32_t j = 1; j < r->lastParts; j++)   // the other parts' queues
+		PHE_CUDA_TRY(cudaMemcpyAsync(cp[j], part_fb(r, j).counters, sizeof(cp[j]), cudaMemcpyDeviceToHost,
+		                             (cudaStream_t)stream), "read counters");
 	PHE_CUDA_TRY(cudaStreamSynchronize((cudaStream_t)stream), "read counters");
 	counts[0] = (uint64_t)r->resX * r->resY;
-	counts[1] = (uint64_t)c[kCtrShadow0] + c1[kCtrShadow0];
-	counts[2] = (uint64_t)c[kCtrBounce] + c1[kCtrBounce];
-	counts[3] = (uint64_t)c[kCtrShadow1] + c1[kCtrShadow1];
+	counts[1] = c[kCtrShadow0];
+	counts[2] = c[kCtrBounce];
+	counts[3] = c[kCtrShadow1];
+	for (uint32_t j = 1; j < r->lastParts; j++) {
+		counts[1] += cp[j][kCtrShadow0];
+		counts[2] += cp[j][kCtrBounce];
+		counts[3] += cp[j][kCtrShadow1];
+	}
 	return PHE_OK;
 }
 

@@ -139,8 +139,8 @@ class CudaTracerRenderer:
         check(lib().phe_renderer_set_frames_in_flight(self.handle, int(frames)), "phe_renderer_set_frames_in_flight")
 
     def set_frame_parts(self, parts: int) -> None:
-        """1 (default): a frame's kernels run as one. 2: the even and odd tile rows run as two parts on
-        two streams inside the frame (same bytes); the frame still ends on the caller's stream."""
+        """1 (default): a frame's kernels run as one. 2..4: the tile rows are dealt to that many parts on
+        their own streams inside the frame (same bytes); the frame still ends on the caller's stream."""
         check(lib().phe_renderer_set_frame_parts(self.handle, int(parts)), "phe_renderer_set_frame_parts")
 
     def join(self, stream=None) -> None:

@@ -487,18 +487,20 @@ def test_frames_in_flight_give_the_sequential_frames(res):
     assert np.array_equal(pip.read(READ_COLOR, stream=stream), seq.read(READ_COLOR, stream=stream))
 
 
-@pytest.mark.parametrize("res,graph", [((256, 160), True), ((256, 160), False), ((120, 40), True), ((8, 8), False)])
-def test_split_frames_give_the_whole_frames(res, graph):
-    """A frame split into two parts (even and odd tile rows on two streams, own queues over shared
-    per-pixel buffers) gives the bytes of the whole frame through camera motion, a TAA reset and a
+@pytest.mark.parametrize("res,graph,parts", [((256, 160), True, 2), ((256, 160), False, 2), ((120, 40), True, 2),
+                                             ((8, 8), False, 2), ((256, 160), True, 3), ((120, 40), False, 4),
+                                             ((64, 24), True, 4)])
+def test_split_frames_give_the_whole_frames(res, graph, parts):
+    """A frame split into parts (tile rows dealt round-robin to parts on their own streams, own queues over
+    shared per-pixel buffers) gives the bytes of the whole frame through camera motion, a TAA reset and a
     light-count change: TAA colour, history, raw colour, roughness, velocity and ray counts. 8x8 has one
-    tile row, so it renders whole."""
+    tile row, so it renders whole; 64x24 has three, so four parts run as three."""
     import torch
     s, b, datas, scene, cam, cam_pos, lights, whole = _setup("c2_256_2000", res, [(0.5, 0.5, 2.0)], graph=graph)
     split = CudaTracerRenderer(use_graph=graph)
     split.setStaticScene(scene)
     split.setTargetResolution(res)
-    split.set_frame_parts(2)
+    split.set_frame_parts(parts)
     plan = _flight_plan(s, cam_pos)
     stream = torch.cuda.Stream()
     for r in (whole, split):
