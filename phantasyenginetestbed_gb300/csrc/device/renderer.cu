@@ -131,7 +131,9 @@ static void drain_streams(phe_renderer* r)
 
 static void free_buffers(phe_renderer* r)
 {
-	drain_streams(r);
+	// Frames on any stream may still use the buffers: the caller's, the part streams of split frames and
+	// the renderer's own frame streams.
+	cudaDeviceSynchronize();
 	// in-place read-backs may still be copying out of these buffers
 	for (int i = 0; i < 2; i++) {
 		if (r->sideDone[i]) cudaEventSynchronize(r->sideDone[i]);

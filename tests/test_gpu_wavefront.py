@@ -520,3 +520,37 @@ def test_split_frames_give_the_whole_frames(res, graph, parts):
     _flight_frame(split, len(plan), plan[0], res, stream)
     _flight_frame(whole, len(plan), plan[0], res, stream)
     assert np.array_equal(split.read(READ_COLOR, stream=stream), whole.read(READ_COLOR, stream=stream))
+
+
+@pytest.mark.parametrize("mode", ["parts", "flight"])
+def test_split_and_flight_frames_across_resolution_changes(mode):
+    """Split frames (2 parts) and two frames in flight across resolution changes (the second one grows
+    the buffers, the third and fourth keep them) give the bytes of the same frames rendered whole, one
+    at a time."""
+    import torch
+    s, b, datas, scene, cam, cam_pos, lights, ref = _setup("c2_256_2000", (64, 48), [(0.5, 0.5, 2.0)], graph=True)
+    r = CudaTracerRenderer(use_graph=True)
+    r.setStaticScene(scene)
+    r.setTargetResolution((64, 48))
+    if mode == "parts":
+        r.set_frame_parts(2)
+    else:
+        r.set_frames_in_flight(2)
+    stream = torch.cuda.Stream()
+    plan = _flight_plan(s, cam_pos)
+    for x in (ref, r):
+        x.set_seed(41, 0)
+    f = 0
+    for res in [(64, 48), (128, 96), (64, 48), (128, 96)]:
+        for x in (ref, r):
+            x.setTargetResolution(res)
+            x.resetTAA(stream=stream)
+        colours = {}
+        for x, name in ((ref, "ref"), (r, "test")):
+            for k in range(3):
+                _flight_frame(x, f + k, plan[k], res, stream)
+            colours[name] = [x.read(w, stream=stream) for w in (READ_COLOR, READ_HISTORY, READ_RAW)] + \
+                            [x.ray_counts(stream=stream)]
+        for a, c in zip(colours["ref"], colours["test"]):
+            assert np.array_equal(a, c), res
+        f += 3
