@@ -546,8 +546,8 @@ __device__ __forceinline__ void taa_pixel(uint32_t x, uint32_t y, uint32_t W, ui
 // issued together, then the contribution loads of the visible slots, so a thread keeps two independent
 // chains in flight; the per-pixel sums keep the slot order.
 constexpr int kResolveBlock = 128;
-constexpr int kResolveMinBlocks = 8;
-constexpr uint32_t kResolveChunk = 4;   // light slots whose loads are issued together
+constexpr int kResolveMinBlocks = 10;
+constexpr uint32_t kResolveChunk = 2;   // light slots whose loads are issued together
 __global__ void __launch_bounds__(kResolveBlock, kResolveMinBlocks)
 resolve_taa_kernel(const FrameParamsDev* __restrict__ fpp, FrameBuffers fb)
 {
