@@ -13,6 +13,8 @@ ROOT = Path(__file__).resolve().parents[1]
 pytestmark = pytest.mark.gpu
 
 SUBSET = ["tests/test_gpu_raycast.py", "tests/test_gpu_wavefront.py::test_frame_matches_oracle_small",
+          "tests/test_gpu_wavefront.py::test_split_frames_give_the_whole_frames",
+          "tests/test_gpu_wavefront.py::test_frames_in_flight_give_the_sequential_frames",
           "tests/test_gpu_textures.py::test_textured_frame_matches_oracle", "tests/test_gpu_batch.py",
           "tests/test_zz_no_alloc.py"]
 
