@@ -618,7 +618,7 @@ def run_ours(args, world, rank, local):
         "roofline": roofline,
         "clocks": clock,
         "e2e": {"value": round(e2e_value, 2), "unit": "Mrays/s",
-                "h2d_bytes_per_step": int(native.lib().phe_renderer_frame_param_bytes()),
+                "h2d_bytes_per_step": int(native.lib().phe_renderer_frame_param_bytes()) * args.frame_parts,
                 "d2h_bytes_per_step": RES[0] * RES[1] * 16,
                 "mode": "pipelined: colour image read back asynchronously (two pinned host images) while the "
                         "next frames render; clock stops when the last image is in host memory",
