@@ -299,7 +299,10 @@ void phe_batch_default_params(phe_batch_params* params);
  * of a launch are ORed into each item's scene status word (phe_scene_status). */
 phe_status phe_batch_create(const phe_scene* const* scenes, uint32_t numScenes, const phe_batch_item* items,
                             uint32_t numItems, const phe_batch_params* params, phe_batch** out);
-/* New buffers / counts for the same number of items (the captured graph is rebuilt on next launch). */
+/* New buffers / counts for the same number of items (the captured graph is rebuilt on next launch).
+ * update and set_params rewrite the batch's device tables in place: they first wait on the host for the
+ * batch's last launch, on whichever stream it ran, and return with the new tables on the device, so the
+ * next launch on any stream reads them. */
 phe_status phe_batch_update(phe_batch* batch, const phe_batch_item* items, uint32_t numItems);
 phe_status phe_batch_set_params(phe_batch* batch, const phe_batch_params* params);
 /* One persistent launch over every item, asynchronous on `stream`. */
@@ -422,7 +425,8 @@ phe_status phe_renderer_kernel_times(phe_renderer* renderer, double msTotal[8], 
  * launched directly (no graph replay); frames timed per kernel run in order on the caller's stream, and
  * the BESIDE_BOUNCE shadow schedule runs IN_ORDER. phe_scene_destroy waits for all device work.
  * Changing the setting waits for the frames in flight; 2 adds a second set of per-frame buffers
- * (~410 MB at 1080p with one light). */
+ * (~410 MB at 1080p with one light). If making them fails, the call returns the error and frames stay
+ * one at a time. */
 phe_status phe_renderer_set_frames_in_flight(phe_renderer* renderer, int frames);
 /* Split frames (no reference counterpart). 1 (default): a frame's kernels run as one sequence. 2..4:
  * the frame's tile rows (8-pixel rows) are dealt round-robin to `parts` parts, part 0 on the caller's
@@ -431,7 +435,8 @@ phe_status phe_renderer_set_frames_in_flight(phe_renderer* renderer, int frames)
  * the stream semantics of one frame are unchanged and every pixel gets the bytes of the whole frame (each
  * pixel's work depends only on the pixel; TAA reads only the previous frame). The parts' kernels overlap
  * on the GPU. Applies to the fused pipeline (at most one part per tile row), not to frames timed per
- * kernel; cannot be combined with two frames in flight; each part past the first adds a set of ray queues. */
+ * kernel; cannot be combined with two frames in flight; each part past the first adds a set of ray queues.
+ * If making them fails, the call returns the error and the previous setting stays. */
 phe_status phe_renderer_set_frame_parts(phe_renderer* renderer, int parts);
 phe_status phe_renderer_join(phe_renderer* renderer, void* stream);
 /* With 2 frames in flight and recording enabled, each frame's GPU latency (start of its first kernel to

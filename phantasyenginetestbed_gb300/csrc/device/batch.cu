@@ -175,6 +175,9 @@ struct phe_batch {
 	uint32_t totalPadded = 0;
 	uint64_t totalRays = 0;
 	cudaGraphExec_t graph = nullptr;
+	// The last phe_batch_launch, which may still read the tables on its stream when they are rewritten.
+	cudaEvent_t launchDone = nullptr;
+	bool launchPending = false;
 	// Ray sorting (params.sortWindow > 0): window table of the item order and the permutation.
 	uint32_t* dPerm = nullptr;             // [totalPadded]
 	uint32_t* dWindowStart = nullptr;      // [items + 1]
@@ -214,6 +217,11 @@ static phe_status check_params(const phe_batch_params* p)
 
 static phe_status upload_table(phe_batch* b)
 {
+	// The tables are rewritten in place: after the last launch that reads them, on whichever stream.
+	if (b->launchPending) {
+		PHE_CUDA_TRY(cudaEventSynchronize(b->launchDone), "wait for the last batch launch");
+		b->launchPending = false;
+	}
 	// Launch order.
 	const size_t n = b->items.size();
 	b->order.resize(n);
@@ -291,7 +299,7 @@ static phe_status upload_table(phe_batch* b)
 		cudaGraphExecDestroy(b->graph);
 		b->graph = nullptr;
 	}
-	return PHE_OK;
+	return finish_uploads("upload batch tables");
 }
 
 static phe_status check_items(const phe_batch_item* items, uint32_t numItems, uint32_t numScenes)
@@ -342,19 +350,22 @@ extern "C" phe_status phe_batch_create(const phe_scene* const* scenes, uint32_t 
 		return cuda_fail(e, "cudaMalloc(batch)");
 	}
 	b->allocation = base;
+	if ((e = cudaEventCreateWithFlags(&b->launchDone, cudaEventDisableTiming)) != cudaSuccess) {
+		cudaFree(base);
+		delete b;
+		return cuda_fail(e, "create batch event");
+	}
 	b->dItems = (BatchItemDev*)base;
 	b->dScenes = (DeviceScene*)(base + itemBytes);
 	b->dCounter = (uint32_t*)(base + itemBytes + sceneBytes);
 	cudaMemset(b->dCounter, 0, 256);
 	e = cudaMemcpy(b->dScenes, b->scenes.data(), numScenes * sizeof(DeviceScene), cudaMemcpyHostToDevice);
 	if (e != cudaSuccess) {
-		cudaFree(base);
-		delete b;
+		phe_batch_destroy(b);
 		return cuda_fail(e, "upload scene table");
 	}
 	if ((st = upload_table(b))) {
-		cudaFree(base);
-		delete b;
+		phe_batch_destroy(b);
 		return st;
 	}
 	*out = b;
@@ -401,7 +412,13 @@ extern "C" phe_status phe_batch_launch(phe_batch* b, void* stream)
 	if (!b) return fail(PHE_ERR_INVALID_ARGUMENT, "phe_batch_launch: null batch");
 	NvtxRange range("phe_batch_launch");
 	cudaStream_t s = (cudaStream_t)stream;
-	if (!b->params.useGraph) return batch_enqueue(b, s);
+	if (!b->params.useGraph) {
+		phe_status st = batch_enqueue(b, s);
+		if (st) return st;
+		PHE_CUDA_TRY(cudaEventRecord(b->launchDone, s), "record batch launch");
+		b->launchPending = true;
+		return PHE_OK;
+	}
 	if (!b->graph) {
 		// Resolve occupancy outside capture.
 		int occ = 0;
@@ -430,6 +447,8 @@ extern "C" phe_status phe_batch_launch(phe_batch* b, void* stream)
 		if (e != cudaSuccess) return cuda_fail(e, "instantiate batch graph");
 	}
 	PHE_CUDA_TRY(cudaGraphLaunch(b->graph, s), "launch batch graph");
+	PHE_CUDA_TRY(cudaEventRecord(b->launchDone, s), "record batch launch");
+	b->launchPending = true;
 	return PHE_OK;
 }
 
@@ -457,6 +476,7 @@ extern "C" phe_status phe_batch_destroy(phe_batch* b)
 	if (b->dPerm) cudaFree(b->dPerm);
 	if (b->dWindowStart) cudaFree(b->dWindowStart);
 	cudaFree(b->allocation);
+	if (b->launchDone) cudaEventDestroy(b->launchDone);
 	delete b;
 	return PHE_OK;
 }

@@ -238,6 +238,14 @@ static void make_fb1(phe_renderer* r)
 		}
 }
 
+// Zeroes newly allocated frame buffers before any frame, on whichever stream, can use them.
+static phe_status clear_new(void* p, size_t bytes)
+{
+	cudaError_t e = cudaMemset(p, 0, bytes);
+	if (e != cudaSuccess) return cuda_fail(e, "clear frame buffers");
+	return finish_uploads("clear frame buffers");
+}
+
 static phe_status allocate_slot1(phe_renderer* r)
 {
 	if (r->allocation1 || !r->allocation) return PHE_OK;
@@ -247,9 +255,8 @@ static phe_status allocate_slot1(phe_renderer* r)
 		r->allocation1 = nullptr;
 		return cuda_fail(e, "cudaMalloc(frame buffers of the second frame in flight)");
 	}
-	if ((e = cudaMemset(r->allocation1, 0, bytes)) != cudaSuccess) return cuda_fail(e, "clear frame buffers");
 	make_fb1(r);
-	return PHE_OK;
+	return clear_new(r->allocation1, bytes);
 }
 
 // Queue buffers of parts 2.. of a split frame.
@@ -264,10 +271,47 @@ static phe_status allocate_parts(phe_renderer* r)
 			r->partAlloc[j] = nullptr;
 			return cuda_fail(e, "cudaMalloc(ray queues of a frame part)");
 		}
-		if ((e = cudaMemset(r->partAlloc[j], 0, bytes)) != cudaSuccess) return cuda_fail(e, "clear frame buffers");
+		make_fb1(r);
+		if (phe_status st = clear_new(r->partAlloc[j], bytes)) return st;
 	}
-	make_fb1(r);
 	return PHE_OK;
+}
+
+// Streams, events and slot-1 buffers of two frames in flight. Each is made once; a call after one that
+// failed part way makes the rest, and with everything present it only checks.
+static phe_status prepare_flight(phe_renderer* r)
+{
+	if (!r->resolveStream) {   // made last: present means the streams and events before it are too
+		for (int j = 0; j < 2; j++) {
+			if (!r->travStream[j])
+				PHE_CUDA_TRY(cudaStreamCreateWithFlags(&r->travStream[j], cudaStreamNonBlocking), "create frame stream");
+			if (!r->travDone[j])
+				PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->travDone[j], cudaEventDisableTiming), "create frame event");
+			if (!r->resolveDone[j])
+				PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->resolveDone[j], cudaEventDisableTiming), "create frame event");
+		}
+		if (!r->callEvent)
+			PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->callEvent, cudaEventDisableTiming), "create frame event");
+		PHE_CUDA_TRY(cudaStreamCreateWithFlags(&r->resolveStream, cudaStreamNonBlocking), "create frame stream");
+	}
+	return allocate_slot1(r);
+}
+
+// Streams, events, parameters and queue buffers of a frame split into `parts` parts, made the same way.
+static phe_status prepare_parts(phe_renderer* r, int parts)
+{
+	if (!r->partFork) PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->partFork, cudaEventDisableTiming), "create part event");
+	for (int j = 1; j < parts; j++) {
+		if (!r->partStream[j])
+			PHE_CUDA_TRY(cudaStreamCreateWithFlags(&r->partStream[j], cudaStreamNonBlocking), "create part stream");
+		if (!r->partJoin[j])
+			PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->partJoin[j], cudaEventDisableTiming), "create part event");
+		if (j >= 2 && !r->partParams[j])
+			PHE_CUDA_TRY(cudaMalloc(&r->partParams[j], sizeof(FrameParamsDev)), "allocate part parameters");
+	}
+	phe_status st = allocate_slot1(r);
+	if (!st) st = allocate_parts(r);
+	return st;
 }
 
 static phe_status allocate(phe_renderer* r, uint32_t resX, uint32_t resY, uint32_t numLights)
@@ -326,7 +370,7 @@ static phe_status allocate(phe_renderer* r, uint32_t resX, uint32_t resY, uint32
 	r->resX = resX;
 	r->resY = resY;
 	r->numLights = numLights;
-	if ((e = cudaMemset(base, 0, total)) != cudaSuccess) return cuda_fail(e, "clear frame buffers");
+	if (phe_status st = clear_new(base, total)) return st;
 	r->parity = 0;
 	if (r->inFlight == 2 || r->frameParts >= 2) {
 		phe_status st = allocate_slot1(r);
@@ -622,20 +666,11 @@ extern "C" phe_status phe_renderer_set_frames_in_flight(phe_renderer* r, int fra
 	r->slotUsed[0] = r->slotUsed[1] = false;
 	r->framePending = false;
 	r->nextSlot = r->lastSlot = 0;
-	r->inFlight = frames;
 	if (frames == 2) {
-		if (!r->resolveStream) {
-			for (int j = 0; j < 2; j++) {
-				PHE_CUDA_TRY(cudaStreamCreateWithFlags(&r->travStream[j], cudaStreamNonBlocking), "create frame stream");
-				PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->travDone[j], cudaEventDisableTiming), "create frame event");
-				PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->resolveDone[j], cudaEventDisableTiming), "create frame event");
-			}
-			PHE_CUDA_TRY(cudaStreamCreateWithFlags(&r->resolveStream, cudaStreamNonBlocking), "create frame stream");
-			PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->callEvent, cudaEventDisableTiming), "create frame event");
-		}
-		phe_status st = allocate_slot1(r);
-		if (st) return st;
+		phe_status st = prepare_flight(r);
+		if (st) return st;   // frames stay one at a time
 	}
+	r->inFlight = frames;
 	return PHE_OK;
 }
 
@@ -651,23 +686,12 @@ extern "C" phe_status phe_renderer_set_frame_parts(phe_renderer* r, int parts)
 		cudaGraphExecDestroy(r->graphExec);
 		r->graphExec = nullptr;
 	}
+	const int prev = r->frameParts;
 	r->frameParts = parts;
-	if (parts >= 2) {
-		if (!r->partFork) PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->partFork, cudaEventDisableTiming), "create part event");
-		for (int j = 1; j < parts; j++) {
-			if (!r->partStream[j]) {
-				PHE_CUDA_TRY(cudaStreamCreateWithFlags(&r->partStream[j], cudaStreamNonBlocking), "create part stream");
-				PHE_CUDA_TRY(cudaEventCreateWithFlags(&r->partJoin[j], cudaEventDisableTiming), "create part event");
-			}
-			if (j >= 2 && !r->partParams[j])
-				PHE_CUDA_TRY(cudaMalloc(&r->partParams[j], sizeof(FrameParamsDev)), "allocate part parameters");
-		}
-		phe_status st = allocate_slot1(r);
-		if (!st) st = allocate_parts(r);
-		if (st) return st;
-	}
+	phe_status st = parts >= 2 ? prepare_parts(r, parts) : PHE_OK;
+	if (st) r->frameParts = prev;   // a failed change keeps the previous split, whose parts are all made
 	make_fb1(r);
-	return PHE_OK;
+	return st;
 }
 
 extern "C" phe_status phe_renderer_set_latency_recording(phe_renderer* r, int enable)
@@ -801,6 +825,10 @@ extern "C" phe_status phe_renderer_render(phe_renderer* r, const phe_sphere_ligh
 	                           ? std::min<uint32_t>((uint32_t)r->frameParts, tileRows) : 1u;
 	uint32_t n[kMaxFrameParts] = {};
 	for (uint32_t k = 0; k < parts; k++) n[k] = (tileRows - k + parts - 1) / parts * 8u * r->resX;
+	{   // everything this frame's shape uses (only checks, unless an earlier call failed part way)
+		phe_status st = pipelined ? prepare_flight(r) : parts >= 2 ? prepare_parts(r, (int)parts) : PHE_OK;
+		if (st) return st;
+	}
 	if (pipelined) {
 		// after the caller's work so far, and after the resolve that last read this slot's buffers
 		PHE_CUDA_TRY(cudaEventRecord(r->callEvent, s), "record caller work");

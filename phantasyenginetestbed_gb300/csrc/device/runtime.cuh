@@ -55,4 +55,14 @@ inline phe_status cuda_fail(cudaError_t e, const char* what)
 		if (e_ != cudaSuccess) return ::phe_gb300::cuda_fail(e_, what); \
 	} while (0)
 
+// Set-up uploads (cudaMemcpy from pageable host memory, cudaMemset of device memory) run on the legacy
+// default stream and may return before the bytes reach the device, and launches on streams created
+// non-blocking are not ordered after that stream. Waiting for it makes such uploads complete before the
+// call that made them returns, so the next launch on any stream reads them.
+inline phe_status finish_uploads(const char* what)
+{
+	cudaError_t e = cudaStreamSynchronize(cudaStreamLegacy);
+	return e == cudaSuccess ? PHE_OK : cuda_fail(e, what);
+}
+
 } // namespace phe_gb300

@@ -33,6 +33,7 @@ phe_status device_info(DeviceInfo** out)
 		uint32_t* pool = nullptr;
 		PHE_CUDA_TRY(cudaMalloc(&pool, sizeof(uint32_t) * kCounterPool), "cudaMalloc(counter pool)");
 		PHE_CUDA_TRY(cudaMemset(pool, 0, sizeof(uint32_t) * kCounterPool), "cudaMemset(counter pool)");
+		if (phe_status up = finish_uploads("clear counter pool")) return up;
 		d.numSMs = prop.multiProcessorCount;
 		d.maxThreadsPerSM = prop.maxThreadsPerMultiProcessor;
 		d.counterPool = pool;
@@ -214,9 +215,11 @@ phe_status upload_shading(phe_scene* sc, const phe_material* mats, uint32_t numM
 	char* base = nullptr;
 	PHE_CUDA_TRY(cudaMalloc(&base, total), "cudaMalloc(materials and textures)");
 	cudaError_t e = cudaMemcpy(base, host.data(), total, cudaMemcpyHostToDevice);
-	if (e != cudaSuccess) {
+	phe_status up = e != cudaSuccess ? cuda_fail(e, "upload materials and textures")
+	                                 : finish_uploads("upload materials and textures");
+	if (up) {
 		cudaFree(base);
-		return cuda_fail(e, "upload materials and textures");
+		return up;
 	}
 	if (sc->shading) {
 		// Frames or casts queued on any stream may still read the old arrays.
@@ -385,6 +388,7 @@ extern "C" phe_status phe_scene_create(const phe_bvh_node* nodes, uint32_t numNo
 	if (dDatas && (e = cudaMemcpy(dDatas, hd.data(), hd.size() * sizeof(phe_triangle_data), cudaMemcpyHostToDevice)) != cudaSuccess)
 		return cleanup(cuda_fail(e, "upload triangle data"));
 	if ((e = cudaMemset(dStatus, 0, statusBytes)) != cudaSuccess) return cleanup(cuda_fail(e, "clear status"));
+	if (phe_status up = finish_uploads("upload scene")) return cleanup(up);
 
 	phe_scene* sc = new phe_scene();
 	sc->dev.nodes = dNodes;

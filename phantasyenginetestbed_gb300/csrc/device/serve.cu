@@ -290,7 +290,10 @@ void upload_scene_table(phe_server* s)
 		t.push_back(sc->dev);
 		s->wideScenes = s->wideScenes || sc->dev.nodes4 || sc->dev.nodes8;
 	}
-	if (!t.empty()) cudaMemcpy(s->dScenes, t.data(), t.size() * sizeof(DeviceScene), cudaMemcpyHostToDevice);
+	// On the wave stream: after the waves still reading the table, before the next wave (the pageable
+	// source is staged before the call returns).
+	if (!t.empty())
+		cudaMemcpyAsync(s->dScenes, t.data(), t.size() * sizeof(DeviceScene), cudaMemcpyHostToDevice, s->waveStream);
 	s->sceneTableDirty = false;
 }
 

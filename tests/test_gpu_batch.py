@@ -135,3 +135,32 @@ def test_batch_rejects_bad_items():
         Batch([scenes[0][2]], [(1, CLOSEST, 32, d, o)])      # scene index out of range
     with pytest.raises(P.PheError):
         Batch([scenes[0][2]], [(0, 7, 32, d, o)])            # unknown kind
+
+
+@pytest.mark.parametrize("graph", [False, True], ids=["direct", "graph"])
+def test_update_right_after_a_launch_on_a_non_blocking_stream(graph):
+    """phe_batch_update rewrites the item table in place while the launch before it may still read it, on
+    a stream that is not ordered after the legacy default stream (torch's side streams are created
+    non-blocking): the update waits for that launch and its upload is complete when it returns, so both
+    launches give the oracle's results."""
+    import torch
+    scenes = _scenes()
+    sizes = [20000, 5000, 777, 4096, 31]
+    items_a, host_a = _mix(scenes, sizes, 11)
+    items_b, host_b = _mix(scenes, sizes, 12)
+    torch.cuda.synchronize()   # the rays' uploads ran on the default stream
+    side = torch.cuda.Stream()
+    batch = Batch([x[2] for x in scenes], items_a, use_graph=graph)
+    for _ in range(2):
+        for it in items_a + items_b:
+            it[4].fill_(0xCD)
+        torch.cuda.synchronize()
+        batch.update(items_a)
+        batch.launch(stream=side)
+        batch.update(items_b)
+        batch.launch(stream=side)
+        side.synchronize()
+        _check(scenes, items_a, host_a)
+        _check(scenes, items_b, host_b)
+    for s_ in scenes:
+        assert s_[2].status() == 0
