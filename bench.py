@@ -79,6 +79,8 @@ def parse():
                     help="shadow-pass schedule: one pass over both queues after the bounce pass (default), the "
                          "primary shadow pass beside the bounce pass, or each after its own pass")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-secondary", action="store_true",
+                    help="frame: skip the compact batched and served runs after the frame's measurement")
     ap.add_argument("--layout", choices=["binary", "wide4", "wide8"], default=DEFAULT_LAYOUT,
                     help="node layout of the frame's scene (every layout gives the same results)")
     ap.add_argument("--workload", choices=["frame", "plain", "batch", "large", "serve", "sizes"], default="frame",
@@ -626,6 +628,8 @@ def run_ours(args, world, rank, local):
         "gpu_launches": launches_per_frame * args.steps,
         "cpu_baseline": cpu,
     }
+    if world == 1 and not args.no_secondary:
+        line["secondary"] = secondary_measures()
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
@@ -634,6 +638,37 @@ def run_ours(args, world, rank, local):
 # ---------------------------------------------------------------------------------------------
 # Additional workloads (not the headline line): uneven batches, large incoherent scene, serving.
 # ---------------------------------------------------------------------------------------------
+
+SECONDARY_SERVE_RATE = 4000.0   # requests/s: saturates the serial server, not the continuous one
+
+
+def secondary_measures() -> dict:
+    """Compact runs of the batched and served workloads, after the frame's timed region, so that the
+    frame line also carries their ratios: the uneven batch mix (measure_batch: autotuned graph launch vs
+    64 plain launches, 10 timed steps each, L2 flushed) and Poisson serving at one rate that saturates
+    the serial server (measure_serve: 2 s of arrivals, continuous batching vs serial). A failure is
+    reported in place of that entry and leaves the frame line intact."""
+    out = {}
+    try:
+        b = measure_batch(10, 3)
+        out["batch"] = {"workload": "64 ray batches of 1K-1M rays over 4 scenes (10K-2M triangles), 70/30 closest/any",
+                        "rays": b["rays"], "batched_graph": {k: b["batched_graph"][k] for k in ("ms", "Mrays_s", "params")},
+                        "plain_64_launches": {k: b["plain_64_launches"][k] for k in ("ms", "Mrays_s")},
+                        "speedup_vs_plain": b["speedup_vs_plain"], "speedup_vs_synchronised": b["speedup_vs_synchronised"],
+                        "l2": b["l2"]}
+    except Exception as e:   # noqa: BLE001 - reported in the line
+        out["batch"] = {"error": f"{type(e).__name__}: {e}"[:300]}
+    try:
+        sv = measure_serve([SECONDARY_SERVE_RATE], 2.0, 8, 0, burst_too=False)
+        row = sv["rates"][str(int(SECONDARY_SERVE_RATE))]
+        out["serve"] = {"workload": "Poisson arrivals of render and ray-query requests over 8 scenes "
+                                    f"({min(sv['scenes_triangles']):,}-{max(sv['scenes_triangles']):,} triangles)",
+                        "rate_req_s": SECONDARY_SERVE_RATE, "arrivals_s": 2.0,
+                        "continuous": row["continuous"], "serial": row["serial"],
+                        "speedup": round(row["continuous"]["Mrays_s"] / max(row["serial"]["Mrays_s"], 1e-9), 3)}
+    except Exception as e:   # noqa: BLE001 - reported in the line
+        out["serve"] = {"error": f"{type(e).__name__}: {e}"[:300]}
+    return out
 
 def _scene_with_bvh(name):
     import phantasyenginetestbed_gb300 as P
@@ -730,6 +765,11 @@ def run_plain(args):
 
 
 def run_batch(args):
+    print(json.dumps(measure_batch(args.steps, args.warmup, save_tuning_to=ROOT / "profiles" / "batch_autotune.json")),
+          flush=True)
+
+
+def measure_batch(steps, warmup, save_tuning_to=None):
     """64 ray batches of uneven size (log-uniform 1K..1M), 50% pinhole / 50% random-surface rays, over 4
     resident scenes (10K/155K/1M/2M triangles), 70/30 closest/any: one autotuned persistent launch
     replayed from a CUDA graph vs 64 plain launches (and vs 64 launches each followed by a device
@@ -767,14 +807,15 @@ def run_batch(args):
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
     batch = Batch(scenes, items, use_graph=False)
     best, best_ms, table = batch.autotune(repeats=3)
-    save_tuning(ROOT / "profiles" / "batch_autotune.json", best, best_ms, table,
-                command=f"python bench.py --workload batch --steps {args.steps} --warmup {args.warmup} "
-                        "(phe_batch_autotune, repeats=3, cold L2)")
+    if save_tuning_to is not None:
+        save_tuning(save_tuning_to, best, best_ms, table,
+                    command=f"python bench.py --workload batch --steps {steps} --warmup {warmup} "
+                            "(phe_batch_autotune, repeats=3, cold L2)")
     batch.set_params(block_size=best["blockSize"], blocks_per_sm=best["blocksPerSM"], order=best["order"], use_graph=True,
                      layout=best["layout"], stack_shared=best["stackShared"], sort_window=best["sortWindow"])
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         batch.launch(stream)
-    t_batched = _timed(lambda: batch.launch(stream), args.steps, stream, flush)
+    t_batched = _timed(lambda: batch.launch(stream), steps, stream, flush)
 
     def plain():
         for si, kind, n, d_rays, out in items:
@@ -785,10 +826,10 @@ def run_batch(args):
             (P.cast_closest if kind == CLOSEST else P.cast_any)(scenes[si], d_rays, out, n, stream=stream)
             torch.cuda.synchronize()
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         plain()
-    t_plain = _timed(plain, args.steps, stream, flush)
-    steps_sync = max(3, args.steps // 5)
+    t_plain = _timed(plain, steps, stream, flush)
+    steps_sync = max(3, steps // 5)
     # wall clock of the synchronised variant (host waits are part of that launch model)
     walls = []
     for _ in range(steps_sync):
@@ -811,7 +852,9 @@ def run_batch(args):
             "speedup_vs_plain": round(mp / mb, 3), "speedup_vs_synchronised": round(ms_sync / mb, 3),
             "autotune_candidates": len(table), "layouts_tried": sorted({r["layout"] for r in table}),
             "l2": "flushed before every timed step"}
-    print(json.dumps(line), flush=True)
+    for x in [batch] + scenes:   # the batch holds the scene handles
+        x.close()
+    return line
 
 
 def run_sizes(args):
@@ -974,6 +1017,11 @@ def run_large(args):
 
 
 def run_serve(args):
+    print(json.dumps(measure_serve([float(x) for x in args.rates.split(",")], args.duration, args.render_slots,
+                                   args.batch_window_us)), flush=True)
+
+
+def measure_serve(rates, duration, render_slots, batch_window_us, burst_too=True):
     """Poisson arrivals of render requests (256x256..1920x1080 log-uniform, 1-4 spp) and ray-query
     requests (4K..512K rays log-uniform, 70/30 closest/any) against 8 resident scenes of 50K..4M
     triangles, under a 120 GB budget, through the continuous-batching server and the serial baseline."""
@@ -1058,32 +1106,34 @@ def run_serve(args):
                 "rays": int(rays), "span_s": round(span_ms / 1e3, 3), "Mrays_s": round(rays / span_ms / 1e3, 1)}
 
     results = {}
-    for rate in [float(x) for x in args.rates.split(",")]:
-        reqs = make_requests(rate, args.duration, int(rate))
+    for rate in rates:
+        reqs = make_requests(rate, duration, int(rate))
         row = {}
         for mode in ("continuous", "serial"):
-            server = Server(memory_budget=120 << 30, render_slots=args.render_slots, serial=(mode == "serial"),
-                            batch_window_us=args.batch_window_us)
+            server = Server(memory_budget=120 << 30, render_slots=render_slots, serial=(mode == "serial"),
+                            batch_window_us=batch_window_us)
             ids = [server.add_scene(sc) for sc in scenes]
             row[mode] = run(server, ids, reqs)
             server.close()
         results[str(int(rate))] = row
-    # Saturation: the highest rate's requests all submitted at once (makespan throughput).
-    burst = {}
-    reqs = make_requests(max(float(x) for x in args.rates.split(",")), args.duration, 99)
-    for mode in ("continuous", "serial"):
-        server = Server(memory_budget=120 << 30, render_slots=args.render_slots, serial=(mode == "serial"),
-                        batch_window_us=args.batch_window_us)
-        ids = [server.add_scene(sc) for sc in scenes]
-        burst[mode] = run(server, ids, reqs, burst=True)
-        server.close()
-    burst["speedup"] = round(burst["continuous"]["Mrays_s"] / max(burst["serial"]["Mrays_s"], 1e-9), 3)
-    results["burst"] = burst
-    line = {"workload": "serve", "metric": METRIC, "unit": "Mrays/s",
+    if burst_too:
+        # Saturation: the highest rate's requests all submitted at once (makespan throughput).
+        burst = {}
+        reqs = make_requests(max(rates), duration, 99)
+        for mode in ("continuous", "serial"):
+            server = Server(memory_budget=120 << 30, render_slots=render_slots, serial=(mode == "serial"),
+                            batch_window_us=batch_window_us)
+            ids = [server.add_scene(sc) for sc in scenes]
+            burst[mode] = run(server, ids, reqs, burst=True)
+            server.close()
+        burst["speedup"] = round(burst["continuous"]["Mrays_s"] / max(burst["serial"]["Mrays_s"], 1e-9), 3)
+        results["burst"] = burst
+    for sc in scenes:
+        sc.close()
+    return {"workload": "serve", "metric": METRIC, "unit": "Mrays/s",
             "scenes_triangles": [int(len(s.tri_verts)) for s, _ in built], "scene_build_s": round(build_s, 1),
-            "budget_bytes": 120 << 30, "arrivals_s": args.duration, "render_slots": args.render_slots,
-            "batch_window_us": args.batch_window_us, "rates": results}
-    print(json.dumps(line), flush=True)
+            "budget_bytes": 120 << 30, "arrivals_s": duration, "render_slots": render_slots,
+            "batch_window_us": batch_window_us, "rates": results}
 
 
 def main():
