@@ -643,11 +643,12 @@ SECONDARY_SERVE_RATE = 4000.0   # requests/s: saturates the serial server, not t
 
 
 def secondary_measures() -> dict:
-    """Compact runs of the batched and served workloads, after the frame's timed region, so that the
-    frame line also carries their ratios: the uneven batch mix (measure_batch: autotuned graph launch vs
-    64 plain launches, 10 timed steps each, L2 flushed) and Poisson serving at one rate that saturates
-    the serial server (measure_serve: 2 s of arrivals, continuous batching vs serial). A failure is
-    reported in place of that entry and leaves the frame line intact."""
+    """Compact runs of the other workloads, after the frame's timed region, so that the frame line also
+    carries them: the uneven batch mix (measure_batch: autotuned graph launch vs 64 plain launches, 10
+    timed steps each, L2 flushed), the large incoherent workload on the binary layout (measure_large: 10
+    timed launches per pass, L2 flushed) and Poisson serving at one rate that saturates the serial server
+    (measure_serve: 2 s of arrivals, continuous batching vs serial). A failure is reported in place of
+    that entry and leaves the frame line intact."""
     out = {}
     try:
         b = measure_batch(10, 3)
@@ -658,6 +659,17 @@ def secondary_measures() -> dict:
                         "l2": b["l2"]}
     except Exception as e:   # noqa: BLE001 - reported in the line
         out["batch"] = {"error": f"{type(e).__name__}: {e}"[:300]}
+    try:
+        lg = measure_large(4096, 16 << 20, 10, 3, layout_names=("binary",))
+        out["large"] = {"workload": f"{lg['triangles']:,} triangles: 16M diffuse closest-hit rays from the hits of a "
+                                    "4096x4096 primary pass, then 16M any-hit shadow rays over 4 lights, one launch each",
+                        "primary": {k: lg["primary"][k] for k in ("ms", "Mrays_s")},
+                        "diffuse_closest": {k: lg["layouts"]["binary"]["diffuse_closest"][k] for k in ("ms", "Mrays_s")},
+                        "shadow_any": {k: lg["layouts"]["binary"]["shadow_any"][k] for k in ("ms", "Mrays_s")},
+                        "hbm_frac": {p: r["frac"] for p, r in lg.get("roofline", {}).items()},
+                        "l2": lg["l2"]}
+    except Exception as e:   # noqa: BLE001 - reported in the line
+        out["large"] = {"error": f"{type(e).__name__}: {e}"[:300]}
     try:
         sv = measure_serve([SECONDARY_SERVE_RATE], 2.0, 8, 0, burst_too=False)
         row = sv["rates"][str(int(SECONDARY_SERVE_RATE))]
@@ -942,10 +954,14 @@ def large_rays(s, b, prim_rays, prim_hits, n, lights, seed):
 
 
 def run_large(args):
+    print(json.dumps(measure_large(args.res, args.rays, args.steps, args.warmup)), flush=True)
+
+
+def measure_large(res_side, N, steps, warmup, layout_names=("binary", "wide4", "wide8")):
     """The large incoherent workload: 8.63M-triangle scene (2048x2048-cell heightfield + 20,000 cubes,
     world x32). A 4096x4096 pinhole primary pass gives the hit points; then ONE launch of 16M diffuse
     closest-hit rays from them (cosine-weighted, seeded PCG64 directions) and ONE launch of 16M any-hit
-    shadow rays toward 4 point lights, each timed over args.steps launches from a cold L2 (the scene is
+    shadow rays toward 4 point lights, each timed over `steps` launches from a cold L2 (the scene is
     ~0.9 GB, 7x the L2), on every node layout the scene offers. HBM traffic per launch comes from a
     one-kernel ncu capture (profiles/large_workload_ncu.md)."""
     import torch
@@ -953,8 +969,7 @@ def run_large(args):
     from phantasyenginetestbed_gb300.renderer import make_lights
     torch.cuda.set_device(0)
     stream = torch.cuda.current_stream()
-    res = (args.res, args.res)
-    N = args.rays
+    res = (res_side, res_side)
     s, b, build_s = _scene_with_bvh("c4_2048_20000")
     scene = P.Scene(b.nodes, b.verts)
     k = s.scale
@@ -978,15 +993,15 @@ def run_large(args):
     layouts = {}
     lay0, avail = scene.layout()
     for layout, name in ((0, "binary"), (1, "wide4"), (2, "wide8")):
-        if layout and not (avail & layout):
+        if name not in layout_names or (layout and not (avail & layout)):
             continue
         scene.set_layout(layout)
         row = {}
         for pas, fn in (("diffuse_closest", lambda: P.cast_closest(scene, d_diffuse, hits, N, stream=stream)),
                         ("shadow_any", lambda: P.cast_any(scene, d_shadow, vis, N, stream=stream))):
-            for _ in range(args.warmup):
+            for _ in range(warmup):
                 fn()
-            t = _timed(fn, max(3, min(args.steps, 20)), stream, flush)
+            t = _timed(fn, max(3, min(steps, 20)), stream, flush)
             m = statistics.median(t)
             row[pas] = {"ms": round(m, 3), "Mrays_s": round(N / m / 1e3, 1), "latency_ms": _percentiles(t)}
         layouts[name] = row
@@ -1013,7 +1028,8 @@ def run_large(args):
                              "how": f"{rec['dram_bytes_per_ray']:.1f} DRAM bytes per ray (ncu, {rec['source']}) x {N} rays / "
                                     f"live launch time"}
         line["roofline"] = roof
-    print(json.dumps(line), flush=True)
+    scene.close()
+    return line
 
 
 def run_serve(args):
