@@ -354,7 +354,9 @@ phe_status phe_renderer_create(phe_renderer** out);
 phe_status phe_renderer_destroy(phe_renderer* renderer);
 /* setStaticScene: the scene must carry triangle data and materials. */
 phe_status phe_renderer_set_static_scene(phe_renderer* renderer, const phe_scene* scene);
-/* setTargetResolution: multiples of 8 (CudaTracerRenderer.cpp:470-471); reallocates frame buffers. */
+/* setTargetResolution: multiples of 8 (CudaTracerRenderer.cpp:470-471). When the buffers are too small,
+ * it reallocates them: it waits for all device work first, and returns with the new buffers cleared, so
+ * the next frame on any stream finds them zeroed. */
 phe_status phe_renderer_set_target_resolution(phe_renderer* renderer, uint32_t resX, uint32_t resY);
 /* updateCamera(ViewFrustum): position, direction, up, vertical FOV in degrees and the TAA pixel
  * offset (ViewFrustum::setPixelOffset, GameScreen.cpp:187-203). */
