@@ -152,6 +152,10 @@ void finish(phe_server* s, Request* r, phe_status st)
 	r->state = kDone;
 	s->bytesInUse -= r->bytes;
 	s->raysCompleted += r->rays;
+	if (r->dMem) {   // a query that failed before its wave freed it
+		cudaFreeAsync(r->dMem, s->waveStream);
+		r->dMem = nullptr;
+	}
 	if (r->done) {
 		s->eventPool.push_back(r->done);
 		r->done = nullptr;
@@ -165,7 +169,10 @@ phe_status admit_query(phe_server* s, Request* r)
 	size_t raysBytes = align256((size_t)d.numRays * sizeof(phe_ray_in));
 	size_t outBytes = align256((size_t)d.numRays * (d.kind == PHE_REQ_ANY ? 1 : sizeof(phe_ray_hit)));
 	cudaError_t e = cudaMallocAsync(&r->dMem, raysBytes + outBytes, s->waveStream);
-	if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync(request)");
+	if (e != cudaSuccess) {
+		r->dMem = nullptr;
+		return cuda_fail(e, "cudaMallocAsync(request)");
+	}
 	e = cudaMemcpyAsync(r->dMem, d.rays, (size_t)d.numRays * sizeof(phe_ray_in), cudaMemcpyHostToDevice, s->waveStream);
 	if (e != cudaSuccess) return cuda_fail(e, "upload request rays");
 	return PHE_OK;
@@ -431,7 +438,9 @@ void worker_loop(phe_server* s)
 					if (!w.busy) {
 						phe_status ps = launch_wave(s, w);
 						if (ps) {
-							for (Request* r : s->admitted) finish(s, r, ps);
+							// queries the wave issued before the failure complete through their events
+							for (Request* r : s->admitted)
+								if (r->state != kIssued) finish(s, r, ps);
 							s->admitted.clear();
 							s->cvDone.notify_all();
 						}
@@ -508,7 +517,7 @@ extern "C" phe_status phe_server_create(const phe_server_config* cfg, phe_server
 	}
 	if (e != cudaSuccess || ps) {
 		phe_status fs = ps ? ps : cuda_fail(e, "phe_server_create");
-		delete s;  // resources of a half-built server are released with the process
+		phe_server_destroy(s);   // releases what was made (no worker thread yet)
 		return fs;
 	}
 	s->worker = std::thread(worker_loop, s);
